@@ -1,0 +1,143 @@
+"""CPU oracle (TEST INFRASTRUCTURE ONLY) — ctypes bindings over oracle/_build/libvren_oracle.so.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may use this package, and
+only as the checker / the timed CPU baseline.  See vren_oracle.h for what is pinned.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import build as _build
+
+_LIB = None
+u32, u64, i32, vp = C.c_uint32, C.c_uint64, C.c_int, C.c_void_p
+
+_PROTOS = {
+    "oracle_round_to_next_power_of_2": (u32, [u32]),
+    "oracle_round_to_next_power_of": (u32, [u32, u32]),
+    "oracle_divide_and_ceil": (u32, [u32, u32]),
+    "oracle_calc_bvh_padded_leaf_count": (u32, [u32]),
+    "oracle_calc_bvh_buffer_length": (u32, [u32]),
+    "oracle_calc_bvh_root_index": (u32, [u32]),
+    "oracle_calc_bvh_level_count": (u32, [u32]),
+    "oracle_reduce_tree_u32": (None, [i32, vp, u32, vp]),
+    "oracle_reduce_tree_vec4": (None, [i32, vp, u32, vp]),
+    "oracle_reduce_u32": (u32, [i32, vp, u64]),
+    "oracle_reduce_f32": (C.c_float, [i32, vp, u64]),
+    "oracle_exclusive_scan_u32": (None, [vp, u64]),
+    "oracle_downsweep_u32": (None, [vp, u32, i32]),
+    "oracle_stable_sort_u32": (None, [vp, vp, u64]),
+    "oracle_bucket_sort_u32x2": (None, [vp, u32, u32, vp, vp]),
+    "oracle_build_bvh": (None, [vp, u32]),
+    "oracle_bvh_point_query": (u32, [vp, u32, vp, vp, u32]),
+    "oracle_cs_slice_table": (None, [vp, u32, vp, vp]),
+    "oracle_cs_light_bvh": (None, [vp, vp, u32, vp, u32, vp, vp, vp]),
+    "oracle_cs_find_unique_clusters": (u32, [vp, vp, u32, u32, vp, i32, vp, u32, vp, i32]),
+    "oracle_cs_assign_lights": (u64, [vp, u32, u32, u32, vp, vp, u32, vp, vp, vp, vp, vp, u64, i32]),
+}
+
+OPS = {"add": 0, "min": 1, "max": 2}
+
+
+def lib() -> C.CDLL:
+    global _LIB
+    if _LIB is None:
+        path = _build.build()
+        dll = C.CDLL(str(path))
+        for name, (res, args) in _PROTOS.items():
+            f = getattr(dll, name)
+            f.restype = res
+            f.argtypes = args
+        _LIB = dll
+    return _LIB
+
+
+def _p(a: np.ndarray | None):
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data
+
+
+# ---- primitives -------------------------------------------------------------------------------
+def reduce_tree_u32(op: str, data: np.ndarray) -> np.ndarray:
+    data = np.ascontiguousarray(data, dtype=np.uint32)
+    P = int(lib().oracle_round_to_next_power_of_2(len(data)))
+    out = np.empty(max(P, 0), dtype=np.uint32)
+    if len(data):
+        lib().oracle_reduce_tree_u32(OPS[op], _p(data), len(data), _p(out))
+    return out
+
+
+def reduce_tree_vec4(op: str, data: np.ndarray) -> np.ndarray:
+    data = np.ascontiguousarray(data, dtype=np.float32).reshape(-1, 4)
+    P = int(lib().oracle_round_to_next_power_of_2(len(data)))
+    out = np.empty((P, 4), dtype=np.float32)
+    if len(data):
+        lib().oracle_reduce_tree_vec4(OPS[op], _p(data), len(data), _p(out))
+    return out
+
+
+def reduce_u32(op: str, data: np.ndarray) -> int:
+    data = np.ascontiguousarray(data, dtype=np.uint32)
+    return int(lib().oracle_reduce_u32(OPS[op], _p(data), len(data)))
+
+
+def reduce_f32(op: str, data: np.ndarray) -> np.float32:
+    data = np.ascontiguousarray(data, dtype=np.float32)
+    return np.float32(lib().oracle_reduce_f32(OPS[op], _p(data), len(data)))
+
+
+def exclusive_scan_u32(data: np.ndarray) -> np.ndarray:
+    out = np.array(data, dtype=np.uint32, copy=True)
+    lib().oracle_exclusive_scan_u32(_p(out), len(out))
+    return out
+
+
+def downsweep_u32(data: np.ndarray, clear_last: bool) -> np.ndarray:
+    out = np.array(data, dtype=np.uint32, copy=True)
+    lib().oracle_downsweep_u32(_p(out), len(out), 1 if clear_last else 0)
+    return out
+
+
+def stable_sort_u32(keys: np.ndarray, values: np.ndarray | None = None):
+    k = np.array(keys, dtype=np.uint32, copy=True)
+    v = None if values is None else np.array(values, dtype=np.uint32, copy=True)
+    lib().oracle_stable_sort_u32(_p(k), _p(v), len(k))
+    return k if v is None else (k, v)
+
+
+def bucket_sort_u32x2(pairs: np.ndarray, key_bits: int):
+    pairs = np.ascontiguousarray(pairs, dtype=np.uint32).reshape(-1, 2)
+    out = np.empty_like(pairs)
+    ends = np.empty(1 << key_bits, dtype=np.uint32)
+    lib().oracle_bucket_sort_u32x2(_p(pairs), len(pairs), key_bits, _p(out), _p(ends))
+    return out, ends
+
+
+def build_bvh(nodes: np.ndarray, padded_leaf_count: int) -> np.ndarray:
+    """nodes: uint32 array of shape (buffer_length, 8) with the leaves filled."""
+    out = np.array(nodes, dtype=np.uint32, copy=True)
+    lib().oracle_build_bvh(_p(out), padded_leaf_count)
+    return out
+
+
+def bvh_point_query(nodes: np.ndarray, root_index: int, p) -> list[int]:
+    nodes = np.ascontiguousarray(nodes, dtype=np.uint32)
+    pt = np.asarray(p, dtype=np.float32)
+    cap = max(1, len(nodes))
+    out = np.empty(cap, dtype=np.uint32)
+    n = int(lib().oracle_bvh_point_query(_p(nodes), root_index, _p(pt), _p(out), cap))
+    return out[: min(n, cap)].tolist()
+
+
+def size_helpers(n: int) -> dict:
+    L = lib()
+    return {
+        "padded": int(L.oracle_calc_bvh_padded_leaf_count(n)),
+        "length": int(L.oracle_calc_bvh_buffer_length(n)),
+        "root": int(L.oracle_calc_bvh_root_index(n)),
+        "levels": int(L.oracle_calc_bvh_level_count(n)),
+    }

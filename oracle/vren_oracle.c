@@ -1,0 +1,731 @@
+/*
+ * vren_oracle.c — CPU oracle for the vren hot path.  TEST INFRASTRUCTURE ONLY: used by the
+ * tests, the smoke check and the benchmark's CPU-baseline leg as the checker, never by the
+ * product path.  See vren_oracle.h for what is pinned (primitives) and what is unpinned
+ * (clustered shading stages).
+ *
+ * Build: gcc -O2 -std=c11 -ffp-contract=off -fopenmp (oracle/build.py).
+ */
+#include "vren_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define INVALID_NODE 0xFFFFFFFEu
+#define LEAF_NODE 0xFFFFFFFFu
+
+static int nthreads(int t)
+{
+#ifdef _OPENMP
+    return t > 0 ? t : omp_get_max_threads();
+#else
+    (void)t;
+    return 1;
+#endif
+}
+
+/* ================================================================================================
+ * Size helpers — vren/vren/base/base.hpp:286-328 and vren/vren/primitives/build_bvh.cpp:158-193,
+ * with the reference's double-precision log/pow where it uses them.
+ * ================================================================================================ */
+uint32_t oracle_round_to_next_power_of_2(uint32_t v)
+{
+    v--;
+    v |= v >> 1; v |= v >> 2; v |= v >> 4; v |= v >> 8; v |= v >> 16;
+    v++;
+    return v;
+}
+
+uint32_t oracle_round_to_next_power_of(uint32_t n, uint32_t base)
+{
+    /* base.hpp:318-323: exp = log(n)/log(base); return (uint32_t) pow(base, ceil(exp)); */
+    double e = log((double)n) / log((double)base);
+    double r = pow((double)base, ceil(e));
+    if (!(r >= 0.0) || r > 4294967295.0) return 0u;
+    return (uint32_t)r;
+}
+
+uint32_t oracle_divide_and_ceil(uint32_t value, uint32_t divider)
+{
+    /* base.hpp:325-328 */
+    return (uint32_t)ceil((double)value / (double)divider);
+}
+
+uint32_t oracle_calc_bvh_padded_leaf_count(uint32_t leaf_count)
+{
+    /* build_bvh.cpp:158-161 */
+    return leaf_count <= 1 ? 32u : oracle_round_to_next_power_of(leaf_count, 32u);
+}
+
+uint32_t oracle_calc_bvh_buffer_length(uint32_t leaf_count)
+{
+    /* build_bvh.cpp:163-175 */
+    uint32_t p = oracle_calc_bvh_padded_leaf_count(leaf_count);
+    uint64_t len = 0;
+    while (p != 0) {
+        len += p;
+        p >>= 5;
+    }
+    return (uint32_t)len;
+}
+
+uint32_t oracle_calc_bvh_root_index(uint32_t leaf_count)
+{
+    /* build_bvh.cpp:183-187 */
+    return oracle_calc_bvh_buffer_length(oracle_calc_bvh_padded_leaf_count(leaf_count)) - 1u;
+}
+
+uint32_t oracle_calc_bvh_level_count(uint32_t leaf_count)
+{
+    /* build_bvh.cpp:189-193: glm::log2 on an integer is the integer log2 */
+    uint32_t p = oracle_calc_bvh_padded_leaf_count(leaf_count);
+    uint32_t l = 0;
+    while (p > 1) { p >>= 1; ++l; }
+    return l / 5u;
+}
+
+/* ================================================================================================
+ * Reduce — tree order of run_cpu_reduce (vren_test/vren_test/primitives/reduce.cpp:326-341) with
+ * the shader's combine b = OP(b, a) (vren/resources/shaders/reduce.comp:266) and the identities
+ * of VRen.cmake:70-75.  GLSL min(x,y) = y < x ? y : x, max(x,y) = x < y ? y : x.
+ * ================================================================================================ */
+static uint32_t u32_apply(int op, uint32_t right, uint32_t left)
+{
+    switch (op) {
+    case ORACLE_ADD: return right + left;
+    case ORACLE_MIN: return left < right ? left : right;
+    default: return right < left ? left : right;
+    }
+}
+
+static float f32_apply(int op, float right, float left)
+{
+    switch (op) {
+    case ORACLE_ADD: return right + left;
+    case ORACLE_MIN: return left < right ? left : right;
+    default: return right < left ? left : right;
+    }
+}
+
+void oracle_reduce_tree_u32(int op, const uint32_t* in, uint32_t n, uint32_t* out)
+{
+    uint32_t P = oracle_round_to_next_power_of_2(n);
+    uint32_t id = op == ORACLE_MIN ? 0xFFFFFFFFu : 0u;
+    for (uint32_t i = 0; i < P; ++i) out[i] = i < n ? in[i] : id;
+    for (uint32_t lvl = 0; (1u << lvl) < P; ++lvl) {
+        for (uint32_t j = 0; j < (P >> (lvl + 1)); ++j) {
+            uint32_t a = (1u << lvl) - 1u + (j << (lvl + 1));
+            uint32_t b = a + (1u << lvl);
+            out[b] = u32_apply(op, out[b], out[a]);
+        }
+    }
+}
+
+void oracle_reduce_tree_vec4(int op, const float* in, uint32_t n, float* out)
+{
+    uint32_t P = oracle_round_to_next_power_of_2(n);
+    float id = op == ORACLE_ADD ? 0.0f : (op == ORACLE_MIN ? 1e35f : -1e35f);
+    for (uint32_t i = 0; i < P; ++i)
+        for (int c = 0; c < 4; ++c) out[4 * i + c] = i < n ? in[4 * i + c] : id;
+    for (uint32_t lvl = 0; (1u << lvl) < P; ++lvl) {
+        for (uint32_t j = 0; j < (P >> (lvl + 1)); ++j) {
+            uint32_t a = (1u << lvl) - 1u + (j << (lvl + 1));
+            uint32_t b = a + (1u << lvl);
+            for (int c = 0; c < 4; ++c) out[4 * b + c] = f32_apply(op, out[4 * b + c], out[4 * a + c]);
+        }
+    }
+}
+
+uint32_t oracle_reduce_u32(int op, const uint32_t* in, uint64_t n)
+{
+    uint32_t acc = op == ORACLE_MIN ? 0xFFFFFFFFu : 0u;
+    for (uint64_t i = 0; i < n; ++i) acc = u32_apply(op, acc, in[i]);
+    return acc;
+}
+
+static uint32_t f32_key(float f)
+{
+    uint32_t b;
+    memcpy(&b, &f, 4);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+static float f32_unkey(uint32_t k)
+{
+    uint32_t b = (k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k;
+    float f;
+    memcpy(&f, &b, 4);
+    return f;
+}
+
+float oracle_reduce_f32(int op, const float* in, uint64_t n)
+{
+    /* min/max in IEEE-754 total order, so the result does not depend on the evaluation order */
+    uint32_t acc = op == ORACLE_MIN ? 0xFFFFFFFFu : 0u;
+    for (uint64_t i = 0; i < n; ++i) {
+        uint32_t k = f32_key(in[i]);
+        if (op == ORACLE_MIN ? k < acc : k > acc) acc = k;
+    }
+    return f32_unkey(acc);
+}
+
+/* ================================================================================================
+ * Scan
+ * ================================================================================================ */
+void oracle_exclusive_scan_u32(uint32_t* data, uint64_t n)
+{
+    /* vren_test/vren_test/primitives/blelloch_scan.cpp:72 std::exclusive_scan(..., 0) */
+    uint32_t run = 0;
+    for (uint64_t i = 0; i < n; ++i) {
+        uint32_t x = data[i];
+        data[i] = run;
+        run += x;
+    }
+}
+
+void oracle_downsweep_u32(uint32_t* data, uint32_t n, int clear_last)
+{
+    /* The reference's dispatch sequence, restated literally:
+     * global levels (blelloch_scan.cpp:139-172, blelloch_scan_downsweep.comp:250-269) for
+     * level = log2(n)-1 down to 10, clearing the last element on the first one, then the
+     * 1024-wide work-group pass (blelloch_scan.cpp:174-188, blelloch_scan_downsweep.comp:275-341)
+     * which reads elements at index < n - clear_last and pads with zeros. */
+    uint32_t log2n = 0;
+    while ((1u << log2n) < n) ++log2n;
+    uint32_t cl = clear_last ? 1u : 0u;
+    for (int level = (int)log2n - 1; level > 9; --level) {
+        uint32_t offset = (1u << level) - 1u, stride = 1u << level;
+        for (uint64_t gid = 0;; ++gid) {
+            uint64_t a = offset + gid * stride * 2u;
+            uint64_t b = a + stride;
+            if (b >= n) break;
+            uint32_t bv = (cl && b == n - 1u) ? 0u : data[b];
+            data[b] = data[a] + bv;
+            data[a] = bv;
+        }
+        cl = 0;
+    }
+    uint32_t* s = (uint32_t*)malloc(1024 * sizeof(uint32_t));
+    uint32_t wgs = (n + 1023u) / 1024u;
+    for (uint32_t w = 0; w < wgs; ++w) {
+        for (uint32_t t = 0; t < 1024; ++t) {
+            uint32_t idx = w * 1024u + t;
+            s[t] = (idx < n - cl) ? data[idx] : 0u;
+        }
+        for (int level = 9; level >= 0; --level) {
+            uint32_t mask = (1u << (level + 1)) - 1u;
+            for (uint32_t t = 0; t < 1024; ++t) {
+                if ((t & mask) == mask) {
+                    uint32_t b = t, a = b - (1u << level);
+                    uint32_t tmp = s[b];
+                    s[b] = s[a] + tmp;
+                    s[a] = tmp;
+                }
+            }
+        }
+        for (uint32_t t = 0; t < 1024; ++t) {
+            uint32_t idx = w * 1024u + t;
+            if (idx < n) data[idx] = s[t];
+        }
+    }
+    free(s);
+}
+
+/* ================================================================================================
+ * Sorts
+ * ================================================================================================ */
+void oracle_stable_sort_u32(uint32_t* keys, uint32_t* values, uint64_t n)
+{
+    /* Stable LSD counting sort, 8 bits per pass: the result equals std::stable_sort by key. */
+    uint32_t* tk = (uint32_t*)malloc(n * sizeof(uint32_t) + 4);
+    uint32_t* tv = values ? (uint32_t*)malloc(n * sizeof(uint32_t) + 4) : NULL;
+    uint64_t count[257];
+    for (int pass = 0; pass < 4; ++pass) {
+        int shift = pass * 8;
+        memset(count, 0, sizeof(count));
+        for (uint64_t i = 0; i < n; ++i) count[((keys[i] >> shift) & 0xFFu) + 1]++;
+        for (int d = 0; d < 256; ++d) count[d + 1] += count[d];
+        for (uint64_t i = 0; i < n; ++i) {
+            uint64_t p = count[(keys[i] >> shift) & 0xFFu]++;
+            tk[p] = keys[i];
+            if (values) tv[p] = values[i];
+        }
+        memcpy(keys, tk, n * sizeof(uint32_t));
+        if (values) memcpy(values, tv, n * sizeof(uint32_t));
+    }
+    free(tk);
+    free(tv);
+}
+
+void oracle_bucket_sort_u32x2(const uint32_t* in, uint32_t n, uint32_t key_bits, uint32_t* out_pairs,
+                              uint32_t* out_ends)
+{
+    /* Group uvec2(key, value) by key & mask (bucket_sort_count.comp:237-241,
+     * bucket_sort_write.comp:271-276), stably.  out_ends = the counters region after the call:
+     * exclusive scan of the counts, then +1 per written element = inclusive scan. */
+    uint32_t nb = 1u << key_bits, mask = nb - 1u;
+    uint32_t* cnt = (uint32_t*)calloc(nb + 1, sizeof(uint32_t));
+    for (uint32_t i = 0; i < n; ++i) cnt[(in[2 * i] & mask) + 1]++;
+    for (uint32_t b = 0; b < nb; ++b) cnt[b + 1] += cnt[b];
+    for (uint32_t i = 0; i < n; ++i) {
+        uint32_t p = cnt[in[2 * i] & mask]++;
+        out_pairs[2 * p] = in[2 * i];
+        out_pairs[2 * p + 1] = in[2 * i + 1];
+    }
+    for (uint32_t b = 0; b < nb; ++b) out_ends[b] = cnt[b];
+    free(cnt);
+}
+
+/* ================================================================================================
+ * BVH — vren/resources/shaders/build_bvh.comp:225-249 per level (build_bvh.cpp:126-151), with the
+ * canonical decisions: a parent's AABB is the min/max over its valid children in IEEE total
+ * order; all-invalid parents get (+inf, -inf) and next = INVALID; pad = 0.
+ * ================================================================================================ */
+static float fmin_total(float a, float b) { return f32_key(b) < f32_key(a) ? b : a; }
+static float fmax_total(float a, float b) { return f32_key(b) > f32_key(a) ? b : a; }
+
+void oracle_build_bvh(oracle_bvh_node* bvh, uint32_t padded_leaf_count)
+{
+    uint32_t src = 0, count = padded_leaf_count;
+    while (count > 1) {
+        uint32_t dst = src + count;
+        for (uint32_t p = 0; p < count / 32u; ++p) {
+            oracle_bvh_node par;
+            int any = 0;
+            for (int a = 0; a < 3; ++a) { par.min[a] = INFINITY; par.max[a] = -INFINITY; }
+            for (uint32_t c = 0; c < 32; ++c) {
+                const oracle_bvh_node* ch = &bvh[src + p * 32u + c];
+                if (ch->next == INVALID_NODE) continue;
+                if (!any) {
+                    for (int a = 0; a < 3; ++a) { par.min[a] = ch->min[a]; par.max[a] = ch->max[a]; }
+                    any = 1;
+                } else {
+                    for (int a = 0; a < 3; ++a) {
+                        par.min[a] = fmin_total(par.min[a], ch->min[a]);
+                        par.max[a] = fmax_total(par.max[a], ch->max[a]);
+                    }
+                }
+            }
+            par.next = any ? src + p * 32u : INVALID_NODE;
+            par.pad = 0;
+            bvh[dst + p] = par;
+        }
+        src = dst;
+        count /= 32u;
+    }
+}
+
+static int aabb_contains(const oracle_bvh_node* n, const float p[3])
+{
+    /* vren_test/vren_test/primitives/build_bvh.cpp:25-34 */
+    return p[0] >= n->min[0] && p[1] >= n->min[1] && p[2] >= n->min[2] && p[0] <= n->max[0] &&
+           p[1] <= n->max[1] && p[2] <= n->max[2];
+}
+
+static void query_r(const oracle_bvh_node* bvh, uint32_t offset, const float p[3], uint32_t* out, uint32_t cap,
+                    uint32_t* cnt)
+{
+    /* vren_test/vren_test/primitives/build_bvh.cpp:36-64 */
+    for (uint32_t i = 0; i < 32; ++i) {
+        const oracle_bvh_node* nd = &bvh[offset + i];
+        if (nd->next == INVALID_NODE) continue;
+        if (aabb_contains(nd, p)) {
+            if (nd->next == LEAF_NODE) {
+                if (*cnt < cap) out[*cnt] = offset + i;
+                (*cnt)++;
+            } else {
+                query_r(bvh, nd->next, p, out, cap, cnt);
+            }
+        }
+    }
+}
+
+uint32_t oracle_bvh_point_query(const oracle_bvh_node* bvh, uint32_t root_index, const float p[3], uint32_t* out,
+                                uint32_t cap)
+{
+    /* vren_test/vren_test/primitives/build_bvh.cpp:66-78 */
+    uint32_t cnt = 0;
+    const oracle_bvh_node* root = &bvh[root_index];
+    if (root->next != INVALID_NODE && aabb_contains(root, p)) query_r(bvh, root->next, p, out, cap, &cnt);
+    return cnt;
+}
+
+/* ================================================================================================
+ * Clustered shading — shared float helpers (all single precision, no contraction)
+ * ================================================================================================ */
+static uint32_t floor_to_u32(float x)
+{
+    float f = floorf(x);
+    if (!(f >= 0.0f)) return 0u;
+    if (f >= 4294967296.0f) return 0xFFFFFFFFu;
+    return (uint32_t)f;
+}
+
+/* out = m * v, m column-major, summed ((c0 + c1) + c2) + c3 */
+static void matvec(const float* m, const float v[4], float out[4])
+{
+    for (int r = 0; r < 4; ++r) {
+        float t0 = m[0 * 4 + r] * v[0];
+        float t1 = m[1 * 4 + r] * v[1];
+        float t2 = m[2 * 4 + r] * v[2];
+        float t3 = m[3 * 4 + r] * v[3];
+        out[r] = ((t0 + t1) + t2) + t3;
+    }
+}
+
+static float glsl_min(float x, float y) { return y < x ? y : x; }
+static float glsl_max(float x, float y) { return x < y ? y : x; }
+
+/* Slice boundaries: REF bound[k] = near * a^k, a = 1 + 2 tan(half_fov) / tiles_y
+ * (find_unique_clusters.comp:65, clustered_shading.glsl:220-222), a^k by repeated double
+ * multiplication; FIXED32 bound[k] = near * r^k, r = (far/near)^(1/32), k <= 32, +inf beyond. */
+void oracle_cs_slice_table(const oracle_cs_view* v, uint32_t tiles_y, float* near_out, float* far_out)
+{
+    double bound[ORACLE_SLICES + 1];
+    const double nr = v->near_plane;
+    if (v->slicing == ORACLE_SLICING_FIXED32) {
+        double r = pow((double)v->far_plane / nr, 1.0 / 32.0);
+        double p = 1.0;
+        for (int k = 0; k <= ORACLE_SLICES; ++k) {
+            bound[k] = k <= 32 ? nr * p : INFINITY;
+            p *= r;
+        }
+    } else {
+        double a = 1.0 + 2.0 * tan((double)v->half_fov_y) / (double)tiles_y;
+        double p = 1.0;
+        for (int k = 0; k <= ORACLE_SLICES; ++k) {
+            bound[k] = nr * p;
+            p *= a;
+        }
+    }
+    for (int k = 0; k < ORACLE_SLICES; ++k) {
+        near_out[k] = (float)bound[k];
+        far_out[k] = (float)bound[k + 1];
+    }
+}
+
+static uint32_t slice_of(float z, const float* bnear, uint32_t kmax)
+{
+    /* largest k in [0, kmax] with bnear[k] <= z; 0 if none */
+    uint32_t k = 0;
+    for (uint32_t i = 0; i <= kmax; ++i)
+        if (bnear[i] <= z) k = i;
+        else break;
+    return k;
+}
+
+/* clustered_shading.glsl:128-164 */
+static uint32_t discretize_normal(const float n[3])
+{
+    if (n[0] == 0.0f && n[1] == 0.0f && n[2] == 0.0f) return 0xFFFFFFFFu;
+    float min_t = 1e35f;
+    uint32_t axis = 0, face = 0;
+    for (uint32_t i = 0; i < 3; ++i) {
+        float sg = n[i] > 0.0f ? 1.0f : (n[i] < 0.0f ? -1.0f : 0.0f);
+        float t = sg / n[i];
+        if (t < min_t) {
+            min_t = t;
+            axis = i;
+            face = (n[i] > 0.0f ? 1u : 0u) * 3u + i;
+        }
+    }
+    float p[3] = {n[0] * min_t, n[1] * min_t, n[2] * min_t};
+    float u = p[(axis + 1) % 3], w = p[(axis + 2) % 3];
+    uint32_t du = floor_to_u32(((u + 1.0f) / 2.0f) * 3.0f);
+    uint32_t dw = floor_to_u32(((w + 1.0f) / 2.0f) * 3.0f);
+    return (face * 9u + du * 3u + dw) & 0x3Fu;
+}
+
+/* ================================================================================================
+ * construct_point_light_bvh — vren/vren/pipeline/clustered_shading.cpp:60-346:
+ * view transform (point_light_position_to_view_space.comp:30), vec4 min/max (reduce trees),
+ * Morton codes (discretize_point_light_positions.comp:62-73), bucket sort on code & 0xFFFF
+ * (stable), leaves (init_light_array_bvh.comp:117-139), build_bvh.
+ * ================================================================================================ */
+void oracle_cs_light_bvh(const float* positions, const float* lights, uint32_t L, const oracle_cs_view* v,
+                         uint32_t morton_bits, float* view_pos, oracle_bvh_node* bvh, uint32_t* light_index)
+{
+    float mn[4] = {INFINITY, INFINITY, INFINITY, INFINITY}, mx[4] = {-INFINITY, -INFINITY, -INFINITY, -INFINITY};
+    for (uint32_t i = 0; i < L; ++i) {
+        float p[4] = {positions[4 * i], positions[4 * i + 1], positions[4 * i + 2], 1.0f};
+        matvec(v->view, p, &view_pos[4 * i]);
+        for (int c = 0; c < 4; ++c) {
+            if (i == 0) { mn[c] = view_pos[4 * i + c]; mx[c] = view_pos[4 * i + c]; }
+            else { mn[c] = fmin_total(mn[c], view_pos[4 * i + c]); mx[c] = fmax_total(mx[c], view_pos[4 * i + c]); }
+        }
+    }
+    const uint32_t bits = morton_bits == 30 ? 10u : 5u;
+    const float scale = (float)(1u << bits);
+    uint32_t* codes = (uint32_t*)malloc((size_t)L * 8 + 8);
+    for (uint32_t i = 0; i < L; ++i) {
+        uint32_t q[3];
+        for (int c = 0; c < 3; ++c) q[c] = floor_to_u32(((view_pos[4 * i + c] - mn[c]) / (mx[c] - mn[c])) * scale);
+        uint32_t code = 0;
+        for (uint32_t b = 0; b < bits; ++b) {
+            code |= ((q[0] >> b) & 1u) << (b * 3u);
+            code |= ((q[1] >> b) & 1u) << (b * 3u + 1u);
+            code |= ((q[2] >> b) & 1u) << (b * 3u + 2u);
+        }
+        codes[2 * i] = code;
+        codes[2 * i + 1] = i;
+    }
+    /* bucket sort on the low 16 bits (bucket_sort.hpp:15-16) for 15-bit codes; the 30-bit
+     * extension sorts on the whole code (stable either way) */
+    {
+        uint32_t* vals = (uint32_t*)malloc((size_t)L * 4 + 4);
+        uint32_t* ks = (uint32_t*)malloc((size_t)L * 4 + 4);
+        for (uint32_t i = 0; i < L; ++i) { ks[i] = morton_bits == 30 ? codes[2 * i] : (codes[2 * i] & 0xFFFFu); vals[i] = i; }
+        oracle_stable_sort_u32(ks, vals, L);
+        for (uint32_t i = 0; i < L; ++i) {
+            light_index[2 * i] = codes[2 * vals[i]];
+            light_index[2 * i + 1] = codes[2 * vals[i] + 1];
+        }
+        free(vals);
+        free(ks);
+    }
+    free(codes);
+    const uint32_t P = oracle_calc_bvh_padded_leaf_count(L);
+    for (uint32_t i = 0; i < P; ++i) {
+        oracle_bvh_node nd;
+        memset(&nd, 0, sizeof(nd));
+        if (i < L) {
+            uint32_t li = light_index[2 * i + 1];
+            float r = lights[4 * li + 3];
+            for (int c = 0; c < 3; ++c) {
+                nd.min[c] = view_pos[4 * li + c] - r;
+                nd.max[c] = view_pos[4 * li + c] + r;
+            }
+            nd.next = LEAF_NODE;
+        } else {
+            for (int c = 0; c < 3; ++c) { nd.min[c] = INFINITY; nd.max[c] = -INFINITY; }
+            nd.next = INVALID_NODE;
+        }
+        bvh[i] = nd;
+    }
+    oracle_build_bvh(bvh, P);
+}
+
+/* ================================================================================================
+ * find_unique_cluster_list — vren/resources/shaders/clustered_shading/find_unique_clusters.comp:46-120
+ * with the canonical decisions: integer texel (WRAP = reference's REPEAT sampler, or SKIP),
+ * slice from the boundary table, tiles in row-major order, keys ascending inside a tile.
+ * ================================================================================================ */
+static int cmp_u32(const void* a, const void* b)
+{
+    uint32_t x = *(const uint32_t*)a, y = *(const uint32_t*)b;
+    return x < y ? -1 : (x > y ? 1 : 0);
+}
+
+static uint32_t pixel_key(const float* depth, const float* normals, uint32_t W, uint32_t H, uint32_t gx, uint32_t gy,
+                          const oracle_cs_view* v, const float* bnear, uint32_t kmax)
+{
+    const uint32_t tx = gx % W, ty = gy % H;
+    const size_t px = (size_t)ty * W + tx;
+    float fx = (float)gx / (float)W, fy = (float)gy / (float)H;
+    float pos[4] = {fx * 2.0f - 1.0f, (1.0f - fy) * 2.0f - 1.0f, depth[px], 1.0f};
+    float vp[4];
+    matvec(v->inv_proj, pos, vp);
+    float z = vp[2] / vp[3];
+    uint32_t k = slice_of(z, bnear, kmax);
+    uint32_t nd = discretize_normal(&normals[3 * px]);
+    uint32_t i = gx >> 5, j = gy >> 5;
+    return (i & 0xFFu) | ((j & 0xFFu) << 8) | ((k & 0x3FFu) << 16) | (nd << 26);
+}
+
+uint32_t oracle_cs_find_unique_clusters(const float* depth, const float* normals, uint32_t W, uint32_t H,
+                                        const oracle_cs_view* v, int policy, uint32_t* keys, uint32_t key_cap,
+                                        uint32_t* refs, int threads)
+{
+    const uint32_t TX = (W + 31) / 32, TY = (H + 31) / 32, T = TX * TY;
+    float bnear[ORACLE_SLICES], bfar[ORACLE_SLICES];
+    oracle_cs_slice_table(v, TY, bnear, bfar);
+    const uint32_t kmax = v->slicing == ORACLE_SLICING_FIXED32 ? 31u : (ORACLE_SLICES - 1u);
+    uint32_t* tile_keys = (uint32_t*)malloc((size_t)T * 1024 * sizeof(uint32_t));
+    uint32_t* tile_count = (uint32_t*)malloc((size_t)T * sizeof(uint32_t));
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads(threads))
+    for (int64_t t = 0; t < (int64_t)T; ++t) {
+        uint32_t ti = (uint32_t)t % TX, tj = (uint32_t)t / TX;
+        uint32_t* tk = tile_keys + (size_t)t * 1024;
+        uint32_t m = 0;
+        for (uint32_t ly = 0; ly < 32; ++ly)
+            for (uint32_t lx = 0; lx < 32; ++lx) {
+                uint32_t gx = ti * 32 + lx, gy = tj * 32 + ly;
+                if (policy == ORACLE_SKIP && (gx >= W || gy >= H)) continue;
+                tk[m++] = pixel_key(depth, normals, W, H, gx, gy, v, bnear, kmax);
+            }
+        qsort(tk, m, sizeof(uint32_t), cmp_u32);
+        uint32_t u = 0;
+        for (uint32_t q = 0; q < m; ++q)
+            if (q == 0 || tk[q] != tk[q - 1]) tk[u++] = tk[q];
+        tile_count[t] = u;
+    }
+    uint32_t* tile_off = (uint32_t*)malloc((size_t)T * sizeof(uint32_t));
+    uint32_t U = 0;
+    for (uint32_t t = 0; t < T; ++t) { tile_off[t] = U; U += tile_count[t]; }
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads(threads))
+    for (int64_t t = 0; t < (int64_t)T; ++t) {
+        uint32_t ti = (uint32_t)t % TX, tj = (uint32_t)t / TX;
+        const uint32_t* tk = tile_keys + (size_t)t * 1024;
+        for (uint32_t q = 0; q < tile_count[t]; ++q)
+            if (tile_off[t] + q < key_cap) keys[tile_off[t] + q] = tk[q];
+        for (uint32_t ly = 0; ly < 32; ++ly)
+            for (uint32_t lx = 0; lx < 32; ++lx) {
+                uint32_t gx = ti * 32 + lx, gy = tj * 32 + ly;
+                if (gx >= W || gy >= H) continue;  /* stores outside the screen are dropped */
+                uint32_t key = pixel_key(depth, normals, W, H, gx, gy, v, bnear, kmax);
+                /* rank of key among the tile's unique keys */
+                uint32_t lo = 0, hi = tile_count[t];
+                while (lo < hi) {
+                    uint32_t mid = (lo + hi) / 2;
+                    if (tk[mid] < key) lo = mid + 1; else hi = mid;
+                }
+                refs[(size_t)gy * W + gx] = tile_off[t] + lo;
+            }
+    }
+    free(tile_keys);
+    free(tile_count);
+    free(tile_off);
+    return U;
+}
+
+/* ================================================================================================
+ * assign_lights — vren/resources/shaders/clustered_shading/assign_lights.comp:121-240 (count and
+ * write variants), cluster AABB of clustered_shading.glsl:193-231, node addressing of
+ * assign_lights.comp:108-119, tests of :84-102.  INVALID nodes never overlap (canonical).
+ * ================================================================================================ */
+typedef struct { float mn[3], mx[3]; } caabb;
+
+static caabb cluster_aabb(uint32_t key, uint32_t TX, uint32_t TY, const oracle_cs_view* v, const float* bnear,
+                          const float* bfar)
+{
+    uint32_t ci = key & 0xFFu, cj = (key >> 8) & 0xFFu, ck = (key >> 16) & 0x3FFu;
+    float x0 = (float)ci / (float)TX, y0 = (float)cj / (float)TY;
+    float x1 = (float)(ci + 1u) / (float)TX, y1 = (float)(cj + 1u) / (float)TY;
+    float a[4] = {x0 * 2.0f - 1.0f, (1.0f - y0) * 2.0f - 1.0f, 0.0f, 1.0f};
+    float b[4] = {x1 * 2.0f - 1.0f, (1.0f - y1) * 2.0f - 1.0f, 0.0f, 1.0f};
+    float va[4], vb[4];
+    matvec(v->inv_proj, a, va);
+    matvec(v->inv_proj, b, vb);
+    for (int c = 0; c < 3; ++c) { va[c] = va[c] / va[3]; vb[c] = vb[c] / vb[3]; }
+    float la = sqrtf((va[0] * va[0] + va[1] * va[1]) + va[2] * va[2]);
+    float lb = sqrtf((vb[0] * vb[0] + vb[1] * vb[1]) + vb[2] * vb[2]);
+    float d1[3] = {va[0] / la, va[1] / la, va[2] / la};
+    float d2[3] = {vb[0] / lb, vb[1] / lb, vb[2] / lb};
+    float cn = bnear[ck], cf = bfar[ck];
+    float s1 = cn / d1[2], s2 = cf / d2[2];
+    caabb r;
+    for (int c = 0; c < 3; ++c) { r.mn[c] = s1 * d1[c]; r.mx[c] = s2 * d2[c]; }
+    return r;
+}
+
+static int test_aabb_aabb(const caabb* c, const oracle_bvh_node* n)
+{
+    return c->mx[0] >= n->min[0] && c->mn[0] <= n->max[0] && c->mx[1] >= n->min[1] && c->mn[1] <= n->max[1] &&
+           c->mx[2] >= n->min[2] && c->mn[2] <= n->max[2];
+}
+
+static int test_sphere_aabb(const float o[3], float r, const caabb* c)
+{
+    float d[3];
+    for (int k = 0; k < 3; ++k) {
+        float p = glsl_max(c->mn[k], glsl_min(o[k], c->mx[k]));
+        d[k] = p - o[k];
+    }
+    float len = sqrtf((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]);
+    return len < r;
+}
+
+static uint32_t lsb(uint32_t x) { return (uint32_t)__builtin_ctz(x); }
+
+/* One traversal; when out != NULL writes the assigned indices (reverse lane order per group). */
+static uint32_t traverse_cluster(const caabb* c, const oracle_bvh_node* bvh, uint32_t root, uint32_t level_count,
+                                 const uint32_t* light_index, const float* view_pos, uint32_t* out)
+{
+    uint32_t ov[8] = {0};
+    uint32_t level = 0, state = 2, acc = 0;
+    for (;;) {
+        if (state == 0) { /* ADVANCE */
+            ov[level] &= ~(1u << lsb(ov[level]));
+            if (ov[level] == 0) state = 1;
+            else { level++; state = 2; }
+        } else if (state == 1) { /* POP */
+            if (level > 0) { level--; state = 0; }
+            else break;
+        } else { /* ENTERING */
+            int64_t addr = (int64_t)root;
+            uint64_t pw = 32;
+            for (uint32_t i = 1; i <= level + 1; ++i) { addr -= (int64_t)pw; pw *= 32; }
+            for (uint32_t i = 0; i < level; ++i) {
+                uint64_t w = 1;
+                for (uint32_t e = 0; e < level - i; ++e) w *= 32;
+                addr += (int64_t)(w * lsb(ov[i]));
+            }
+            if (level + 1 < level_count) {
+                uint32_t mask = 0;
+                for (uint32_t lane = 0; lane < 32; ++lane) {
+                    const oracle_bvh_node* nd = &bvh[addr + lane];
+                    if (nd->next != INVALID_NODE && test_aabb_aabb(c, nd)) mask |= 1u << lane;
+                }
+                ov[level] = mask;
+                if (mask == 0) state = 1;
+                else level++;
+            } else {
+                uint32_t mask = 0, idx[32];
+                for (uint32_t lane = 0; lane < 32; ++lane) {
+                    const oracle_bvh_node* nd = &bvh[addr + lane];
+                    idx[lane] = 0;
+                    if (nd->next == INVALID_NODE) continue;
+                    uint32_t li = light_index[2 * (addr + lane) + 1];
+                    idx[lane] = li;
+                    float o[3] = {view_pos[4 * li], view_pos[4 * li + 1], view_pos[4 * li + 2]};
+                    float r = (nd->max[0] - nd->min[0]) / 2.0f;
+                    if (test_sphere_aabb(o, r, c)) mask |= 1u << lane;
+                }
+                if (out) {
+                    for (uint32_t lane = 0; lane < 32; ++lane) {
+                        if (!(mask & (1u << lane))) continue;
+                        uint32_t slot = (uint32_t)__builtin_popcount(mask & ~((1u << lane) - 1u)) - 1u;
+                        out[acc + slot] = idx[lane];
+                    }
+                }
+                acc += (uint32_t)__builtin_popcount(mask);
+                state = 1;
+            }
+        }
+    }
+    return acc;
+}
+
+uint64_t oracle_cs_assign_lights(const uint32_t* keys, uint32_t U, uint32_t W, uint32_t H, const oracle_cs_view* v,
+                                 const oracle_bvh_node* bvh, uint32_t L, const uint32_t* light_index,
+                                 const float* view_pos, uint32_t* counts, uint32_t* offsets, uint32_t* indices,
+                                 uint64_t index_cap, int threads)
+{
+    const uint32_t TX = (W + 31) / 32, TY = (H + 31) / 32;
+    if (L == 0) {
+        for (uint32_t c = 0; c < U; ++c) { counts[c] = 0; offsets[c] = 0; }
+        return 0;
+    }
+    float bnear[ORACLE_SLICES], bfar[ORACLE_SLICES];
+    oracle_cs_slice_table(v, TY, bnear, bfar);
+    const uint32_t root = oracle_calc_bvh_root_index(L);
+    const uint32_t levels = oracle_calc_bvh_level_count(L);
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads(threads))
+    for (int64_t c = 0; c < (int64_t)U; ++c) {
+        caabb box = cluster_aabb(keys[c], TX, TY, v, bnear, bfar);
+        counts[c] = traverse_cluster(&box, bvh, root, levels, light_index, view_pos, NULL);
+    }
+    uint64_t total = 0;
+    for (uint32_t c = 0; c < U; ++c) { offsets[c] = (uint32_t)total; total += counts[c]; }
+    if (total > index_cap) return total;
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads(threads))
+    for (int64_t c = 0; c < (int64_t)U; ++c) {
+        caabb box = cluster_aabb(keys[c], TX, TY, v, bnear, bfar);
+        traverse_cluster(&box, bvh, root, levels, light_index, view_pos, indices + offsets[c]);
+    }
+    return total;
+}

@@ -1,0 +1,174 @@
+// BuildBVH — vren::build_bvh (vren/vren/primitives/build_bvh.cpp:95-156, build_bvh.comp:32-55).
+//
+// The reference dispatches once per level; a 32-lane subgroup turns 32 children into one parent
+// with subgroupMin/Max over the valid lanes.  Here one launch builds two levels: a 1024-thread CTA
+// reads 1024 consecutive nodes, each warp reduces its 32 children into a parent (warp-wide
+// redux.sync on order-preserving integer keys), and warp 0 reduces the CTA's 32 parents into the
+// grandparent.  A 32^3-leaf light BVH therefore takes two launches instead of three dispatches and
+// two barriers.
+//
+// Parents: next = index of the first child when at least one child is valid, else
+// VREN_BVH_INVALID_NODE; the AABB is the min/max over the valid children (+inf/-inf when none);
+// pad = 0.  min/max use IEEE-754 total order (-0 < +0), which makes them independent of the
+// reduction order; the oracle states the same rule.
+#include "common.cuh"
+#include "internal.h"
+
+namespace vren_gb300 {
+
+VREN_DEFINE_ERROR_WORD(bvh)
+
+__device__ __forceinline__ uint32_t fkey(float f)
+{
+    uint32_t b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float unkey(uint32_t k)
+{
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k);
+}
+
+struct NodeF {
+    float mn[3];
+    uint32_t next;
+    float mx[3];
+    uint32_t pad;
+};
+
+// Reduce the 32 nodes held by the lanes of a warp into their parent (valid in lane 0's return).
+__device__ __forceinline__ NodeF warp_parent(const NodeF& c, bool present, uint32_t first_child_index)
+{
+    const bool valid = present && c.next != VREN_BVH_INVALID_NODE;
+    const uint32_t vmask = __ballot_sync(0xFFFFFFFFu, valid);
+    NodeF p;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const uint32_t kmin = __reduce_min_sync(0xFFFFFFFFu, valid ? fkey(c.mn[a]) : 0xFFFFFFFFu);
+        const uint32_t kmax = __reduce_max_sync(0xFFFFFFFFu, valid ? fkey(c.mx[a]) : 0u);
+        p.mn[a] = vmask ? unkey(kmin) : __int_as_float(0x7F800000);   // +inf
+        p.mx[a] = vmask ? unkey(kmax) : __int_as_float(0xFF800000);   // -inf
+    }
+    p.next = vmask ? first_child_index : VREN_BVH_INVALID_NODE;
+    p.pad = 0u;
+    return p;
+}
+
+__device__ __forceinline__ NodeF load_node(const vren_bvh_node* b, uint32_t i)
+{
+    const float4* p = reinterpret_cast<const float4*>(b + i);
+    float4 lo = p[0], hi = p[1];
+    NodeF n;
+    n.mn[0] = lo.x; n.mn[1] = lo.y; n.mn[2] = lo.z; n.next = __float_as_uint(lo.w);
+    n.mx[0] = hi.x; n.mx[1] = hi.y; n.mx[2] = hi.z; n.pad = __float_as_uint(hi.w);
+    return n;
+}
+
+__device__ __forceinline__ void store_node(vren_bvh_node* b, uint32_t i, const NodeF& n)
+{
+    float4* p = reinterpret_cast<float4*>(b + i);
+    p[0] = make_float4(n.mn[0], n.mn[1], n.mn[2], __uint_as_float(n.next));
+    p[1] = make_float4(n.mx[0], n.mx[1], n.mx[2], __uint_as_float(n.pad));
+}
+
+// Level `src` (count nodes starting at src_off) -> parents at dst1_off (count/32 nodes) and, when
+// two_levels, grandparents at dst2_off (count/1024 nodes).
+__global__ void __launch_bounds__(1024) build_bvh_kernel(vren_bvh_node* __restrict__ bvh, uint32_t src_off,
+                                                         uint32_t count, uint32_t dst1_off, uint32_t dst2_off,
+                                                         int two_levels)
+{
+    __shared__ NodeF s_parent[32];
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const uint32_t local = blockIdx.x * 1024u + tid;
+    const bool present = local < count;
+    NodeF c{};
+    if (present) c = load_node(bvh, src_off + local);
+    const uint32_t parent_local = local >> 5;
+    NodeF p = warp_parent(c, present, src_off + (parent_local << 5));
+    if (lane == 0 && present) {
+        store_node(bvh, dst1_off + parent_local, p);
+        if (two_levels) s_parent[warp] = p;
+    }
+    if (!two_levels) return;
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t gp_local = blockIdx.x;
+        const uint32_t parents_here = (count >> 5) - blockIdx.x * 32u < 32u ? (count >> 5) - blockIdx.x * 32u : 32u;
+        const bool pres = lane < parents_here;
+        NodeF q = pres ? s_parent[lane] : NodeF{};
+        NodeF g = warp_parent(q, pres, dst1_off + (gp_local << 5));
+        if (lane == 0) store_node(bvh, dst2_off + gp_local, g);
+    }
+}
+
+}  // namespace vren_gb300
+
+using namespace vren_gb300;
+
+extern "C" uint32_t vren_calc_bvh_padded_leaf_count(uint32_t leaf_count)
+{
+    if (leaf_count <= 1) return 32u;
+    uint64_t p = 32;
+    while (p < leaf_count) p <<= 5;
+    return p > 0xFFFFFFFFull ? 0u : (uint32_t)p;
+}
+
+extern "C" uint32_t vren_calc_bvh_buffer_length(uint32_t leaf_count)
+{
+    uint64_t p = vren_calc_bvh_padded_leaf_count(leaf_count);
+    uint64_t len = 0;
+    while (p != 0) {
+        len += p;
+        p >>= 5;
+    }
+    return len > 0xFFFFFFFFull ? 0u : (uint32_t)len;
+}
+
+extern "C" size_t vren_calc_bvh_buffer_size(uint32_t leaf_count)
+{
+    return (size_t)vren_calc_bvh_buffer_length(vren_calc_bvh_padded_leaf_count(leaf_count)) * sizeof(vren_bvh_node);
+}
+
+extern "C" uint32_t vren_calc_bvh_root_index(uint32_t leaf_count)
+{
+    uint32_t len = vren_calc_bvh_buffer_length(vren_calc_bvh_padded_leaf_count(leaf_count));
+    return len ? len - 1 : 0u;
+}
+
+extern "C" uint32_t vren_calc_bvh_level_count(uint32_t leaf_count)
+{
+    uint32_t p = vren_calc_bvh_padded_leaf_count(leaf_count);
+    uint32_t l = 0;
+    while ((1ull << (l + 1)) <= p) ++l;  // integer log2
+    return l / 5;
+}
+
+extern "C" int vren_build_bvh(vren_stream_t s, vren_bvh_node* bvh, uint32_t padded_leaf_count)
+{
+    // build_bvh.cpp:102: leaf_count >= 32 and a power of 32.
+    if (!bvh || padded_leaf_count < 32 || vren_calc_bvh_padded_leaf_count(padded_leaf_count) != padded_leaf_count)
+        return VREN_ERR_ARG;
+    if ((uintptr_t)bvh & 15u) return VREN_ERR_ARG;
+    return build_bvh_levels(as_stream(s), bvh, 0, padded_leaf_count);
+}
+
+namespace vren_gb300 {
+int build_bvh_levels(cudaStream_t st, vren_bvh_node* bvh, uint32_t src, uint32_t count)
+{
+    while (count > 1) {
+        const uint32_t dst1 = src + count;
+        if (count >= 1024) {
+            const uint32_t dst2 = dst1 + count / 32;
+            build_bvh_kernel<<<count / 1024, 1024, 0, st>>>(bvh, src, count, dst1, dst2, 1);
+            VREN_LAUNCH_CHECK();
+            src = dst1 + count / 32;
+            count /= 1024;
+        } else {
+            build_bvh_kernel<<<1, count, 0, st>>>(bvh, src, count, dst1, 0, 0);
+            VREN_LAUNCH_CHECK();
+            src = dst1;
+            count /= 32;
+        }
+    }
+    return VREN_OK;
+}
+}  // namespace vren_gb300

@@ -1,0 +1,80 @@
+// C ABI support: status strings, device error word, wait limit and the integer size helpers of
+// vren/vren/base/base.hpp:281-328.
+#include "common.cuh"
+
+#include <cmath>
+
+namespace vren_gb300 {
+uint32_t g_wait_limit = kDefaultWaitLimit;
+}
+
+using namespace vren_gb300;
+
+// One error word per translation unit (see VREN_DEFINE_ERROR_WORD).
+extern "C" int vren_internal_error_reduce(int clear);
+extern "C" int vren_internal_error_scan(int clear);
+extern "C" int vren_internal_error_radix(int clear);
+extern "C" int vren_internal_error_bvh(int clear);
+
+extern "C" const char* vren_status_string(int status)
+{
+    switch (status) {
+    case VREN_OK: return "ok";
+    case VREN_ERR_ARG: return "invalid argument";
+    case VREN_ERR_CAPACITY: return "capacity exceeded";
+    case VREN_ERR_TIMEOUT: return "device wait timed out";
+    case VREN_ERR_CUDA: return "CUDA runtime error";
+    case VREN_ERR_STATE: return "invalid state";
+    default: return "unknown status";
+    }
+}
+
+extern "C" int vren_device_error(int clear)
+{
+    if (cudaDeviceSynchronize() != cudaSuccess) return VREN_ERR_CUDA;
+    int (*const words[])(int) = {vren_internal_error_reduce, vren_internal_error_scan, vren_internal_error_radix,
+                                 vren_internal_error_bvh};
+    int first = 0;
+    for (auto w : words) {
+        int e = w(clear);
+        if (e != 0 && first == 0) first = e;
+    }
+    return first;
+}
+
+extern "C" uint32_t vren_set_wait_limit(uint32_t rounds)
+{
+    uint32_t prev = g_wait_limit;
+    g_wait_limit = rounds ? rounds : kDefaultWaitLimit;
+    return prev;
+}
+
+extern "C" uint32_t vren_round_to_next_power_of_2(uint32_t v)
+{
+    // Same bit trick as the reference: 0 maps to 0, values above 2^31 wrap to 0.
+    v--;
+    v |= v >> 1;
+    v |= v >> 2;
+    v |= v >> 4;
+    v |= v >> 8;
+    v |= v >> 16;
+    v++;
+    return v;
+}
+
+extern "C" uint32_t vren_round_to_next_power_of(uint32_t n, uint32_t base)
+{
+    // Smallest power of `base` that is >= n (the reference's ceil(log(n)/log(base)) in double,
+    // restated with integers).  n = 0 gives 0 (the reference's pow(base, -inf)).
+    if (base < 2) return 0;
+    if (n == 0) return 0;
+    uint64_t p = 1;
+    while (p < n) p *= base;
+    return p > 0xFFFFFFFFull ? 0u : (uint32_t)p;
+}
+
+extern "C" uint32_t vren_divide_and_ceil(uint32_t value, uint32_t divider)
+{
+    if (divider == 0) return 0;
+    return (uint32_t)(((uint64_t)value + divider - 1) / divider);
+}

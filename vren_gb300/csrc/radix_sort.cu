@@ -1,0 +1,500 @@
+// Onesweep LSD radix sort and stable bucket sort.
+//
+// Reference: vren::radix_sort (vren/vren/primitives/radix_sort.cpp:203-392) sorts uint32 keys with
+// eight 4-bit passes, each made of a buffer fill, a per-work-group 16-bin count
+// (radix_sort_local_count.comp), an up-sweep reduce of the counts, a 16-lane scan
+// (radix_sort_global_offset.comp), a down-sweep and a reorder that issues 16 ballots per key and
+// scatters uncoalesced (radix_sort_reorder.comp:183-241): ~48 commands per sort.
+// vren::bucket_sort (bucket_sort.cpp:119-208) counts with global atomics, scans 65536 counters and
+// scatters with atomics, so its order inside a bucket is unspecified.
+//
+// Here: one histogram kernel reads the keys once and builds the digit histograms of every pass;
+// then one kernel per digit pass ("onesweep", Adinets & Merrill 2022):
+//   1. a CTA takes the next tile ticket (tiles start in order, so look-back always terminates);
+//   2. each warp loads 32*ITEMS consecutive keys, striped, with coalesced loads;
+//   3. stable in-warp ranks from DIGIT_BITS ballots per key (peers = lanes with an equal digit)
+//      and per-warp digit counters in shared memory;
+//   4. the tile's digit counts are published and each digit's global offset is resolved by
+//      decoupled look-back over the preceding tiles (one thread per digit, bounded wait);
+//   5. keys (and values) are staged in shared memory in digit order and written out so that
+//      consecutive threads write consecutive addresses of the same digit run.
+// Status words ([flag:2 | count:30]) alternate between two buffers: pass p reads buffer p&1 and
+// clears the rows of buffer (p+1)&1 for its own tile, so no pass needs a separate memset.
+#include "common.cuh"
+#include "internal.h"
+
+#include <type_traits>
+
+namespace vren_gb300 {
+
+VREN_DEFINE_ERROR_WORD(radix)
+
+enum ElemMode { kKeys = 0, kPairs = 1, kUvec2 = 2 };
+
+constexpr int kSortThreads = 256;
+constexpr int kSortWarps = kSortThreads / 32;
+constexpr int kMaxPasses = 8;
+constexpr int kMaxRadix = 256;
+
+// Scratch layout in uint32 words.
+constexpr uint32_t kTicketWords = 16;                      // [0, 8): pass tickets, [8]: histogram done ticket
+constexpr uint32_t kHistOffset = kTicketWords;              // hist[pass][radix]
+constexpr uint32_t kOffsOffset = kHistOffset + kMaxPasses * kMaxRadix;  // exclusive digit offsets
+constexpr uint32_t kStatusOffset = kOffsOffset + kMaxPasses * kMaxRadix;
+constexpr uint32_t kZeroWords = kOffsOffset;               // region cleared at the start of a sort
+
+struct PassInfo {
+    uint32_t shift[kMaxPasses];
+    uint32_t width[kMaxPasses];
+    uint32_t count;
+};
+
+template <int MODE> struct KeyOf;
+
+__device__ __forceinline__ uint32_t digit_of(uint32_t key, uint32_t shift, uint32_t width)
+{
+    return (key >> shift) & ((1u << width) - 1u);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Histogram of all passes.  Also clears status buffer 0 (used by the first pass).
+// ------------------------------------------------------------------------------------------------
+template <int RADIX, int MODE>
+__global__ void __launch_bounds__(kSortThreads) onesweep_hist_kernel(
+    const uint32_t* __restrict__ keys, uint32_t n, PassInfo passes, uint32_t* __restrict__ scratch,
+    uint32_t status_words)
+{
+    __shared__ uint32_t s_hist[kMaxPasses * RADIX];
+    const uint32_t tid = threadIdx.x;
+    for (uint32_t i = tid; i < passes.count * RADIX; i += kSortThreads) s_hist[i] = 0u;
+    __syncthreads();
+
+    auto count_key = [&](uint32_t k) {
+#pragma unroll
+        for (int p = 0; p < kMaxPasses; ++p)
+            if (p < (int)passes.count) atomicAdd(&s_hist[p * RADIX + digit_of(k, passes.shift[p], passes.width[p])], 1u);
+    };
+
+    const uint32_t grid_threads = gridDim.x * kSortThreads;
+    if (MODE == kUvec2) {
+        // Elements are (key, value) pairs; a uint4 holds two.
+        const uint32_t npair = n / 2;
+        const uint4* p4 = reinterpret_cast<const uint4*>(keys);
+        for (uint32_t i = blockIdx.x * kSortThreads + tid; i < npair; i += grid_threads) {
+            uint4 q = __ldg(p4 + i);
+            count_key(q.x);
+            count_key(q.z);
+        }
+        if ((n & 1u) && blockIdx.x == 0 && tid == 0) count_key(keys[2 * (n - 1)]);
+    } else {
+        const uint32_t nvec = n / 4;
+        const uint4* p4 = reinterpret_cast<const uint4*>(keys);
+        for (uint32_t i = blockIdx.x * kSortThreads + tid; i < nvec; i += grid_threads) {
+            uint4 q = __ldg(p4 + i);
+            count_key(q.x); count_key(q.y); count_key(q.z); count_key(q.w);
+        }
+        if (blockIdx.x == 0 && tid < (n & 3u)) count_key(keys[nvec * 4 + tid]);
+    }
+    __syncthreads();
+
+    uint32_t* g_hist = scratch + kHistOffset;
+    for (uint32_t i = tid; i < passes.count * RADIX; i += kSortThreads) {
+        uint32_t v = s_hist[i];
+        if (v) atomicAdd(&g_hist[(i / RADIX) * kMaxRadix + (i % RADIX)], v);
+    }
+
+    // Clear status buffer 0.
+    uint32_t* status0 = scratch + kStatusOffset;
+    for (uint32_t i = blockIdx.x * kSortThreads + tid; i < status_words; i += grid_threads) status0[i] = 0u;
+
+    // Last CTA turns the histograms into exclusive digit offsets.
+    __shared__ bool s_last;
+    __syncthreads();
+    if (tid == 0) {
+        __threadfence();
+        s_last = (atomicAdd(scratch + 8, 1u) == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    if (tid < passes.count) {
+        uint32_t run = 0;
+        for (int d = 0; d < RADIX; ++d) {
+            uint32_t c = ld_relaxed_u32(g_hist + tid * kMaxRadix + d);
+            scratch[kOffsOffset + tid * kMaxRadix + d] = run;
+            run += c;
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// One digit pass.
+// ------------------------------------------------------------------------------------------------
+template <int DIGIT_BITS, int ITEMS, int MODE>
+__global__ void __launch_bounds__(kSortThreads) onesweep_pass_kernel(
+    const uint32_t* __restrict__ in_keys, const uint32_t* __restrict__ in_vals,
+    uint32_t* __restrict__ out_keys, uint32_t* __restrict__ out_vals,
+    uint32_t n, uint32_t pass, uint32_t shift, uint32_t width, uint32_t num_tiles,
+    uint32_t* __restrict__ scratch, uint32_t wait_limit)
+{
+    constexpr int RADIX = 1 << DIGIT_BITS;
+    constexpr int TILE = kSortThreads * ITEMS;
+    constexpr bool HAS_VALS = (MODE != kKeys);
+    using Elem = typename std::conditional<MODE == kUvec2, uint2, uint32_t>::type;
+
+    __shared__ Elem s_keys[TILE];
+    __shared__ uint32_t s_vals[MODE == kPairs ? TILE : 1];
+    __shared__ uint32_t s_warp_hist[kSortWarps][RADIX];
+    __shared__ uint32_t s_tile_excl[RADIX];
+    __shared__ int32_t s_delta[RADIX];
+    __shared__ uint32_t s_tile;
+
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    if (tid == 0) s_tile = atomicAdd(scratch + pass, 1u);
+    for (uint32_t i = tid; i < kSortWarps * RADIX; i += kSortThreads) (&s_warp_hist[0][0])[i] = 0u;
+    __syncthreads();
+    const uint32_t tile = s_tile;
+
+    uint32_t* status = scratch + kStatusOffset + (size_t)(pass & 1u) * num_tiles * RADIX;
+    uint32_t* status_next = scratch + kStatusOffset + (size_t)((pass + 1u) & 1u) * num_tiles * RADIX;
+    for (uint32_t d = tid; d < RADIX; d += kSortThreads) status_next[(size_t)tile * RADIX + d] = 0u;
+
+    // Striped load: item j of lane l is element warp_base + 32*j + l.
+    const uint32_t warp_base = tile * TILE + warp * (32 * ITEMS);
+    Elem key[ITEMS];
+    uint32_t val[ITEMS];
+    uint32_t pos[ITEMS];
+#pragma unroll
+    for (int j = 0; j < ITEMS; ++j) {
+        const uint32_t idx = warp_base + 32 * j + lane;
+        key[j] = Elem{};
+        val[j] = 0u;
+        if (idx < n) {
+            if (MODE == kUvec2) {
+                (reinterpret_cast<uint2*>(&key[j]))[0] = __ldcs(reinterpret_cast<const uint2*>(in_keys) + idx);
+            } else {
+                (reinterpret_cast<uint32_t*>(&key[j]))[0] = __ldcs(in_keys + idx);
+                if (MODE == kPairs) val[j] = __ldcs(in_vals + idx);
+            }
+        }
+    }
+
+    // Stable in-warp ranking.
+#pragma unroll
+    for (int j = 0; j < ITEMS; ++j) {
+        const uint32_t idx = warp_base + 32 * j + lane;
+        const bool valid = idx < n;
+        uint32_t k;
+        if (MODE == kUvec2) k = (reinterpret_cast<uint2*>(&key[j]))->x;
+        else k = *(reinterpret_cast<uint32_t*>(&key[j]));
+        const uint32_t d = valid ? digit_of(k, shift, width) : 0u;
+        uint32_t peers = __ballot_sync(0xFFFFFFFFu, valid);
+#pragma unroll
+        for (int b = 0; b < DIGIT_BITS; ++b) {
+            const bool bit = (d >> b) & 1u;
+            const uint32_t m = __ballot_sync(0xFFFFFFFFu, bit);
+            peers &= bit ? m : ~m;
+        }
+        uint32_t before = 0;
+        if (valid) before = s_warp_hist[warp][d];
+        __syncwarp();
+        if (valid && (peers & lanemask_lt()) == 0) s_warp_hist[warp][d] = before + __popc(peers);
+        __syncwarp();
+        pos[j] = valid ? (d | ((before + __popc(peers & lanemask_lt())) << 8)) : 0xFFFFFFFFu;
+    }
+    __syncthreads();
+
+    // Per-digit: warp prefixes, tile count, publish, look-back.
+    for (uint32_t d = tid; d < RADIX; d += kSortThreads) {
+        uint32_t run = 0;
+#pragma unroll
+        for (int w = 0; w < kSortWarps; ++w) {
+            uint32_t c = s_warp_hist[w][d];
+            s_warp_hist[w][d] = run;
+            run += c;
+        }
+        const uint32_t count = run;
+        uint32_t* my = status + (size_t)tile * RADIX + d;
+        uint32_t prefix = 0;
+        if (tile == 0) {
+            st_release_u32(my, kFlagPrefix | count);
+        } else {
+            st_release_u32(my, kFlagAggregate | count);
+            int64_t t = (int64_t)tile - 1;
+            while (t >= 0) {
+                uint32_t w = wait_for_flag(status + (size_t)t * RADIX + d, wait_limit,
+                                           [] { VREN_RECORD_ERROR(VREN_ERR_TIMEOUT); });
+                prefix += w & kValueMask;
+                if (w & kFlagPrefix) break;
+                --t;
+            }
+            st_release_u32(my, kFlagPrefix | (prefix + count));
+        }
+        s_tile_excl[d] = count;  // replaced by the exclusive scan below
+        s_delta[d] = (int32_t)(ld_relaxed_u32(scratch + kOffsOffset + pass * kMaxRadix + d) + prefix);
+    }
+    __syncthreads();
+    // Exclusive scan of the tile's digit counts (RADIX <= 256 <= threads).
+    if (tid < 32) {
+        uint32_t carry = 0;
+        for (int base = 0; base < RADIX; base += 32) {
+            const uint32_t d = base + tid;
+            const uint32_t c = (d < (uint32_t)RADIX) ? s_tile_excl[d] : 0u;
+            uint32_t incl = c;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                if (tid >= (uint32_t)o) incl += y;
+            }
+            if (d < (uint32_t)RADIX) {
+                const uint32_t excl = carry + incl - c;
+                s_tile_excl[d] = excl;
+                s_delta[d] -= (int32_t)excl;
+            }
+            carry += __shfl_sync(0xFFFFFFFFu, incl, 31);
+        }
+    }
+    __syncthreads();
+
+    // Stage in digit order.
+#pragma unroll
+    for (int j = 0; j < ITEMS; ++j) {
+        if (pos[j] != 0xFFFFFFFFu) {
+            const uint32_t d = pos[j] & 0xFFu;
+            const uint32_t p = s_tile_excl[d] + s_warp_hist[warp][d] + (pos[j] >> 8);
+            s_keys[p] = key[j];
+            if (MODE == kPairs) s_vals[p] = val[j];
+        }
+    }
+    __syncthreads();
+
+    // Write out: consecutive threads take consecutive staged elements.
+    const uint32_t tile_valid = (tile + 1) * TILE <= n ? TILE : n - tile * TILE;
+#pragma unroll
+    for (int j = 0; j < ITEMS; ++j) {
+        const uint32_t p = j * kSortThreads + tid;
+        if (p < tile_valid) {
+            const Elem e = s_keys[p];
+            uint32_t k;
+            if (MODE == kUvec2) k = (reinterpret_cast<const uint2*>(&e))->x;
+            else k = *(reinterpret_cast<const uint32_t*>(&e));
+            const uint32_t d = digit_of(k, shift, width);
+            const uint32_t dst = (uint32_t)((int32_t)p + s_delta[d]);
+            if (dst >= n) continue;  // only reachable after a timed-out look-back (error recorded)
+            if (MODE == kUvec2) {
+                reinterpret_cast<uint2*>(out_keys)[dst] = *(reinterpret_cast<const uint2*>(&e));
+            } else {
+                out_keys[dst] = k;
+                if (MODE == kPairs) out_vals[dst] = s_vals[p];
+            }
+        }
+    }
+    (void)HAS_VALS;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Bucket end offsets from the sorted output: end[b] = number of elements with bucket <= b.
+// Thread i (i in [-1, n)) writes end[b] = i + 1 for every b in [bucket(i), bucket(i+1)).
+// ------------------------------------------------------------------------------------------------
+__global__ void bucket_end_offsets_kernel(const uint2* __restrict__ sorted, uint32_t n, uint32_t key_mask,
+                                          uint32_t* __restrict__ ends)
+{
+    const uint32_t nb = key_mask + 1u;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x - 1; i < (int64_t)n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t lo = (i < 0) ? 0u : (sorted[i].x & key_mask);
+        const uint32_t hi = (i + 1 < (int64_t)n) ? (sorted[i + 1].x & key_mask) : nb;
+        const uint32_t v = (uint32_t)(i + 1);
+        for (uint32_t b = (i < 0 ? 0u : lo); b < hi; ++b) ends[b] = v;
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// Host side
+// ------------------------------------------------------------------------------------------------
+template <int DB> constexpr int items_for() { return DB >= 8 ? 15 : 16; }
+
+static uint32_t tiles_for(uint32_t n, uint32_t digit_bits)
+{
+    const uint32_t tile = kSortThreads * (digit_bits >= 8 ? 15u : 16u);
+    return (n + tile - 1) / tile;
+}
+
+static uint32_t radix_of(uint32_t digit_bits) { return 1u << digit_bits; }
+
+static size_t scratch1_bytes(uint32_t n, uint32_t digit_bits)
+{
+    const uint64_t tiles = tiles_for(n, digit_bits);
+    return (size_t)(kStatusOffset + 2ull * (tiles ? tiles : 1) * radix_of(digit_bits)) * sizeof(uint32_t);
+}
+
+static bool supported_bits(uint32_t db) { return db == 4 || db == 5 || db == 6 || db == 8; }
+
+template <int DB, int MODE>
+static int run_passes(cudaStream_t st, const uint32_t* src_k, const uint32_t* src_v, uint32_t* dst_k, uint32_t* dst_v,
+                      uint32_t* tmp_k, uint32_t* tmp_v, uint32_t n, const PassInfo& passes, uint32_t* scratch)
+{
+    constexpr int ITEMS = items_for<DB>();
+    constexpr int RADIX = 1 << DB;
+    const uint32_t tiles = tiles_for(n, DB);
+
+    VREN_CUDA_TRY(cudaMemsetAsync(scratch, 0, kZeroWords * sizeof(uint32_t), st));
+    uint32_t hist_grid = (n / 4 + kSortThreads - 1) / kSortThreads;
+    if (hist_grid > (uint32_t)kNumSMsHint * 4) hist_grid = kNumSMsHint * 4;
+    if (hist_grid == 0) hist_grid = 1;
+    onesweep_hist_kernel<RADIX, MODE><<<hist_grid, kSortThreads, 0, st>>>(src_k, n, passes, scratch, tiles * RADIX);
+    VREN_LAUNCH_CHECK();
+
+    const uint32_t P = passes.count;
+    for (uint32_t p = 0; p < P; ++p) {
+        // dst of pass p: the final buffer when (P-1-p) is even, else the temporary.
+        const bool to_final = ((P - 1 - p) % 2) == 0;
+        uint32_t* ok = to_final ? dst_k : tmp_k;
+        uint32_t* ov = to_final ? dst_v : tmp_v;
+        onesweep_pass_kernel<DB, ITEMS, MODE><<<tiles, kSortThreads, 0, st>>>(
+            src_k, src_v, ok, ov, n, p, passes.shift[p], passes.width[p], tiles, scratch, g_wait_limit);
+        VREN_LAUNCH_CHECK();
+        src_k = ok;
+        src_v = ov;
+    }
+    return VREN_OK;
+}
+
+template <int MODE>
+static int radix_dispatch(cudaStream_t st, uint32_t db, const uint32_t* src_k, const uint32_t* src_v, uint32_t* dst_k,
+                          uint32_t* dst_v, uint32_t* tmp_k, uint32_t* tmp_v, uint32_t n, const PassInfo& passes,
+                          uint32_t* scratch)
+{
+    switch (db) {
+    case 4: return run_passes<4, MODE>(st, src_k, src_v, dst_k, dst_v, tmp_k, tmp_v, n, passes, scratch);
+    case 5: return run_passes<5, MODE>(st, src_k, src_v, dst_k, dst_v, tmp_k, tmp_v, n, passes, scratch);
+    case 6: return run_passes<6, MODE>(st, src_k, src_v, dst_k, dst_v, tmp_k, tmp_v, n, passes, scratch);
+    case 8: return run_passes<8, MODE>(st, src_k, src_v, dst_k, dst_v, tmp_k, tmp_v, n, passes, scratch);
+    default: return VREN_ERR_ARG;
+    }
+}
+
+static PassInfo make_passes(uint32_t key_bits, uint32_t digit_bits)
+{
+    PassInfo pi{};
+    pi.count = (key_bits + digit_bits - 1) / digit_bits;
+    // Spread the bits evenly: widths differ by at most one, none exceeds digit_bits.
+    uint32_t shift = 0;
+    for (uint32_t p = 0; p < pi.count; ++p) {
+        uint32_t remaining = key_bits - shift;
+        uint32_t left = pi.count - p;
+        uint32_t w = (remaining + left - 1) / left;
+        pi.shift[p] = shift;
+        pi.width[p] = w;
+        shift += w;
+    }
+    return pi;
+}
+
+}  // namespace vren_gb300
+
+using namespace vren_gb300;
+
+extern "C" size_t vren_radix_sort_scratch1_bytes(uint32_t n, uint32_t digit_bits)
+{
+    if (!supported_bits(digit_bits)) return 0;
+    return scratch1_bytes(n, digit_bits);
+}
+
+extern "C" int vren_radix_sort_u32_ex(vren_stream_t s, uint32_t* keys, uint32_t* values, uint32_t n, uint32_t digit_bits,
+                                      void* scratch1, uint32_t* scratch_keys, uint32_t* scratch_values)
+{
+    if (!supported_bits(digit_bits) || !scratch1 || (n > 0 && (!keys || !scratch_keys))) return VREN_ERR_ARG;
+    if (values && !scratch_values) return VREN_ERR_ARG;
+    if (n >= (1u << 30)) return VREN_ERR_ARG;
+    if (((uintptr_t)keys & 15u) || ((uintptr_t)scratch1 & 15u)) return VREN_ERR_ARG;
+    if (n <= 1) return VREN_OK;
+    cudaStream_t st = as_stream(s);
+    PassInfo passes = make_passes(32, digit_bits);
+    uint32_t* sc = static_cast<uint32_t*>(scratch1);
+    const uint32_t* src_k = keys;
+    const uint32_t* src_v = values;
+    if (passes.count % 2 == 1) {
+        // With an odd pass count the first pass would run in place: start from a copy.
+        VREN_CUDA_TRY(cudaMemcpyAsync(scratch_keys, keys, (size_t)n * 4, cudaMemcpyDeviceToDevice, st));
+        if (values) VREN_CUDA_TRY(cudaMemcpyAsync(scratch_values, values, (size_t)n * 4, cudaMemcpyDeviceToDevice, st));
+        src_k = scratch_keys;
+        src_v = scratch_values;
+    }
+    if (values)
+        return radix_dispatch<kPairs>(st, digit_bits, src_k, src_v, keys, values, scratch_keys, scratch_values, n, passes, sc);
+    return radix_dispatch<kKeys>(st, digit_bits, src_k, nullptr, keys, nullptr, scratch_keys, nullptr, n, passes, sc);
+}
+
+extern "C" int vren_radix_sort_u32(vren_stream_t s, uint32_t* keys, uint32_t n, void* scratch1, uint32_t* scratch2)
+{
+    // radix_sort.cpp:212-215: "Length must be higher than 1024 and a power of 2"
+    if (!(n >= 1024 && (n & (n - 1)) == 0)) return VREN_ERR_ARG;
+    return vren_radix_sort_u32_ex(s, keys, nullptr, n, 8, scratch1, scratch2, nullptr);
+}
+
+static uint32_t bucket_digit_bits(uint32_t key_bits)
+{
+    const uint32_t passes = (key_bits + 7) / 8;
+    const uint32_t w = (key_bits + passes - 1) / passes;
+    return w <= 4 ? 4 : w == 5 ? 5 : w == 6 ? 6 : 8;
+}
+
+extern "C" size_t vren_bucket_sort_output_bytes(uint32_t n, uint32_t key_bits)
+{
+    if (key_bits == 0 || key_bits > 16) return 0;
+    const size_t pairs = ((size_t)n * 8 + 255) / 256 * 256;
+    return pairs + ((size_t)1 << key_bits) * sizeof(uint32_t);
+}
+
+extern "C" size_t vren_bucket_sort_scratch_bytes(uint32_t n, uint32_t key_bits)
+{
+    if (key_bits == 0 || key_bits > 16) return 0;
+    const size_t status = scratch1_bytes(n, bucket_digit_bits(key_bits));
+    const size_t tmp = ((size_t)n * 8 + 255) / 256 * 256;  // ping-pong elements for a two-pass sort
+    return ((status + 255) / 256 * 256) + tmp;
+}
+
+extern "C" int vren_bucket_sort_u32x2(vren_stream_t s, const uint32_t* in, uint32_t n, void* out, uint32_t key_bits,
+                                      void* scratch)
+{
+    if (key_bits == 0 || key_bits > 16 || !out || !scratch || (n > 0 && !in)) return VREN_ERR_ARG;
+    if (n >= (1u << 30)) return VREN_ERR_ARG;
+    if (((uintptr_t)in & 15u) || ((uintptr_t)out & 255u) || ((uintptr_t)scratch & 255u)) return VREN_ERR_ARG;
+    cudaStream_t st = as_stream(s);
+    uint32_t* out_pairs = static_cast<uint32_t*>(out);
+    uint32_t* ends = reinterpret_cast<uint32_t*>(static_cast<char*>(out) + ((size_t)n * 8 + 255) / 256 * 256);
+    const uint32_t db = bucket_digit_bits(key_bits);
+    uint32_t* sc = static_cast<uint32_t*>(scratch);
+    uint32_t* tmp = reinterpret_cast<uint32_t*>(static_cast<char*>(scratch) + (scratch1_bytes(n, db) + 255) / 256 * 256);
+    if (n > 0) {
+        PassInfo passes = make_passes(key_bits, db);
+        int rc = radix_dispatch<kUvec2>(st, db, in, nullptr, out_pairs, nullptr, tmp, nullptr, n, passes, sc);
+        if (rc != VREN_OK) return rc;
+    }
+    const uint32_t key_mask = (1u << key_bits) - 1u;
+    uint32_t grid = (n + 1 + 255) / 256;
+    if (grid > 4096) grid = 4096;
+    bucket_end_offsets_kernel<<<grid, 256, 0, st>>>(reinterpret_cast<const uint2*>(out_pairs), n, key_mask, ends);
+    VREN_LAUNCH_CHECK();
+    return VREN_OK;
+}
+
+namespace vren_gb300 {
+size_t sort_uvec2_scratch_bytes(uint32_t n, uint32_t key_bits, uint32_t digit_bits)
+{
+    (void)key_bits;
+    return supported_bits(digit_bits) ? scratch1_bytes(n, digit_bits) : 0;
+}
+
+int sort_uvec2(cudaStream_t st, const uint32_t* in, uint32_t* out, uint32_t* tmp, uint32_t n, uint32_t key_bits,
+               uint32_t digit_bits, void* scratch)
+{
+    if (n == 0) return VREN_OK;
+    if (!supported_bits(digit_bits) || key_bits == 0 || key_bits > 32) return VREN_ERR_ARG;
+    PassInfo passes = make_passes(key_bits, digit_bits);
+    if (passes.count > (uint32_t)kMaxPasses) return VREN_ERR_ARG;
+    return radix_dispatch<kUvec2>(st, digit_bits, in, nullptr, out, nullptr, tmp, nullptr, n, passes,
+                                  static_cast<uint32_t*>(scratch));
+}
+}  // namespace vren_gb300

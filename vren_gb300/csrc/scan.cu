@@ -1,0 +1,308 @@
+// Exclusive scan (vren::blelloch_scan, vren/vren/primitives/blelloch_scan.cpp:191-216) and the
+// reference's public down-sweep (blelloch_scan.cpp:107-189, blelloch_scan_downsweep.comp:33-125).
+//
+// The reference runs an up-sweep (reduce) and then log2(n)-10 global down-sweep dispatches plus
+// one shared-memory dispatch, all with strided access.  Here the scan is one kernel: each CTA
+// loads a 4096-element tile with uint4 loads, reduces it, publishes the aggregate, resolves its
+// exclusive prefix by decoupled look-back over the preceding tiles of its segment, and writes
+// the exclusive sums with uint4 stores — 8 bytes of HBM traffic per element.
+//
+// Scratch layout (uint32 words): [0] start ticket, [1] done ticket, [2] epoch, [3] unused,
+// then one 64-bit status word per tile: [epoch:30 | flag:2 | value:32].  Status words from an
+// earlier call carry an older epoch and read as "not published", so the scratch needs no
+// clearing between calls; the last CTA to finish resets the tickets and advances the epoch.
+// The scratch must be zero-filled before its first use (and again after VREN_ERR_TIMEOUT).
+#include "common.cuh"
+#include "internal.h"
+
+namespace vren_gb300 {
+
+VREN_DEFINE_ERROR_WORD(scan)
+
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 16;
+constexpr uint32_t kScanTile = kScanThreads * kScanItems;  // 4096
+constexpr uint32_t kScanHeaderWords = 4;
+
+__device__ __forceinline__ uint64_t ld_acquire_u64(const uint64_t* p)
+{
+    uint64_t v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_u64(uint64_t* p, uint64_t v)
+{
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// status word helpers
+__device__ __forceinline__ uint64_t make_status(uint32_t epoch, uint32_t flag, uint32_t value)
+{
+    return ((uint64_t)((epoch << 2) | flag) << 32) | value;
+}
+
+// `in` may equal `data` (in place).  When n_dev is given the element count is min(*n_dev, n)
+// (a single segment whose length is only known on the device); tiles past it do nothing.
+// When total_out is given the segment-0 total is written there.
+__global__ void __launch_bounds__(kScanThreads) exclusive_scan_kernel(
+    const uint32_t* in, uint32_t* data, uint32_t n, uint32_t tiles_per_seg, uint32_t total_tiles,
+    uint32_t* __restrict__ scratch, uint32_t wait_limit, const uint32_t* __restrict__ n_dev,
+    uint32_t* __restrict__ total_out)
+{
+    __shared__ uint32_t s_tile;
+    __shared__ uint32_t s_epoch;
+    __shared__ uint32_t s_warp_sum[kScanThreads / 32];
+    __shared__ uint32_t s_prefix;
+
+    uint64_t* status = reinterpret_cast<uint64_t*>(scratch + kScanHeaderWords);
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+
+    if (tid == 0) {
+        s_tile = atomicAdd(scratch + 0, 1u);
+        s_epoch = ld_relaxed_u32(scratch + 2) & 0x3FFFFFFFu;
+    }
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint32_t epoch = s_epoch;
+    const uint32_t seg = tile / tiles_per_seg;
+    const uint32_t tile_in_seg = tile - seg * tiles_per_seg;
+    const size_t seg_off = (size_t)seg * n;
+    if (n_dev) {
+        const uint32_t m = *n_dev;
+        n = m < n ? m : n;
+    }
+    const uint32_t tiles_eff = (n + kScanTile - 1) / kScanTile;
+    if (tile_in_seg >= tiles_eff) {
+        if (total_out && tiles_eff == 0 && tile == 0 && tid == 0) *total_out = 0u;
+        goto done;
+    }
+    {
+    const uint32_t* seg_in = in + seg_off;
+    uint32_t* seg_data = data + seg_off;
+    const uint32_t base = tile_in_seg * kScanTile + tid * kScanItems;
+
+    // Load 16 consecutive elements.
+    uint32_t v[kScanItems];
+    const bool full = (tile_in_seg + 1) * kScanTile <= n;
+    const bool aligned = ((reinterpret_cast<uintptr_t>(seg_data) & 15u) == 0) &&
+                         ((reinterpret_cast<uintptr_t>(seg_in) & 15u) == 0);
+    if (full && aligned) {
+        const uint4* p = reinterpret_cast<const uint4*>(seg_in + base);
+#pragma unroll
+        for (int k = 0; k < kScanItems / 4; ++k) {
+            uint4 q = p[k];
+            v[4 * k + 0] = q.x; v[4 * k + 1] = q.y; v[4 * k + 2] = q.z; v[4 * k + 3] = q.w;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) v[k] = (base + k < n) ? seg_in[base + k] : 0u;
+    }
+
+    // Thread-local exclusive scan.
+    uint32_t thread_sum = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        uint32_t x = v[k];
+        v[k] = thread_sum;
+        thread_sum += x;
+    }
+    // Warp inclusive scan of thread sums.
+    uint32_t incl = thread_sum;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+        if (lane >= (uint32_t)d) incl += y;
+    }
+    if (lane == 31) s_warp_sum[warp] = incl;
+    __syncthreads();
+    uint32_t warp_prefix = 0, tile_sum = 0;
+#pragma unroll
+    for (int w = 0; w < kScanThreads / 32; ++w) {
+        uint32_t ws = s_warp_sum[w];
+        if (w < (int)warp) warp_prefix += ws;
+        tile_sum += ws;
+    }
+
+    // Decoupled look-back.
+    if (warp == 0) {
+        uint64_t* my_status = status + tile;
+        uint32_t prefix = 0;
+        if (tile_in_seg == 0) {
+            if (lane == 0) st_release_u64(my_status, make_status(epoch, 2u, tile_sum));
+        } else {
+            if (lane == 0) st_release_u64(my_status, make_status(epoch, 1u, tile_sum));
+            const uint32_t seg_first = tile - tile_in_seg;
+            int64_t pos = (int64_t)tile - 1;
+            bool timed_out = false;
+            while (true) {
+                const int64_t idx = pos - lane;
+                uint32_t flag = 2u, val = 0u;  // lanes before the segment start act as a zero prefix
+                if (idx >= (int64_t)seg_first) {
+                    uint32_t ns = 32;
+                    for (uint32_t round = 0;; ++round) {
+                        uint64_t w = ld_acquire_u64(status + idx);
+                        uint32_t hi = (uint32_t)(w >> 32);
+                        if ((hi >> 2) == epoch && (hi & 3u) != 0) {
+                            flag = hi & 3u;
+                            val = (uint32_t)w;
+                            break;
+                        }
+                        if (round >= wait_limit) {
+                            timed_out = true;
+                            break;
+                        }
+                        __nanosleep(ns);
+                        if (ns < 1024) ns <<= 1;
+                    }
+                }
+                const uint32_t prefix_mask = __ballot_sync(0xFFFFFFFFu, flag == 2u);
+                // Sum lanes up to and including the nearest inclusive prefix.
+                const uint32_t stop = prefix_mask ? (uint32_t)(__ffs(prefix_mask) - 1) : 31u;
+                uint32_t contrib = (lane <= stop) ? val : 0u;
+#pragma unroll
+                for (int d = 16; d > 0; d >>= 1) contrib += __shfl_xor_sync(0xFFFFFFFFu, contrib, d);
+                prefix += contrib;
+                if (prefix_mask) break;
+                pos -= 32;
+            }
+            if (__any_sync(0xFFFFFFFFu, timed_out) && lane == 0) VREN_RECORD_ERROR(VREN_ERR_TIMEOUT);
+            if (lane == 0) st_release_u64(my_status, make_status(epoch, 2u, prefix + tile_sum));
+        }
+        if (lane == 0) {
+            s_prefix = prefix;
+            if (total_out && seg == 0 && tile_in_seg == tiles_eff - 1) *total_out = prefix + tile_sum;
+        }
+    }
+    __syncthreads();
+    const uint32_t offset = s_prefix + warp_prefix + (incl - thread_sum);
+
+    if (full && aligned) {
+        uint4* p = reinterpret_cast<uint4*>(seg_data + base);
+#pragma unroll
+        for (int k = 0; k < kScanItems / 4; ++k)
+            p[k] = make_uint4(v[4 * k] + offset, v[4 * k + 1] + offset, v[4 * k + 2] + offset, v[4 * k + 3] + offset);
+    } else {
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k)
+            if (base + k < n) seg_data[base + k] = v[k] + offset;
+    }
+    }
+
+done:
+    // Last CTA resets the tickets and advances the epoch for the next call.
+    if (tid == 0) {
+        __threadfence();
+        uint32_t done = atomicAdd(scratch + 1, 1u);
+        if (done == total_tiles - 1) {
+            scratch[0] = 0u;
+            scratch[1] = 0u;
+            scratch[2] = (epoch + 1u) & 0x3FFFFFFFu;
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// Down-sweep on an up-sweep tree (the reference's global levels blelloch_scan_downsweep.comp:33-53
+// and its shared-memory pass :56-125).  Levels d >= 12 only touch positions that are the last
+// element of a 4096-element chunk, and they form a down-sweep over the array of chunk roots.
+// So the host recurses: the chunk roots (stride 4096) are down-swept first, which leaves each
+// chunk root holding the value arriving from above; then one CTA per chunk runs the 12 in-chunk
+// levels in shared memory.  The top-most array sets its root to zero unless the root is kept.
+// ------------------------------------------------------------------------------------------------
+constexpr int kDownThreads = 1024;
+constexpr uint32_t kDownChunkLog2 = 12;
+constexpr uint32_t kDownChunk = 1u << kDownChunkLog2;
+
+// Elements of this level: e_j = seg[(j+1)*stride - 1], chunks of C = 2^chunk_log2 elements.
+__global__ void __launch_bounds__(kDownThreads) downsweep_chunk_kernel(
+    uint32_t* __restrict__ data, uint32_t seg_len, uint64_t stride, uint32_t chunk_log2, int top, int keep_root)
+{
+    __shared__ uint32_t s[kDownChunk];
+    const uint32_t C = 1u << chunk_log2;
+    uint32_t* seg = data + (size_t)blockIdx.y * seg_len;
+    const uint64_t chunk_base = (uint64_t)blockIdx.x * C;
+    const uint32_t tid = threadIdx.x;
+
+    for (uint32_t i = tid; i < C; i += kDownThreads) s[i] = seg[(size_t)((chunk_base + i + 1) * stride - 1)];
+    __syncthreads();
+    if (top && tid == 0 && !keep_root) s[C - 1] = 0u;
+    __syncthreads();
+    for (int d = (int)chunk_log2 - 1; d >= 0; --d) {
+        const uint32_t half = 1u << d;
+        const uint32_t pairs = C >> (d + 1);
+        for (uint32_t k = tid; k < pairs; k += kDownThreads) {
+            const uint32_t a = k * (half << 1) + half - 1;
+            const uint32_t b = a + half;
+            const uint32_t t = s[b];
+            s[b] = s[a] + t;
+            s[a] = t;
+        }
+        __syncthreads();
+    }
+    for (uint32_t i = tid; i < C; i += kDownThreads) seg[(size_t)((chunk_base + i + 1) * stride - 1)] = s[i];
+}
+
+static int downsweep_level(cudaStream_t st, uint32_t* data, uint32_t seg_len, uint32_t blocks, uint64_t stride,
+                           uint32_t log2m, int keep_root)
+{
+    if (log2m <= kDownChunkLog2) {
+        downsweep_chunk_kernel<<<dim3(1, blocks), kDownThreads, 0, st>>>(data, seg_len, stride, log2m, 1, keep_root);
+        VREN_LAUNCH_CHECK();
+        return VREN_OK;
+    }
+    int rc = downsweep_level(st, data, seg_len, blocks, stride << kDownChunkLog2, log2m - kDownChunkLog2, keep_root);
+    if (rc != VREN_OK) return rc;
+    dim3 grid(1u << (log2m - kDownChunkLog2), blocks);
+    downsweep_chunk_kernel<<<grid, kDownThreads, 0, st>>>(data, seg_len, stride, kDownChunkLog2, 0, keep_root);
+    VREN_LAUNCH_CHECK();
+    return VREN_OK;
+}
+
+}  // namespace vren_gb300
+
+using namespace vren_gb300;
+
+extern "C" size_t vren_exclusive_scan_scratch_bytes(uint32_t n, uint32_t blocks)
+{
+    uint64_t tiles = (uint64_t)((n + kScanTile - 1) / kScanTile) * (blocks ? blocks : 1);
+    return (size_t)(kScanHeaderWords * sizeof(uint32_t) + tiles * sizeof(uint64_t));
+}
+
+extern "C" int vren_exclusive_scan_u32(vren_stream_t s, uint32_t* data, uint32_t n, uint32_t blocks, void* scratch)
+{
+    if (blocks == 0 || !scratch || (n > 0 && !data)) return VREN_ERR_ARG;
+    if (n == 0) return VREN_OK;
+    if (n > (1u << 31)) return VREN_ERR_ARG;
+    const uint32_t tiles_per_seg = (n + kScanTile - 1) / kScanTile;
+    const uint64_t total = (uint64_t)tiles_per_seg * blocks;
+    if (total > 0x7FFFFFFFull) return VREN_ERR_ARG;
+    exclusive_scan_kernel<<<(uint32_t)total, kScanThreads, 0, as_stream(s)>>>(
+        data, data, n, tiles_per_seg, (uint32_t)total, static_cast<uint32_t*>(scratch), g_wait_limit, nullptr, nullptr);
+    VREN_LAUNCH_CHECK();
+    return VREN_OK;
+}
+
+namespace vren_gb300 {
+size_t scan_scratch_bytes(uint32_t n_cap) { return vren_exclusive_scan_scratch_bytes(n_cap, 1); }
+
+int scan_exclusive_u32(cudaStream_t st, const uint32_t* in, uint32_t* out, uint32_t n_cap, const uint32_t* n_dev,
+                       uint32_t* total_out, void* scratch)
+{
+    const uint32_t tiles = (n_cap + kScanTile - 1) / kScanTile;
+    const uint32_t grid = tiles ? tiles : 1;
+    exclusive_scan_kernel<<<grid, kScanThreads, 0, st>>>(in, out, tiles ? n_cap : 0, grid, grid,
+                                                         static_cast<uint32_t*>(scratch), g_wait_limit, n_dev, total_out);
+    VREN_LAUNCH_CHECK();
+    return VREN_OK;
+}
+}  // namespace vren_gb300
+
+extern "C" int vren_scan_downsweep_u32(vren_stream_t s, uint32_t* data, uint32_t n, uint32_t blocks, int clear_last)
+{
+    if (blocks == 0 || blocks > 65535 || !data || n == 0 || (n & (n - 1))) return VREN_ERR_ARG;
+    uint32_t log2n = 0;
+    while ((1u << log2n) < n) ++log2n;
+    // n < 1024 is a single reference work-group: its zero padding always reaches the root.
+    const int keep_root = (n >= 1024 && !clear_last) ? 1 : 0;
+    return downsweep_level(as_stream(s), data, n, blocks, 1, log2n, keep_root);
+}
