@@ -176,6 +176,153 @@ uint32_t vren_calc_bvh_root_index(uint32_t leaf_count);         /* build_bvh.cpp
 uint32_t vren_calc_bvh_level_count(uint32_t leaf_count);        /* build_bvh.cpp:189-193 */
 int vren_build_bvh(vren_stream_t s, vren_bvh_node* bvh, uint32_t padded_leaf_count);
 
+
+/* ------------------------------------------------------------------------------------------------
+ * Clustered shading — vren::clustered_shading::{construct_point_light_bvh, find_unique_cluster_list,
+ * assign_lights, shade} (vren/vren/pipeline/clustered_shading.hpp:13-141) and
+ * vren::cluster_and_shade (clustered_shading.hpp:147-182, clustered_shading.cpp:817-1172).
+ *
+ * Data layouts (device memory, as in the reference):
+ *   light positions  vec4[L], world space, w ignored        (light.hpp:190, light.cpp:260)
+ *   point lights     {vec3 color; float intensity}[L]       (gpu_repr.hpp:146-149); intensity is
+ *                    the light radius
+ *   view positions   vec4[L]: view * vec4(p.xyz, 1)          (point_light_position_to_view_space.comp:30)
+ *   light index      uvec2[L]: (morton code, light index), sorted by code, ties by light index
+ *   BVH              vren_bvh_node[vren_calc_bvh_buffer_length(L)]
+ *   depth            f32[W*H] NDC depth in [0, 1], row-major   (the reference's D32 depth buffer)
+ *   normals          f32x3[W*H]                              (the reference's G-buffer normals)
+ *   cluster keys     u32[U]: i | j << 8 | k << 16 | normal << 26 (find_unique_clusters.comp:72-76)
+ *   cluster refs     u32[W*H]: index of the pixel's key in the key list
+ *   counts/offsets   u32[U]; indices u32[sum(counts)]        (assign_lights.comp:57-70)
+ *
+ * Canonical semantics where the reference is nondeterministic or implementation-defined (the full
+ * list is in the design doc): key lists are ordered by tile (row-major) then ascending key; texels are
+ * fetched at integer coordinates (x mod W, y mod H) like the reference's REPEAT sampler, or
+ * skipped; depth slices come from a boundary table built on the host; light ties sort by index;
+ * invalid BVH nodes are never traversed or assigned; float arithmetic follows a fixed order of
+ * correctly rounded single-precision operations.
+ * ------------------------------------------------------------------------------------------------ */
+#define VREN_CS_SLICES 1024
+enum { VREN_CS_SLICING_REF = 0, VREN_CS_SLICING_FIXED32 = 1 };
+enum { VREN_CS_OFFSCREEN_WRAP = 0, VREN_CS_OFFSCREEN_SKIP = 1 };
+
+/* vren::camera (vren/vren/camera.hpp:14-33) */
+typedef struct vren_camera {
+    float position[3];
+    float yaw, pitch;
+    float fov_y, aspect_ratio, near_plane, far_plane;
+} vren_camera;
+
+/* Camera-derived matrices, column-major m[c*4 + r] like glm. */
+typedef struct vren_cs_view {
+    float view[16];      /* world -> view (camera.cpp:66-72) */
+    float inv_proj[16];  /* inverse of the projection (camera.cpp:74-84) */
+    float inv_view[16];  /* view -> world */
+    float eye[3];        /* camera position in world space */
+    float near_plane, far_plane, half_fov_y;
+    uint32_t slicing;    /* VREN_CS_SLICING_* */
+    uint32_t reserved;
+} vren_cs_view;
+
+/* Per-frame parameter block that the kernels read from device memory (8448 bytes).
+ * slice_near[k] / slice_far[k] are the view-space depth bounds of slice k:
+ *   REF:     near * a^k and near * a^(k+1), a = 1 + 2 tan(fov_y/2) / tiles_y (find_unique_clusters.comp:65,
+ *            clustered_shading.glsl:220-222), a^k by repeated double multiplication, rounded to float;
+ *   FIXED32: near * (far/near)^(k/32) for k <= 32, +inf beyond (max_slice = 31).
+ * A pixel at view depth z falls in the largest slice k <= max_slice with slice_near[k] <= z (0 if none). */
+typedef struct vren_cs_frame {
+    vren_cs_view view;
+    uint32_t width, height, tiles_x, tiles_y;
+    uint32_t max_slice;
+    uint32_t offscreen;  /* VREN_CS_OFFSCREEN_* */
+    uint32_t reserved[2];
+    float slice_near[VREN_CS_SLICES];
+    float slice_far[VREN_CS_SLICES];
+} vren_cs_frame;
+
+/* Host: matrices of a vren::camera (computed in double, rounded to float). */
+void vren_cs_view_from_camera(const vren_camera* camera, uint32_t slicing, vren_cs_view* out);
+/* Host: fills a frame block (slice tables included). */
+int vren_cs_frame_build(const vren_cs_view* view, uint32_t width, uint32_t height, int offscreen,
+                        vren_cs_frame* out);
+/* Stream-ordered copy of a host frame block into device memory (a kernel launch carrying the block
+ * by value, so it can be captured in a CUDA graph). */
+int vren_cs_frame_upload(vren_stream_t s, const vren_cs_frame* host_frame, vren_cs_frame* device_frame);
+
+/* construct_point_light_bvh (clustered_shading.cpp:60-346): view transform, min/max, 15-bit Morton
+ * codes (discretize_point_light_positions.comp:62-73; morton_bits = 30 selects 10 bits per axis),
+ * stable sort by code, leaves = AABB(view position +- intensity) (init_light_array_bvh.comp:117-139),
+ * BuildBVH.  `leaf_spheres` (optional, vec4[padded leaf count]) receives, per leaf, the light's view
+ * position and the radius the traversal tests, (max.x - min.x) / 2 (assign_lights.comp:214); invalid
+ * leaves get radius -1.  light_count = 0 writes nothing. */
+size_t vren_cs_light_bvh_scratch_bytes(uint32_t light_count, uint32_t morton_bits);
+int vren_cs_construct_light_bvh(vren_stream_t s, const float* light_positions, const float* point_lights,
+                                uint32_t light_count, const vren_cs_frame* frame, uint32_t morton_bits,
+                                float* view_positions, vren_bvh_node* bvh, uint32_t* light_index,
+                                float* leaf_spheres, void* scratch);
+
+/* find_unique_cluster_list (clustered_shading.cpp:363-448, find_unique_clusters.comp:46-120).
+ * key_count receives the number of keys written (the reference's dispatch_params.x); a list longer
+ * than key_capacity is truncated and VREN_ERR_CAPACITY recorded.  tiles_x*tiles_y*1024 keys always fit. */
+size_t vren_cs_unique_clusters_scratch_bytes(uint32_t width, uint32_t height);
+int vren_cs_find_unique_clusters(vren_stream_t s, const float* depth, const float* normals, uint32_t width,
+                                 uint32_t height, const vren_cs_frame* frame, uint32_t* cluster_keys,
+                                 uint32_t key_capacity, uint32_t* key_count, uint32_t* cluster_refs,
+                                 void* scratch);
+
+/* assign_lights (clustered_shading.cpp:473-690, assign_lights.comp:121-240): per cluster, the lights
+ * whose sphere overlaps the cluster box, in the reference's order (BVH leaf groups in ascending
+ * order, lanes of a group in descending order).  counts/offsets have key_capacity entries, the
+ * first *key_count of which are written; `total` (optional) receives the number of assignments;
+ * indices beyond index_capacity are dropped and VREN_ERR_CAPACITY recorded.  `leaf_spheres` is
+ * optional (from vren_cs_construct_light_bvh); without it the leaf data are read from the BVH,
+ * the light index and the view positions as the reference does. */
+size_t vren_cs_assign_lights_scratch_bytes(uint32_t key_capacity);
+int vren_cs_assign_lights(vren_stream_t s, const uint32_t* cluster_keys, const uint32_t* key_count,
+                          uint32_t key_capacity, const vren_cs_frame* frame, const vren_bvh_node* bvh,
+                          uint32_t light_count, const uint32_t* light_index, const float* view_positions,
+                          const float* leaf_spheres, uint32_t* counts, uint32_t* offsets, uint32_t* indices,
+                          uint32_t index_capacity, uint32_t* total, void* scratch);
+
+/* vren::cluster_and_shade: owns its buffers (an arena sized at creation) and runs the stages above
+ * for one frame.  With a non-default stream the sequence is captured once into a CUDA graph per
+ * frame shape and replayed. */
+typedef struct vren_cluster_and_shade vren_cluster_and_shade;
+
+typedef struct vren_cs_outputs {
+    const float* view_positions;
+    const vren_bvh_node* bvh;
+    const uint32_t* light_index;
+    const float* leaf_spheres;
+    const uint32_t* cluster_keys;
+    const uint32_t* key_count;
+    const uint32_t* cluster_refs;
+    const uint32_t* counts;
+    const uint32_t* offsets;
+    const uint32_t* indices;
+    const uint32_t* total;
+    const vren_cs_frame* frame;
+    uint32_t key_capacity;
+    uint32_t index_capacity;
+} vren_cs_outputs;
+
+typedef struct vren_cs_options {
+    uint32_t morton_bits;     /* 15 (reference) or 30 */
+    uint32_t use_graph;       /* capture/replay a CUDA graph on non-default streams */
+    uint32_t sort_digit_bits; /* 4, 6 or 8: digit width of the light sort */
+    uint32_t assign_warps;    /* warps per CTA of the traversal kernels (1..32) */
+} vren_cs_options;
+
+int vren_cs_create(vren_cluster_and_shade** out, uint32_t max_width, uint32_t max_height, uint32_t max_lights,
+                   uint32_t max_assignments);
+void vren_cs_destroy(vren_cluster_and_shade* cs);
+int vren_cs_set_options(vren_cluster_and_shade* cs, const vren_cs_options* options);
+/* Runs construct_point_light_bvh, find_unique_cluster_list and assign_lights for one frame. */
+int vren_cs_cluster(vren_cluster_and_shade* cs, vren_stream_t s, const vren_cs_view* view, uint32_t width,
+                    uint32_t height, int offscreen, const float* depth, const float* normals,
+                    const float* light_positions, const float* point_lights, uint32_t light_count);
+int vren_cs_get_outputs(const vren_cluster_and_shade* cs, vren_cs_outputs* out);
+
 #ifdef __cplusplus
 }
 #endif

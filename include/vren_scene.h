@@ -39,10 +39,11 @@ typedef struct vren_scene_camera {
     uint32_t width, height;
 } vren_scene_camera;
 
-/* Depth buffer from `num_planes` random planes: per pixel the nearest positive hit of the ray
- * through the pixel centre, view z clamped to [near, far] (a miss gives far), stored as NDC depth
- * (f32[W*H], row-major).  normals (f32x3[W*H]) receive the hit plane's unit normal (misses:
- * (0, 0, -1)).  Either output may be NULL. */
+/* Depth buffer from `num_planes` random oriented planar discs (centre in the frustum, view z
+ * log-uniform in [1, 0.9 far], normal facing the camera, radius 20-80 % of the frustum half-height
+ * at that depth): per pixel the nearest positive hit of the ray through the pixel centre, view z
+ * clamped to [near, far] (a miss gives far), stored as NDC depth (f32[W*H], row-major).  normals
+ * (f32x3[W*H]) receive the hit plane's unit normal (misses: (0, 0, -1)).  Either output may be NULL. */
 void vren_gen_depth_planes(uint64_t seed, const vren_scene_camera* cam, uint32_t num_planes,
                            float* depth, float* normals, int threads);
 

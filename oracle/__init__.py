@@ -141,3 +141,54 @@ def size_helpers(n: int) -> dict:
         "root": int(L.oracle_calc_bvh_root_index(n)),
         "levels": int(L.oracle_calc_bvh_level_count(n)),
     }
+
+
+# ---- clustered shading --------------------------------------------------------------------------
+def _view_ptr(view):
+    import ctypes
+    return ctypes.cast(ctypes.byref(view), ctypes.c_void_p).value
+
+
+def cs_slice_table(view, tiles_y: int):
+    near = np.empty(1024, np.float32)
+    far = np.empty(1024, np.float32)
+    lib().oracle_cs_slice_table(_view_ptr(view), tiles_y, _p(near), _p(far))
+    return near, far
+
+
+def cs_light_bvh(positions: np.ndarray, lights: np.ndarray, L: int, view, morton_bits: int = 15):
+    P = int(lib().oracle_calc_bvh_padded_leaf_count(L))
+    length = int(lib().oracle_calc_bvh_buffer_length(P))
+    vp = np.zeros(L * 4, np.float32)
+    bvh = np.zeros((length, 8), np.uint32)
+    li = np.zeros(L * 2, np.uint32)
+    if L:
+        lib().oracle_cs_light_bvh(_p(np.ascontiguousarray(positions, np.float32)),
+                                  _p(np.ascontiguousarray(lights, np.float32)), L, _view_ptr(view), morton_bits,
+                                  _p(vp), _p(bvh), _p(li))
+    return vp, bvh, li
+
+
+def cs_find_unique_clusters(depth, normals, W: int, H: int, view, policy: int = 0, threads: int = 0):
+    T = ((W + 31) // 32) * ((H + 31) // 32)
+    keys = np.zeros(T * 1024, np.uint32)
+    refs = np.zeros(W * H, np.uint32)
+    U = lib().oracle_cs_find_unique_clusters(_p(np.ascontiguousarray(depth, np.float32)),
+                                             _p(np.ascontiguousarray(normals, np.float32)), W, H, _view_ptr(view),
+                                             policy, _p(keys), len(keys), _p(refs), threads)
+    return keys[:U].copy(), refs
+
+
+def cs_assign_lights(keys, W: int, H: int, view, bvh, L: int, light_index, view_pos, threads: int = 0,
+                     index_cap: int | None = None):
+    U = len(keys)
+    counts = np.zeros(max(U, 1), np.uint32)
+    offsets = np.zeros(max(U, 1), np.uint32)
+    cap = index_cap if index_cap is not None else 1 << 26
+    indices = np.zeros(cap, np.uint32)
+    total = lib().oracle_cs_assign_lights(_p(np.ascontiguousarray(keys, np.uint32)), U, W, H, _view_ptr(view),
+                                          _p(np.ascontiguousarray(bvh, np.uint32)), L,
+                                          _p(np.ascontiguousarray(light_index, np.uint32)),
+                                          _p(np.ascontiguousarray(view_pos, np.float32)), _p(counts), _p(offsets),
+                                          _p(indices), cap, threads)
+    return counts[:U], offsets[:U], indices[: min(total, cap)].copy(), int(total)

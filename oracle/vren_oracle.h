@@ -83,6 +83,7 @@ typedef struct oracle_cs_view {
     float eye[3];
     float near_plane, far_plane, half_fov_y;
     uint32_t slicing;
+    uint32_t reserved;
 } oracle_cs_view;
 
 /* Slice tables: near[k], far[k] for k in [0, 1024). */

@@ -79,3 +79,44 @@ def test_argument_errors_need_no_gpu(native):
     assert native.vren_build_bvh(None, None, 33) == 1
     assert native.vren_scan_downsweep_u32(None, None, 3, 1, 1) == 1
     assert native.vren_bucket_sort_u32x2(None, None, 10, None, 17, None) == 1
+
+
+@pytest.mark.parametrize("W,H", [(640, 360), (1280, 720), (1920, 1080), (2560, 1440), (100, 37)])
+@pytest.mark.parametrize("slicing", ["ref", "fixed32"])
+def test_slice_tables_match_oracle(native, W, H, slicing):
+    import oracle
+    import vren_gb300.clustered_shading as cs
+
+    view = cs.view_from_camera(cs.scene_camera(W, H), slicing)
+    f = cs.frame_build(view, W, H)
+    near, far = oracle.cs_slice_table(view, (H + 31) // 32)
+    assert np.array_equal(np.array(f.slice_near, np.float32), near)
+    assert np.array_equal(np.array(f.slice_far, np.float32), far)
+    assert f.tiles_x == (W + 31) // 32 and f.tiles_y == (H + 31) // 32
+    assert f.max_slice == (31 if slicing == "fixed32" else 1023)
+    head = near[: f.max_slice + 1]
+    assert np.all(head[1:] >= head[:-1])  # non-decreasing (+inf once a^k overflows)
+
+
+def test_camera_matrices(native):
+    import vren_gb300.clustered_shading as cs
+
+    cam = cs.scene_camera(1920, 1080, near=0.1, far=1000.0)
+    v = cs.view_from_camera(cam)
+    view = np.array(v.view, np.float64).reshape(4, 4).T  # row-major
+    assert np.allclose(view, np.eye(4))
+    inv_proj = np.array(v.inv_proj, np.float64).reshape(4, 4).T
+    t = np.tan(np.float32(np.deg2rad(45.0)) / 2)
+    proj = np.zeros((4, 4))
+    proj[0, 0] = 1 / (t * 1920 / 1080)
+    proj[1, 1] = 1 / t
+    proj[2, 2] = 1000 / (1000 - 0.1)
+    proj[2, 3] = -(1000 * 0.1) / (1000 - 0.1)
+    proj[3, 2] = 1
+    assert np.allclose(inv_proj @ proj, np.eye(4), atol=1e-5)
+    # a moved camera: view * inv_view = I
+    cam2 = cs.scene_camera(640, 360, position=(1, 2, 3), yaw=0.4, pitch=0.1)
+    v2 = cs.view_from_camera(cam2)
+    a = np.array(v2.view, np.float64).reshape(4, 4).T
+    b = np.array(v2.inv_view, np.float64).reshape(4, 4).T
+    assert np.allclose(a @ b, np.eye(4), atol=1e-5)

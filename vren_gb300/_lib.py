@@ -96,3 +96,22 @@ def check(status: int, what: str = "") -> None:
 
 def device_error(clear: bool = True) -> int:
     return int(lib().vren_device_error(1 if clear else 0))
+
+# ---- clustered shading ----------------------------------------------------------------------------
+PROTOTYPES_CS: dict[str, tuple] = {
+    "vren_cs_view_from_camera": (None, [vp, u32, vp]),
+    "vren_cs_frame_build": (i32, [vp, u32, u32, i32, vp]),
+    "vren_cs_frame_upload": (i32, [vp, vp, vp]),
+    "vren_cs_light_bvh_scratch_bytes": (sz, [u32, u32]),
+    "vren_cs_construct_light_bvh": (i32, [vp, vp, vp, u32, vp, u32, vp, vp, vp, vp, vp]),
+    "vren_cs_unique_clusters_scratch_bytes": (sz, [u32, u32]),
+    "vren_cs_find_unique_clusters": (i32, [vp, vp, vp, u32, u32, vp, vp, u32, vp, vp, vp]),
+    "vren_cs_assign_lights_scratch_bytes": (sz, [u32]),
+    "vren_cs_assign_lights": (i32, [vp, vp, vp, u32, vp, vp, u32, vp, vp, vp, vp, vp, vp, u32, vp, vp]),
+    "vren_cs_create": (i32, [C.POINTER(vp), u32, u32, u32, u32]),
+    "vren_cs_destroy": (None, [vp]),
+    "vren_cs_set_options": (i32, [vp, vp]),
+    "vren_cs_cluster": (i32, [vp, vp, vp, u32, u32, i32, vp, vp, vp, vp, u32]),
+    "vren_cs_get_outputs": (i32, [vp, vp]),
+}
+PROTOTYPES.update(PROTOTYPES_CS)

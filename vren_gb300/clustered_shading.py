@@ -1,0 +1,214 @@
+"""Python mirror of vren::clustered_shading and vren::cluster_and_shade over the C ABI.
+
+Reference: vren/vren/pipeline/clustered_shading.hpp:13-182.  The stage classes keep the reference
+names; their buffers are CUDA tensors.  Frame parameters (camera matrices, slice tables) travel in a
+device-resident ``vren_cs_frame`` block built on the host.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from ._lib import check, lib
+from .primitives import _ptr, _stream, alloc_scratch, calc_bvh_buffer_length, calc_bvh_padded_leaf_count
+
+SLICES = 1024
+SLICING = {"ref": 0, "fixed32": 1}
+OFFSCREEN = {"wrap": 0, "skip": 1}
+
+
+class Camera(C.Structure):
+    """vren::camera (vren/vren/camera.hpp:14-33)."""
+    _fields_ = [("position", C.c_float * 3), ("yaw", C.c_float), ("pitch", C.c_float), ("fov_y", C.c_float),
+                ("aspect_ratio", C.c_float), ("near_plane", C.c_float), ("far_plane", C.c_float)]
+
+
+class View(C.Structure):
+    _fields_ = [("view", C.c_float * 16), ("inv_proj", C.c_float * 16), ("inv_view", C.c_float * 16),
+                ("eye", C.c_float * 3), ("near_plane", C.c_float), ("far_plane", C.c_float),
+                ("half_fov_y", C.c_float), ("slicing", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class Frame(C.Structure):
+    _fields_ = [("view", View), ("width", C.c_uint32), ("height", C.c_uint32), ("tiles_x", C.c_uint32),
+                ("tiles_y", C.c_uint32), ("max_slice", C.c_uint32), ("offscreen", C.c_uint32),
+                ("reserved", C.c_uint32 * 2), ("slice_near", C.c_float * SLICES), ("slice_far", C.c_float * SLICES)]
+
+
+class Options(C.Structure):
+    _fields_ = [("morton_bits", C.c_uint32), ("use_graph", C.c_uint32), ("sort_digit_bits", C.c_uint32),
+                ("assign_warps", C.c_uint32)]
+
+
+class Outputs(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in ("view_positions", "bvh", "light_index", "leaf_spheres", "cluster_keys",
+                                           "key_count", "cluster_refs", "counts", "offsets", "indices", "total",
+                                           "frame")] + [("key_capacity", C.c_uint32), ("index_capacity", C.c_uint32)]
+
+
+def scene_camera(width: int, height: int, fov_y_deg: float = 45.0, near: float = 0.1, far: float = 1000.0,
+                 position=(0.0, 0.0, 0.0), yaw: float = 0.0, pitch: float = 0.0) -> Camera:
+    cam = Camera()
+    cam.position[:] = list(position)
+    cam.yaw, cam.pitch = yaw, pitch
+    cam.fov_y = np.float32(np.deg2rad(fov_y_deg))
+    cam.aspect_ratio = width / height
+    cam.near_plane, cam.far_plane = near, far
+    return cam
+
+
+def view_from_camera(cam: Camera, slicing: str = "ref") -> View:
+    v = View()
+    lib().vren_cs_view_from_camera(C.byref(cam), SLICING[slicing], C.byref(v))
+    return v
+
+
+def frame_build(view: View, width: int, height: int, offscreen: str = "wrap") -> Frame:
+    f = Frame()
+    check(lib().vren_cs_frame_build(C.byref(view), width, height, OFFSCREEN[offscreen], C.byref(f)), "frame_build")
+    return f
+
+
+def frame_to_device(frame: Frame, device=None, stream=None) -> torch.Tensor:
+    buf = torch.empty(C.sizeof(Frame) // 4, dtype=torch.int32, device=device or "cuda")
+    check(lib().vren_cs_frame_upload(_stream(stream), C.byref(frame), _ptr(buf)), "frame_upload")
+    return buf
+
+
+class construct_point_light_bvh:
+    """vren::clustered_shading::construct_point_light_bvh (clustered_shading.hpp:19-46)."""
+
+    def __init__(self, morton_bits: int = 15):
+        self.morton_bits = morton_bits
+        self._scratch = None
+
+    @staticmethod
+    def get_required_bvh_buffer_size(light_count: int) -> int:
+        return calc_bvh_buffer_length(light_count) * 32
+
+    def __call__(self, stream, positions: torch.Tensor, lights: torch.Tensor, light_count: int,
+                 frame_dev: torch.Tensor, view_positions: torch.Tensor, bvh: torch.Tensor,
+                 light_index: torch.Tensor, leaf_spheres: torch.Tensor | None = None):
+        need = int(lib().vren_cs_light_bvh_scratch_bytes(light_count, self.morton_bits))
+        if self._scratch is None or self._scratch.numel() * 4 < need:
+            self._scratch = alloc_scratch(need, positions.device)
+        check(lib().vren_cs_construct_light_bvh(
+            _stream(stream), _ptr(positions), _ptr(lights), light_count, _ptr(frame_dev), self.morton_bits,
+            _ptr(view_positions), _ptr(bvh), _ptr(light_index),
+            _ptr(leaf_spheres) if leaf_spheres is not None else None, _ptr(self._scratch)), "construct_point_light_bvh")
+
+
+class find_unique_cluster_list:
+    """vren::clustered_shading::find_unique_cluster_list (clustered_shading.hpp:52-74)."""
+
+    def __init__(self):
+        self._scratch = None
+
+    def __call__(self, stream, width: int, height: int, frame_dev: torch.Tensor, depth: torch.Tensor,
+                 normals: torch.Tensor, cluster_keys: torch.Tensor, key_count: torch.Tensor,
+                 cluster_refs: torch.Tensor):
+        need = int(lib().vren_cs_unique_clusters_scratch_bytes(width, height))
+        if self._scratch is None or self._scratch.numel() * 4 < need:
+            self._scratch = alloc_scratch(need, depth.device)
+        check(lib().vren_cs_find_unique_clusters(
+            _stream(stream), _ptr(depth), _ptr(normals), width, height, _ptr(frame_dev), _ptr(cluster_keys),
+            cluster_keys.numel(), _ptr(key_count), _ptr(cluster_refs), _ptr(self._scratch)), "find_unique_cluster_list")
+
+
+class assign_lights:
+    """vren::clustered_shading::assign_lights (clustered_shading.hpp:80-108)."""
+
+    def __init__(self):
+        self._scratch = None
+
+    def __call__(self, stream, cluster_keys: torch.Tensor, key_count: torch.Tensor, frame_dev: torch.Tensor,
+                 bvh: torch.Tensor, light_count: int, light_index: torch.Tensor, view_positions: torch.Tensor,
+                 counts: torch.Tensor, offsets: torch.Tensor, indices: torch.Tensor, total: torch.Tensor,
+                 leaf_spheres: torch.Tensor | None = None):
+        cap = cluster_keys.numel()
+        need = int(lib().vren_cs_assign_lights_scratch_bytes(cap))
+        if self._scratch is None or self._scratch.numel() * 4 < need:
+            self._scratch = alloc_scratch(need, cluster_keys.device)
+        check(lib().vren_cs_assign_lights(
+            _stream(stream), _ptr(cluster_keys), _ptr(key_count), cap, _ptr(frame_dev),
+            _ptr(bvh) if bvh is not None else None, light_count,
+            _ptr(light_index) if light_index is not None else None,
+            _ptr(view_positions) if view_positions is not None else None,
+            _ptr(leaf_spheres) if leaf_spheres is not None else None,
+            _ptr(counts), _ptr(offsets), _ptr(indices) if indices is not None else None,
+            indices.numel() if indices is not None else 0, _ptr(total), _ptr(self._scratch)), "assign_lights")
+
+
+class cluster_and_shade:
+    """vren::cluster_and_shade (clustered_shading.hpp:147-182): owns an arena sized at creation."""
+
+    def __init__(self, max_width: int, max_height: int, max_lights: int, max_assignments: int,
+                 morton_bits: int = 15, use_graph: bool = True, sort_digit_bits: int = 8, assign_warps: int = 8):
+        h = C.c_void_p()
+        check(lib().vren_cs_create(C.byref(h), max_width, max_height, max_lights, max_assignments), "cs_create")
+        self._h = h
+        self.set_options(morton_bits, use_graph, sort_digit_bits, assign_warps)
+
+    def set_options(self, morton_bits=15, use_graph=True, sort_digit_bits=8, assign_warps=8):
+        o = Options(morton_bits, 1 if use_graph else 0, sort_digit_bits, assign_warps)
+        check(lib().vren_cs_set_options(self._h, C.byref(o)), "cs_set_options")
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().vren_cs_destroy(h)
+            self._h = None
+
+    def cluster(self, stream, view: View, width: int, height: int, depth: torch.Tensor, normals: torch.Tensor,
+                positions: torch.Tensor | None, lights: torch.Tensor | None, light_count: int,
+                offscreen: str = "wrap"):
+        check(lib().vren_cs_cluster(self._h, _stream(stream), C.byref(view), width, height, OFFSCREEN[offscreen],
+                                    _ptr(depth), _ptr(normals), _ptr(positions) if positions is not None else None,
+                                    _ptr(lights) if lights is not None else None, light_count), "cs_cluster")
+
+    def outputs(self) -> Outputs:
+        o = Outputs()
+        check(lib().vren_cs_get_outputs(self._h, C.byref(o)), "cs_get_outputs")
+        return o
+
+
+_CUDART = None
+
+
+def _cudart():
+    global _CUDART
+    if _CUDART is None:
+        import ctypes.util
+        import glob
+        import os
+
+        cands = [ctypes.util.find_library("cudart"), "libcudart.so"]
+        cands += sorted(glob.glob("/usr/local/cuda/lib64/libcudart.so*"))
+        cands += sorted(glob.glob(os.path.join(os.path.dirname(torch.__file__), "lib", "libcudart*.so*")))
+        for c in cands:
+            if not c:
+                continue
+            try:
+                _CUDART = C.CDLL(c)
+                break
+            except OSError:
+                continue
+        if _CUDART is None:
+            raise RuntimeError("libcudart not found")
+        _CUDART.cudaMemcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
+        _CUDART.cudaMemcpy.restype = C.c_int
+    return _CUDART
+
+
+def read_device(ptr: int, count: int, dtype=np.uint32) -> np.ndarray:
+    """Copies `count` elements at a device address into a numpy array (synchronizes)."""
+    out = np.empty(count, dtype=dtype)
+    if count == 0:
+        return out
+    torch.cuda.synchronize()
+    res = _cudart().cudaMemcpy(out.ctypes.data, ptr, out.nbytes, 2)  # cudaMemcpyDeviceToHost
+    if res != 0:
+        raise RuntimeError(f"cudaMemcpy failed: {res}")
+    return out

@@ -102,8 +102,12 @@ static void unit_sphere(vren_pcg32* rng, double n[3])
 void vren_gen_depth_planes(uint64_t seed, const vren_scene_camera* cam, uint32_t num_planes, float* depth,
                            float* normals, int threads)
 {
+    /* Oriented planar discs: centre inside the frustum (view z log-uniform in [1, 0.9 far], x/y
+     * uniform in the cross-section), unit normal uniform on the hemisphere facing the camera,
+     * radius 20-80 % of the frustum's half-height at the centre's depth.  Unbounded planes would
+     * let the nearest one cover almost the whole view. */
     enum { kMaxPlanes = 1024 };
-    double pn[kMaxPlanes][3], pc[kMaxPlanes];
+    double pn[kMaxPlanes][3], pc[kMaxPlanes], ctr[kMaxPlanes][3], rad2[kMaxPlanes];
     if (num_planes > kMaxPlanes) num_planes = kMaxPlanes;
     const double W = cam->width, H = cam->height;
     const double aspect = W / H;
@@ -116,11 +120,14 @@ void vren_gen_depth_planes(uint64_t seed, const vren_scene_camera* cam, uint32_t
         double nn[3];
         unit_sphere(&rng, nn);
         if (nn[2] > 0.0) { nn[0] = -nn[0]; nn[1] = -nn[1]; nn[2] = -nn[2]; } /* face the camera */
-        /* a point inside the frustum: view z log-uniform in [1, far], x/y inside the cross-section */
-        double z0 = exp(log(1.0) + uniform01(&rng) * (log(f_) - log(1.0)));
+        double z0 = exp(uniform01(&rng) * log(0.9 * f_));
+        if (z0 < 1.0) z0 = 1.0;
         double x0 = (2.0 * uniform01(&rng) - 1.0) * z0 * t * aspect;
         double y0 = (2.0 * uniform01(&rng) - 1.0) * z0 * t;
+        double r = (0.2 + 0.6 * uniform01(&rng)) * z0 * t;
         pn[i][0] = nn[0]; pn[i][1] = nn[1]; pn[i][2] = nn[2];
+        ctr[i][0] = x0; ctr[i][1] = y0; ctr[i][2] = z0;
+        rad2[i] = r * r;
         pc[i] = nn[0] * x0 + nn[1] * y0 + nn[2] * z0;
     }
     const double m22 = f_ / (f_ - n_), m32 = -(f_ * n_) / (f_ - n_);
@@ -137,7 +144,11 @@ void vren_gen_depth_planes(uint64_t seed, const vren_scene_camera* cam, uint32_t
                 double den = pn[i][0] * d[0] + pn[i][1] * d[1] + pn[i][2] * d[2];
                 if (den == 0.0) continue;
                 double tt = pc[i] / den;
-                if (tt > 0.0 && tt < best) { best = tt; hit = (int)i; }
+                if (!(tt > 0.0 && tt < best)) continue;
+                double q0 = tt * d[0] - ctr[i][0], q1 = tt * d[1] - ctr[i][1], q2 = tt * d[2] - ctr[i][2];
+                if (q0 * q0 + q1 * q1 + q2 * q2 > rad2[i]) continue;
+                best = tt;
+                hit = (int)i;
             }
             double z = hit >= 0 ? best : f_;
             if (z < n_) z = n_;
