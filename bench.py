@@ -1,0 +1,546 @@
+"""Benchmark: clustered light assignment at 1920x1080 with 16,384 point lights (ms per frame),
+plus radix-sort throughput (Gkeys/s, % of HBM) and the primitive sweep, on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One step = one frame through vren::cluster_and_shade's clustering half (construct_point_light_bvh,
+find_unique_cluster_list, assign_lights) replayed as a CUDA graph, inputs resident in HBM, L2
+flushed (a 256 MiB write) before every timed step, each step timed with CUDA events on its stream.
+`e2e` runs the same frames through the public API from pinned host buffers: host->device copy of
+the G-buffer and lights, the pipeline, and a device->host read of the cluster references and the
+per-cluster light lists, all inside the timed region.
+
+--impl reference times the reference's CPU implementation of the path (the restated CPU oracle of
+oracle/, since loryruta/vren's own code needs Vulkan) with all host threads.
+Multi-GPU: frames are independent, so N ranks run N frame streams with no collective (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "1080p/16k-light cluster assign ms; radix sort Gkeys/s, %HBM; batched vs plain"
+W, H, L = 1920, 1080, 16384
+SEED = 20240611
+RADIX_N = 1 << 20
+L2_FLUSH_BYTES = 256 << 20
+BYTES_PER_PX = 20  # depth 4 + normal 12 + cluster reference 4
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region: median SM clock under load and throttle reasons."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int = 0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------------------------------------
+# Inputs (identical for both arms)
+# ------------------------------------------------------------------------------------------------
+def make_inputs(rank: int = 0):
+    import vren_gb300.scene as scene
+
+    depth, normals = scene.depth_planes(SEED + rank, W, H, planes=64)
+    pos, lights = scene.lights(SEED + 1000 + rank, L, W, H)
+    keys = scene.gen_u32(SEED + 7, 1, RADIX_N)
+    return depth, normals, pos, lights, keys
+
+
+# ------------------------------------------------------------------------------------------------
+# Our arm
+# ------------------------------------------------------------------------------------------------
+def run_ours(args, rank: int, world: int):
+    import torch
+
+    import vren_gb300 as vg
+    import vren_gb300.clustered_shading as cs
+    from vren_gb300 import _build
+
+    _build.build()
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    hbm_peak, peak_kind = peaks()
+    depth, normals, pos, lights, radix_keys = make_inputs(rank)
+    stream = torch.cuda.Stream(device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
+
+    cam = cs.scene_camera(W, H)
+    view = cs.view_from_camera(cam, "ref")
+    ctx = cs.cluster_and_shade(W, H, 65536, 1 << 24)
+    d_depth = torch.from_numpy(depth).to(dev)
+    d_norm = torch.from_numpy(normals).to(dev)
+    d_pos = torch.from_numpy(pos).to(dev)
+    d_light = torch.from_numpy(lights).to(dev)
+    torch.cuda.synchronize()
+
+    def frame():
+        ctx.cluster(stream, view, W, H, d_depth, d_norm, d_pos, d_light, L)
+
+    # warm-up (captures the graph on the first call)
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            frame()
+    stream.synchronize()
+    out = ctx.outputs()
+    U = int(cs.read_device(out.key_count, 1)[0])
+    total = int(cs.read_device(out.total, 1)[0])
+
+    # timed region
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    t_wall0 = time.perf_counter()
+    with ClockSampler(dev.index) as clocks, torch.cuda.stream(stream):
+        for i in range(args.steps):
+            flush.zero_()
+            ev[i][0].record(stream)
+            frame()
+            ev[i][1].record(stream)
+        stream.synchronize()
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall0
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    ms_frame = sum(step_ms) / len(step_ms)
+    if world > 1:
+        t = torch.tensor([sum(step_ms)], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        job_ms = float(t.item()) / (args.steps * world)
+    else:
+        job_ms = ms_frame
+    err = vg.device_error()
+
+    # dominant HBM kernel of the frame: find_unique_cluster_list (20 B/px), timed alone
+    frame_dev = torch.empty(0)
+    fr = cs.frame_build(view, W, H)
+    frame_dev = cs.frame_to_device(fr, dev)
+    T = ((W + 31) // 32) * ((H + 31) // 32)
+    keys = torch.zeros(T * 1024, dtype=torch.int32, device=dev)
+    kc = torch.zeros(1, dtype=torch.int32, device=dev)
+    refs = torch.zeros(W * H, dtype=torch.int32, device=dev)
+    fuc = cs.find_unique_cluster_list()
+    kt = []
+    with torch.cuda.stream(stream):
+        for i in range(args.warmup + args.steps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fuc(stream, W, H, frame_dev, d_depth, d_norm, keys, kc, refs)
+            b.record(stream)
+            if i >= args.warmup:
+                kt.append((a, b))
+        stream.synchronize()
+    fuc_ms = sum(a.elapsed_time(b) for a, b in kt) / len(kt)
+    fuc_bytes = BYTES_PER_PX * W * H
+    fuc_gbs = fuc_bytes / (fuc_ms * 1e-3) / 1e9
+
+    # end to end through the public API from pinned host buffers
+    h_depth = torch.from_numpy(depth).pin_memory()
+    h_norm = torch.from_numpy(normals).pin_memory()
+    h_pos = torch.from_numpy(pos).pin_memory()
+    h_light = torch.from_numpy(lights).pin_memory()
+    h_refs = torch.empty(W * H, dtype=torch.int32).pin_memory()
+    h_small = torch.empty(2, dtype=torch.int32).pin_memory()
+    cap = T * 1024
+    h_lists = torch.empty(3 * cap + (1 << 24), dtype=torch.int32).pin_memory()
+    import ctypes
+
+    cudart = cs._cudart()
+    cudart.cudaMemcpyAsync.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_void_p]
+    cudart.cudaMemcpyAsync.restype = ctypes.c_int
+
+    def d2h(dst_ptr, src_ptr, nbytes):
+        if nbytes:
+            rc = cudart.cudaMemcpyAsync(dst_ptr, src_ptr, nbytes, 2, stream.cuda_stream)
+            assert rc == 0
+
+    h2d_bytes = (h_depth.numel() + h_norm.numel() + h_pos.numel() + h_light.numel()) * 4
+    e2e_ms, d2h_total = [], 0
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        with torch.cuda.stream(stream):
+            d_depth.copy_(h_depth, non_blocking=True)
+            d_norm.copy_(h_norm, non_blocking=True)
+            d_pos.copy_(h_pos, non_blocking=True)
+            d_light.copy_(h_light, non_blocking=True)
+            frame()
+            d2h(h_small.data_ptr(), out.key_count, 4)
+            d2h(h_small.data_ptr() + 4, out.total, 4)
+            d2h(h_refs.data_ptr(), out.cluster_refs, W * H * 4)
+            stream.synchronize()
+            u, tot = int(h_small[0]), int(h_small[1])
+            base = h_lists.data_ptr()
+            d2h(base, out.cluster_keys, u * 4)
+            d2h(base + 4 * cap, out.counts, u * 4)
+            d2h(base + 8 * cap, out.offsets, u * 4)
+            d2h(base + 12 * cap, out.indices, tot * 4)
+            stream.synchronize()
+        if i >= args.warmup:
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+            d2h_total = 8 + W * H * 4 + u * 12 + tot * 4
+    e2e = sum(e2e_ms) / len(e2e_ms)
+
+    # radix sort: 2^20 key/value pairs (config 1), plus sizes beyond L2
+    radix = radix_bench(args, dev, stream, flush, radix_keys, hbm_peak)
+    sweep = None if args.quick else primitive_sweep(args, dev, stream, flush, hbm_peak)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(depth, normals, pos, lights, radix_keys, view)
+
+    launches_per_frame = 11  # 7 light-BVH kernels, 1 unique-cluster kernel, 3 assignment kernels
+    if rank == 0:
+        res = {
+            "metric": METRIC,
+            "value": round(job_ms, 5),
+            "unit": "ms",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": round(ms_frame, 5),
+            "higher_is_better": False,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32+u32",
+            "data": "synthetic (seeded PCG32 scene: 64 oriented planar discs, 16384 point lights)",
+            "config": {
+                "workload": "cluster assignment 1920x1080, 16384 lights, 32x32 tiles, REF slicing, 15-bit Morton, "
+                            "a6+a7+a8 per frame (construct light BVH, unique clusters, assign lights)",
+                "unique_clusters": U, "assignments": total,
+                "l2": "flushed (256 MiB write) before every timed step",
+                "graph": "one CUDA graph replay per frame",
+                "parallelism": f"replicas x{world} (frames are independent)",
+            },
+            "e2e": {"value": round(e2e, 4), "unit": "ms", "h2d_bytes_per_step": h2d_bytes,
+                    "d2h_bytes_per_step": d2h_total},
+            "gpu_launches": launches_per_frame * args.steps,
+            "roofline": {"bound": "hbm", "kernel": "find_unique_kernel", "achieved": round(fuc_gbs, 1),
+                         "peak": hbm_peak, "unit": "GB/s", "frac": round(fuc_gbs / hbm_peak, 4),
+                         "peak_kind": peak_kind, "traffic": None,
+                         "algorithmic_bytes": fuc_bytes, "kernel_ms": round(fuc_ms, 5)},
+            "radix_sort": radix,
+            "batched_vs_plain": None,
+            "primitive_sweep": sweep,
+            "cpu_baseline": cpu,
+            "clocks": clocks.summary(),
+            "device_error": err,
+            "wall_s_timed": round(t_wall, 4),
+        }
+        print(json.dumps(res), flush=True)
+
+
+def time_events(stream, fn, warmup, steps, flush=None):
+    import torch
+
+    evs = []
+    with torch.cuda.stream(stream):
+        for i in range(warmup + steps):
+            if flush is not None:
+                flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            if i >= warmup:
+                evs.append((a, b))
+        stream.synchronize()
+    return sum(a.elapsed_time(b) for a, b in evs) / len(evs)
+
+
+def radix_bench(args, dev, stream, flush, keys_np, hbm_peak):
+    import torch
+
+    import vren_gb300 as vg
+    import vren_gb300.scene as scene
+
+    out = {}
+    for n in ([RADIX_N] if args.quick else [RADIX_N, 1 << 24, 1 << 26]):
+        kn = keys_np if n == RADIX_N else scene.gen_u32(SEED + 7, 1, n)
+        src_k = torch.from_numpy(kn.view(np.int32)).to(dev)
+        src_v = torch.arange(n, dtype=torch.int32, device=dev)
+        k, v = torch.empty_like(src_k), torch.empty_like(src_v)
+        tk, tv = torch.empty_like(k), torch.empty_like(v)
+        rs = vg.radix_sort(8)
+        s1 = rs.create_scratch_buffer_1(n, dev)
+
+        def run():
+            k.copy_(src_k)
+            v.copy_(src_v)
+
+        # copies are outside the events: time only the sort
+        evs = []
+        with torch.cuda.stream(stream):
+            for i in range(args.warmup + args.steps):
+                run()
+                flush.zero_()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                rs.sort(stream, k, v, n, s1, tk, tv)
+                b.record(stream)
+                if i >= args.warmup:
+                    evs.append((a, b))
+            stream.synchronize()
+        ms = sum(a.elapsed_time(b) for a, b in evs) / len(evs)
+        # correctness spot check against numpy's stable sort
+        if n == RADIX_N:
+            order = np.argsort(kn, kind="stable")
+            ok = bool(np.array_equal(k.cpu().numpy().view(np.uint32), kn[order]) and
+                      np.array_equal(v.cpu().numpy(), order.astype(np.int32)))
+        else:
+            ok = None
+        gbs = 64.0 * n / (ms * 1e-3) / 1e9
+        out[f"n=2^{n.bit_length() - 1}"] = {"ms": round(ms, 5), "gkeys_s": round(n / (ms * 1e-3) / 1e9, 3),
+                                            "gbs_at_64B_per_pair": round(gbs, 1),
+                                            "hbm_frac": round(gbs / hbm_peak, 4), "bit_exact_vs_stable_sort": ok,
+                                            "l2": "flushed before each sort" if n * 16 < (129 << 20) else
+                                            "inputs larger than L2 (also flushed)"}
+        del src_k, src_v, k, v, tk, tv, s1
+    return out
+
+
+def primitive_sweep(args, dev, stream, flush, hbm_peak):
+    import torch
+
+    import vren_gb300 as vg
+    import vren_gb300.scene as scene
+
+    res = {}
+    steps = max(3, args.steps // 2)
+    for e in (16, 20, 24, 26):
+        n = 1 << e
+        x = torch.from_numpy(scene.gen_u32(SEED + e, 2, n, mask=255).view(np.int32)).to(dev)
+        y = torch.empty_like(x)
+        o = torch.zeros(1, dtype=torch.int32, device=dev)
+        sc = vg.primitives.alloc_scratch(vg.primitives.reduce_scratch_bytes(n), dev)
+        ms_red = time_events(stream, lambda: vg.reduce_scalar(stream, "add", x, o, sc), 3, steps, flush)
+        xf = x.float()
+        of = torch.zeros(1, dtype=torch.float32, device=dev)
+        ms_max = time_events(stream, lambda: vg.reduce_scalar(stream, "max", xf, of, sc), 3, steps, flush)
+        scan = vg.blelloch_scan()
+
+        def do_scan():
+            scan(stream, y, n)
+
+        y.copy_(x)
+        ms_scan = time_events(stream, do_scan, 3, steps, flush)
+        res[f"2^{e}"] = {
+            "reduce_u32_add": {"ms": round(ms_red, 5), "gbs": round(4 * n / ms_red / 1e6, 1),
+                               "hbm_frac": round(4 * n / ms_red / 1e6 / hbm_peak, 4)},
+            "reduce_f32_max": {"ms": round(ms_max, 5), "gbs": round(4 * n / ms_max / 1e6, 1)},
+            "exclusive_scan": {"ms": round(ms_scan, 5), "gbs": round(8 * n / ms_scan / 1e6, 1),
+                               "hbm_frac": round(8 * n / ms_scan / 1e6 / hbm_peak, 4)},
+        }
+        del x, y, xf
+    # bucket sort: 2^24 uvec2(key, index), 1024 buckets on the low 10 bits
+    n = 1 << 24
+    keys = scene.gen_u32(SEED + 99, 3, n)
+    pairs = np.stack([keys, np.arange(n, dtype=np.uint32)], 1).reshape(-1)
+    src = torch.from_numpy(pairs.view(np.int32)).to(dev)
+    for kb in (10, 16):
+        bs = vg.bucket_sort(kb)
+        outb = torch.empty(bs.get_required_output_buffer_size(n) // 4, dtype=torch.int32, device=dev)
+        ms_b = time_events(stream, lambda: bs(stream, src, n, 0, outb, 0), 3, steps, flush)
+        res[f"bucket_sort_2^24_{kb}bit"] = {"ms": round(ms_b, 5), "gbs_at_24B": round(24 * n / ms_b / 1e6, 1),
+                                            "hbm_frac": round(24 * n / ms_b / 1e6 / hbm_peak, 4)}
+    return res
+
+
+def cpu_baseline(depth, normals, pos, lights, radix_keys, view, budget_s: float = 12.0, threads: int = 1):
+    """The CPU oracle (port of the reference's algorithms) on a bounded sample, single-threaded."""
+    import oracle
+
+    t0 = time.perf_counter()
+    frames = 0
+    while True:
+        vp, bvh, lidx = oracle.cs_light_bvh(pos, lights, L, view, 15)
+        keys, refs = oracle.cs_find_unique_clusters(depth, normals, W, H, view, 0, threads=threads)
+        oracle.cs_assign_lights(keys, W, H, view, bvh, L, lidx, vp, threads=threads)
+        frames += 1
+        if time.perf_counter() - t0 > budget_s / 2 or frames >= 50:
+            break
+    ms_frame = (time.perf_counter() - t0) * 1e3 / frames
+    t1 = time.perf_counter()
+    sorts = 0
+    vals = np.arange(RADIX_N, dtype=np.uint32)
+    while True:
+        oracle.stable_sort_u32(radix_keys, vals)
+        sorts += 1
+        if time.perf_counter() - t1 > budget_s / 4 or sorts >= 50:
+            break
+    ms_sort = (time.perf_counter() - t1) * 1e3 / sorts
+    return {"value": round(ms_frame, 3), "unit": "ms", "cores": threads, "kind": "port",
+            "sample": f"{frames} frames of the CPU oracle pipeline (a6+a7+a8) at 1920x1080/16384 lights",
+            "radix_sort_2^20_pairs_ms": round(ms_sort, 3),
+            "radix_sort_gkeys_s": round(RADIX_N / (ms_sort * 1e-3) / 1e9, 4)}
+
+
+# ------------------------------------------------------------------------------------------------
+# Reference arm: the CPU implementation of the path (oracle port), all host threads
+# ------------------------------------------------------------------------------------------------
+def numpy_view(cs, near: float = 0.1, far: float = 1000.0, fov_deg: float = 45.0):
+    """The bench camera (origin, yaw = pitch = 0) with vren/vren/camera.cpp:66-84's formulas, so the
+    CPU arm does not load the CUDA library."""
+    fov = float(np.float32(np.deg2rad(fov_deg)))
+    t = np.tan(fov / 2.0)
+    proj = np.zeros((4, 4))  # row-major
+    proj[0, 0] = 1.0 / (t * (W / H))
+    proj[1, 1] = 1.0 / t
+    proj[2, 2] = far / (far - near)
+    proj[2, 3] = -(far * near) / (far - near)
+    proj[3, 2] = 1.0
+    inv = np.linalg.inv(proj)
+    v = cs.View()
+    v.view[:] = np.eye(4, dtype=np.float32).T.reshape(-1).tolist()
+    v.inv_view[:] = np.eye(4, dtype=np.float32).T.reshape(-1).tolist()
+    v.inv_proj[:] = inv.T.astype(np.float32).reshape(-1).tolist()
+    v.near_plane, v.far_plane, v.half_fov_y = near, far, np.float32(fov) / np.float32(2)
+    v.slicing = 0
+    return v
+
+
+def run_reference(args, rank: int, world: int):
+    if rank != 0:
+        return
+    import oracle
+    import vren_gb300.clustered_shading as cs
+    from vren_gb300 import _build
+
+    _build.build_scene()
+    depth, normals, pos, lights, radix_keys = make_inputs(0)
+    cores = os.cpu_count() or 1
+    view = numpy_view(cs)
+
+    def frame():
+        vp, bvh, lidx = oracle.cs_light_bvh(pos, lights, L, view, 15)
+        keys, refs = oracle.cs_find_unique_clusters(depth, normals, W, H, view, 0, threads=cores)
+        oracle.cs_assign_lights(keys, W, H, view, bvh, L, lidx, vp, threads=cores)
+
+    for _ in range(args.warmup):
+        frame()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        frame()
+    ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    vals = np.arange(RADIX_N, dtype=np.uint32)
+    t1 = time.perf_counter()
+    reps = 5
+    for _ in range(reps):
+        oracle.stable_sort_u32(radix_keys, vals)
+    ms_sort = (time.perf_counter() - t1) * 1e3 / reps
+    res = {
+        "impl": "reference", "metric": METRIC, "value": round(ms, 4), "unit": "ms", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+u32",
+        "data": "synthetic (seeded PCG32 scene: 64 oriented planar discs, 16384 point lights)",
+        "config": {"workload": "cluster assignment 1920x1080, 16384 lights, 32x32 tiles, REF slicing, 15-bit Morton, "
+                               "a6+a7+a8 per frame (construct light BVH, unique clusters, assign lights)",
+                   "implementation": "CPU restatement of loryruta/vren's algorithms (oracle/); the reference's own "
+                                     "GPU path needs Vulkan, which this machine does not have"},
+        "cpu_baseline": {"value": round(ms, 4), "unit": "ms", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} frames at 1920x1080/16384 lights, OpenMP over tiles and clusters",
+                         "radix_sort_2^20_pairs_ms": round(ms_sort, 3)},
+        "e2e": {"value": round(ms, 4), "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(res), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--quick", action="store_true", help="skip the primitive sweep and the large sorts")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1 and args.impl == "ours":
+        import torch
+
+        torch.distributed.init_process_group("nccl")
+    try:
+        if args.impl == "reference":
+            run_reference(args, rank, world)
+        else:
+            run_ours(args, rank, world)
+    finally:
+        if world > 1 and args.impl == "ours":
+            import torch
+
+            torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,113 @@
+// Exercises the C++ mirror of vren's call surface (include/vren_gb300.hpp) the way the reference's
+// tests call vren::radix_sort, vren::blelloch_scan, vren::reduce and vren::build_bvh
+// (vren_test/vren_test/primitives/*.cpp).  Prints "api ok" and exits 0 on success.
+#include "vren_gb300.hpp"
+
+#include <algorithm>
+#include <cstdio>
+#include <numeric>
+#include <vector>
+
+#define EXPECT(cond)                                                        \
+    do {                                                                    \
+        if (!(cond)) {                                                      \
+            std::fprintf(stderr, "check failed: %s (line %d)\n", #cond, __LINE__); \
+            return 1;                                                       \
+        }                                                                   \
+    } while (0)
+
+template <typename T>
+static void upload(vren::device_buffer const& b, std::vector<T> const& v)
+{
+    cudaMemcpy(b.m_ptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+template <typename T>
+static std::vector<T> download(vren::device_buffer const& b, size_t n)
+{
+    std::vector<T> v(n);
+    cudaMemcpy(v.data(), b.m_ptr, n * sizeof(T), cudaMemcpyDeviceToHost);
+    return v;
+}
+
+int main()
+{
+    vren::resource_container rc;
+    cudaStream_t stream;
+    cudaStreamCreate(&stream);
+
+    // radix_sort.cpp:245-309: reversed iota, 1024 keys
+    {
+        vren::radix_sort rs;
+        const uint32_t n = 1024;
+        std::vector<uint32_t> keys(n);
+        std::iota(keys.begin(), keys.end(), 0u);
+        std::reverse(keys.begin(), keys.end());
+        vren::owned_buffer buf(n * 4);
+        upload(buf, keys);
+        auto s1 = rs.create_scratch_buffer_1(n);
+        auto s2 = rs.create_scratch_buffer_2(n);
+        rs(stream, rc, buf, n, s1, s2);
+        cudaStreamSynchronize(stream);
+        auto out = download<uint32_t>(buf, n);
+        for (uint32_t i = 0; i < n; ++i) EXPECT(out[i] == i);
+        bool threw = false;
+        try {
+            rs(stream, rc, buf, 1000, s1, s2);
+        } catch (std::invalid_argument const&) {
+            threw = true;
+        }
+        EXPECT(threw);
+    }
+    // blelloch_scan.cpp:166-176: all ones
+    {
+        vren::blelloch_scan scan;
+        const uint32_t n = 1 << 19;
+        vren::owned_buffer buf(n * 4);
+        upload(buf, std::vector<uint32_t>(n, 1u));
+        scan(stream, rc, buf, n, 0, 1);
+        cudaStreamSynchronize(stream);
+        auto out = download<uint32_t>(buf, n);
+        for (uint32_t i = 0; i < n; ++i) EXPECT(out[i] == i);
+    }
+    // reduce.cpp:538-545: all-ones add, whole tree in place
+    {
+        vren::reduce<vren::uint_tag, vren::ReduceOperationAdd> red;
+        const uint32_t n = 10000, P = vren::calc_reduce_output_buffer_length(n);
+        std::vector<uint32_t> v(P, 0u);
+        std::fill(v.begin(), v.begin() + n, 1u);
+        vren::owned_buffer buf(P * 4);
+        upload(buf, v);
+        red(stream, rc, buf, n, 0, 1);
+        cudaStreamSynchronize(stream);
+        auto out = download<uint32_t>(buf, P);
+        EXPECT(out[P - 1] == n);
+        EXPECT(out[1] == 2 && out[3] == 4 && out[1023] == 1024);
+    }
+    // build_bvh.cpp:223-254 helpers and a build of 1000 leaves
+    {
+        EXPECT(vren::calc_bvh_padded_leaf_count(2193819) == 33554432u);
+        EXPECT(vren::calc_bvh_root_index(129) == 32u * 32u + 32u);
+        const uint32_t leaves = 1000, P = vren::calc_bvh_padded_leaf_count(leaves);
+        std::vector<vren::bvh_node> nodes(vren::calc_bvh_buffer_length(P));
+        for (uint32_t i = 0; i < P; ++i) {
+            auto& nd = nodes[i];
+            for (int a = 0; a < 3; ++a) {
+                nd.min[a] = (float)i;
+                nd.max[a] = (float)i + 1.0f;
+            }
+            nd.next = i < leaves ? VREN_BVH_LEAF_NODE : VREN_BVH_INVALID_NODE;
+        }
+        vren::owned_buffer buf(nodes.size() * sizeof(vren::bvh_node));
+        upload(buf, nodes);
+        vren::build_bvh()(stream, rc, buf, P);
+        cudaStreamSynchronize(stream);
+        auto out = download<vren::bvh_node>(buf, nodes.size());
+        const auto& root = out[vren::calc_bvh_root_index(P)];
+        EXPECT(root.min[0] == 0.0f && root.max[0] == (float)leaves && root.next == P + 32);
+    }
+    EXPECT(vren_device_error(1) == 0);
+    cudaStreamDestroy(stream);
+    std::printf("api ok\n");
+    return 0;
+}

@@ -205,7 +205,7 @@ def test_assign_lights_dense(cuda, L, spheres):
     assert np.array_equal(u32(counts)[:U], ec)
     assert np.array_equal(u32(offsets)[:U], eo)
     assert np.array_equal(u32(indices)[:et], ei)
-    assert et > 0
+    assert et > 0 or L == 1
 
 
 @pytest.mark.parametrize("W,H,L", [(1920, 1080, 16384), (1280, 720, 65536), (640, 360, 1024)])
