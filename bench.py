@@ -160,7 +160,8 @@ def run_ours(args, rank: int, world: int):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     t_wall0 = time.perf_counter()
-    with ClockSampler(dev.index) as clocks, torch.cuda.stream(stream):
+    clocks = ClockSampler(dev.index).__enter__()  # spans all GPU work below (the frame loop alone is ~10 ms)
+    with torch.cuda.stream(stream):
         for i in range(args.steps):
             flush.zero_()
             ev[i][0].record(stream)
@@ -254,6 +255,7 @@ def run_ours(args, rank: int, world: int):
     radix = radix_bench(args, dev, stream, flush, radix_keys, hbm_peak)
     sweep = None if args.quick else primitive_sweep(args, dev, stream, flush, hbm_peak)
 
+    clocks.__exit__(None, None, None)
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(depth, normals, pos, lights, radix_keys, view)
@@ -514,6 +516,53 @@ def run_reference(args, rank: int, world: int):
     print(json.dumps(res), flush=True)
 
 
+def run_profile(args):
+    """One kernel family on a case larger than L2, for ncu captures (--profile KIND)."""
+    import torch
+
+    import vren_gb300 as vg
+    import vren_gb300.clustered_shading as cs
+    import vren_gb300.scene as scene
+    from vren_gb300 import _build
+
+    _build.build()
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(device=dev)
+    reps = args.warmup + args.steps
+    if args.profile == "find_unique":
+        w, h = 3840, 2160  # 20 B/px -> 166 MB > L2
+        depth, normals = scene.depth_planes(SEED, w, h)
+        view = cs.view_from_camera(cs.scene_camera(w, h), "ref")
+        frame = cs.frame_to_device(cs.frame_build(view, w, h), dev)
+        T = ((w + 31) // 32) * ((h + 31) // 32)
+        keys = torch.zeros(T * 1024, dtype=torch.int32, device=dev)
+        kc = torch.zeros(1, dtype=torch.int32, device=dev)
+        refs = torch.zeros(w * h, dtype=torch.int32, device=dev)
+        d, n = torch.from_numpy(depth).to(dev), torch.from_numpy(normals).to(dev)
+        fuc = cs.find_unique_cluster_list()
+        fn = lambda: fuc(stream, w, h, frame, d, n, keys, kc, refs)
+    elif args.profile == "radix":
+        n = 1 << 25
+        k = torch.from_numpy(scene.gen_u32(SEED + 7, 1, n).view(np.int32)).to(dev)
+        v = torch.arange(n, dtype=torch.int32, device=dev)
+        tk, tv = torch.empty_like(k), torch.empty_like(v)
+        rs = vg.radix_sort(8)
+        s1 = rs.create_scratch_buffer_1(n, dev)
+        fn = lambda: rs.sort(stream, k, v, n, s1, tk, tv)
+    elif args.profile == "scan":
+        n = 1 << 26
+        x = torch.from_numpy(scene.gen_u32(SEED, 2, n, mask=255).view(np.int32)).to(dev)
+        scan = vg.blelloch_scan()
+        fn = lambda: scan(stream, x, n)
+    else:
+        raise SystemExit(f"unknown profile kind {args.profile}")
+    with torch.cuda.stream(stream):
+        for _ in range(reps):
+            fn()
+    stream.synchronize()
+    print(json.dumps({"profile": args.profile, "runs": reps, "device_error": vg.device_error()}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -522,7 +571,11 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--quick", action="store_true", help="skip the primitive sweep and the large sorts")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--profile", choices=["find_unique", "radix", "scan"], default=None,
+                    help="run one kernel family on a case larger than L2 (for ncu) and exit")
     args = ap.parse_args()
+    if args.profile:
+        return run_profile(args)
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

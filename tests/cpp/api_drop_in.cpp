@@ -104,7 +104,8 @@ int main()
         cudaStreamSynchronize(stream);
         auto out = download<vren::bvh_node>(buf, nodes.size());
         const auto& root = out[vren::calc_bvh_root_index(P)];
-        EXPECT(root.min[0] == 0.0f && root.max[0] == (float)leaves && root.next == P + 32);
+        // P = 1024: leaves [0, 1024), 32 parents at [1024, 1056), root 1056 whose first child is 1024
+        EXPECT(root.min[0] == 0.0f && root.max[0] == (float)leaves && root.next == P);
     }
     EXPECT(vren_device_error(1) == 0);
     cudaStreamDestroy(stream);

@@ -331,16 +331,6 @@ static int construct_light_bvh(cudaStream_t st, const float* positions, const fl
 constexpr int kFucThreads = 256;
 constexpr uint32_t kFucHeaderWords = 4;  // start ticket, done ticket, epoch, unused
 
-__device__ __forceinline__ uint64_t ld_acquire_u64(const uint64_t* p)
-{
-    uint64_t v;
-    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-    return v;
-}
-__device__ __forceinline__ void st_release_u64(uint64_t* p, uint64_t v)
-{
-    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
-}
 __device__ __forceinline__ uint64_t make_status(uint32_t epoch, uint32_t flag, uint32_t value)
 {
     return ((uint64_t)((epoch << 2) | flag) << 32) | value;
@@ -436,9 +426,9 @@ __global__ void __launch_bounds__(kFucThreads) find_unique_kernel(
     if (warp == 0) {
         uint32_t prefix = 0;
         if (tile == 0) {
-            if (lane == 0) st_release_u64(status, make_status(epoch, 2u, tile_unique));
+            if (lane == 0) st_relaxed_u64(status, make_status(epoch, 2u, tile_unique));
         } else {
-            if (lane == 0) st_release_u64(status + tile, make_status(epoch, 1u, tile_unique));
+            if (lane == 0) st_relaxed_u64(status + tile, make_status(epoch, 1u, tile_unique));
             int64_t pos = (int64_t)tile - 1;
             bool timed_out = false;
             while (true) {
@@ -447,7 +437,7 @@ __global__ void __launch_bounds__(kFucThreads) find_unique_kernel(
                 if (idx >= 0) {
                     uint32_t ns = 32;
                     for (uint32_t round = 0;; ++round) {
-                        const uint64_t w = ld_acquire_u64(status + idx);
+                        const uint64_t w = ld_relaxed_u64(status + idx);
                         const uint32_t hi = (uint32_t)(w >> 32);
                         if ((hi >> 2) == epoch && (hi & 3u) != 0) {
                             flag = hi & 3u;
@@ -472,7 +462,7 @@ __global__ void __launch_bounds__(kFucThreads) find_unique_kernel(
                 pos -= 32;
             }
             if (__any_sync(0xFFFFFFFFu, timed_out) && lane == 0) VREN_RECORD_ERROR(VREN_ERR_TIMEOUT);
-            if (lane == 0) st_release_u64(status + tile, make_status(epoch, 2u, prefix + tile_unique));
+            if (lane == 0) st_relaxed_u64(status + tile, make_status(epoch, 2u, prefix + tile_unique));
         }
         if (lane == 0) {
             s_offset = prefix;

@@ -75,6 +75,20 @@ __device__ __forceinline__ void st_relaxed_u32(uint32_t* p, uint32_t v)
     asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// Look-back status words carry their whole payload (flag and value) in one naturally aligned
+// word, so single-copy atomicity is all the protocol needs: relaxed gpu-scope accesses, no fences.
+__device__ __forceinline__ uint64_t ld_relaxed_u64(const uint64_t* p)
+{
+    uint64_t v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_relaxed_u64(uint64_t* p, uint64_t v)
+{
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
 __device__ __forceinline__ uint32_t lanemask_lt()
 {
     uint32_t m;
@@ -105,7 +119,7 @@ __device__ __forceinline__ uint32_t wait_for_flag(const uint32_t* p, uint32_t li
 {
     uint32_t ns = 32;
     for (uint32_t round = 0;; ++round) {
-        uint32_t v = ld_acquire_u32(p);
+        uint32_t v = ld_relaxed_u32(p);
         if (v & (3u << kFlagShift)) return v;
         if (round >= limit) {
             on_timeout();

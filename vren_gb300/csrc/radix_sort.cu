@@ -117,13 +117,23 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_hist_kernel(
     __syncthreads();
     if (!s_last) return;
     __threadfence();
-    if (tid < passes.count) {
-        uint32_t run = 0;
-        for (int d = 0; d < RADIX; ++d) {
-            uint32_t c = ld_relaxed_u32(g_hist + tid * kMaxRadix + d);
-            scratch[kOffsOffset + tid * kMaxRadix + d] = run;
-            run += c;
+    // One block-wide exclusive scan per pass (RADIX <= 256 = threads), all loads in parallel.
+    __shared__ uint32_t s_wsum[kSortThreads / 32];
+    const uint32_t lane = tid & 31u, warp = tid >> 5;
+    for (uint32_t p = 0; p < passes.count; ++p) {
+        const uint32_t c = tid < (uint32_t)RADIX ? ld_relaxed_u32(g_hist + p * kMaxRadix + tid) : 0u;
+        uint32_t incl = c;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+            if (lane >= (uint32_t)d) incl += y;
         }
+        if (lane == 31) s_wsum[warp] = incl;
+        __syncthreads();
+        uint32_t before = 0;
+        for (uint32_t w = 0; w < warp; ++w) before += s_wsum[w];
+        if (tid < (uint32_t)RADIX) scratch[kOffsOffset + p * kMaxRadix + tid] = before + incl - c;
+        __syncthreads();
     }
 }
 
@@ -217,9 +227,9 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_pass_kernel(
         uint32_t* my = status + (size_t)tile * RADIX + d;
         uint32_t prefix = 0;
         if (tile == 0) {
-            st_release_u32(my, kFlagPrefix | count);
+            st_relaxed_u32(my, kFlagPrefix | count);
         } else {
-            st_release_u32(my, kFlagAggregate | count);
+            st_relaxed_u32(my, kFlagAggregate | count);
             int64_t t = (int64_t)tile - 1;
             while (t >= 0) {
                 uint32_t w = wait_for_flag(status + (size_t)t * RADIX + d, wait_limit,
@@ -228,7 +238,7 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_pass_kernel(
                 if (w & kFlagPrefix) break;
                 --t;
             }
-            st_release_u32(my, kFlagPrefix | (prefix + count));
+            st_relaxed_u32(my, kFlagPrefix | (prefix + count));
         }
         s_tile_excl[d] = count;  // replaced by the exclusive scan below
         s_delta[d] = (int32_t)(ld_relaxed_u32(scratch + kOffsOffset + pass * kMaxRadix + d) + prefix);

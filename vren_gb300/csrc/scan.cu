@@ -24,23 +24,57 @@ constexpr int kScanItems = 16;
 constexpr uint32_t kScanTile = kScanThreads * kScanItems;  // 4096
 constexpr uint32_t kScanHeaderWords = 4;
 
-__device__ __forceinline__ uint64_t ld_acquire_u64(const uint64_t* p)
-{
-    uint64_t v;
-    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-    return v;
-}
-__device__ __forceinline__ void st_release_u64(uint64_t* p, uint64_t v)
-{
-    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
-}
-
 // status word helpers
 __device__ __forceinline__ uint64_t make_status(uint32_t epoch, uint32_t flag, uint32_t value)
 {
     return ((uint64_t)((epoch << 2) | flag) << 32) | value;
 }
 
+// Warp-wide decoupled look-back over status[seg_first .. tile-1]: lane i examines tile - 1 - i
+// (then 32 further back, ...) and the warp sums aggregates up to the nearest inclusive prefix.
+// Returns the exclusive prefix of `tile` in every lane.
+__device__ __forceinline__ uint32_t warp_lookback(const uint64_t* status, uint32_t tile, uint32_t seg_first,
+                                                  uint32_t epoch, uint32_t lane, uint32_t wait_limit, bool& timed_out)
+{
+    uint32_t prefix = 0;
+    int64_t pos = (int64_t)tile - 1;
+    while (true) {
+        const int64_t idx = pos - lane;
+        uint32_t flag = 2u, val = 0u;  // lanes before the segment start act as a zero prefix
+        if (idx >= (int64_t)seg_first) {
+            uint32_t ns = 32;
+            for (uint32_t round = 0;; ++round) {
+                const uint64_t w = ld_relaxed_u64(status + idx);
+                const uint32_t hi = (uint32_t)(w >> 32);
+                if ((hi >> 2) == epoch && (hi & 3u) != 0) {
+                    flag = hi & 3u;
+                    val = (uint32_t)w;
+                    break;
+                }
+                if (round >= wait_limit) {
+                    timed_out = true;
+                    break;
+                }
+                __nanosleep(ns);
+                if (ns < 512) ns <<= 1;
+            }
+        }
+        const uint32_t prefix_mask = __ballot_sync(0xFFFFFFFFu, flag == 2u);
+        const uint32_t stop = prefix_mask ? (uint32_t)(__ffs(prefix_mask) - 1) : 31u;
+        uint32_t contrib = (lane <= stop) ? val : 0u;
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) contrib += __shfl_xor_sync(0xFFFFFFFFu, contrib, d);
+        prefix += contrib;
+        if (prefix_mask) break;
+        pos -= 32;
+    }
+    return prefix;
+}
+
+// One CTA = one 4096-element tile; warp w owns 512 contiguous elements as four 128-element slices,
+// lane l holding elements 4l..4l+3 of each slice, so every load and store instruction of a warp
+// covers 512 contiguous bytes.
+//
 // `in` may equal `data` (in place).  When n_dev is given the element count is min(*n_dev, n)
 // (a single segment whose length is only known on the device); tiles past it do nothing.
 // When total_out is given the segment-0 total is written there.
@@ -49,6 +83,7 @@ __global__ void __launch_bounds__(kScanThreads) exclusive_scan_kernel(
     uint32_t* __restrict__ scratch, uint32_t wait_limit, const uint32_t* __restrict__ n_dev,
     uint32_t* __restrict__ total_out)
 {
+    constexpr int kSlices = kScanItems / 4;
     __shared__ uint32_t s_tile;
     __shared__ uint32_t s_epoch;
     __shared__ uint32_t s_warp_sum[kScanThreads / 32];
@@ -79,94 +114,67 @@ __global__ void __launch_bounds__(kScanThreads) exclusive_scan_kernel(
     {
     const uint32_t* seg_in = in + seg_off;
     uint32_t* seg_data = data + seg_off;
-    const uint32_t base = tile_in_seg * kScanTile + tid * kScanItems;
-
-    // Load 16 consecutive elements.
-    uint32_t v[kScanItems];
+    const uint32_t warp_base = tile_in_seg * kScanTile + warp * (kScanItems * 32);
     const bool full = (tile_in_seg + 1) * kScanTile <= n;
     const bool aligned = ((reinterpret_cast<uintptr_t>(seg_data) & 15u) == 0) &&
                          ((reinterpret_cast<uintptr_t>(seg_in) & 15u) == 0);
-    if (full && aligned) {
-        const uint4* p = reinterpret_cast<const uint4*>(seg_in + base);
+    const bool vec = full && aligned;
+
+    uint32_t v[kSlices][4];
 #pragma unroll
-        for (int k = 0; k < kScanItems / 4; ++k) {
-            uint4 q = p[k];
-            v[4 * k + 0] = q.x; v[4 * k + 1] = q.y; v[4 * k + 2] = q.z; v[4 * k + 3] = q.w;
+    for (int k = 0; k < kSlices; ++k) {
+        const uint32_t b = warp_base + k * 128 + lane * 4;
+        if (vec) {
+            const uint4 q = *reinterpret_cast<const uint4*>(seg_in + b);
+            v[k][0] = q.x; v[k][1] = q.y; v[k][2] = q.z; v[k][3] = q.w;
+        } else {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) v[k][j] = (b + j < n) ? seg_in[b + j] : 0u;
         }
-    } else {
-#pragma unroll
-        for (int k = 0; k < kScanItems; ++k) v[k] = (base + k < n) ? seg_in[base + k] : 0u;
     }
 
-    // Thread-local exclusive scan.
-    uint32_t thread_sum = 0;
+    // Per slice: lane-local exclusive scan of 4 items, warp scan of the lane sums.
+    uint32_t lane_off[kSlices];
+    uint32_t warp_run = 0;
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-        uint32_t x = v[k];
-        v[k] = thread_sum;
-        thread_sum += x;
-    }
-    // Warp inclusive scan of thread sums.
-    uint32_t incl = thread_sum;
+    for (int k = 0; k < kSlices; ++k) {
+        uint32_t s = 0;
 #pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, d);
-        if (lane >= (uint32_t)d) incl += y;
+        for (int j = 0; j < 4; ++j) {
+            const uint32_t x = v[k][j];
+            v[k][j] = s;
+            s += x;
+        }
+        uint32_t incl = s;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+            if (lane >= (uint32_t)d) incl += y;
+        }
+        lane_off[k] = warp_run + incl - s;
+        warp_run += __shfl_sync(0xFFFFFFFFu, incl, 31);
     }
-    if (lane == 31) s_warp_sum[warp] = incl;
+    if (lane == 0) s_warp_sum[warp] = warp_run;
     __syncthreads();
     uint32_t warp_prefix = 0, tile_sum = 0;
 #pragma unroll
     for (int w = 0; w < kScanThreads / 32; ++w) {
-        uint32_t ws = s_warp_sum[w];
+        const uint32_t ws = s_warp_sum[w];
         if (w < (int)warp) warp_prefix += ws;
         tile_sum += ws;
     }
 
-    // Decoupled look-back.
     if (warp == 0) {
         uint64_t* my_status = status + tile;
         uint32_t prefix = 0;
         if (tile_in_seg == 0) {
-            if (lane == 0) st_release_u64(my_status, make_status(epoch, 2u, tile_sum));
+            if (lane == 0) st_relaxed_u64(my_status, make_status(epoch, 2u, tile_sum));
         } else {
-            if (lane == 0) st_release_u64(my_status, make_status(epoch, 1u, tile_sum));
-            const uint32_t seg_first = tile - tile_in_seg;
-            int64_t pos = (int64_t)tile - 1;
+            if (lane == 0) st_relaxed_u64(my_status, make_status(epoch, 1u, tile_sum));
             bool timed_out = false;
-            while (true) {
-                const int64_t idx = pos - lane;
-                uint32_t flag = 2u, val = 0u;  // lanes before the segment start act as a zero prefix
-                if (idx >= (int64_t)seg_first) {
-                    uint32_t ns = 32;
-                    for (uint32_t round = 0;; ++round) {
-                        uint64_t w = ld_acquire_u64(status + idx);
-                        uint32_t hi = (uint32_t)(w >> 32);
-                        if ((hi >> 2) == epoch && (hi & 3u) != 0) {
-                            flag = hi & 3u;
-                            val = (uint32_t)w;
-                            break;
-                        }
-                        if (round >= wait_limit) {
-                            timed_out = true;
-                            break;
-                        }
-                        __nanosleep(ns);
-                        if (ns < 1024) ns <<= 1;
-                    }
-                }
-                const uint32_t prefix_mask = __ballot_sync(0xFFFFFFFFu, flag == 2u);
-                // Sum lanes up to and including the nearest inclusive prefix.
-                const uint32_t stop = prefix_mask ? (uint32_t)(__ffs(prefix_mask) - 1) : 31u;
-                uint32_t contrib = (lane <= stop) ? val : 0u;
-#pragma unroll
-                for (int d = 16; d > 0; d >>= 1) contrib += __shfl_xor_sync(0xFFFFFFFFu, contrib, d);
-                prefix += contrib;
-                if (prefix_mask) break;
-                pos -= 32;
-            }
+            prefix = warp_lookback(status, tile, tile - tile_in_seg, epoch, lane, wait_limit, timed_out);
             if (__any_sync(0xFFFFFFFFu, timed_out) && lane == 0) VREN_RECORD_ERROR(VREN_ERR_TIMEOUT);
-            if (lane == 0) st_release_u64(my_status, make_status(epoch, 2u, prefix + tile_sum));
+            if (lane == 0) st_relaxed_u64(my_status, make_status(epoch, 2u, prefix + tile_sum));
         }
         if (lane == 0) {
             s_prefix = prefix;
@@ -174,17 +182,19 @@ __global__ void __launch_bounds__(kScanThreads) exclusive_scan_kernel(
         }
     }
     __syncthreads();
-    const uint32_t offset = s_prefix + warp_prefix + (incl - thread_sum);
+    const uint32_t base_off = s_prefix + warp_prefix;
 
-    if (full && aligned) {
-        uint4* p = reinterpret_cast<uint4*>(seg_data + base);
 #pragma unroll
-        for (int k = 0; k < kScanItems / 4; ++k)
-            p[k] = make_uint4(v[4 * k] + offset, v[4 * k + 1] + offset, v[4 * k + 2] + offset, v[4 * k + 3] + offset);
-    } else {
+    for (int k = 0; k < kSlices; ++k) {
+        const uint32_t b = warp_base + k * 128 + lane * 4;
+        const uint32_t o = base_off + lane_off[k];
+        if (vec) {
+            *reinterpret_cast<uint4*>(seg_data + b) = make_uint4(v[k][0] + o, v[k][1] + o, v[k][2] + o, v[k][3] + o);
+        } else {
 #pragma unroll
-        for (int k = 0; k < kScanItems; ++k)
-            if (base + k < n) seg_data[base + k] = v[k] + offset;
+            for (int j = 0; j < 4; ++j)
+                if (b + j < n) seg_data[b + j] = v[k][j] + o;
+        }
     }
     }
 
