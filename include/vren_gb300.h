@@ -108,6 +108,15 @@ size_t vren_exclusive_scan_scratch_bytes(uint32_t n, uint32_t blocks);
 int vren_exclusive_scan_u32(vren_stream_t s, uint32_t* data, uint32_t n, uint32_t blocks,
                             void* scratch);
 
+/* Same result as vren_exclusive_scan_u32, for callers that cannot provide scratch memory (an
+ * engine allocator that owns all device memory, a plugin without access to an allocator, a frame
+ * loop that must not call cudaMalloc): no counterpart in the reference.  Allocates nothing; the
+ * look-back scratch is a fixed 32 KiB device array inside the library, so n * blocks must not
+ * exceed 2^24 elements (VREN_ERR_CAPACITY otherwise).  Calls share that array: calls that overlap
+ * on the GPU race and must be serialised by the caller.  The first call on a device resolves the
+ * array's address and should come before any stream capture. */
+int vren_exclusive_scan_u32_noalloc(vren_stream_t s, uint32_t* data, uint32_t n, uint32_t blocks);
+
 /* The reference's public down-sweep (blelloch_scan.cpp:107-189) applied to a buffer that
  * holds an up-sweep tree: n must be a power of two.  For n >= 1024 the root value is
  * kept unless `clear_last`; for n < 1024 the reference's single work-group pass always

@@ -38,6 +38,7 @@ PROTOTYPES: dict[str, tuple] = {
     "vren_exclusive_scan_scratch_bytes": (sz, [u32, u32]),
     "vren_exclusive_scan_u32": (i32, [vp, vp, u32, u32, vp]),
     "vren_scan_downsweep_u32": (i32, [vp, vp, u32, u32, i32]),
+    "vren_exclusive_scan_u32_noalloc": (i32, [vp, vp, u32, u32]),
     "vren_radix_sort_scratch1_bytes": (sz, [u32, u32]),
     "vren_radix_sort_u32": (i32, [vp, vp, u32, vp, vp]),
     "vren_radix_sort_u32_ex": (i32, [vp, vp, vp, u32, u32, vp, vp, vp]),

@@ -316,3 +316,70 @@ extern "C" int vren_scan_downsweep_u32(vren_stream_t s, uint32_t* data, uint32_t
     const int keep_root = (n >= 1024 && !clear_last) ? 1 : 0;
     return downsweep_level(as_stream(s), data, n, blocks, 1, log2n, keep_root);
 }
+
+// ================================================================================================
+// Exclusive scan without any allocation by the caller.
+//
+// Some callers cannot hand the library a scratch buffer: code that runs inside an engine whose
+// allocator owns all device memory and forbids extra allocations, plugins loaded into a host
+// application that exposes no allocator, or frame loops that must not call cudaMalloc because it
+// can synchronise the device.  For them this variant keeps the look-back scratch in a fixed
+// device array that is part of the library image: every GPU that loads the library holds it
+// (32 KiB + 16 B) until the process exits.  The largest input is therefore bounded:
+// n * blocks <= kNoAllocMaxElements (2^24 elements); larger inputs are rejected with
+// VREN_ERR_CAPACITY before anything is enqueued.
+//
+// All calls share the array and it keeps the last call's contents, so each call first clears the
+// part it uses (tickets, epoch, one status word per tile) with cudaMemsetAsync on the caller's
+// stream.  Two calls that overlap on the GPU (other streams, other host threads) race on the array
+// and must be serialised by the caller.  The first call on a device looks the array's device
+// address up (cudaGetSymbolAddress, with that device current) and caches it; make that first call
+// before capturing a stream into a CUDA graph.
+// ================================================================================================
+#include <mutex>
+
+namespace vren_gb300 {
+constexpr uint32_t kNoAllocMaxElements = 1u << 24;
+constexpr uint32_t kNoAllocMaxTiles = kNoAllocMaxElements / kScanTile;  // 4096
+constexpr uint32_t kNoAllocWords = kScanHeaderWords + 2u * kNoAllocMaxTiles;
+
+static __device__ __align__(256) uint32_t g_noalloc_scan_scratch[kNoAllocWords];
+
+constexpr int kNoAllocMaxDevices = 64;
+static std::mutex g_noalloc_mutex;
+static void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// Device address of g_noalloc_scan_scratch on the current device (looked up once per device).
+static int noalloc_scratch(uint32_t** out)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) return VREN_ERR_CUDA;
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (g_noalloc_ptr[dev] == nullptr) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_scan_scratch) != cudaSuccess || p == nullptr) return VREN_ERR_CUDA;
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = static_cast<uint32_t*>(g_noalloc_ptr[dev]);
+    return VREN_OK;
+}
+}  // namespace vren_gb300
+
+extern "C" int vren_exclusive_scan_u32_noalloc(vren_stream_t s, uint32_t* data, uint32_t n, uint32_t blocks)
+{
+    if (blocks == 0 || (n > 0 && !data)) return VREN_ERR_ARG;
+    if (n == 0) return VREN_OK;
+    if ((uint64_t)n * blocks > kNoAllocMaxElements) return VREN_ERR_CAPACITY;
+    const uint32_t tiles_per_seg = (n + kScanTile - 1) / kScanTile;
+    const uint32_t total = tiles_per_seg * blocks;
+    if (total > kNoAllocMaxTiles) return VREN_ERR_CAPACITY;
+    uint32_t* scratch = nullptr;
+    int rc = noalloc_scratch(&scratch);
+    if (rc != VREN_OK) return rc;
+    cudaStream_t st = as_stream(s);
+    VREN_CUDA_TRY(cudaMemsetAsync(scratch, 0, (kScanHeaderWords + 2u * total) * sizeof(uint32_t), st));
+    exclusive_scan_kernel<<<total, kScanThreads, 0, st>>>(data, data, n, tiles_per_seg, total, scratch, g_wait_limit,
+                                                          nullptr, nullptr);
+    VREN_LAUNCH_CHECK();
+    return VREN_OK;
+}
