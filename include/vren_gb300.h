@@ -293,6 +293,54 @@ int vren_cs_assign_lights(vren_stream_t s, const uint32_t* cluster_keys, const u
                           const float* leaf_spheres, uint32_t* counts, uint32_t* offsets, uint32_t* indices,
                           uint32_t index_capacity, uint32_t* total, void* scratch);
 
+/* shade (clustered_shading.cpp:696-811, shade.comp:69-141, pbr.glsl:6-112): per on-screen pixel
+ * whose view depth is below far - 0.001, Cook-Torrance/GGX over the lights of its cluster plus the
+ * directional lights (the reference's constants: PI = 3.14, NDF with a = roughness, Smith with
+ * k = roughness); VREN_CS_SHADE_COLOR adds 0.03 * albedo and applies pow(1/2.2) like the
+ * reference, VREN_CS_SHADE_RADIANCE writes the point-light sum only (the quantity the adjoint
+ * differentiates).  Falloff: VREN_CS_FALLOFF_REF = 1 - min(d/r, 1)^1.5 (pbr.glsl:231);
+ * VREN_CS_FALLOFF_WINDOWED_INV_SQ = saturate(1 - (d/r)^4)^2 / (d^2 + 1) (Karis 2013).
+ * Pixels that are not shaded are left untouched (the reference does not store them). */
+enum { VREN_CS_FALLOFF_REF = 0, VREN_CS_FALLOFF_WINDOWED_INV_SQ = 1 };
+enum { VREN_CS_SHADE_COLOR = 0, VREN_CS_SHADE_RADIANCE = 1 };
+
+typedef struct vren_cs_gbuffer {
+    const float* depth;     /* f32[W*H], NDC depth */
+    const float* normals;   /* f32x3[W*H], world space */
+    const float* albedo;    /* f32x3[W*H] */
+    const float* roughness; /* f32[W*H] */
+    const float* metallic;  /* f32[W*H] */
+} vren_cs_gbuffer;
+
+typedef struct vren_cs_light_lists {
+    const uint32_t* cluster_refs; /* u32[W*H] */
+    const uint32_t* counts;       /* per cluster */
+    const uint32_t* offsets;      /* per cluster */
+    const uint32_t* indices;      /* light indices */
+} vren_cs_light_lists;
+
+/* directional_lights: {float direction[3], pad, color[3], pad}[count] (gpu_repr.hpp:151-155) */
+int vren_cs_shade(vren_stream_t s, const vren_cs_frame* frame, uint32_t width, uint32_t height,
+                  const vren_cs_gbuffer* gbuffer, const vren_cs_light_lists* lists, const float* light_positions,
+                  const float* point_lights, uint32_t light_count, const float* directional_lights,
+                  uint32_t directional_count, int falloff, int output_mode, float* out_rgb /* f32x3[W*H] */);
+
+/* Adjoint of VREN_CS_SHADE_RADIANCE (no counterpart in the reference): given the upstream gradient
+ * G (f32x3[W*H]) of a scalar loss with respect to the radiance image, writes dLoss/d(light
+ * position) (f32x3[L]), dLoss/d(light colour) (f32x3[L]) and dLoss/d(light radius) (f32[L]), the
+ * light-to-cluster assignment being held fixed.  Per-light terms are recomputed, nothing per
+ * (pixel, light) pair is stored: one CTA per 32x32 tile sums each of its (cluster, light) slots
+ * over the tile's pixels in a fixed order, the slots are grouped by light with the stable bucket
+ * sort, and each light's slots are summed in slot order — the result is deterministic.
+ * `assignments` is the number of assigned (cluster, light) pairs (the `total` output of
+ * vren_cs_assign_lights, read on the host); light_count <= 65536. */
+size_t vren_cs_shade_backward_scratch_bytes(uint32_t light_count, uint32_t assignments);
+int vren_cs_shade_backward(vren_stream_t s, const vren_cs_frame* frame, uint32_t width, uint32_t height,
+                           const vren_cs_gbuffer* gbuffer, const vren_cs_light_lists* lists, uint32_t assignments,
+                           const float* light_positions, const float* point_lights, uint32_t light_count,
+                           int falloff, const float* grad_radiance, float* grad_positions, float* grad_colors,
+                           float* grad_radii, void* scratch);
+
 /* vren::cluster_and_shade: owns its buffers (an arena sized at creation) and runs the stages above
  * for one frame.  With a non-default stream the sequence is captured once into a CUDA graph per
  * frame shape and replayed. */

@@ -54,6 +54,13 @@ void vren_gen_depth_planes(uint64_t seed, const vren_scene_camera* cam, uint32_t
 void vren_gen_lights(uint64_t seed, const vren_scene_camera* cam, uint32_t count, float* positions,
                      float* lights);
 
+/* Point lights placed on visible surfaces of a depth buffer (a random pixel closer than the far
+ * plane, pulled towards the camera by 10-60 % of the light's radius); radius lognormal(ln 2, 0.5),
+ * colour uniform [0,1]^3.  Used by the differentiable-shading workload, where lights spread over the
+ * whole frustum box would leave most gradients zero. */
+void vren_gen_lights_near_surfaces(uint64_t seed, const vren_scene_camera* cam, const float* depth, uint32_t count,
+                                   float* positions, float* lights);
+
 /* G-buffer material channels: normals uniform on the hemisphere facing the camera (n.z <= 0),
  * albedo uniform [0,1]^3, roughness uniform [0.05, 1], metallic Bernoulli(0.5) in {0, 1}.
  * Any output may be NULL. */

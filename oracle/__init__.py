@@ -36,6 +36,9 @@ _PROTOS = {
     "oracle_cs_light_bvh": (None, [vp, vp, u32, vp, u32, vp, vp, vp]),
     "oracle_cs_find_unique_clusters": (u32, [vp, vp, u32, u32, vp, i32, vp, u32, vp, i32]),
     "oracle_cs_assign_lights": (u64, [vp, u32, u32, u32, vp, vp, u32, vp, vp, vp, vp, vp, u64, i32]),
+    "oracle_cs_shade_f64": (None, [vp, u32, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, u32, i32, i32, vp, vp, i32]),
+    "oracle_cs_shade_grad_f64": (None, [vp, u32, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, u32, i32, vp, vp, i32]),
+    "oracle_cs_shade_light_loss_f64": (C.c_double, [vp, u32, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, u32, vp, i32, vp]),
 }
 
 OPS = {"add": 0, "min": 1, "max": 2}
@@ -192,3 +195,40 @@ def cs_assign_lights(keys, W: int, H: int, view, bvh, L: int, light_index, view_
                                           _p(np.ascontiguousarray(view_pos, np.float32)), _p(counts), _p(offsets),
                                           _p(indices), cap, threads)
     return counts[:U], offsets[:U], indices[: min(total, cap)].copy(), int(total)
+
+
+# ---- shading (FP64) -----------------------------------------------------------------------------
+def _f32(a):
+    return np.ascontiguousarray(a, np.float32)
+
+
+def _u32(a):
+    return np.ascontiguousarray(a, np.uint32)
+
+
+def cs_shade_f64(view, W, H, gb, lists, lpos, lights, L, falloff=1, mode=1, threads=0):
+    """gb = (depth, normals, albedo, roughness, metallic); lists = (refs, counts, offsets, indices)."""
+    out = np.zeros(W * H * 3, np.float64)
+    shaded = np.zeros(W * H, np.uint8)
+    g = [_f32(x) for x in gb]
+    ls = [_u32(x) for x in lists]
+    lib().oracle_cs_shade_f64(_view_ptr(view), W, H, *(_p(x) for x in g), *(_p(x) for x in ls), _p(_f32(lpos)),
+                              _p(_f32(lights)), L, falloff, mode, _p(out), _p(shaded), threads or 8)
+    return out, shaded.astype(bool)
+
+
+def cs_shade_grad_f64(view, W, H, gb, lists, lpos, lights, L, grad, falloff=1, threads=0):
+    g7 = np.zeros(L * 7, np.float64)
+    g = [_f32(x) for x in gb]
+    ls = [_u32(x) for x in lists]
+    lib().oracle_cs_shade_grad_f64(_view_ptr(view), W, H, *(_p(x) for x in g), *(_p(x) for x in ls),
+                                   _p(_f32(lpos)), _p(_f32(lights)), L, falloff, _p(_f32(grad)), _p(g7), threads or 8)
+    return g7.reshape(L, 7)
+
+
+def cs_shade_light_loss_f64(view, W, H, gb, lists, l, theta, grad, falloff=1):
+    g = [_f32(x) for x in gb]
+    ls = [_u32(x) for x in lists]
+    th = np.ascontiguousarray(theta, np.float64)
+    return float(lib().oracle_cs_shade_light_loss_f64(_view_ptr(view), W, H, *(_p(x) for x in g),
+                                                      *(_p(x) for x in ls), l, _p(th), falloff, _p(_f32(grad))))

@@ -15,20 +15,37 @@ ORACLE_DIR = Path(__file__).resolve().parent
 BUILD_DIR = ORACLE_DIR / "_build"
 LIB = BUILD_DIR / "libvren_oracle.so"
 SOURCES = [ORACLE_DIR / "vren_oracle.c"]
+CXX_SOURCES = [ORACLE_DIR / "vren_oracle_shade.cpp"]
 HEADERS = [ORACLE_DIR / "vren_oracle.h"]
 
 
 def build(verbose: bool = False) -> Path:
     BUILD_DIR.mkdir(exist_ok=True)
-    deps = SOURCES + HEADERS
+    deps = SOURCES + CXX_SOURCES + HEADERS
     if LIB.exists() and all(d.stat().st_mtime <= LIB.stat().st_mtime for d in deps):
         return LIB
     cc = shutil.which("gcc") or shutil.which("cc")
-    if cc is None:
-        raise RuntimeError("gcc is required to build the oracle")
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cc is None or cxx is None:
+        raise RuntimeError("gcc and g++ are required to build the oracle")
     tmp = LIB.with_suffix(".so.tmp")
-    cmd = [cc, "-O2", "-std=gnu11", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", "-fopenmp",
-           *map(str, SOURCES), "-o", str(tmp), "-lm"]
+    common = ["-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", f"-I{ORACLE_DIR}"]
+    objs = []
+    for src in SOURCES:
+        obj = BUILD_DIR / (src.stem + ".o")
+        cmd = [cc, "-std=gnu11", *common, "-c", str(src), "-o", str(obj)]
+        if verbose:
+            print(" ".join(cmd))
+        subprocess.run(cmd, check=True)
+        objs.append(obj)
+    for src in CXX_SOURCES:
+        obj = BUILD_DIR / (src.stem + ".o")
+        cmd = [cxx, "-std=c++17", *common, "-c", str(src), "-o", str(obj)]
+        if verbose:
+            print(" ".join(cmd))
+        subprocess.run(cmd, check=True)
+        objs.append(obj)
+    cmd = [cxx, "-shared", "-fopenmp", *map(str, objs), "-o", str(tmp), "-lm"]
     if verbose:
         print(" ".join(cmd))
     subprocess.run(cmd, check=True)

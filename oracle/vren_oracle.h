@@ -105,6 +105,23 @@ uint64_t oracle_cs_assign_lights(const uint32_t* keys, uint32_t U, uint32_t W, u
                                  const float* view_pos, uint32_t* counts, uint32_t* offsets, uint32_t* indices,
                                  uint64_t index_cap, int threads);
 
+/* ---- shading in FP64 (vren_oracle_shade.cpp): forward, forward-mode gradient, per-light loss ---- */
+void oracle_cs_shade_f64(const oracle_cs_view* v, uint32_t W, uint32_t H, const float* depth, const float* normals,
+                         const float* albedo, const float* rough, const float* metal, const uint32_t* refs,
+                         const uint32_t* counts, const uint32_t* offsets, const uint32_t* indices, const float* lpos,
+                         const float* lights, uint32_t L, int falloff, int mode, double* out, uint8_t* shaded,
+                         int threads);
+void oracle_cs_shade_grad_f64(const oracle_cs_view* v, uint32_t W, uint32_t H, const float* depth,
+                              const float* normals, const float* albedo, const float* rough, const float* metal,
+                              const uint32_t* refs, const uint32_t* counts, const uint32_t* offsets,
+                              const uint32_t* indices, const float* lpos, const float* lights, uint32_t L, int falloff,
+                              const float* grad, double* g7, int threads);
+double oracle_cs_shade_light_loss_f64(const oracle_cs_view* v, uint32_t W, uint32_t H, const float* depth,
+                                      const float* normals, const float* albedo, const float* rough, const float* metal,
+                                      const uint32_t* refs, const uint32_t* counts, const uint32_t* offsets,
+                                      const uint32_t* indices, uint32_t l, const double* theta, int falloff,
+                                      const float* grad);
+
 #ifdef __cplusplus
 }
 #endif

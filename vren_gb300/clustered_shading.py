@@ -202,6 +202,67 @@ def _cudart():
     return _CUDART
 
 
+FALLOFF = {"ref": 0, "windowed_inv_sq": 1}
+SHADE_MODE = {"color": 0, "radiance": 1}
+
+
+class GBuffer(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in ("depth", "normals", "albedo", "roughness", "metallic")]
+
+
+class LightLists(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in ("cluster_refs", "counts", "offsets", "indices")]
+
+
+def _addr(x):
+    if x is None:
+        return None
+    return x.data_ptr() if isinstance(x, torch.Tensor) else int(x)
+
+
+def gbuffer(depth, normals, albedo, roughness, metallic) -> GBuffer:
+    return GBuffer(*(_addr(t) for t in (depth, normals, albedo, roughness, metallic)))
+
+
+def light_lists(cluster_refs, counts, offsets, indices) -> LightLists:
+    return LightLists(*(_addr(t) for t in (cluster_refs, counts, offsets, indices)))
+
+
+class shade:
+    """vren::clustered_shading::shade (clustered_shading.hpp:114-140)."""
+
+    def __init__(self, falloff: str = "ref", mode: str = "color"):
+        self.falloff = FALLOFF[falloff]
+        self.mode = SHADE_MODE[mode]
+
+    def __call__(self, stream, frame_dev, width: int, height: int, gbuf: GBuffer, lists: LightLists, positions,
+                 lights, light_count: int, out: torch.Tensor, directional=None, directional_count: int = 0):
+        check(lib().vren_cs_shade(_stream(stream), _addr(frame_dev), width, height, C.byref(gbuf), C.byref(lists),
+                                  _addr(positions), _addr(lights), light_count, _addr(directional), directional_count,
+                                  self.falloff, self.mode, _addr(out)), "shade")
+
+
+class shade_backward:
+    """Adjoint of the radiance image with respect to point-light positions, colours and radii."""
+
+    def __init__(self, falloff: str = "windowed_inv_sq"):
+        self.falloff = FALLOFF[falloff]
+        self._scratch = None
+
+    def __call__(self, stream, frame_dev, width: int, height: int, gbuf: GBuffer, lists: LightLists,
+                 assignments: int, positions, lights, light_count: int, grad_radiance, grad_positions, grad_colors,
+                 grad_radii):
+        need = int(lib().vren_cs_shade_backward_scratch_bytes(light_count, assignments)) + 256
+        dev = grad_radiance.device
+        if self._scratch is None or self._scratch.numel() * 4 < need:
+            self._scratch = alloc_scratch(need, dev)
+        sc = (self._scratch.data_ptr() + 255) // 256 * 256
+        check(lib().vren_cs_shade_backward(_stream(stream), _addr(frame_dev), width, height, C.byref(gbuf),
+                                           C.byref(lists), assignments, _addr(positions), _addr(lights), light_count,
+                                           self.falloff, _addr(grad_radiance), _addr(grad_positions),
+                                           _addr(grad_colors), _addr(grad_radii), sc), "shade_backward")
+
+
 def read_device(ptr: int, count: int, dtype=np.uint32) -> np.ndarray:
     """Copies `count` elements at a device address into a numpy array (synchronizes)."""
     out = np.empty(count, dtype=dtype)

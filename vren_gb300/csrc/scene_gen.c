@@ -237,3 +237,47 @@ void vren_gen_normal01(uint64_t seed, uint64_t stream, float* out, uint64_t n, i
         for (uint64_t i = (uint64_t)c * chunk; i < end; ++i) out[i] = (float)std_normal(&rng);
     }
 }
+
+void vren_gen_lights_near_surfaces(uint64_t seed, const vren_scene_camera* cam, const float* depth, uint32_t count,
+                                   float* positions, float* lights)
+{
+    const double W = cam->width, H = cam->height;
+    const double aspect = W / H;
+    const double t = tan((double)cam->fov_y * 0.5);
+    const double n_ = cam->near_plane, f_ = cam->far_plane;
+    const double m22 = f_ / (f_ - n_), m32 = -(f_ * n_) / (f_ - n_);
+    vren_pcg32 rng;
+    vren_pcg32_seed(&rng, seed, 303u);
+    for (uint32_t i = 0; i < count; ++i) {
+        double p[3] = {0.0, 0.0, 0.5 * (n_ + f_)};
+        for (int attempt = 0; attempt < 64; ++attempt) {
+            const uint32_t x = vren_pcg32_next(&rng) % cam->width, y = vren_pcg32_next(&rng) % cam->height;
+            const double D = depth[(size_t)y * cam->width + x];
+            const double z = m32 / (D - m22);
+            if (!(z < f_ * 0.999)) continue;
+            const double ndc_x = 2.0 * ((double)x + 0.5) / W - 1.0, ndc_y = 1.0 - 2.0 * ((double)y + 0.5) / H;
+            p[0] = ndc_x * t * aspect * z;
+            p[1] = ndc_y * t * z;
+            p[2] = z;
+            break;
+        }
+        const double r = exp(log(2.0) + 0.5 * std_normal(&rng));
+        /* pull the light towards the camera by 10-60 % of its radius so it lights the surface */
+        const double len = sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
+        const double back = (0.1 + 0.5 * uniform01(&rng)) * r;
+        const double s = len > back ? (len - back) / len : 0.5;
+        const double cr = uniform01(&rng), cg = uniform01(&rng), cb = uniform01(&rng);
+        if (positions) {
+            positions[4 * i + 0] = (float)(p[0] * s);
+            positions[4 * i + 1] = (float)(p[1] * s);
+            positions[4 * i + 2] = (float)(p[2] * s);
+            positions[4 * i + 3] = 1.0f;
+        }
+        if (lights) {
+            lights[4 * i + 0] = (float)cr;
+            lights[4 * i + 1] = (float)cg;
+            lights[4 * i + 2] = (float)cb;
+            lights[4 * i + 3] = (float)r;
+        }
+    }
+}

@@ -29,6 +29,7 @@ def lib() -> C.CDLL:
         _LIB.vren_gen_lights.argtypes = [u64, vp, u32, vp, vp]
         _LIB.vren_gen_gbuffer.argtypes = [u64, u32, u32, vp, vp, vp, vp, i32]
         _LIB.vren_gen_normal01.argtypes = [u64, u64, vp, u64, i32]
+        _LIB.vren_gen_lights_near_surfaces.argtypes = [u64, vp, vp, u32, vp, vp]
     return _LIB
 
 
@@ -78,3 +79,13 @@ def normal01(seed: int, stream: int, n: int, threads: int = 0) -> np.ndarray:
     out = np.empty(n, np.float32)
     lib().vren_gen_normal01(seed, stream, _p(out), n, threads)
     return out
+
+
+def lights_near_surfaces(seed: int, count: int, depth: np.ndarray, width: int, height: int, fov_y_deg: float = 45.0,
+                         near: float = 0.1, far: float = 1000.0):
+    cam = scene_camera(width, height, fov_y_deg, near, far)
+    pos = np.empty(count * 4, np.float32)
+    li = np.empty(count * 4, np.float32)
+    d = np.ascontiguousarray(depth, np.float32)
+    lib().vren_gen_lights_near_surfaces(seed, C.byref(cam), _p(d), count, _p(pos), _p(li))
+    return pos, li
