@@ -61,6 +61,18 @@ int vren_device_error(int clear);
  * previous value. */
 uint32_t vren_set_wait_limit(uint32_t rounds);
 
+/* Kernel variant knobs, read when work is enqueued (no counterpart in the reference; the autotuner
+ * and benchmarks set them).  Every variant gives identical results.
+ *   VREN_TUNE_SCAN_SLICES  128-element slices per warp in a scan tile: 4 (4096/tile) or 8 (8192/tile)
+ *   VREN_TUNE_SPIN_POLLS   look-back polls before a waiting thread starts to back off with nanosleep
+ *   VREN_TUNE_RADIX_RANK   digit ranking in a sort pass: 0 = one ballot per digit bit,
+ *                          1 = match.any + shared-memory atomic per peer group
+ *   VREN_TUNE_RADIX_ITEMS  keys per thread in a sort pass: 0 = 15/16 (3840/4096 per tile), 1 = 23/24 */
+enum { VREN_TUNE_SCAN_SLICES = 0, VREN_TUNE_SPIN_POLLS = 1, VREN_TUNE_RADIX_RANK = 2, VREN_TUNE_RADIX_ITEMS = 3,
+       VREN_TUNE_COUNT = 4 };
+int vren_tuning_set(int knob, int value);
+int vren_tuning_get(int knob);
+
 /* ------------------------------------------------------------------------------------------------
  * Size helpers (vren/vren/base/base.hpp:281-328, integer restatements)
  * ------------------------------------------------------------------------------------------------ */

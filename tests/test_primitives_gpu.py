@@ -310,3 +310,65 @@ def test_build_bvh_bad_length(cuda):
     buf = torch.zeros(64 * 8, dtype=torch.int32, device=cuda)
     with pytest.raises(ValueError):
         vg.build_bvh()(None, buf, 64)
+
+
+# ------------------------------------------------------------------------------------------------
+# Tuning variants give identical results
+# ------------------------------------------------------------------------------------------------
+@pytest.fixture
+def restore_tuning(native):
+    saved = {k: native.vren_tuning_get(v) for k, v in vg._lib.TUNE.items()}
+    yield native
+    for k, v in saved.items():
+        native.vren_tuning_set(vg._lib.TUNE[k], v)
+
+
+@pytest.mark.parametrize("rank", [0, 1])
+@pytest.mark.parametrize("items", [0, 1])
+@pytest.mark.parametrize("spin", [0, 64])
+def test_radix_variants_identical(cuda, restore_tuning, rank, items, spin):
+    lib = restore_tuning
+    assert lib.vren_tuning_set(vg._lib.TUNE["radix_rank"], rank) == 0
+    assert lib.vren_tuning_set(vg._lib.TUNE["radix_items"], items) == 0
+    assert lib.vren_tuning_set(vg._lib.TUNE["spin_polls"], spin) == 0
+    rng = np.random.default_rng(rank * 4 + items)
+    n = (1 << 20) + 13
+    keys = rng.integers(0, 2**32, n, dtype=np.uint64).astype(np.uint32)
+    keys[::3] = keys[1::3][: len(keys[::3])]
+    vals = np.arange(n, dtype=np.uint32)
+    for bits in (8, 6, 4):
+        rs = vg.radix_sort(bits)
+        k, v = dev_u32(keys, cuda), dev_u32(vals, cuda)
+        rs.sort(None, k, v, n, rs.create_scratch_buffer_1(n, cuda), torch.empty_like(k), torch.empty_like(v))
+        ek, ev = oracle.stable_sort_u32(keys, vals)
+        assert np.array_equal(host_u32(k), ek) and np.array_equal(host_u32(v), ev), bits
+    pairs = np.stack([keys[:200000], vals[:200000]], 1).reshape(-1)
+    for kb in (16, 10):
+        bs = vg.bucket_sort(kb)
+        out = torch.zeros(bs.get_required_output_buffer_size(200000) // 4, dtype=torch.int32, device=cuda)
+        bs(None, dev_u32(pairs, cuda), 200000, 0, out, 0)
+        ep, ee = oracle.bucket_sort_u32x2(pairs.reshape(-1, 2), kb)
+        got = host_u32(out)
+        assert np.array_equal(got[: 400000].reshape(-1, 2), ep)
+
+
+@pytest.mark.parametrize("slices", [4, 8])
+@pytest.mark.parametrize("spin", [0, 64, 4096])
+def test_scan_variants_identical(cuda, restore_tuning, slices, spin):
+    lib = restore_tuning
+    assert lib.vren_tuning_set(vg._lib.TUNE["scan_slices"], slices) == 0
+    assert lib.vren_tuning_set(vg._lib.TUNE["spin_polls"], spin) == 0
+    rng = np.random.default_rng(slices + spin)
+    scan = vg.blelloch_scan()
+    for n, blocks in ((1, 1), (8191, 1), (8193, 3), ((1 << 22) + 5, 1)):
+        x = rng.integers(0, 256, n * blocks).astype(np.uint32)
+        buf = dev_u32(x, cuda)
+        scan(None, buf, n, 0, blocks)
+        got = host_u32(buf).reshape(blocks, n)
+        for b in range(blocks):
+            assert np.array_equal(got[b], oracle.exclusive_scan_u32(x[b * n:(b + 1) * n]))
+
+
+def test_tuning_rejects_unknown_values(native):
+    assert native.vren_tuning_set(vg._lib.TUNE["scan_slices"], 5) == vg._lib.VREN_ERR_ARG
+    assert native.vren_tuning_set(99, 1) == vg._lib.VREN_ERR_ARG

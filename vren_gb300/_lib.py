@@ -18,6 +18,7 @@ VREN_ERR_CUDA = 4
 VREN_ERR_STATE = 5
 
 REDUCE_OPS = {"add": 0, "min": 1, "max": 2}
+TUNE = {"scan_slices": 0, "spin_polls": 1, "radix_rank": 2, "radix_items": 3}
 
 u32, u64, i32, sz, vp, fp = C.c_uint32, C.c_uint64, C.c_int, C.c_size_t, C.c_void_p, C.c_float
 
@@ -26,6 +27,8 @@ PROTOTYPES: dict[str, tuple] = {
     "vren_status_string": (C.c_char_p, [i32]),
     "vren_device_error": (i32, [i32]),
     "vren_set_wait_limit": (u32, [u32]),
+    "vren_tuning_set": (i32, [i32, i32]),
+    "vren_tuning_get": (i32, [i32]),
     "vren_round_to_next_power_of_2": (u32, [u32]),
     "vren_round_to_next_power_of": (u32, [u32, u32]),
     "vren_divide_and_ceil": (u32, [u32, u32]),

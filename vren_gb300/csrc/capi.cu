@@ -44,6 +44,42 @@ extern "C" int vren_device_error(int clear)
     return first;
 }
 
+namespace vren_gb300 {
+// Kernel variant knobs (tile sizes, ranking method, polling policy), set by the autotuner or the
+// caller; every launcher reads its knob when it enqueues work.
+static int g_tuning[VREN_TUNE_COUNT] = {
+    /* VREN_TUNE_SCAN_SLICES */ 4,
+    /* VREN_TUNE_SPIN_POLLS */ 64,
+    /* VREN_TUNE_RADIX_RANK */ 0,
+    /* VREN_TUNE_RADIX_ITEMS */ 0,
+};
+int tuning(int knob) { return (knob >= 0 && knob < VREN_TUNE_COUNT) ? g_tuning[knob] : 0; }
+}  // namespace vren_gb300
+
+extern "C" int vren_tuning_set(int knob, int value)
+{
+    if (knob < 0 || knob >= VREN_TUNE_COUNT) return VREN_ERR_ARG;
+    switch (knob) {
+    case VREN_TUNE_SCAN_SLICES:
+        if (value != 4 && value != 8) return VREN_ERR_ARG;
+        break;
+    case VREN_TUNE_SPIN_POLLS:
+        if (value < 0 || value > (1 << 20)) return VREN_ERR_ARG;
+        break;
+    case VREN_TUNE_RADIX_RANK:
+        if (value != 0 && value != 1) return VREN_ERR_ARG;
+        break;
+    case VREN_TUNE_RADIX_ITEMS:
+        if (value != 0 && value != 1) return VREN_ERR_ARG;
+        break;
+    default: break;
+    }
+    g_tuning[knob] = value;
+    return VREN_OK;
+}
+
+extern "C" int vren_tuning_get(int knob) { return tuning(knob); }
+
 extern "C" uint32_t vren_set_wait_limit(uint32_t rounds)
 {
     uint32_t prev = g_wait_limit;

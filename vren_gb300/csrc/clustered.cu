@@ -38,8 +38,8 @@ __device__ __forceinline__ uint32_t discretize_normal(float nx, float ny, float 
     uint32_t axis = 0, face = 0;
 #pragma unroll
     for (uint32_t i = 0; i < 3; ++i) {
-        const float sg = n[i] > 0.0f ? 1.0f : (n[i] < 0.0f ? -1.0f : 0.0f);
-        const float t = fdiv(sg, n[i]);
+        // sign(n)/n: +-1/n correctly rounded is |rcp_rn(n)|; 0/0 (and NaN) never compare below min_t
+        const float t = n[i] != 0.0f ? fabsf(__frcp_rn(n[i])) : __int_as_float(0x7FC00000);
         if (t < min_t) {
             min_t = t;
             axis = i;
@@ -48,8 +48,9 @@ __device__ __forceinline__ uint32_t discretize_normal(float nx, float ny, float 
     }
     const float u = fmul(n[(axis + 1) % 3], min_t);
     const float w = fmul(n[(axis + 2) % 3], min_t);
-    const uint32_t du = floor_to_u32(fmul(fdiv(fadd(u, 1.0f), 2.0f), 3.0f));
-    const uint32_t dw = floor_to_u32(fmul(fdiv(fadd(w, 1.0f), 2.0f), 3.0f));
+    // x / 2 and x * 0.5 are the same correctly rounded value
+    const uint32_t du = floor_to_u32(fmul(fmul(fadd(u, 1.0f), 0.5f), 3.0f));
+    const uint32_t dw = floor_to_u32(fmul(fmul(fadd(w, 1.0f), 0.5f), 3.0f));
     return (face * 9u + du * 3u + dw) & 0x3Fu;
 }
 
@@ -346,7 +347,7 @@ __global__ void __launch_bounds__(kFucThreads) find_unique_kernel(
     const float* __restrict__ depth, const float* __restrict__ normals, uint32_t W, uint32_t H,
     const vren_cs_frame* __restrict__ F, uint32_t* __restrict__ keys, uint32_t key_cap,
     uint32_t* __restrict__ key_count, uint32_t* __restrict__ refs, uint32_t* __restrict__ scratch,
-    uint32_t num_tiles, uint32_t wait_limit)
+    uint32_t num_tiles, uint32_t wait_limit, uint32_t spin)
 {
     __shared__ uint32_t s_bits[2048];
     __shared__ uint32_t s_prefix[2048];
@@ -373,6 +374,12 @@ __global__ void __launch_bounds__(kFucThreads) find_unique_kernel(
     const float m2[4] = {ip[2], ip[6], ip[10], ip[14]};
     const float m3[4] = {ip[3], ip[7], ip[11], ip[15]};
     const float fW = (float)W, fH = (float)H;
+    // For a perspective projection the z and w rows of its inverse have exact zeros in the x and y
+    // columns and non-zero last coefficients.  Then X and Y only contribute signed zeros to a partial
+    // sum that is either non-zero already or followed by the non-zero last term, so skipping them
+    // leaves every bit of vz and vw unchanged.
+    const bool xy_free = m2[0] == 0.0f && m2[1] == 0.0f && m3[0] == 0.0f && m3[1] == 0.0f && m2[3] != 0.0f &&
+                         m3[3] != 0.0f;
 
     uint32_t sub[4];
 #pragma unroll
@@ -381,11 +388,17 @@ __global__ void __launch_bounds__(kFucThreads) find_unique_kernel(
         sub[q] = 0xFFFFFFFFu;
         if (skip_offscreen && (gx >= W || gy >= H)) continue;
         const uint32_t px = (gy % H) * W + (gx % W);
-        const float fx = fdiv((float)gx, fW), fy = fdiv((float)gy, fH);
-        const float X = fsub(fmul(fx, 2.0f), 1.0f), Y = fsub(fmul(fsub(1.0f, fy), 2.0f), 1.0f);
         const float D = __ldg(depth + px);
-        const float vz = fadd(fadd(fadd(fmul(m2[0], X), fmul(m2[1], Y)), fmul(m2[2], D)), fmul(m2[3], 1.0f));
-        const float vw = fadd(fadd(fadd(fmul(m3[0], X), fmul(m3[1], Y)), fmul(m3[2], D)), fmul(m3[3], 1.0f));
+        float vz, vw;
+        if (xy_free) {
+            vz = fadd(fmul(m2[2], D), m2[3]);
+            vw = fadd(fmul(m3[2], D), m3[3]);
+        } else {
+            const float fx = fdiv((float)gx, fW), fy = fdiv((float)gy, fH);
+            const float X = fsub(fmul(fx, 2.0f), 1.0f), Y = fsub(fmul(fsub(1.0f, fy), 2.0f), 1.0f);
+            vz = fadd(fadd(fadd(fmul(m2[0], X), fmul(m2[1], Y)), fmul(m2[2], D)), fmul(m2[3], 1.0f));
+            vw = fadd(fadd(fadd(fmul(m3[0], X), fmul(m3[1], Y)), fmul(m3[2], D)), fmul(m3[3], 1.0f));
+        }
         const uint32_t k = slice_of(fdiv(vz, vw), s_bound, kmax);
         const uint32_t nd = discretize_normal(__ldg(normals + 3 * px), __ldg(normals + 3 * px + 1), __ldg(normals + 3 * px + 2));
         const uint32_t s = ((k & 0x3FFu) | (nd << 10)) & 0xFFFFu;
@@ -448,8 +461,10 @@ __global__ void __launch_bounds__(kFucThreads) find_unique_kernel(
                             timed_out = true;
                             break;
                         }
-                        __nanosleep(ns);
-                        if (ns < 1024) ns <<= 1;
+                        if (round >= spin) {
+                            __nanosleep(ns);
+                            if (ns < 512) ns <<= 1;
+                        }
                     }
                 }
                 const uint32_t pm = __ballot_sync(0xFFFFFFFFu, flag == 2u);
@@ -868,7 +883,8 @@ extern "C" int vren_cs_find_unique_clusters(vren_stream_t s, const float* depth,
     const uint32_t tiles = ((width + 31) / 32) * ((height + 31) / 32);
     find_unique_kernel<<<tiles, kFucThreads, 0, as_stream(s)>>>(depth, normals, width, height, frame, cluster_keys,
                                                                 key_capacity, key_count, cluster_refs,
-                                                                static_cast<uint32_t*>(scratch), tiles, g_wait_limit);
+                                                                static_cast<uint32_t*>(scratch), tiles, g_wait_limit,
+                                                                (uint32_t)tuning(VREN_TUNE_SPIN_POLLS));
     VREN_LAUNCH_CHECK();
     return VREN_OK;
 }
@@ -941,7 +957,7 @@ int cs_enqueue(vren_cluster_and_shade* cs, cudaStream_t st, uint32_t W, uint32_t
     const uint32_t tiles = ((W + 31) / 32) * ((H + 31) / 32);
     find_unique_kernel<<<tiles, kFucThreads, 0, st>>>(depth, normals, W, H, cs->frame, cs->keys, cs->key_cap,
                                                       cs->key_count, cs->refs, static_cast<uint32_t*>(cs->fuc_scratch),
-                                                      tiles, g_wait_limit);
+                                                      tiles, g_wait_limit, (uint32_t)tuning(VREN_TUNE_SPIN_POLLS));
     VREN_LAUNCH_CHECK();
     return assign_lights(st, cs->keys, cs->key_count, cs->key_cap, cs->frame, cs->bvh, L, cs->light_index,
                          cs->view_pos, cs->spheres, cs->counts, cs->offsets, cs->indices, cs->max_assign, cs->total,

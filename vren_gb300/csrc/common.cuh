@@ -114,8 +114,10 @@ constexpr uint32_t kValueMask = (1u << kFlagShift) - 1u;
 
 // Spin until *p carries a flag; returns the word, or a prefix-flagged 0 after the wait
 // limit (and records VREN_ERR_TIMEOUT through the caller-provided error recorder).
+// The first `spin` polls re-read immediately; later ones back off with __nanosleep (32 ns doubling
+// to 512 ns).  `limit` bounds the total number of polls.
 template <typename OnTimeout>
-__device__ __forceinline__ uint32_t wait_for_flag(const uint32_t* p, uint32_t limit, OnTimeout on_timeout)
+__device__ __forceinline__ uint32_t wait_for_flag(const uint32_t* p, uint32_t limit, uint32_t spin, OnTimeout on_timeout)
 {
     uint32_t ns = 32;
     for (uint32_t round = 0;; ++round) {
@@ -125,8 +127,10 @@ __device__ __forceinline__ uint32_t wait_for_flag(const uint32_t* p, uint32_t li
             on_timeout();
             return kFlagPrefix;
         }
-        __nanosleep(ns);
-        if (ns < 1024) ns <<= 1;
+        if (round >= spin) {
+            __nanosleep(ns);
+            if (ns < 512) ns <<= 1;
+        }
     }
 }
 

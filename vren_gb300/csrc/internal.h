@@ -9,6 +9,9 @@
 
 namespace vren_gb300 {
 
+// Current value of a VREN_TUNE_* knob (capi.cu).
+int tuning(int knob);
+
 // Exclusive scan of min(*n_dev, n_cap) elements (n_cap when n_dev is null), in -> out (may alias);
 // the total is written to *total_out when given.  Scratch: scan_scratch_bytes(n_cap), zero-filled
 // before first use.

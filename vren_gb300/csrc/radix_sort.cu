@@ -138,25 +138,28 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_hist_kernel(
 }
 
 // ------------------------------------------------------------------------------------------------
-// One digit pass.
+// One digit pass.  RANK 0: peers from one ballot per digit bit and per-warp counters updated by the
+// group's first lane; RANK 1: peers from match.any and one shared-memory atomic per peer group.
+// Both give the same (stable) ranks.  Keys/values are staged in dynamic shared memory.
 // ------------------------------------------------------------------------------------------------
-template <int DIGIT_BITS, int ITEMS, int MODE>
+template <int DIGIT_BITS, int ITEMS, int MODE, int RANK>
 __global__ void __launch_bounds__(kSortThreads) onesweep_pass_kernel(
     const uint32_t* __restrict__ in_keys, const uint32_t* __restrict__ in_vals,
     uint32_t* __restrict__ out_keys, uint32_t* __restrict__ out_vals,
     uint32_t n, uint32_t pass, uint32_t shift, uint32_t width, uint32_t num_tiles,
-    uint32_t* __restrict__ scratch, uint32_t wait_limit)
+    uint32_t* __restrict__ scratch, uint32_t wait_limit, uint32_t spin)
 {
     constexpr int RADIX = 1 << DIGIT_BITS;
     constexpr int TILE = kSortThreads * ITEMS;
-    constexpr bool HAS_VALS = (MODE != kKeys);
     using Elem = typename std::conditional<MODE == kUvec2, uint2, uint32_t>::type;
 
-    __shared__ Elem s_keys[TILE];
-    __shared__ uint32_t s_vals[MODE == kPairs ? TILE : 1];
+    extern __shared__ uint4 s_stage[];
+    Elem* s_keys = reinterpret_cast<Elem*>(s_stage);
+    uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_keys + TILE);
     __shared__ uint32_t s_warp_hist[kSortWarps][RADIX];
     __shared__ uint32_t s_tile_excl[RADIX];
     __shared__ int32_t s_delta[RADIX];
+    __shared__ uint32_t s_wsum[kSortWarps];
     __shared__ uint32_t s_tile;
 
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
@@ -189,7 +192,7 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_pass_kernel(
         }
     }
 
-    // Stable in-warp ranking.
+    // Stable in-warp ranking, items in order.
 #pragma unroll
     for (int j = 0; j < ITEMS; ++j) {
         const uint32_t idx = warp_base + 32 * j + lane;
@@ -198,71 +201,72 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_pass_kernel(
         if (MODE == kUvec2) k = (reinterpret_cast<uint2*>(&key[j]))->x;
         else k = *(reinterpret_cast<uint32_t*>(&key[j]));
         const uint32_t d = valid ? digit_of(k, shift, width) : 0u;
-        uint32_t peers = __ballot_sync(0xFFFFFFFFu, valid);
+        if (RANK == 1) {
+            // invalid lanes get a value no digit can take, so they form groups of one
+            const uint32_t peers = __match_any_sync(0xFFFFFFFFu, valid ? d : (0x10000u + lane));
+            const uint32_t leader = __ffs(peers) - 1;
+            uint32_t base = 0;
+            if (valid && lane == leader) base = atomicAdd(&s_warp_hist[warp][d], (uint32_t)__popc(peers));
+            base = __shfl_sync(0xFFFFFFFFu, base, leader);
+            pos[j] = valid ? (d | ((base + __popc(peers & lanemask_lt())) << 8)) : 0xFFFFFFFFu;
+        } else {
+            uint32_t peers = __ballot_sync(0xFFFFFFFFu, valid);
 #pragma unroll
-        for (int b = 0; b < DIGIT_BITS; ++b) {
-            const bool bit = (d >> b) & 1u;
-            const uint32_t m = __ballot_sync(0xFFFFFFFFu, bit);
-            peers &= bit ? m : ~m;
+            for (int b = 0; b < DIGIT_BITS; ++b) {
+                const bool bit = (d >> b) & 1u;
+                const uint32_t m = __ballot_sync(0xFFFFFFFFu, bit);
+                peers &= bit ? m : ~m;
+            }
+            uint32_t before = 0;
+            if (valid) before = s_warp_hist[warp][d];
+            __syncwarp();
+            if (valid && (peers & lanemask_lt()) == 0) s_warp_hist[warp][d] = before + __popc(peers);
+            __syncwarp();
+            pos[j] = valid ? (d | ((before + __popc(peers & lanemask_lt())) << 8)) : 0xFFFFFFFFu;
         }
-        uint32_t before = 0;
-        if (valid) before = s_warp_hist[warp][d];
-        __syncwarp();
-        if (valid && (peers & lanemask_lt()) == 0) s_warp_hist[warp][d] = before + __popc(peers);
-        __syncwarp();
-        pos[j] = valid ? (d | ((before + __popc(peers & lanemask_lt())) << 8)) : 0xFFFFFFFFu;
     }
     __syncthreads();
 
-    // Per-digit: warp prefixes, tile count, publish, look-back.
-    for (uint32_t d = tid; d < RADIX; d += kSortThreads) {
-        uint32_t run = 0;
+    // Thread d: warp prefixes of digit d, the tile's count, publish it.
+    uint32_t count = 0;
+    if (tid < (uint32_t)RADIX) {
+        const uint32_t d = tid;
 #pragma unroll
         for (int w = 0; w < kSortWarps; ++w) {
-            uint32_t c = s_warp_hist[w][d];
-            s_warp_hist[w][d] = run;
-            run += c;
+            const uint32_t c = s_warp_hist[w][d];
+            s_warp_hist[w][d] = count;
+            count += c;
         }
-        const uint32_t count = run;
-        uint32_t* my = status + (size_t)tile * RADIX + d;
+        st_relaxed_u32(status + (size_t)tile * RADIX + d, (tile == 0 ? kFlagPrefix : kFlagAggregate) | count);
+    }
+    // Block-wide exclusive scan of the counts over digits (all warps), while the aggregates travel.
+    uint32_t incl = count;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= (uint32_t)o) incl += y;
+    }
+    if (lane == 31) s_wsum[warp] = incl;
+    __syncthreads();
+    if (tid < (uint32_t)RADIX) {
+        const uint32_t d = tid;
+        uint32_t excl = incl - count;
+        for (uint32_t w = 0; w < warp; ++w) excl += s_wsum[w];
+        s_tile_excl[d] = excl;
+        // Decoupled look-back for digit d.
         uint32_t prefix = 0;
-        if (tile == 0) {
-            st_relaxed_u32(my, kFlagPrefix | count);
-        } else {
-            st_relaxed_u32(my, kFlagAggregate | count);
+        if (tile != 0) {
             int64_t t = (int64_t)tile - 1;
             while (t >= 0) {
-                uint32_t w = wait_for_flag(status + (size_t)t * RADIX + d, wait_limit,
-                                           [] { VREN_RECORD_ERROR(VREN_ERR_TIMEOUT); });
+                const uint32_t w = wait_for_flag(status + (size_t)t * RADIX + d, wait_limit, spin,
+                                                 [] { VREN_RECORD_ERROR(VREN_ERR_TIMEOUT); });
                 prefix += w & kValueMask;
                 if (w & kFlagPrefix) break;
                 --t;
             }
-            st_relaxed_u32(my, kFlagPrefix | (prefix + count));
+            st_relaxed_u32(status + (size_t)tile * RADIX + d, kFlagPrefix | (prefix + count));
         }
-        s_tile_excl[d] = count;  // replaced by the exclusive scan below
-        s_delta[d] = (int32_t)(ld_relaxed_u32(scratch + kOffsOffset + pass * kMaxRadix + d) + prefix);
-    }
-    __syncthreads();
-    // Exclusive scan of the tile's digit counts (RADIX <= 256 <= threads).
-    if (tid < 32) {
-        uint32_t carry = 0;
-        for (int base = 0; base < RADIX; base += 32) {
-            const uint32_t d = base + tid;
-            const uint32_t c = (d < (uint32_t)RADIX) ? s_tile_excl[d] : 0u;
-            uint32_t incl = c;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-                if (tid >= (uint32_t)o) incl += y;
-            }
-            if (d < (uint32_t)RADIX) {
-                const uint32_t excl = carry + incl - c;
-                s_tile_excl[d] = excl;
-                s_delta[d] -= (int32_t)excl;
-            }
-            carry += __shfl_sync(0xFFFFFFFFu, incl, 31);
-        }
+        s_delta[d] = (int32_t)(ld_relaxed_u32(scratch + kOffsOffset + pass * kMaxRadix + d) + prefix) - (int32_t)excl;
     }
     __syncthreads();
 
@@ -299,7 +303,6 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_pass_kernel(
             }
         }
     }
-    (void)HAS_VALS;
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -322,11 +325,19 @@ __global__ void bucket_end_offsets_kernel(const uint2* __restrict__ sorted, uint
 // ------------------------------------------------------------------------------------------------
 // Host side
 // ------------------------------------------------------------------------------------------------
-template <int DB> constexpr int items_for() { return DB >= 8 ? 15 : 16; }
+// Keys per thread: variant 0 = 15 (8-bit digits) / 16, variant 1 = 23 / 24 (bigger tiles).
+template <int DB, int V> constexpr int items_for() { return V == 1 ? (DB >= 8 ? 23 : 24) : (DB >= 8 ? 15 : 16); }
 
+static uint32_t tile_of(uint32_t digit_bits, int variant)
+{
+    const uint32_t items = variant == 1 ? (digit_bits >= 8 ? 23u : 24u) : (digit_bits >= 8 ? 15u : 16u);
+    return kSortThreads * items;
+}
+
+// Scratch is sized for the smaller tile (more tiles), so every variant fits.
 static uint32_t tiles_for(uint32_t n, uint32_t digit_bits)
 {
-    const uint32_t tile = kSortThreads * (digit_bits >= 8 ? 15u : 16u);
+    const uint32_t tile = tile_of(digit_bits, 0);
     return (n + tile - 1) / tile;
 }
 
@@ -340,13 +351,30 @@ static size_t scratch1_bytes(uint32_t n, uint32_t digit_bits)
 
 static bool supported_bits(uint32_t db) { return db == 4 || db == 5 || db == 6 || db == 8; }
 
+template <int DB, int MODE, int V, int RANK>
+static int launch_pass(cudaStream_t st, const uint32_t* sk, const uint32_t* sv, uint32_t* ok, uint32_t* ov, uint32_t n,
+                       uint32_t p, uint32_t shift, uint32_t width, uint32_t tiles, uint32_t* scratch, uint32_t spin)
+{
+    constexpr int ITEMS = items_for<DB, V>();
+    constexpr size_t elem = MODE == kUvec2 ? 8 : 4;
+    constexpr size_t smem = (size_t)kSortThreads * ITEMS * (elem + (MODE == kPairs ? 4 : 0));
+    auto kern = onesweep_pass_kernel<DB, ITEMS, MODE, RANK>;
+    VREN_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<tiles, kSortThreads, smem, st>>>(sk, sv, ok, ov, n, p, shift, width, tiles, scratch, g_wait_limit, spin);
+    VREN_LAUNCH_CHECK();
+    return VREN_OK;
+}
+
 template <int DB, int MODE>
 static int run_passes(cudaStream_t st, const uint32_t* src_k, const uint32_t* src_v, uint32_t* dst_k, uint32_t* dst_v,
                       uint32_t* tmp_k, uint32_t* tmp_v, uint32_t n, const PassInfo& passes, uint32_t* scratch)
 {
-    constexpr int ITEMS = items_for<DB>();
     constexpr int RADIX = 1 << DB;
-    const uint32_t tiles = tiles_for(n, DB);
+    const int variant = tuning(VREN_TUNE_RADIX_ITEMS) == 1 ? 1 : 0;
+    const int rank = tuning(VREN_TUNE_RADIX_RANK) == 1 ? 1 : 0;
+    const uint32_t spin = (uint32_t)tuning(VREN_TUNE_SPIN_POLLS);
+    const uint32_t tiles = (n + tile_of(DB, variant) - 1) / tile_of(DB, variant);
+    const uint32_t status_tiles = tiles_for(n, DB);  // rows per status buffer (scratch layout)
 
     VREN_CUDA_TRY(cudaMemsetAsync(scratch, 0, kZeroWords * sizeof(uint32_t), st));
     uint32_t hist_grid = (n / 4 + kSortThreads - 1) / kSortThreads;
@@ -361,12 +389,18 @@ static int run_passes(cudaStream_t st, const uint32_t* src_k, const uint32_t* sr
         const bool to_final = ((P - 1 - p) % 2) == 0;
         uint32_t* ok = to_final ? dst_k : tmp_k;
         uint32_t* ov = to_final ? dst_v : tmp_v;
-        onesweep_pass_kernel<DB, ITEMS, MODE><<<tiles, kSortThreads, 0, st>>>(
-            src_k, src_v, ok, ov, n, p, passes.shift[p], passes.width[p], tiles, scratch, g_wait_limit);
-        VREN_LAUNCH_CHECK();
+        int rc;
+        if (variant == 1)
+            rc = rank == 1 ? launch_pass<DB, MODE, 1, 1>(st, src_k, src_v, ok, ov, n, p, passes.shift[p], passes.width[p], tiles, scratch, spin)
+                           : launch_pass<DB, MODE, 1, 0>(st, src_k, src_v, ok, ov, n, p, passes.shift[p], passes.width[p], tiles, scratch, spin);
+        else
+            rc = rank == 1 ? launch_pass<DB, MODE, 0, 1>(st, src_k, src_v, ok, ov, n, p, passes.shift[p], passes.width[p], tiles, scratch, spin)
+                           : launch_pass<DB, MODE, 0, 0>(st, src_k, src_v, ok, ov, n, p, passes.shift[p], passes.width[p], tiles, scratch, spin);
+        if (rc != VREN_OK) return rc;
         src_k = ok;
         src_v = ov;
     }
+    (void)status_tiles;
     return VREN_OK;
 }
 

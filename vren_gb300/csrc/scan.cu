@@ -34,7 +34,8 @@ __device__ __forceinline__ uint64_t make_status(uint32_t epoch, uint32_t flag, u
 // (then 32 further back, ...) and the warp sums aggregates up to the nearest inclusive prefix.
 // Returns the exclusive prefix of `tile` in every lane.
 __device__ __forceinline__ uint32_t warp_lookback(const uint64_t* status, uint32_t tile, uint32_t seg_first,
-                                                  uint32_t epoch, uint32_t lane, uint32_t wait_limit, bool& timed_out)
+                                                  uint32_t epoch, uint32_t lane, uint32_t wait_limit, uint32_t spin,
+                                                  bool& timed_out)
 {
     uint32_t prefix = 0;
     int64_t pos = (int64_t)tile - 1;
@@ -55,8 +56,10 @@ __device__ __forceinline__ uint32_t warp_lookback(const uint64_t* status, uint32
                     timed_out = true;
                     break;
                 }
-                __nanosleep(ns);
-                if (ns < 512) ns <<= 1;
+                if (round >= spin) {
+                    __nanosleep(ns);
+                    if (ns < 512) ns <<= 1;
+                }
             }
         }
         const uint32_t prefix_mask = __ballot_sync(0xFFFFFFFFu, flag == 2u);
@@ -78,12 +81,14 @@ __device__ __forceinline__ uint32_t warp_lookback(const uint64_t* status, uint32
 // `in` may equal `data` (in place).  When n_dev is given the element count is min(*n_dev, n)
 // (a single segment whose length is only known on the device); tiles past it do nothing.
 // When total_out is given the segment-0 total is written there.
+template <int SLICES>
 __global__ void __launch_bounds__(kScanThreads) exclusive_scan_kernel(
     const uint32_t* in, uint32_t* data, uint32_t n, uint32_t tiles_per_seg, uint32_t total_tiles,
-    uint32_t* __restrict__ scratch, uint32_t wait_limit, const uint32_t* __restrict__ n_dev,
+    uint32_t* __restrict__ scratch, uint32_t wait_limit, uint32_t spin, const uint32_t* __restrict__ n_dev,
     uint32_t* __restrict__ total_out)
 {
-    constexpr int kSlices = kScanItems / 4;
+    constexpr int kSlices = SLICES;
+    constexpr uint32_t kTile = SLICES * 128u * (kScanThreads / 32);
     __shared__ uint32_t s_tile;
     __shared__ uint32_t s_epoch;
     __shared__ uint32_t s_warp_sum[kScanThreads / 32];
@@ -106,7 +111,7 @@ __global__ void __launch_bounds__(kScanThreads) exclusive_scan_kernel(
         const uint32_t m = *n_dev;
         n = m < n ? m : n;
     }
-    const uint32_t tiles_eff = (n + kScanTile - 1) / kScanTile;
+    const uint32_t tiles_eff = (n + kTile - 1) / kTile;
     if (tile_in_seg >= tiles_eff) {
         if (total_out && tiles_eff == 0 && tile == 0 && tid == 0) *total_out = 0u;
         goto done;
@@ -114,8 +119,8 @@ __global__ void __launch_bounds__(kScanThreads) exclusive_scan_kernel(
     {
     const uint32_t* seg_in = in + seg_off;
     uint32_t* seg_data = data + seg_off;
-    const uint32_t warp_base = tile_in_seg * kScanTile + warp * (kScanItems * 32);
-    const bool full = (tile_in_seg + 1) * kScanTile <= n;
+    const uint32_t warp_base = tile_in_seg * kTile + warp * (kSlices * 128u);
+    const bool full = (tile_in_seg + 1) * kTile <= n;
     const bool aligned = ((reinterpret_cast<uintptr_t>(seg_data) & 15u) == 0) &&
                          ((reinterpret_cast<uintptr_t>(seg_in) & 15u) == 0);
     const bool vec = full && aligned;
@@ -172,7 +177,7 @@ __global__ void __launch_bounds__(kScanThreads) exclusive_scan_kernel(
         } else {
             if (lane == 0) st_relaxed_u64(my_status, make_status(epoch, 1u, tile_sum));
             bool timed_out = false;
-            prefix = warp_lookback(status, tile, tile - tile_in_seg, epoch, lane, wait_limit, timed_out);
+            prefix = warp_lookback(status, tile, tile - tile_in_seg, epoch, lane, wait_limit, spin, timed_out);
             if (__any_sync(0xFFFFFFFFu, timed_out) && lane == 0) VREN_RECORD_ERROR(VREN_ERR_TIMEOUT);
             if (lane == 0) st_relaxed_u64(my_status, make_status(epoch, 2u, prefix + tile_sum));
         }
@@ -268,6 +273,28 @@ static int downsweep_level(cudaStream_t st, uint32_t* data, uint32_t seg_len, ui
     return VREN_OK;
 }
 
+// Dispatches the tile size chosen by VREN_TUNE_SCAN_SLICES (scratch is always sized for 4096-element
+// tiles, the smaller one, so either variant fits).
+static int scan_launch(cudaStream_t st, const uint32_t* in, uint32_t* out, uint32_t n, uint32_t blocks, void* scratch,
+                       const uint32_t* n_dev, uint32_t* total_out)
+{
+    const int slices = tuning(VREN_TUNE_SCAN_SLICES) == 8 ? 8 : 4;
+    const uint32_t tile = (uint32_t)slices * 1024u;
+    const uint32_t tiles_per_seg = (n + tile - 1) / tile;
+    const uint64_t total = (uint64_t)(tiles_per_seg ? tiles_per_seg : 1) * blocks;
+    if (total > 0x7FFFFFFFull) return VREN_ERR_ARG;
+    const uint32_t spin = (uint32_t)tuning(VREN_TUNE_SPIN_POLLS);
+    uint32_t* sc = static_cast<uint32_t*>(scratch);
+    if (slices == 8)
+        exclusive_scan_kernel<8><<<(uint32_t)total, kScanThreads, 0, st>>>(
+            in, out, n, tiles_per_seg ? tiles_per_seg : 1, (uint32_t)total, sc, g_wait_limit, spin, n_dev, total_out);
+    else
+        exclusive_scan_kernel<4><<<(uint32_t)total, kScanThreads, 0, st>>>(
+            in, out, n, tiles_per_seg ? tiles_per_seg : 1, (uint32_t)total, sc, g_wait_limit, spin, n_dev, total_out);
+    VREN_LAUNCH_CHECK();
+    return VREN_OK;
+}
+
 }  // namespace vren_gb300
 
 using namespace vren_gb300;
@@ -283,13 +310,7 @@ extern "C" int vren_exclusive_scan_u32(vren_stream_t s, uint32_t* data, uint32_t
     if (blocks == 0 || !scratch || (n > 0 && !data)) return VREN_ERR_ARG;
     if (n == 0) return VREN_OK;
     if (n > (1u << 31)) return VREN_ERR_ARG;
-    const uint32_t tiles_per_seg = (n + kScanTile - 1) / kScanTile;
-    const uint64_t total = (uint64_t)tiles_per_seg * blocks;
-    if (total > 0x7FFFFFFFull) return VREN_ERR_ARG;
-    exclusive_scan_kernel<<<(uint32_t)total, kScanThreads, 0, as_stream(s)>>>(
-        data, data, n, tiles_per_seg, (uint32_t)total, static_cast<uint32_t*>(scratch), g_wait_limit, nullptr, nullptr);
-    VREN_LAUNCH_CHECK();
-    return VREN_OK;
+    return scan_launch(as_stream(s), data, data, n, blocks, scratch, nullptr, nullptr);
 }
 
 namespace vren_gb300 {
@@ -298,12 +319,7 @@ size_t scan_scratch_bytes(uint32_t n_cap) { return vren_exclusive_scan_scratch_b
 int scan_exclusive_u32(cudaStream_t st, const uint32_t* in, uint32_t* out, uint32_t n_cap, const uint32_t* n_dev,
                        uint32_t* total_out, void* scratch)
 {
-    const uint32_t tiles = (n_cap + kScanTile - 1) / kScanTile;
-    const uint32_t grid = tiles ? tiles : 1;
-    exclusive_scan_kernel<<<grid, kScanThreads, 0, st>>>(in, out, tiles ? n_cap : 0, grid, grid,
-                                                         static_cast<uint32_t*>(scratch), g_wait_limit, n_dev, total_out);
-    VREN_LAUNCH_CHECK();
-    return VREN_OK;
+    return scan_launch(st, in, out, n_cap, 1, scratch, n_dev, total_out);
 }
 }  // namespace vren_gb300
 
@@ -378,8 +394,8 @@ extern "C" int vren_exclusive_scan_u32_noalloc(vren_stream_t s, uint32_t* data, 
     if (rc != VREN_OK) return rc;
     cudaStream_t st = as_stream(s);
     VREN_CUDA_TRY(cudaMemsetAsync(scratch, 0, (kScanHeaderWords + 2u * total) * sizeof(uint32_t), st));
-    exclusive_scan_kernel<<<total, kScanThreads, 0, st>>>(data, data, n, tiles_per_seg, total, scratch, g_wait_limit,
-                                                          nullptr, nullptr);
+    exclusive_scan_kernel<4><<<total, kScanThreads, 0, st>>>(data, data, n, tiles_per_seg, total, scratch, g_wait_limit,
+                                                             (uint32_t)tuning(VREN_TUNE_SPIN_POLLS), nullptr, nullptr);
     VREN_LAUNCH_CHECK();
     return VREN_OK;
 }
