@@ -143,6 +143,49 @@ def test_find_unique_clusters_special_normals(cuda):
     assert np.array_equal(u32(refs), erefs)
 
 
+@pytest.mark.parametrize("slicing", ["ref", "fixed32"])
+def test_find_unique_clusters_adversarial(cuda, slicing):
+    """Depths at and one or two ulps either side of every slice boundary (the slice estimate must be
+    corrected against the table), and normals whose largest components are equal, a few ulps apart,
+    infinite, NaN, signed zero, subnormal or huge."""
+    W, H = 256, 192
+    view = make_view(W, H, slicing)
+    fr = cs.frame_build(view, W, H)
+    n, f = float(view.near_plane), float(view.far_plane)
+    bounds = np.array(fr.slice_near[: fr.max_slice + 1], dtype=np.float64)
+    bounds = bounds[np.isfinite(bounds) & (bounds < f)]
+    d_at = (f / (f - n) * (1.0 - n / bounds)).astype(np.float32)
+    cand = [d_at]
+    for s in (1, 2):
+        cand.append(np.nextafter(d_at, np.float32(2), dtype=np.float32) if s == 1 else
+                    np.nextafter(np.nextafter(d_at, np.float32(2)), np.float32(2)))
+        cand.append(np.nextafter(d_at, np.float32(-2)) if s == 1 else
+                    np.nextafter(np.nextafter(d_at, np.float32(-2)), np.float32(-2)))
+    cand = np.concatenate(cand + [np.array([0.0, 1.0, np.inf, -np.inf], np.float32)]).astype(np.float32)
+    rng = np.random.default_rng(11)
+    depth = cand[rng.integers(0, len(cand), W * H)].astype(np.float32)
+
+    m = rng.uniform(0.2, 1.0, W * H).astype(np.float32)
+    k = rng.integers(0, 4, W * H).astype(np.int32)
+    near_m = m.view(np.int32) - k  # 0..3 ulps below m
+    normals = np.zeros((W * H, 3), np.float32)
+    perm = rng.permuted(np.tile([0, 1, 2], (W * H, 1)), axis=1)
+    rows = np.arange(W * H)
+    normals[rows, perm[:, 0]] = m * np.where(rng.random(W * H) < 0.5, -1, 1)
+    normals[rows, perm[:, 1]] = near_m.view(np.float32) * np.where(rng.random(W * H) < 0.5, -1, 1)
+    normals[rows, perm[:, 2]] = rng.uniform(-1, 1, W * H).astype(np.float32) * m
+    special = np.array([[np.inf, 1, 0], [1, -np.inf, np.inf], [np.nan, 0.5, 0.5], [np.nan, np.nan, 0.0],
+                        [-0.0, 0.0, 0.0], [0.0, -0.0, np.nan], [1e-38, 2e-38, -1e-45], [1e-36, 0, 0],
+                        [3e38, -3e38, 1], [2e38, 1e38, 0], [0.5, 0.5, 0.5], [-0.5, 0.5, -0.5]], np.float32)
+    normals[::3] = special[rng.integers(0, len(special), len(normals[::3]))]
+    normals = normals.reshape(-1)
+    _, keys, kc, refs = run_unique(cuda, depth, normals, W, H, view)
+    ekeys, erefs = oracle.cs_find_unique_clusters(depth, normals, W, H, view, 0)
+    U = int(u32(kc)[0])
+    assert U == len(ekeys) and np.array_equal(u32(keys)[:U], ekeys)
+    assert np.array_equal(u32(refs), erefs)
+
+
 def test_find_unique_clusters_repeated_calls(cuda):
     """The look-back scratch is reused across calls (epoch-tagged status words)."""
     W, H = 640, 360

@@ -48,7 +48,7 @@ namespace vren_gb300 {
 // Kernel variant knobs (tile sizes, ranking method, polling policy), set by the autotuner or the
 // caller; every launcher reads its knob when it enqueues work.
 static int g_tuning[VREN_TUNE_COUNT] = {
-    /* VREN_TUNE_SCAN_SLICES */ 4,
+    /* VREN_TUNE_SCAN_SLICES */ 8,
     /* VREN_TUNE_SPIN_POLLS */ 64,
     /* VREN_TUNE_RADIX_RANK */ 0,
     /* VREN_TUNE_RADIX_ITEMS */ 0,

@@ -29,42 +29,77 @@ __device__ __forceinline__ float mv_row(const float* m, int r, float x, float y,
 __device__ __forceinline__ float glsl_min(float x, float y) { return y < x ? y : x; }
 __device__ __forceinline__ float glsl_max(float x, float y) { return x < y ? y : x; }
 
-// clustered_shading.glsl:128-164
+// clustered_shading.glsl:128-164.  The reference walks the three axes with t_i = sign(n_i) / n_i
+// (= |rcp_rn(n_i)|, NaN for a zero or NaN component) and keeps the first strictly smaller t below
+// 1e35; the cube face and the 3x3 cell on it follow from that axis and t.  Here with one correctly
+// rounded reciprocal instead of three: rcp_rn is monotone non-increasing in |n|, so the smallest t
+// over the usable components is rcp_rn(max |n_i|), and the first component whose t rounds to that
+// value is the largest |n_i| or an earlier one within rounding of it (tested exactly, only when it is
+// that close).  x / 2 and x * 0.5 are the same correctly rounded value.
 __device__ __forceinline__ uint32_t discretize_normal(float nx, float ny, float nz)
 {
     if (nx == 0.0f && ny == 0.0f && nz == 0.0f) return 0xFFFFFFFFu;
-    const float n[3] = {nx, ny, nz};
+    const float ax = fabsf(nx), ay = fabsf(ny), az = fabsf(nz);
+    const float M = fmaxf(fmaxf(ax, ay), az);  // NaN components drop out
     float min_t = 1e35f;
     uint32_t axis = 0, face = 0;
-#pragma unroll
-    for (uint32_t i = 0; i < 3; ++i) {
-        // sign(n)/n: +-1/n correctly rounded is |rcp_rn(n)|; 0/0 (and NaN) never compare below min_t
-        const float t = n[i] != 0.0f ? fabsf(__frcp_rn(n[i])) : __int_as_float(0x7FC00000);
-        if (t < min_t) {
+    if (M > 0.0f) {
+        const float t = __frcp_rn(M);
+        if (t < 1e35f) {
+            // a < M rounds to the same reciprocal only within 2^-21 relative of M
+            const float close = fmul(M, 0.9999f);
+            if (ax == M || (ax >= close && __frcp_rn(ax) == t)) axis = 0;
+            else if (ay == M || (ay >= close && __frcp_rn(ay) == t)) axis = 1;
+            else axis = 2;
+            const float na = axis == 0 ? nx : (axis == 1 ? ny : nz);
             min_t = t;
-            axis = i;
-            face = (n[i] > 0.0f ? 1u : 0u) * 3u + i;
+            face = (na > 0.0f ? 1u : 0u) * 3u + axis;
         }
     }
-    const float u = fmul(n[(axis + 1) % 3], min_t);
-    const float w = fmul(n[(axis + 2) % 3], min_t);
-    // x / 2 and x * 0.5 are the same correctly rounded value
+    const float n1 = axis == 0 ? ny : (axis == 1 ? nz : nx);
+    const float n2 = axis == 0 ? nz : (axis == 1 ? nx : ny);
+    const float u = fmul(n1, min_t);
+    const float w = fmul(n2, min_t);
     const uint32_t du = floor_to_u32(fmul(fmul(fadd(u, 1.0f), 0.5f), 3.0f));
     const uint32_t dw = floor_to_u32(fmul(fmul(fadd(w, 1.0f), 0.5f), 3.0f));
     return (face * 9u + du * 3u + dw) & 0x3Fu;
 }
 
-// Largest k in [0, kmax] with bound[k] <= z (0 if none); bound is non-decreasing.
-__device__ __forceinline__ uint32_t slice_of(float z, const float* bound, uint32_t kmax)
+// Largest k in [lo, hi] with bound[k] <= z, given bound[lo] <= z; bound is non-decreasing.
+__device__ __forceinline__ uint32_t slice_search(float z, const float* __restrict__ bound, uint32_t lo, uint32_t hi)
 {
-    if (!(bound[0] <= z)) return 0u;
-    uint32_t lo = 0, hi = kmax;
     while (lo < hi) {
         const uint32_t mid = (lo + hi + 1u) >> 1;
-        if (bound[mid] <= z) lo = mid;
+        if (__ldg(bound + mid) <= z) lo = mid;
         else hi = mid - 1u;
     }
     return lo;
+}
+
+// Largest k in [0, kmax] with bound[k] <= z (0 if none) for a non-decreasing, geometric table (bound[k] = bound[0] * r^k up to rounding, as both slicing modes
+// build it): a logarithmic estimate, then at most two steps each way against the table before a
+// binary search takes over, so the table alone decides the result.  inv_log2_r = 1 / log2(r).
+__device__ __forceinline__ uint32_t slice_of_geometric(float z, const float* __restrict__ bound, uint32_t kmax, float b0,
+                                                      float inv_log2_r)
+{
+    if (!(b0 <= z)) return 0u;
+    if (kmax == 0u) return 0u;
+    const float e = __log2f(__fdividef(z, b0)) * inv_log2_r;
+    uint32_t k = e >= (float)kmax ? kmax : (e > 0.0f ? (uint32_t)e : 0u);
+    if (__ldg(bound + k) <= z) {
+        if (k < kmax && __ldg(bound + k + 1u) <= z) {
+            ++k;
+            if (k < kmax && __ldg(bound + k + 1u) <= z) k = slice_search(z, bound, k + 1u, kmax);
+        }
+    } else {
+        // bound[0] <= z < bound[k], so k >= 1
+        --k;
+        if (!(__ldg(bound + k) <= z)) {
+            --k;
+            if (!(__ldg(bound + k) <= z)) k = slice_search(z, bound, 0u, k - 1u);
+        }
+    }
+    return k;
 }
 
 struct Box {
@@ -351,7 +386,6 @@ __global__ void __launch_bounds__(kFucThreads) find_unique_kernel(
 {
     __shared__ uint32_t s_bits[2048];
     __shared__ uint32_t s_prefix[2048];
-    __shared__ float s_bound[VREN_CS_SLICES];
     __shared__ uint32_t s_warp_sum[kFucThreads / 32];
     __shared__ uint32_t s_tile, s_epoch, s_offset;
 
@@ -362,8 +396,6 @@ __global__ void __launch_bounds__(kFucThreads) find_unique_kernel(
     }
 #pragma unroll
     for (int k = 0; k < 8; ++k) s_bits[tid * 8 + k] = 0u;
-#pragma unroll
-    for (int k = 0; k < VREN_CS_SLICES / kFucThreads; ++k) s_bound[k * kFucThreads + tid] = F->slice_near[k * kFucThreads + tid];
     __syncthreads();
     const uint32_t tile = s_tile, epoch = s_epoch;
     const uint32_t TX = (W + 31) / 32;
@@ -380,30 +412,45 @@ __global__ void __launch_bounds__(kFucThreads) find_unique_kernel(
     // leaves every bit of vz and vw unchanged.
     const bool xy_free = m2[0] == 0.0f && m2[1] == 0.0f && m3[0] == 0.0f && m3[1] == 0.0f && m2[3] != 0.0f &&
                          m3[3] != 0.0f;
+    const float* bound = F->slice_near;
+    const float b0 = __ldg(bound);
+    const float inv_log2_r = kmax ? __frcp_rn(__log2f(__fdividef(__ldg(bound + 1), b0))) : 0.0f;
 
+    // Loads first (all four rows in flight), then the keys.
+    float D[4], N[4][3];
+    bool on[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const uint32_t gx = tx * 32u + lane, gy = ty * 32u + warp + 8u * q;
+        on[q] = !(skip_offscreen && (gx >= W || gy >= H));
+        // texel (x mod W, y mod H); a tile overhangs the image by less than 32 pixels
+        const uint32_t xw = gx < W ? gx : gx % W, yw = gy < H ? gy : gy % H;
+        const size_t px = (size_t)yw * W + xw;
+        D[q] = on[q] ? __ldg(depth + px) : 0.0f;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) N[q][c] = on[q] ? __ldg(normals + 3 * px + c) : 0.0f;
+    }
     uint32_t sub[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-        const uint32_t gx = tx * 32u + lane, gy = ty * 32u + (tid >> 5) + 8u * q;
-        sub[q] = 0xFFFFFFFFu;
-        if (skip_offscreen && (gx >= W || gy >= H)) continue;
-        const uint32_t px = (gy % H) * W + (gx % W);
-        const float D = __ldg(depth + px);
+        const uint32_t gx = tx * 32u + lane, gy = ty * 32u + warp + 8u * q;
         float vz, vw;
         if (xy_free) {
-            vz = fadd(fmul(m2[2], D), m2[3]);
-            vw = fadd(fmul(m3[2], D), m3[3]);
+            vz = fadd(fmul(m2[2], D[q]), m2[3]);
+            vw = fadd(fmul(m3[2], D[q]), m3[3]);
         } else {
             const float fx = fdiv((float)gx, fW), fy = fdiv((float)gy, fH);
             const float X = fsub(fmul(fx, 2.0f), 1.0f), Y = fsub(fmul(fsub(1.0f, fy), 2.0f), 1.0f);
-            vz = fadd(fadd(fadd(fmul(m2[0], X), fmul(m2[1], Y)), fmul(m2[2], D)), fmul(m2[3], 1.0f));
-            vw = fadd(fadd(fadd(fmul(m3[0], X), fmul(m3[1], Y)), fmul(m3[2], D)), fmul(m3[3], 1.0f));
+            vz = fadd(fadd(fadd(fmul(m2[0], X), fmul(m2[1], Y)), fmul(m2[2], D[q])), fmul(m2[3], 1.0f));
+            vw = fadd(fadd(fadd(fmul(m3[0], X), fmul(m3[1], Y)), fmul(m3[2], D[q])), fmul(m3[3], 1.0f));
         }
-        const uint32_t k = slice_of(fdiv(vz, vw), s_bound, kmax);
-        const uint32_t nd = discretize_normal(__ldg(normals + 3 * px), __ldg(normals + 3 * px + 1), __ldg(normals + 3 * px + 2));
+        const uint32_t k = slice_of_geometric(fdiv(vz, vw), bound, kmax, b0, inv_log2_r);
+        const uint32_t nd = discretize_normal(N[q][0], N[q][1], N[q][2]);
         const uint32_t s = ((k & 0x3FFu) | (nd << 10)) & 0xFFFFu;
-        sub[q] = s;
-        atomicOr(&s_bits[s >> 5], 1u << (s & 31u));
+        sub[q] = on[q] ? s : 0xFFFFFFFFu;
+        // one shared-memory atomic per run of equal sub-keys along the row
+        const uint32_t left = __shfl_up_sync(0xFFFFFFFFu, sub[q], 1);
+        if (on[q] && (lane == 0 || left != s)) atomicOr(&s_bits[s >> 5], 1u << (s & 31u));
     }
     __syncthreads();
 

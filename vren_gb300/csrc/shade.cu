@@ -44,21 +44,25 @@ struct Px {
 __device__ __forceinline__ float dot3(const float* a, const float* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
 
 // World position of pixel (x, y); returns false when the pixel is not shaded (shade.comp:86).
+// Each row starts from the constant column and adds the depth term with one fused multiply-add:
+// the homogeneous w of a perspective inverse is m[11] * D + m[15] with D close to 1 for distant
+// pixels (about -9.999 * D + 10), and rounding m[11] * D on its own before the sum would cost
+// three to four significant digits of the view depth there.
 __device__ __forceinline__ bool pixel_world(const vren_cs_frame* F, uint32_t x, uint32_t y, uint32_t W, uint32_t H,
                                             float D, float p[3])
 {
     const float fx = (float)x / (float)W, fy = (float)y / (float)H;
-    const float v0[4] = {fx * 2.0f - 1.0f, (1.0f - fy) * 2.0f - 1.0f, D, 1.0f};
+    const float nx = fx * 2.0f - 1.0f, ny = (1.0f - fy) * 2.0f - 1.0f;
     const float* ip = F->view.inv_proj;
     float v[4];
 #pragma unroll
-    for (int r = 0; r < 4; ++r) v[r] = ip[r] * v0[0] + ip[4 + r] * v0[1] + ip[8 + r] * v0[2] + ip[12 + r] * v0[3];
+    for (int r = 0; r < 4; ++r) v[r] = fmaf(ip[4 + r], ny, fmaf(ip[r], nx, fmaf(ip[8 + r], D, ip[12 + r])));
 #pragma unroll
-    for (int r = 0; r < 4; ++r) v[r] = v[r] / v[3];
+    for (int r = 0; r < 3; ++r) v[r] = v[r] / v[3];
     if (!(v[2] < F->view.far_plane - 0.001f)) return false;
     const float* iv = F->view.inv_view;
 #pragma unroll
-    for (int r = 0; r < 3; ++r) p[r] = iv[r] * v[0] + iv[4 + r] * v[1] + iv[8 + r] * v[2] + iv[12 + r] * v[3];
+    for (int r = 0; r < 3; ++r) p[r] = fmaf(iv[8 + r], v[2], fmaf(iv[4 + r], v[1], fmaf(iv[r], v[0], iv[12 + r])));
     return true;
 }
 
