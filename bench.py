@@ -254,8 +254,15 @@ def run_ours(args, rank: int, world: int):
     # radix sort: 2^20 key/value pairs (config 1), plus sizes beyond L2
     radix = radix_bench(args, dev, stream, flush, radix_keys, hbm_peak)
     sweep = None if args.quick else primitive_sweep(args, dev, stream, flush, hbm_peak)
+    shade = shade_bench(args, dev, stream, flush, ctx)
 
     clocks.__exit__(None, None, None)
+    clk = clocks.summary()
+    peak32 = fp32_peak_tflops(clk["sm_mhz"])
+    shade["roofline"] = {"bound": "fp32", "peak": round(peak32, 2), "unit": "TFLOP/s",
+                         "peak_kind": "nominal (152 SMs x 128 FP32 lanes x 2 at the sampled SM clock)",
+                         "forward_frac": round(shade["forward_tflops"] / peak32, 4),
+                         "backward_frac": round(shade["backward_tflops"] / peak32, 4)}
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(depth, normals, pos, lights, radix_keys, view)
@@ -293,8 +300,9 @@ def run_ours(args, rank: int, world: int):
             "radix_sort": radix,
             "batched_vs_plain": None,
             "primitive_sweep": sweep,
+            "shade": shade,
             "cpu_baseline": cpu,
-            "clocks": clocks.summary(),
+            "clocks": clk,
             "device_error": err,
             "wall_s_timed": round(t_wall, 4),
         }
@@ -368,6 +376,73 @@ def radix_bench(args, dev, stream, flush, keys_np, hbm_peak):
                                             "inputs larger than L2 (also flushed)"}
         del src_k, src_v, k, v, tk, tv, s1
     return out
+
+
+# Arithmetic operations per (pixel, assigned light) pair, counted once on the restated formulas
+# (pbr_apply_point_light with the windowed inverse-square falloff; every +, -, *, /, sqrt, min and max of
+# the GLSL expression is one operation): distance and falloff 26, half vector 12, GGX NDF 14, N.L 7,
+# Smith G 9, H.V 6, Schlick power 5, specular 5, three colour channels 54.  The adjoint recomputes
+# the forward (135 without the accumulation) and adds 150 for the reverse sweep.
+SHADE_FWD_FLOPS_PER_PAIR = 138
+SHADE_BWD_FLOPS_PER_PAIR = 285
+SHADE_W, SHADE_H, SHADE_L = 1920, 1080, 4096
+
+
+def fp32_peak_tflops(sm_mhz):
+    """Nominal FP32 CUDA-core rate: 152 SMs x 128 lanes x 2 (fused multiply-add) at the sampled clock."""
+    return 152 * 128 * 2 * (sm_mhz or 2070.0) * 1e6 / 1e12
+
+
+def shade_bench(args, dev, stream, flush, ctx):
+    """Differentiable shading at 1920x1080 with 4096 lights and the windowed inverse-square falloff:
+    forward radiance and the adjoint w.r.t. light position/colour/radius for an N(0,1) upstream
+    gradient, light lists from the clustering pipeline."""
+    import torch
+
+    import vren_gb300.clustered_shading as cs
+    import vren_gb300.scene as scene
+
+    W_, H_, L_ = SHADE_W, SHADE_H, SHADE_L
+    depth, normals_planes = scene.depth_planes(SEED + 500, W_, H_, planes=64)
+    gn, galb, grough, gmetal = scene.gbuffer(SEED + 501, W_, H_)
+    pos, lights = scene.lights_near_surfaces(SEED + 502, L_, depth, W_, H_)
+    grad = scene.normal01(SEED + 503, 9, W_ * H_ * 3)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    d_depth, d_np, d_pos, d_light = t(depth), t(normals_planes), t(pos), t(lights)
+    d_n, d_alb, d_r, d_m, d_grad = t(gn), t(galb), t(grough), t(gmetal), t(grad)
+    view = cs.view_from_camera(cs.scene_camera(W_, H_), "ref")
+    with torch.cuda.stream(stream):
+        ctx.cluster(stream, view, W_, H_, d_depth, d_np, d_pos, d_light, L_)
+    stream.synchronize()
+    out = ctx.outputs()
+    U = int(cs.read_device(out.key_count, 1)[0])
+    total = int(cs.read_device(out.total, 1)[0])
+    refs = cs.read_device(out.cluster_refs, W_ * H_)
+    counts = cs.read_device(out.counts, U)
+    pairs = int(counts[refs].astype(np.int64).sum()) if U else 0
+    gb = cs.gbuffer(d_depth, d_n, d_alb, d_r, d_m)
+    ll = cs.light_lists(out.cluster_refs, out.counts, out.offsets, out.indices)
+    img = torch.empty(W_ * H_ * 3, dtype=torch.float32, device=dev)
+    fwd = cs.shade("windowed_inv_sq", "radiance")
+    bwd = cs.shade_backward("windowed_inv_sq")
+    gpos = torch.zeros(L_ * 3, dtype=torch.float32, device=dev)
+    gcol = torch.zeros(L_ * 3, dtype=torch.float32, device=dev)
+    grr = torch.zeros(L_, dtype=torch.float32, device=dev)
+    steps = max(3, args.steps // 2)
+    ms_f = time_events(stream, lambda: fwd(stream, out.frame, W_, H_, gb, ll, d_pos, d_light, L_, img), 3, steps, flush)
+    ms_b = time_events(stream, lambda: bwd(stream, out.frame, W_, H_, gb, ll, total, d_pos, d_light, L_, d_grad, gpos,
+                                           gcol, grr), 3, steps, flush)
+    ok = bool(torch.isfinite(img).all().item() and torch.isfinite(gpos).all().item())
+    return {
+        "workload": "1920x1080 G-buffer, 4096 lights near visible surfaces, windowed inverse-square falloff, "
+                    "radiance output; adjoint for an N(0,1) upstream gradient",
+        "pairs": pairs, "unique_clusters": U, "assignments": total,
+        "forward_ms": round(ms_f, 5), "backward_ms": round(ms_b, 5),
+        "forward_tflops": round(SHADE_FWD_FLOPS_PER_PAIR * pairs / (ms_f * 1e-3) / 1e12, 3),
+        "backward_tflops": round(SHADE_BWD_FLOPS_PER_PAIR * pairs / (ms_b * 1e-3) / 1e12, 3),
+        "flops_per_pair": {"forward": SHADE_FWD_FLOPS_PER_PAIR, "backward": SHADE_BWD_FLOPS_PER_PAIR},
+        "finite": ok,
+    }
 
 
 def primitive_sweep(args, dev, stream, flush, hbm_peak):

@@ -27,3 +27,19 @@ def gb(s):
 
 def lists(s):
     return (s["refs"], s["counts"], s["offsets"], s["indices"])
+
+
+def ndotv(s):
+    """Per-pixel N.V in float64 (world position reconstructed from the depth as the oracle does)."""
+    v, W, H = s["view"], s["W"], s["H"]
+    ip = np.array(v.inv_proj, np.float64)
+    iv = np.array(v.inv_view, np.float64)
+    ys, xs = np.mgrid[0:H, 0:W]
+    v0 = [xs.reshape(-1) / W * 2 - 1, (1 - ys.reshape(-1) / H) * 2 - 1, s["depth"].astype(np.float64),
+          np.ones(W * H)]
+    vv = [sum(ip[4 * k + r] * v0[k] for k in range(4)) for r in range(4)]
+    vv = [x / vv[3] for x in vv]
+    p = np.stack([sum(iv[4 * k + r] * vv[k] for k in range(4)) for r in range(3)], 1)
+    e = np.array(v.eye, np.float64) - p
+    V = e / np.linalg.norm(e, axis=1, keepdims=True)
+    return (s["normals"].reshape(-1, 3).astype(np.float64) * V).sum(1)

@@ -39,9 +39,49 @@ struct ShadeArgs {
 struct Px {
     float p[3], N[3], V[3], alb[3];
     float rough, metal, NdotV;
+    float omn2;  // 1 - |N|^2
 };
 
 __device__ __forceinline__ float dot3(const float* a, const float* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+// a x b, each component one product and one fused multiply-add (accurate when the result is small).
+__device__ __forceinline__ void cross3(const float* a, const float* b, float* c)
+{
+    c[0] = fmaf(a[1], b[2], -(a[2] * b[1]));
+    c[1] = fmaf(a[2], b[0], -(a[0] * b[2]));
+    c[2] = fmaf(a[0], b[1], -(a[1] * b[0]));
+}
+
+// 1 - |n|^2 to within a few ulps of its own size: the squares as exact product pairs, summed with
+// error-free transformations (Knuth's two-sum), then 1 - hi (exact for hi in [0.5, 2]) - lo.
+__device__ __forceinline__ float one_minus_norm2(const float* n)
+{
+    float hi = 0.0f, lo = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float ph = __fmul_rn(n[c], n[c]);
+        const float pl = fmaf(n[c], n[c], -ph);
+        const float s = __fadd_rn(hi, ph);
+        const float bb = __fsub_rn(s, hi);
+        const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(ph, bb));
+        hi = s;
+        lo = __fadd_rn(lo, __fadd_rn(err, pl));
+    }
+    return __fsub_rn(__fsub_rn(1.0f, hi), lo);
+}
+
+// GGX denominator D = NdotH^2 (a2 - 1) + 1 (pbr.glsl:24-35) for NdotH = max(N.H, 0), H = hv / |hv|.
+// Written as a2 h^2 + (1 - h^2) with Lagrange's identity
+//     1 - (N.H)^2 = ((1 - |N|^2) |hv|^2 + |N x hv|^2) / |hv|^2,
+// whose terms stay accurate near the specular peak, where 1 - (N.H)^2 computed from a rounded N.H
+// would cancel (a2 = roughness^2 can be 0.0025, so D's relative error there would be ~1e-4).
+__device__ __forceinline__ float ggx_den(const float* N, const float* hv, float nhu, float hl2, float omn2, float a2)
+{
+    if (!(nhu > 0.0f)) return 1.0f;
+    float c[3];
+    cross3(N, hv, c);
+    return (a2 * nhu * nhu + fmaf(hl2, omn2, dot3(c, c))) / hl2;
+}
 
 // World position of pixel (x, y); returns false when the pixel is not shaded (shade.comp:86).
 // Each row starts from the constant column and adds the depth term with one fused multiply-add:
@@ -82,6 +122,7 @@ __device__ __forceinline__ void load_px(const ShadeArgs& a, uint32_t x, uint32_t
     q.rough = a.g.roughness[px];
     q.metal = a.g.metallic[px];
     q.NdotV = fmaxf(dot3(q.N, q.V), 0.0f);
+    q.omn2 = one_minus_norm2(q.N);
 }
 
 // pbr_apply_light (pbr.glsl:184-215) for light direction L (from the light towards the point) and
@@ -89,11 +130,11 @@ __device__ __forceinline__ void load_px(const ShadeArgs& a, uint32_t x, uint32_t
 __device__ __forceinline__ void apply_light(const Px& q, const float L[3], const float rad[3], float out[3])
 {
     float hv[3] = {q.V[0] - L[0], q.V[1] - L[1], q.V[2] - L[2]};
-    const float hl = sqrtf(dot3(hv, hv));
+    const float hl2 = dot3(hv, hv);
+    const float hl = sqrtf(hl2);
     const float H[3] = {hv[0] / hl, hv[1] / hl, hv[2] / hl};
     const float a2 = q.rough * q.rough;
-    const float NdotH = fmaxf(dot3(q.N, H), 0.0f);
-    const float D = NdotH * NdotH * (a2 - 1.0f) + 1.0f;
+    const float D = ggx_den(q.N, hv, dot3(q.N, hv), hl2, q.omn2, a2);
     const float NDF = a2 / (kPi * D * D);
     const float k = q.rough;
     const float nl = -dot3(q.N, L);
@@ -196,12 +237,13 @@ __device__ __forceinline__ void pair_backward(const Px& q, float4 lp, float4 lc,
     const float col[3] = {lc.x, lc.y, lc.z};
 
     float hv[3] = {q.V[0] - L[0], q.V[1] - L[1], q.V[2] - L[2]};
-    const float hl = sqrtf(dot3(hv, hv));
+    const float hl2 = dot3(hv, hv);
+    const float hl = sqrtf(hl2);
     const float H[3] = {hv[0] / hl, hv[1] / hl, hv[2] / hl};
     const float a2 = q.rough * q.rough;
-    const float nh_raw = dot3(q.N, H);
-    const float NdotH = fmaxf(nh_raw, 0.0f);
-    const float D = NdotH * NdotH * (a2 - 1.0f) + 1.0f;
+    const float nhu = dot3(q.N, hv);  // |hv| (N.H)
+    const float NdotH = fmaxf(nhu / hl, 0.0f);
+    const float D = ggx_den(q.N, hv, nhu, hl2, q.omn2, a2);
     const float NDF = a2 / (kPi * D * D);
     const float k = q.rough;
     const float nl_raw = -dot3(q.N, L);
@@ -243,17 +285,17 @@ __device__ __forceinline__ void pair_backward(const Px& q, float4 lp, float4 lc,
     gNdotL += gG * ggxV * k / (dl * dl);
     const float gNdotH = gNDF * (-4.0f * a2 * NdotH * (a2 - 1.0f) / (kPi * D * D * D));
     const float gnl = nl_raw > 0.0f ? gNdotL : 0.0f;
-    const float gnh = nh_raw > 0.0f ? gNdotH : 0.0f;
+    const float gnh = nhu > 0.0f ? gNdotH : 0.0f;
     const float ghv = hvr > 0.0f ? gHdotV : 0.0f;
-    float gL[3], gH[3];
+    // Through H = hv / |hv| and hv = V - L: d(N.H)/dhv = (N - (N.H) H) / |hv|, written as
+    // hv x (N x hv) / |hv|^3 (no cancellation near the peak); d(H.V)/dhv = (V - (H.V) H) / |hv|.
+    float nxh[3], tri[3];
+    cross3(q.N, hv, nxh);
+    cross3(hv, nxh, tri);
+    const float sn = gnh / (hl2 * hl), sv = ghv / hl;
+    float gL[3];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        gL[c] = -gnl * q.N[c];
-        gH[c] = gnh * q.N[c] + ghv * q.V[c];
-    }
-    const float gHH = dot3(gH, H);
-#pragma unroll
-    for (int c = 0; c < 3; ++c) gL[c] -= (gH[c] - H[c] * gHH) / hl;  // hv = V - L
+    for (int c = 0; c < 3; ++c) gL[c] = -gnl * q.N[c] - sn * tri[c] - sv * (q.V[c] - H[c] * hvr);
     // attenuation: t = dist / r
     const float gt = gatt * datt_dt;
     const float gdist = gatt * datt_ddist_direct + gt / r;
@@ -272,7 +314,7 @@ struct PxRec {
     float4 n_rough;   // N.xyz, roughness
     float4 v_metal;   // V.xyz, metallic
     float4 alb_nv;    // albedo.xyz, NdotV
-    float4 g;         // upstream gradient
+    float4 g;         // upstream gradient, 1 - |N|^2
 };
 
 constexpr int kBwdThreads = 256;
@@ -310,7 +352,7 @@ __global__ void __launch_bounds__(kBwdThreads) shade_backward_slots_kernel(Shade
             rec.n_rough = make_float4(q.N[0], q.N[1], q.N[2], q.rough);
             rec.v_metal = make_float4(q.V[0], q.V[1], q.V[2], q.metal);
             rec.alb_nv = make_float4(q.alb[0], q.alb[1], q.alb[2], q.NdotV);
-            rec.g = make_float4(grad[3 * px], grad[3 * px + 1], grad[3 * px + 2], 0.0f);
+            rec.g = make_float4(grad[3 * px], grad[3 * px + 1], grad[3 * px + 2], q.omn2);
             cmin = min(cmin, ref);
             cmax = max(cmax, ref);
         } else {
@@ -359,6 +401,7 @@ __global__ void __launch_bounds__(kBwdThreads) shade_backward_slots_kernel(Shade
             q.N[0] = rec.n_rough.x; q.N[1] = rec.n_rough.y; q.N[2] = rec.n_rough.z; q.rough = rec.n_rough.w;
             q.V[0] = rec.v_metal.x; q.V[1] = rec.v_metal.y; q.V[2] = rec.v_metal.z; q.metal = rec.v_metal.w;
             q.alb[0] = rec.alb_nv.x; q.alb[1] = rec.alb_nv.y; q.alb[2] = rec.alb_nv.z; q.NdotV = rec.alb_nv.w;
+            q.omn2 = rec.g.w;
             const float gin[3] = {rec.g.x, rec.g.y, rec.g.z};
             pair_backward(q, lp, lc, a.falloff, gin, g7);
         }
