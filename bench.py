@@ -393,10 +393,10 @@ def fp32_peak_tflops(sm_mhz):
     return 152 * 128 * 2 * (sm_mhz or 2070.0) * 1e6 / 1e12
 
 
-def shade_bench(args, dev, stream, flush, ctx):
-    """Differentiable shading at 1920x1080 with 4096 lights and the windowed inverse-square falloff:
-    forward radiance and the adjoint w.r.t. light position/colour/radius for an N(0,1) upstream
-    gradient, light lists from the clustering pipeline."""
+def shade_profile_setup(dev, stream, ctx):
+    """Inputs of the differentiable-shading workload (1920x1080 G-buffer, 4096 lights near visible
+    surfaces, windowed inverse-square falloff, N(0,1) upstream gradient), light lists from the
+    clustering pipeline, and forward / adjoint closures."""
     import torch
 
     import vren_gb300.clustered_shading as cs
@@ -428,15 +428,29 @@ def shade_bench(args, dev, stream, flush, ctx):
     gpos = torch.zeros(L_ * 3, dtype=torch.float32, device=dev)
     gcol = torch.zeros(L_ * 3, dtype=torch.float32, device=dev)
     grr = torch.zeros(L_, dtype=torch.float32, device=dev)
+    keep = (d_depth, d_np, d_pos, d_light, d_n, d_alb, d_r, d_m, d_grad, img, gpos, gcol, grr)
+    return {
+        "forward": lambda: fwd(stream, out.frame, W_, H_, gb, ll, d_pos, d_light, L_, img),
+        "backward": lambda: bwd(stream, out.frame, W_, H_, gb, ll, total, d_pos, d_light, L_, d_grad, gpos, gcol, grr),
+        "pairs": pairs, "unique_clusters": U, "assignments": total, "img": img, "gpos": gpos, "keep": keep,
+    }
+
+
+def shade_bench(args, dev, stream, flush, ctx):
+    """Differentiable shading at 1920x1080 with 4096 lights: forward radiance and the adjoint w.r.t.
+    light position/colour/radius, each timed alone with CUDA events (L2 flushed between runs)."""
+    import torch
+
+    sb = shade_profile_setup(dev, stream, ctx)
     steps = max(3, args.steps // 2)
-    ms_f = time_events(stream, lambda: fwd(stream, out.frame, W_, H_, gb, ll, d_pos, d_light, L_, img), 3, steps, flush)
-    ms_b = time_events(stream, lambda: bwd(stream, out.frame, W_, H_, gb, ll, total, d_pos, d_light, L_, d_grad, gpos,
-                                           gcol, grr), 3, steps, flush)
-    ok = bool(torch.isfinite(img).all().item() and torch.isfinite(gpos).all().item())
+    ms_f = time_events(stream, sb["forward"], 3, steps, flush)
+    ms_b = time_events(stream, sb["backward"], 3, steps, flush)
+    pairs = sb["pairs"]
+    ok = bool(torch.isfinite(sb["img"]).all().item() and torch.isfinite(sb["gpos"]).all().item())
     return {
         "workload": "1920x1080 G-buffer, 4096 lights near visible surfaces, windowed inverse-square falloff, "
                     "radiance output; adjoint for an N(0,1) upstream gradient",
-        "pairs": pairs, "unique_clusters": U, "assignments": total,
+        "pairs": pairs, "unique_clusters": sb["unique_clusters"], "assignments": sb["assignments"],
         "forward_ms": round(ms_f, 5), "backward_ms": round(ms_b, 5),
         "forward_tflops": round(SHADE_FWD_FLOPS_PER_PAIR * pairs / (ms_f * 1e-3) / 1e12, 3),
         "backward_tflops": round(SHADE_BWD_FLOPS_PER_PAIR * pairs / (ms_b * 1e-3) / 1e12, 3),
@@ -629,6 +643,10 @@ def run_profile(args):
         x = torch.from_numpy(scene.gen_u32(SEED, 2, n, mask=255).view(np.int32)).to(dev)
         scan = vg.blelloch_scan()
         fn = lambda: scan(stream, x, n)
+    elif args.profile in ("shade", "shade_backward"):
+        ctx = cs.cluster_and_shade(SHADE_W, SHADE_H, 65536, 1 << 24)
+        sb = shade_profile_setup(dev, stream, ctx)
+        fn = sb["forward"] if args.profile == "shade" else sb["backward"]
     else:
         raise SystemExit(f"unknown profile kind {args.profile}")
     with torch.cuda.stream(stream):
@@ -646,7 +664,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--quick", action="store_true", help="skip the primitive sweep and the large sorts")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--profile", choices=["find_unique", "radix", "scan"], default=None,
+    ap.add_argument("--profile", choices=["find_unique", "radix", "scan", "shade", "shade_backward"], default=None,
                     help="run one kernel family on a case larger than L2 (for ncu) and exit")
     args = ap.parse_args()
     if args.profile:

@@ -375,18 +375,23 @@ __device__ __forceinline__ uint64_t make_status(uint32_t epoch, uint32_t flag, u
 // One CTA per 32x32 tile (find_unique_clusters.comp:46-120).  The reference sorts the tile's 1024
 // (key, pixel) pairs with a 55-stage bitonic network; here the 16 varying key bits (slice and
 // normal; the tile coordinates are constant inside a tile) index a 65536-bit set in shared
-// memory, so the sorted unique keys and every pixel's rank fall out of one popcount prefix.
-// Tiles are ordered by a dynamic ticket; decoupled look-back over the tiles gives each tile's
-// offset in the key list (row-major tile order).
-__global__ void __launch_bounds__(kFucThreads) find_unique_kernel(
+// memory, so the sorted unique keys and every pixel's rank fall out of a popcount prefix.  A
+// 2048-bit occupancy mask records which words of the set are non-zero, so the prefix visits only
+// those (a tile holds a handful of distinct keys).  Thread t owns a strip of four horizontally
+// adjacent pixels (row t / 8, columns 4 (t % 8) .. + 3), read with 128-bit loads when the row is
+// 16-byte aligned; along a strip a pixel whose depth (normal) bits equal its left neighbour's
+// reuses that neighbour's slice (normal bin), and only the first pixel of each run of equal
+// sub-keys along a row touches the set.  Tiles are ordered by a dynamic ticket; decoupled
+// look-back over the tiles gives each tile's offset in the key list (row-major tile order).
+__global__ void __launch_bounds__(kFucThreads, 6) find_unique_kernel(
     const float* __restrict__ depth, const float* __restrict__ normals, uint32_t W, uint32_t H,
     const vren_cs_frame* __restrict__ F, uint32_t* __restrict__ keys, uint32_t key_cap,
     uint32_t* __restrict__ key_count, uint32_t* __restrict__ refs, uint32_t* __restrict__ scratch,
-    uint32_t num_tiles, uint32_t wait_limit, uint32_t spin)
+    uint32_t num_tiles, uint32_t wait_limit, uint32_t spin, int vec)
 {
-    __shared__ uint32_t s_bits[2048];
+    __shared__ __align__(16) uint32_t s_bits[2048];
     __shared__ uint32_t s_prefix[2048];
-    __shared__ uint32_t s_warp_sum[kFucThreads / 32];
+    __shared__ uint32_t s_used[64];  // bit w: word w of s_bits is non-zero
     __shared__ uint32_t s_tile, s_epoch, s_offset;
 
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
@@ -394,8 +399,9 @@ __global__ void __launch_bounds__(kFucThreads) find_unique_kernel(
         s_tile = atomicAdd(scratch + 0, 1u);
         s_epoch = ld_relaxed_u32(scratch + 2) & 0x3FFFFFFFu;
     }
-#pragma unroll
-    for (int k = 0; k < 8; ++k) s_bits[tid * 8 + k] = 0u;
+    reinterpret_cast<uint4*>(s_bits)[tid] = make_uint4(0u, 0u, 0u, 0u);
+    reinterpret_cast<uint4*>(s_bits)[tid + kFucThreads] = make_uint4(0u, 0u, 0u, 0u);
+    if (tid < 64) s_used[tid] = 0u;
     __syncthreads();
     const uint32_t tile = s_tile, epoch = s_epoch;
     const uint32_t TX = (W + 31) / 32;
@@ -409,81 +415,109 @@ __global__ void __launch_bounds__(kFucThreads) find_unique_kernel(
     // For a perspective projection the z and w rows of its inverse have exact zeros in the x and y
     // columns and non-zero last coefficients.  Then X and Y only contribute signed zeros to a partial
     // sum that is either non-zero already or followed by the non-zero last term, so skipping them
-    // leaves every bit of vz and vw unchanged.
+    // leaves every bit of vz and vw unchanged (and the slice depends on the depth alone).
     const bool xy_free = m2[0] == 0.0f && m2[1] == 0.0f && m3[0] == 0.0f && m3[1] == 0.0f && m2[3] != 0.0f &&
                          m3[3] != 0.0f;
     const float* bound = F->slice_near;
     const float b0 = __ldg(bound);
     const float inv_log2_r = kmax ? __frcp_rn(__log2f(__fdividef(__ldg(bound + 1), b0))) : 0.0f;
 
-    // Loads first (all four rows in flight), then the keys.
+    const uint32_t row = tid >> 3, strip = tid & 7u;
+    const uint32_t gy = ty * 32u + row, gx0 = tx * 32u + strip * 4u;
+    const bool full = vec && gy < H && gx0 + 3u < W;  // whole strip on screen, 16-byte aligned
     float D[4], N[4][3];
     bool on[4];
+    if (full) {
+        const size_t px0 = (size_t)gy * W + gx0;
+        const float4 d4 = __ldg(reinterpret_cast<const float4*>(depth + px0));
+        const float4* np = reinterpret_cast<const float4*>(normals + 3 * px0);
+        const float4 a = __ldg(np), b = __ldg(np + 1), c = __ldg(np + 2);
+        D[0] = d4.x; D[1] = d4.y; D[2] = d4.z; D[3] = d4.w;
+        N[0][0] = a.x; N[0][1] = a.y; N[0][2] = a.z;
+        N[1][0] = a.w; N[1][1] = b.x; N[1][2] = b.y;
+        N[2][0] = b.z; N[2][1] = b.w; N[2][2] = c.x;
+        N[3][0] = c.y; N[3][1] = c.z; N[3][2] = c.w;
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        const uint32_t gx = tx * 32u + lane, gy = ty * 32u + warp + 8u * q;
-        on[q] = !(skip_offscreen && (gx >= W || gy >= H));
-        // texel (x mod W, y mod H); a tile overhangs the image by less than 32 pixels
-        const uint32_t xw = gx < W ? gx : gx % W, yw = gy < H ? gy : gy % H;
-        const size_t px = (size_t)yw * W + xw;
-        D[q] = on[q] ? __ldg(depth + px) : 0.0f;
+        for (int j = 0; j < 4; ++j) on[j] = true;
+    } else {
 #pragma unroll
-        for (int c = 0; c < 3; ++c) N[q][c] = on[q] ? __ldg(normals + 3 * px + c) : 0.0f;
-    }
-    uint32_t sub[4];
+        for (int j = 0; j < 4; ++j) {
+            const uint32_t gx = gx0 + j;
+            on[j] = !(skip_offscreen && (gx >= W || gy >= H));
+            // texel (x mod W, y mod H); a tile overhangs the image by less than 32 pixels
+            const uint32_t xw = gx < W ? gx : gx % W, yw = gy < H ? gy : gy % H;
+            const size_t px = (size_t)yw * W + xw;
+            D[j] = on[j] ? __ldg(depth + px) : 0.0f;
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        const uint32_t gx = tx * 32u + lane, gy = ty * 32u + warp + 8u * q;
-        float vz, vw;
-        if (xy_free) {
-            vz = fadd(fmul(m2[2], D[q]), m2[3]);
-            vw = fadd(fmul(m3[2], D[q]), m3[3]);
-        } else {
-            const float fx = fdiv((float)gx, fW), fy = fdiv((float)gy, fH);
-            const float X = fsub(fmul(fx, 2.0f), 1.0f), Y = fsub(fmul(fsub(1.0f, fy), 2.0f), 1.0f);
-            vz = fadd(fadd(fadd(fmul(m2[0], X), fmul(m2[1], Y)), fmul(m2[2], D[q])), fmul(m2[3], 1.0f));
-            vw = fadd(fadd(fadd(fmul(m3[0], X), fmul(m3[1], Y)), fmul(m3[2], D[q])), fmul(m3[3], 1.0f));
+            for (int c = 0; c < 3; ++c) N[j][c] = on[j] ? __ldg(normals + 3 * px + c) : 0.0f;
         }
-        const uint32_t k = slice_of_geometric(fdiv(vz, vw), bound, kmax, b0, inv_log2_r);
-        const uint32_t nd = discretize_normal(N[q][0], N[q][1], N[q][2]);
-        const uint32_t s = ((k & 0x3FFu) | (nd << 10)) & 0xFFFFu;
-        sub[q] = on[q] ? s : 0xFFFFFFFFu;
-        // one shared-memory atomic per run of equal sub-keys along the row
-        const uint32_t left = __shfl_up_sync(0xFFFFFFFFu, sub[q], 1);
-        if (on[q] && (lane == 0 || left != s)) atomicOr(&s_bits[s >> 5], 1u << (s & 31u));
+    }
+
+    uint32_t sub[4], k = 0, nd = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const bool same_d = j > 0 && xy_free && __float_as_uint(D[j]) == __float_as_uint(D[j - 1]);
+        if (!same_d) {
+            float vz, vw;
+            if (xy_free) {
+                vz = fadd(fmul(m2[2], D[j]), m2[3]);
+                vw = fadd(fmul(m3[2], D[j]), m3[3]);
+            } else {
+                const float fx = fdiv((float)(gx0 + j), fW), fy = fdiv((float)gy, fH);
+                const float X = fsub(fmul(fx, 2.0f), 1.0f), Y = fsub(fmul(fsub(1.0f, fy), 2.0f), 1.0f);
+                vz = fadd(fadd(fadd(fmul(m2[0], X), fmul(m2[1], Y)), fmul(m2[2], D[j])), fmul(m2[3], 1.0f));
+                vw = fadd(fadd(fadd(fmul(m3[0], X), fmul(m3[1], Y)), fmul(m3[2], D[j])), fmul(m3[3], 1.0f));
+            }
+            k = slice_of_geometric(fdiv(vz, vw), bound, kmax, b0, inv_log2_r);
+        }
+        const bool same_n = j > 0 && __float_as_uint(N[j][0]) == __float_as_uint(N[j - 1][0]) &&
+                            __float_as_uint(N[j][1]) == __float_as_uint(N[j - 1][1]) &&
+                            __float_as_uint(N[j][2]) == __float_as_uint(N[j - 1][2]);
+        if (!same_n) nd = discretize_normal(N[j][0], N[j][1], N[j][2]);
+        sub[j] = on[j] ? (((k & 0x3FFu) | (nd << 10)) & 0xFFFFu) : 0xFFFFFFFFu;
+    }
+    // One set insert per run of equal sub-keys along the row (lane - 1 holds the strip to the left).
+    const uint32_t left3 = __shfl_up_sync(0xFFFFFFFFu, sub[3], 1);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const uint32_t left = j ? sub[j - 1] : (strip ? left3 : 0xFFFFFFFFu);
+        if (on[j] && sub[j] != left) {
+            const uint32_t w = sub[j] >> 5;
+            if (atomicOr(&s_bits[w], 1u << (sub[j] & 31u)) == 0u) atomicOr(&s_used[w >> 5], 1u << (w & 31u));
+        }
     }
     __syncthreads();
 
-    // Popcount prefix over the 2048 words (thread t owns words 8t .. 8t+7).
-    uint32_t cnt[8], run = 0;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        cnt[k] = __popc(s_bits[tid * 8 + k]);
-        run += cnt[k];
-    }
-    uint32_t incl = run;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, d);
-        if (lane >= (uint32_t)d) incl += y;
-    }
-    if (lane == 31) s_warp_sum[warp] = incl;
-    __syncthreads();
-    uint32_t base = incl - run, tile_unique = 0;
-#pragma unroll
-    for (int w = 0; w < kFucThreads / 32; ++w) {
-        if (w < (int)warp) base += s_warp_sum[w];
-        tile_unique += s_warp_sum[w];
-    }
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        s_prefix[tid * 8 + k] = base;
-        base += cnt[k];
-    }
-
-    // Decoupled look-back over tiles for this tile's offset.
-    uint64_t* status = reinterpret_cast<uint64_t*>(scratch + kFucHeaderWords);
     if (warp == 0) {
+        // Lane l owns words [64 l, 64 l + 64): unique counts, exclusive scan, per-word prefixes.
+        const uint32_t u0 = s_used[2 * lane], u1 = s_used[2 * lane + 1];
+        uint32_t cnt = 0;
+        for (uint32_t m = u0; m; m &= m - 1u) cnt += __popc(s_bits[64u * lane + __ffs(m) - 1u]);
+        for (uint32_t m = u1; m; m &= m - 1u) cnt += __popc(s_bits[64u * lane + 32u + __ffs(m) - 1u]);
+        uint32_t incl = cnt;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+            if (lane >= (uint32_t)d) incl += y;
+        }
+        const uint32_t excl = incl - cnt;
+        const uint32_t tile_unique = __shfl_sync(0xFFFFFFFFu, incl, 31);
+        {
+            uint32_t run = excl;
+            for (uint32_t m = u0; m; m &= m - 1u) {
+                const uint32_t w = 64u * lane + __ffs(m) - 1u;
+                s_prefix[w] = run;
+                run += __popc(s_bits[w]);
+            }
+            for (uint32_t m = u1; m; m &= m - 1u) {
+                const uint32_t w = 64u * lane + 32u + __ffs(m) - 1u;
+                s_prefix[w] = run;
+                run += __popc(s_bits[w]);
+            }
+        }
+
+        // Decoupled look-back over tiles for this tile's offset.
+        uint64_t* status = reinterpret_cast<uint64_t*>(scratch + kFucHeaderWords);
         uint32_t prefix = 0;
         if (tile == 0) {
             if (lane == 0) st_relaxed_u64(status, make_status(epoch, 2u, tile_unique));
@@ -534,33 +568,43 @@ __global__ void __launch_bounds__(kFucThreads) find_unique_kernel(
                 if (total > key_cap) VREN_RECORD_ERROR(VREN_ERR_CAPACITY);
             }
         }
+
+        // Keys, ascending: word w bit b is the sub-key 32 w + b.
+        const uint32_t low = ((ty & 0xFFu) << 8) | (tx & 0xFFu);
+        uint32_t pos = prefix + excl;
+        for (int h = 0; h < 2; ++h) {
+            for (uint32_t m = h ? u1 : u0; m; m &= m - 1u) {
+                const uint32_t w = 64u * lane + 32u * h + __ffs(m) - 1u;
+                for (uint32_t bits = s_bits[w]; bits; bits &= bits - 1u) {
+                    if (pos < key_cap) keys[pos] = ((w * 32u + __ffs(bits) - 1u) << 16) | low;
+                    ++pos;
+                }
+            }
+        }
     }
     __syncthreads();
     const uint32_t off = s_offset;
 
-    // Keys, ascending: word w bit b is the sub-key 32w + b.
-    const uint32_t low = ((ty & 0xFFu) << 8) | (tx & 0xFFu);
+    // Per-pixel references (only on-screen pixels; the reference's imageStore drops the rest).
+    uint32_t r[4];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        const uint32_t w = tid * 8 + k;
-        uint32_t bits = s_bits[w];
-        uint32_t pos = off + s_prefix[w];
-        while (bits) {
-            const uint32_t b = __ffs(bits) - 1;
-            bits &= bits - 1u;
-            if (pos < key_cap) keys[pos] = ((w * 32u + b) << 16) | low;
-            ++pos;
+    for (int j = 0; j < 4; ++j) {
+        const uint32_t sj = sub[j];
+        if (j > 0 && sj == sub[j - 1]) {
+            r[j] = r[j - 1];
+        } else if (sj != 0xFFFFFFFFu) {
+            const uint32_t w = sj >> 5;
+            r[j] = off + s_prefix[w] + __popc(s_bits[w] & ((1u << (sj & 31u)) - 1u));
+        } else {
+            r[j] = 0u;
         }
     }
-    // Per-pixel references (only on-screen pixels; the reference's imageStore drops the rest).
+    if (full) {
+        *reinterpret_cast<uint4*>(refs + (size_t)gy * W + gx0) = make_uint4(r[0], r[1], r[2], r[3]);
+    } else if (gy < H) {
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        const uint32_t gx = tx * 32u + lane, gy = ty * 32u + (tid >> 5) + 8u * q;
-        if (gx < W && gy < H) {
-            const uint32_t s = sub[q];
-            const uint32_t rank = s_prefix[s >> 5] + __popc(s_bits[s >> 5] & ((1u << (s & 31u)) - 1u));
-            refs[(size_t)gy * W + gx] = off + rank;
-        }
+        for (int j = 0; j < 4; ++j)
+            if (gx0 + j < W) refs[(size_t)gy * W + gx0 + j] = r[j];
     }
 
     if (tid == 0) {
@@ -572,6 +616,20 @@ __global__ void __launch_bounds__(kFucThreads) find_unique_kernel(
             scratch[2] = (epoch + 1u) & 0x3FFFFFFFu;
         }
     }
+}
+
+static int launch_find_unique(cudaStream_t st, const float* depth, const float* normals, uint32_t W, uint32_t H,
+                              const vren_cs_frame* frame, uint32_t* keys, uint32_t key_cap, uint32_t* key_count,
+                              uint32_t* refs, uint32_t* scratch)
+{
+    const uint32_t tiles = ((W + 31) / 32) * ((H + 31) / 32);
+    const int vec = (W % 4u == 0u) && ((uintptr_t)depth % 16u == 0u) && ((uintptr_t)normals % 16u == 0u) &&
+                    ((uintptr_t)refs % 16u == 0u);
+    find_unique_kernel<<<tiles, kFucThreads, 0, st>>>(depth, normals, W, H, frame, keys, key_cap, key_count, refs,
+                                                      scratch, tiles, g_wait_limit,
+                                                      (uint32_t)tuning(VREN_TUNE_SPIN_POLLS), vec);
+    VREN_LAUNCH_CHECK();
+    return VREN_OK;
 }
 
 // ================================================================================================
@@ -927,13 +985,8 @@ extern "C" int vren_cs_find_unique_clusters(vren_stream_t s, const float* depth,
     if (!depth || !normals || !frame || !cluster_keys || !key_count || !cluster_refs || !scratch) return VREN_ERR_ARG;
     if (width == 0 || height == 0 || width > 8192 || height > 8192) return VREN_ERR_ARG;
     if ((uintptr_t)scratch & 7u) return VREN_ERR_ARG;
-    const uint32_t tiles = ((width + 31) / 32) * ((height + 31) / 32);
-    find_unique_kernel<<<tiles, kFucThreads, 0, as_stream(s)>>>(depth, normals, width, height, frame, cluster_keys,
-                                                                key_capacity, key_count, cluster_refs,
-                                                                static_cast<uint32_t*>(scratch), tiles, g_wait_limit,
-                                                                (uint32_t)tuning(VREN_TUNE_SPIN_POLLS));
-    VREN_LAUNCH_CHECK();
-    return VREN_OK;
+    return launch_find_unique(as_stream(s), depth, normals, width, height, frame, cluster_keys, key_capacity,
+                              key_count, cluster_refs, static_cast<uint32_t*>(scratch));
 }
 
 extern "C" size_t vren_cs_assign_lights_scratch_bytes(uint32_t key_capacity) { return scan_scratch_bytes(key_capacity); }
@@ -1001,11 +1054,9 @@ int cs_enqueue(vren_cluster_and_shade* cs, cudaStream_t st, uint32_t W, uint32_t
                                  cs->view_pos, cs->bvh, cs->light_index, cs->spheres, cs->lbvh_scratch);
         if (rc != VREN_OK) return rc;
     }
-    const uint32_t tiles = ((W + 31) / 32) * ((H + 31) / 32);
-    find_unique_kernel<<<tiles, kFucThreads, 0, st>>>(depth, normals, W, H, cs->frame, cs->keys, cs->key_cap,
-                                                      cs->key_count, cs->refs, static_cast<uint32_t*>(cs->fuc_scratch),
-                                                      tiles, g_wait_limit, (uint32_t)tuning(VREN_TUNE_SPIN_POLLS));
-    VREN_LAUNCH_CHECK();
+    rc = launch_find_unique(st, depth, normals, W, H, cs->frame, cs->keys, cs->key_cap, cs->key_count, cs->refs,
+                            static_cast<uint32_t*>(cs->fuc_scratch));
+    if (rc != VREN_OK) return rc;
     return assign_lights(st, cs->keys, cs->key_count, cs->key_cap, cs->frame, cs->bvh, L, cs->light_index,
                          cs->view_pos, cs->spheres, cs->counts, cs->offsets, cs->indices, cs->max_assign, cs->total,
                          cs->assign_scratch, cs->opt.assign_warps);

@@ -2,14 +2,24 @@
 // vren/resources/shaders/pbr.glsl:6-112) and its hand-written adjoint with respect to the point
 // lights' positions, colours and radii (the light-to-cluster assignment held fixed).
 //
-// Forward: one thread per pixel, the loop over its cluster's lights.
+// Both passes work tile by tile (one CTA per 32x32 tile).  The CTA stages the tile's pixels in
+// shared memory (world position, normal, view vector, material, upstream gradient), then groups
+// them by cluster with a stable compaction, so a warp always works on pixels that share one light
+// list: no lane idles on another cluster's lights, and every light record a warp reads is the same
+// for all its lanes.
+// Forward: a warp takes 32 pixels of one cluster and walks the cluster's lights.
 // Adjoint (deterministic, nothing stored per (pixel, light) pair):
-//   1. one CTA per 32x32 tile stages the tile's G-buffer and upstream gradient in shared memory;
-//      each warp takes (cluster, light) slots of the tile and sums the pair gradients over the
-//      tile's pixels of that cluster — lanes stride the pixels in a fixed order, then a fixed
-//      butterfly reduction — into one 7-float partial per slot;
+//   1. a warp takes one (cluster, light) slot of the tile and sums the pair gradients over the
+//      cluster's pixels - lanes stride them in pixel order, then a fixed butterfly reduction - into
+//      one 7-float partial per slot;
 //   2. the slots are grouped by light with the stable bucket sort of (light, slot) pairs;
 //   3. one warp per light sums its slots' partials in slot order.
+//
+// The world position of a pixel is reconstructed as an unevaluated sum of two floats (about 44
+// significant bits), and a light's offset is formed as (p_hi - light) + p_lo: lights sit within
+// a fraction of a unit of surfaces hundreds of units from the camera, where rounding p to single
+// precision first would cost the offset (and the gradient, which scales with 1 / distance) four
+// significant digits.
 #include "common.cuh"
 #include "internal.h"
 
@@ -37,7 +47,7 @@ struct ShadeArgs {
 };
 
 struct Px {
-    float p[3], N[3], V[3], alb[3];
+    float p[3], plo[3], N[3], V[3], alb[3];
     float rough, metal, NdotV;
     float omn2;  // 1 - |N|^2
 };
@@ -52,20 +62,116 @@ __device__ __forceinline__ void cross3(const float* a, const float* b, float* c)
     c[2] = fmaf(a[0], b[1], -(a[1] * b[0]));
 }
 
+// ------------------------------------------------------------------------------------------------
+// Double-float arithmetic: x = hi + lo with |lo| <= ulp(hi) / 2.  Knuth's two-sum and the fused
+// multiply-add two-product are error-free transformations (Dekker 1971; Ogita, Rump, Oishi 2005).
+// ------------------------------------------------------------------------------------------------
+struct ff {
+    float hi, lo;
+};
+
+__device__ __forceinline__ ff two_sum(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+
+__device__ __forceinline__ ff two_prod(float a, float b)
+{
+    const float p = __fmul_rn(a, b);
+    return {p, fmaf(a, b, -p)};
+}
+
+__device__ __forceinline__ ff ff_add(ff a, ff b)
+{
+    const ff s = two_sum(a.hi, b.hi);
+    return two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+
+__device__ __forceinline__ ff ff_mul_f(ff a, float c)
+{
+    const ff p = two_prod(a.hi, c);
+    return two_sum(p.hi, fmaf(a.lo, c, p.lo));
+}
+
+__device__ __forceinline__ ff ff_div(ff a, ff b)
+{
+    const float q = __fdiv_rn(a.hi, b.hi);
+    const ff qb = ff_mul_f(b, q);
+    const ff r = ff_add(a, {-qb.hi, -qb.lo});
+    return two_sum(q, __fdiv_rn(r.hi, b.hi));
+}
+
+// x / n as double-float for integers x, n < 2^24: the remainder of the correctly rounded quotient
+// is exactly representable, so one fused multiply-add recovers it.
+__device__ __forceinline__ ff ratio(uint32_t x, uint32_t n)
+{
+    const float fx = (float)x, fn = (float)n;
+    const float q = __fdiv_rn(fx, fn);
+    return {q, __fdiv_rn(fmaf(-q, fn, fx), fn)};
+}
+
+// World position of pixel (x, y) as p + plo; returns false when the pixel is not shaded
+// (shade.comp:86: view depth at the far plane).  A non-finite depth takes the single-precision
+// path of the same formulas (plo = 0).
+__device__ __forceinline__ bool pixel_world(const vren_cs_frame* F, uint32_t x, uint32_t y, uint32_t W, uint32_t H,
+                                            float D, float p[3], float plo[3])
+{
+    const float* ip = F->view.inv_proj;
+    const float* iv = F->view.inv_view;
+    if (!isfinite(D)) {
+        const float nx = ((float)x / (float)W) * 2.0f - 1.0f, ny = (1.0f - (float)y / (float)H) * 2.0f - 1.0f;
+        float v[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) v[r] = ip[r] * nx + ip[4 + r] * ny + ip[8 + r] * D + ip[12 + r];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) v[r] = v[r] / v[3];
+        if (!(v[2] < F->view.far_plane - 0.001f)) return false;
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            p[r] = iv[r] * v[0] + iv[4 + r] * v[1] + iv[8 + r] * v[2] + iv[12 + r];
+            plo[r] = 0.0f;
+        }
+        return true;
+    }
+    const ff fx = ratio(x, W), fy = ratio(y, H);
+    // NDC: fx * 2 - 1 and (1 - fy) * 2 - 1 = 1 - 2 fy (doubling is exact)
+    const ff nx = ff_add(two_sum(2.0f * fx.hi, -1.0f), {2.0f * fx.lo, 0.0f});
+    const ff ny = ff_add(two_sum(1.0f, -2.0f * fy.hi), {-2.0f * fy.lo, 0.0f});
+    ff v[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        ff acc = ff_add(two_prod(ip[8 + r], D), {ip[12 + r], 0.0f});
+        acc = ff_add(acc, ff_mul_f(nx, ip[r]));
+        v[r] = ff_add(acc, ff_mul_f(ny, ip[4 + r]));
+    }
+    ff vv[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) vv[r] = ff_div(v[r], v[3]);
+    if (!(vv[2].hi < F->view.far_plane - 0.001f)) return false;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        ff acc = ff_add(ff_mul_f(vv[0], iv[r]), {iv[12 + r], 0.0f});
+        acc = ff_add(acc, ff_mul_f(vv[1], iv[4 + r]));
+        acc = ff_add(acc, ff_mul_f(vv[2], iv[8 + r]));
+        p[r] = acc.hi;
+        plo[r] = acc.lo;
+    }
+    return true;
+}
+
 // 1 - |n|^2 to within a few ulps of its own size: the squares as exact product pairs, summed with
-// error-free transformations (Knuth's two-sum), then 1 - hi (exact for hi in [0.5, 2]) - lo.
+// two-sum, then 1 - hi (exact for hi in [0.5, 2]) - lo.
 __device__ __forceinline__ float one_minus_norm2(const float* n)
 {
     float hi = 0.0f, lo = 0.0f;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        const float ph = __fmul_rn(n[c], n[c]);
-        const float pl = fmaf(n[c], n[c], -ph);
-        const float s = __fadd_rn(hi, ph);
-        const float bb = __fsub_rn(s, hi);
-        const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(ph, bb));
-        hi = s;
-        lo = __fadd_rn(lo, __fadd_rn(err, pl));
+        const ff sq = two_prod(n[c], n[c]);
+        const ff s = two_sum(hi, sq.hi);
+        hi = s.hi;
+        lo = __fadd_rn(lo, __fadd_rn(s.lo, sq.lo));
     }
     return __fsub_rn(__fsub_rn(1.0f, hi), lo);
 }
@@ -83,46 +189,32 @@ __device__ __forceinline__ float ggx_den(const float* N, const float* hv, float 
     return (a2 * nhu * nhu + fmaf(hl2, omn2, dot3(c, c))) / hl2;
 }
 
-// World position of pixel (x, y); returns false when the pixel is not shaded (shade.comp:86).
-// Each row starts from the constant column and adds the depth term with one fused multiply-add:
-// the homogeneous w of a perspective inverse is m[11] * D + m[15] with D close to 1 for distant
-// pixels (about -9.999 * D + 10), and rounding m[11] * D on its own before the sum would cost
-// three to four significant digits of the view depth there.
-__device__ __forceinline__ bool pixel_world(const vren_cs_frame* F, uint32_t x, uint32_t y, uint32_t W, uint32_t H,
-                                            float D, float p[3])
+// Light offset d = p - light position with the low part of p folded in.
+__device__ __forceinline__ void light_offset(const Px& q, float4 lp, float d[3])
 {
-    const float fx = (float)x / (float)W, fy = (float)y / (float)H;
-    const float nx = fx * 2.0f - 1.0f, ny = (1.0f - fy) * 2.0f - 1.0f;
-    const float* ip = F->view.inv_proj;
-    float v[4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r) v[r] = fmaf(ip[4 + r], ny, fmaf(ip[r], nx, fmaf(ip[8 + r], D, ip[12 + r])));
-#pragma unroll
-    for (int r = 0; r < 3; ++r) v[r] = v[r] / v[3];
-    if (!(v[2] < F->view.far_plane - 0.001f)) return false;
-    const float* iv = F->view.inv_view;
-#pragma unroll
-    for (int r = 0; r < 3; ++r) p[r] = fmaf(iv[8 + r], v[2], fmaf(iv[4 + r], v[1], fmaf(iv[r], v[0], iv[12 + r])));
-    return true;
+    d[0] = (q.p[0] - lp.x) + q.plo[0];
+    d[1] = (q.p[1] - lp.y) + q.plo[1];
+    d[2] = (q.p[2] - lp.z) + q.plo[2];
 }
 
-__device__ __forceinline__ void load_px(const ShadeArgs& a, uint32_t x, uint32_t y, const float p[3], Px& q)
+// Per-pixel record staged in shared memory (96 bytes).
+struct PxRec {
+    float4 p_ref;     // p.xyz, cluster reference (bits; 0xFFFFFFFF = not shaded)
+    float4 n_rough;   // N.xyz, roughness
+    float4 v_metal;   // V.xyz, metallic
+    float4 alb_nv;    // albedo.xyz, NdotV
+    float4 g;         // upstream gradient, 1 - |N|^2
+    float4 plo;       // low part of p
+};
+
+__device__ __forceinline__ void rec_to_px(const PxRec& rec, Px& q)
 {
-    const size_t px = (size_t)y * a.W + x;
-    const float* eye = a.frame->view.eye;
-    float v[3] = {eye[0] - p[0], eye[1] - p[1], eye[2] - p[2]};
-    const float lv = sqrtf(dot3(v, v));
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        q.p[c] = p[c];
-        q.V[c] = v[c] / lv;
-        q.N[c] = a.g.normals[3 * px + c];
-        q.alb[c] = a.g.albedo[3 * px + c];
-    }
-    q.rough = a.g.roughness[px];
-    q.metal = a.g.metallic[px];
-    q.NdotV = fmaxf(dot3(q.N, q.V), 0.0f);
-    q.omn2 = one_minus_norm2(q.N);
+    q.p[0] = rec.p_ref.x; q.p[1] = rec.p_ref.y; q.p[2] = rec.p_ref.z;
+    q.plo[0] = rec.plo.x; q.plo[1] = rec.plo.y; q.plo[2] = rec.plo.z;
+    q.N[0] = rec.n_rough.x; q.N[1] = rec.n_rough.y; q.N[2] = rec.n_rough.z; q.rough = rec.n_rough.w;
+    q.V[0] = rec.v_metal.x; q.V[1] = rec.v_metal.y; q.V[2] = rec.v_metal.z; q.metal = rec.v_metal.w;
+    q.alb[0] = rec.alb_nv.x; q.alb[1] = rec.alb_nv.y; q.alb[2] = rec.alb_nv.z; q.NdotV = rec.alb_nv.w;
+    q.omn2 = rec.g.w;
 }
 
 // pbr_apply_light (pbr.glsl:184-215) for light direction L (from the light towards the point) and
@@ -167,43 +259,16 @@ __device__ __forceinline__ float falloff_value(int mode, float dist, float r)
     return w * w / (dist * dist + 1.0f);
 }
 
-__global__ void __launch_bounds__(256) shade_forward_kernel(ShadeArgs a)
+// pbr_apply_point_light (pbr.glsl:218-232) for one light.
+__device__ __forceinline__ void point_light_fwd(const Px& q, float4 lp, float4 lc, int falloff, float out[3])
 {
-    const uint32_t x = blockIdx.x * 32 + (threadIdx.x & 31u);
-    const uint32_t y = blockIdx.y * 8 + (threadIdx.x >> 5);
-    if (x >= a.W || y >= a.H) return;
-    const size_t px = (size_t)y * a.W + x;
-    float p[3];
-    if (!pixel_world(a.frame, x, y, a.W, a.H, a.g.depth[px], p)) return;
-    Px q;
-    load_px(a, x, y, p, q);
-    float Lo[3] = {0.0f, 0.0f, 0.0f};
-    const uint32_t c = a.lists.cluster_refs[px];
-    const uint32_t cnt = a.L ? a.lists.counts[c] : 0u;
-    const uint32_t off = a.L ? a.lists.offsets[c] : 0u;
-    for (uint32_t i = 0; i < cnt; ++i) {
-        const uint32_t l = a.lists.indices[off + i];
-        const float4 lp = a.lpos[l], lc = a.lights[l];
-        float d[3] = {p[0] - lp.x, p[1] - lp.y, p[2] - lp.z};
-        const float dist = sqrtf(dot3(d, d));
-        const float Ld[3] = {d[0] / dist, d[1] / dist, d[2] / dist};
-        const float att = falloff_value(a.falloff, dist, lc.w);
-        const float rad[3] = {lc.x * att, lc.y * att, lc.z * att};
-        apply_light(q, Ld, rad, Lo);
-    }
-    for (uint32_t i = 0; i < a.ndir; ++i) {
-        const float4 dd = a.dir[2 * i], dc = a.dir[2 * i + 1];
-        const float Ld[3] = {dd.x, dd.y, dd.z};
-        const float rad[3] = {dc.x, dc.y, dc.z};
-        apply_light(q, Ld, rad, Lo);
-    }
-    float o[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k)
-        o[k] = a.mode == VREN_CS_SHADE_COLOR ? powf(0.03f * q.alb[k] + Lo[k], 1.0f / 2.2f) : Lo[k];
-    a.out[3 * px + 0] = o[0];
-    a.out[3 * px + 1] = o[1];
-    a.out[3 * px + 2] = o[2];
+    float d[3];
+    light_offset(q, lp, d);
+    const float dist = sqrtf(dot3(d, d));
+    const float Ld[3] = {d[0] / dist, d[1] / dist, d[2] / dist};
+    const float att = falloff_value(falloff, dist, lc.w);
+    const float rad[3] = {lc.x * att, lc.y * att, lc.z * att};
+    apply_light(q, Ld, rad, out);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -214,7 +279,8 @@ __device__ __forceinline__ void pair_backward(const Px& q, float4 lp, float4 lc,
                                               float g7[7])
 {
     const float r = lc.w;
-    float d[3] = {q.p[0] - lp.x, q.p[1] - lp.y, q.p[2] - lp.z};
+    float d[3];
+    light_offset(q, lp, d);
     const float dd = dot3(d, d);
     const float dist = sqrtf(dd);
     const float L[3] = {d[0] / dist, d[1] / dist, d[2] / dist};
@@ -308,107 +374,278 @@ __device__ __forceinline__ void pair_backward(const Px& q, float4 lp, float4 lc,
     }
 }
 
-// Per-pixel record staged in shared memory by the adjoint (80 bytes).
-struct PxRec {
-    float4 p_ref;     // p.xyz, cluster reference (bits; 0xFFFFFFFF = not shaded)
-    float4 n_rough;   // N.xyz, roughness
-    float4 v_metal;   // V.xyz, metallic
-    float4 alb_nv;    // albedo.xyz, NdotV
-    float4 g;         // upstream gradient, 1 - |N|^2
+// ------------------------------------------------------------------------------------------------
+// Tile staging shared by both passes.  Dynamic shared memory layout:
+//   PxRec px[1024] | uint32 cstart[1025] | uint32 aux[1025] | uint16 lc[1024] | uint16 order[1024]
+// cstart[c] = first position in order[] of local cluster c (packed with the running task count in
+// the forward pass); order[] lists the tile's shaded pixels grouped by cluster, in pixel order.
+// ------------------------------------------------------------------------------------------------
+constexpr int kTileThreads = 256;
+constexpr uint32_t kNoCluster = 0xFFFFu;
+constexpr size_t kStageBytes = 1024 * sizeof(PxRec) + 2 * 1025 * 4 + 2 * 1024 * 2;
+
+struct Stage {
+    PxRec* px;
+    uint32_t* cstart;
+    uint32_t* aux;
+    uint16_t* lc;
+    uint16_t* order;
+    uint32_t cmin, nc;
 };
 
-constexpr int kBwdThreads = 256;
-
-__global__ void __launch_bounds__(kBwdThreads) shade_backward_slots_kernel(ShadeArgs a, const float* __restrict__ grad,
-                                                                           float* __restrict__ slot_grad,
-                                                                           uint32_t n_slots)
+__device__ __forceinline__ Stage stage_layout(float4* dyn)
 {
-    extern __shared__ float4 s_dyn[];
-    PxRec* s_px = reinterpret_cast<PxRec*>(s_dyn);
-    __shared__ uint32_t s_coff[1025];
-    __shared__ uint32_t s_cmin, s_cmax;
+    Stage S;
+    S.px = reinterpret_cast<PxRec*>(dyn);
+    S.cstart = reinterpret_cast<uint32_t*>(S.px + 1024);
+    S.aux = S.cstart + 1025;
+    S.lc = reinterpret_cast<uint16_t*>(S.aux + 1025);
+    S.order = S.lc + 1024;
+    S.cmin = S.nc = 0;
+    return S;
+}
+
+// Exclusive scan of v[0, n) in place (n <= 1025), all threads of the CTA; returns the total.
+__device__ __forceinline__ uint32_t block_scan_1025(uint32_t* v, uint32_t n, uint32_t* s_warp)
+{
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-    const uint32_t TX = (a.W + 31) / 32;
-    const uint32_t tx = blockIdx.x % TX, ty = blockIdx.x / TX;
-    if (tid == 0) {
-        s_cmin = 0xFFFFFFFFu;
-        s_cmax = 0u;
+    // thread t owns entries 5t .. 5t+4 (5 * 256 >= 1025)
+    uint32_t x[5], run = 0;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        const uint32_t i = 5 * tid + k;
+        x[k] = i < n ? v[i] : 0u;
+        run += x[k];
+    }
+    uint32_t incl = run;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+        if (lane >= (uint32_t)d) incl += y;
+    }
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    uint32_t base = incl - run, total = 0;
+#pragma unroll
+    for (int w = 0; w < kTileThreads / 32; ++w) {
+        const uint32_t t = s_warp[w];
+        if (w < (int)warp) base += t;
+        total += t;
+    }
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        const uint32_t i = 5 * tid + k;
+        if (i < n) v[i] = base;
+        base += x[k];
     }
     __syncthreads();
-    uint32_t cmin = 0xFFFFFFFFu, cmax = 0u;
+    return total;
+}
+
+// Stages tile (tx, ty) and groups its shaded pixels by cluster.  Returns false (uniformly) when the
+// tile has no shaded pixel.  A non-null grad loads the upstream gradient as well.
+__device__ __forceinline__ bool stage_tile(const ShadeArgs& a, const float* __restrict__ grad, uint32_t tx, uint32_t ty,
+                                           Stage& S, uint32_t* s_misc)
+{
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    if (tid == 0) {
+        s_misc[8] = 0xFFFFFFFFu;
+        s_misc[9] = 0u;
+    }
+    __syncthreads();
+    uint32_t cmin = 0xFFFFFFFFu, cmax = 0u, refs[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        const uint32_t i = tid + k * kBwdThreads;
+        const uint32_t i = tid + k * kTileThreads;
         const uint32_t x = tx * 32 + (i & 31u), y = ty * 32 + (i >> 5);
         PxRec rec;
         uint32_t ref = 0xFFFFFFFFu;
-        float p[3];
-        if (x < a.W && y < a.H && pixel_world(a.frame, x, y, a.W, a.H, a.g.depth[(size_t)y * a.W + x], p)) {
+        Px q;
+        if (x < a.W && y < a.H && pixel_world(a.frame, x, y, a.W, a.H, a.g.depth[(size_t)y * a.W + x], q.p, q.plo)) {
             const size_t px = (size_t)y * a.W + x;
-            Px q;
-            load_px(a, x, y, p, q);
+            const float* eye = a.frame->view.eye;
+            // eye - (p + plo)
+            const float e[3] = {(eye[0] - q.p[0]) - q.plo[0], (eye[1] - q.p[1]) - q.plo[1],
+                                (eye[2] - q.p[2]) - q.plo[2]};
+            const float le = sqrtf(dot3(e, e));
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                q.V[c] = e[c] / le;
+                q.N[c] = a.g.normals[3 * px + c];
+                q.alb[c] = a.g.albedo[3 * px + c];
+            }
             ref = a.lists.cluster_refs[px];
             rec.p_ref = make_float4(q.p[0], q.p[1], q.p[2], __uint_as_float(ref));
-            rec.n_rough = make_float4(q.N[0], q.N[1], q.N[2], q.rough);
-            rec.v_metal = make_float4(q.V[0], q.V[1], q.V[2], q.metal);
-            rec.alb_nv = make_float4(q.alb[0], q.alb[1], q.alb[2], q.NdotV);
-            rec.g = make_float4(grad[3 * px], grad[3 * px + 1], grad[3 * px + 2], q.omn2);
+            rec.n_rough = make_float4(q.N[0], q.N[1], q.N[2], a.g.roughness[px]);
+            rec.v_metal = make_float4(q.V[0], q.V[1], q.V[2], a.g.metallic[px]);
+            rec.alb_nv = make_float4(q.alb[0], q.alb[1], q.alb[2], fmaxf(dot3(q.N, q.V), 0.0f));
+            const float om = one_minus_norm2(q.N);
+            rec.g = grad ? make_float4(grad[3 * px], grad[3 * px + 1], grad[3 * px + 2], om)
+                         : make_float4(0.0f, 0.0f, 0.0f, om);
+            rec.plo = make_float4(q.plo[0], q.plo[1], q.plo[2], 0.0f);
             cmin = min(cmin, ref);
             cmax = max(cmax, ref);
         } else {
             rec.p_ref = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(0xFFFFFFFFu));
         }
-        s_px[i] = rec;
+        S.px[i] = rec;
+        refs[k] = ref;
     }
     cmin = __reduce_min_sync(0xFFFFFFFFu, cmin);
     cmax = __reduce_max_sync(0xFFFFFFFFu, cmax);
     if (lane == 0) {
-        atomicMin(&s_cmin, cmin);
-        atomicMax(&s_cmax, cmax);
+        atomicMin(&s_misc[8], cmin);
+        atomicMax(&s_misc[9], cmax);
     }
     __syncthreads();
-    cmin = s_cmin;
-    cmax = s_cmax;
-    if (cmin > cmax) return;  // nothing shaded in this tile
-    const uint32_t nc = cmax - cmin + 1;  // <= 1024 (keys of one tile)
-    for (uint32_t c = tid; c <= nc; c += kBwdThreads)
-        s_coff[c] = c < nc ? a.lists.offsets[cmin + c] : a.lists.offsets[cmax] + a.lists.counts[cmax];
+    cmin = s_misc[8];
+    cmax = s_misc[9];
+    if (cmin > cmax) return false;
+    const uint32_t nc = cmax - cmin + 1;  // <= 1024: a tile's clusters are consecutive in the key list
+    if (nc > 1024u) {  // references that no find_unique_cluster_list output can hold
+        if (tid == 0) VREN_RECORD_ERROR(VREN_ERR_ARG);
+        return false;
+    }
+    S.cmin = cmin;
+    S.nc = nc;
+    for (uint32_t c = tid; c <= nc; c += kTileThreads) S.cstart[c] = 0u;
     __syncthreads();
-    const uint32_t s_begin = s_coff[0];
-    uint32_t s_end = s_coff[nc];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const uint32_t i = tid + k * kTileThreads;
+        const uint32_t l = refs[k] == 0xFFFFFFFFu ? kNoCluster : refs[k] - cmin;
+        S.lc[i] = (uint16_t)l;
+        if (l != kNoCluster) atomicAdd(&S.cstart[l], 1u);
+    }
+    __syncthreads();
+    block_scan_1025(S.cstart, nc + 1, s_misc);
+    // Stable grouping: warp 0 walks the 32 rows of pixels in order; peers of one cluster within a
+    // row are ranked by lane, and a per-cluster running count carries the earlier rows.
+    for (uint32_t c = tid; c < nc; c += kTileThreads) S.aux[c] = 0u;
+    __syncthreads();
+    if (warp == 0) {
+        for (uint32_t row = 0; row < 32; ++row) {
+            const uint32_t i = row * 32 + lane;
+            const uint32_t l = S.lc[i];
+            const uint32_t peers = __match_any_sync(0xFFFFFFFFu, l);
+            if (l != kNoCluster) {
+                const uint32_t rank = __popc(peers & lanemask_lt());
+                S.order[S.cstart[l] + S.aux[l] + rank] = (uint16_t)i;
+            }
+            __syncwarp();
+            if (l != kNoCluster && (peers & lanemask_lt()) == 0u) S.aux[l] += __popc(peers);
+            __syncwarp();
+        }
+    }
+    __syncthreads();
+    return true;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Forward
+// ------------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(kTileThreads) shade_forward_kernel(ShadeArgs a)
+{
+    extern __shared__ float4 s_dyn[];
+    __shared__ uint32_t s_misc[16];
+    Stage S = stage_layout(s_dyn);
+    const uint32_t TX = (a.W + 31) / 32;
+    const uint32_t tx = blockIdx.x % TX, ty = blockIdx.x / TX;
+    if (!stage_tile(a, nullptr, tx, ty, S, s_misc)) return;
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const uint32_t nc = S.nc;
+    // tasks: (cluster, chunk of 32 of its pixels); aux[c] = first task of cluster c
+    for (uint32_t c = tid; c <= nc; c += kTileThreads)
+        S.aux[c] = c < nc ? (S.cstart[c + 1] - S.cstart[c] + 31u) / 32u : 0u;
+    __syncthreads();
+    const uint32_t ntasks = block_scan_1025(S.aux, nc + 1, s_misc);
+    for (uint32_t task = warp; task < ntasks; task += kTileThreads / 32) {
+        uint32_t lo = 0, hi = nc - 1;  // last cluster whose first task <= task
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi + 1) >> 1;
+            if (S.aux[mid] <= task) lo = mid;
+            else hi = mid - 1;
+        }
+        const uint32_t c = lo;
+        const uint32_t j = (task - S.aux[c]) * 32u + lane;
+        const uint32_t n = S.cstart[c + 1] - S.cstart[c];
+        const bool valid = j < n;
+        const uint32_t pix = valid ? S.order[S.cstart[c] + j] : 0u;
+        Px q;
+        rec_to_px(S.px[pix], q);
+        float Lo[3] = {0.0f, 0.0f, 0.0f};
+        if (a.L) {
+            const uint32_t cref = S.cmin + c;
+            const uint32_t cnt = a.lists.counts[cref], off = a.lists.offsets[cref];
+            for (uint32_t i = 0; i < cnt; ++i) {
+                const uint32_t l = a.lists.indices[off + i];
+                const float4 lp = a.lpos[l], lc = a.lights[l];
+                if (valid) point_light_fwd(q, lp, lc, a.falloff, Lo);
+            }
+        }
+        if (!valid) continue;
+        for (uint32_t i = 0; i < a.ndir; ++i) {
+            const float4 dd = a.dir[2 * i], dc = a.dir[2 * i + 1];
+            const float Ld[3] = {dd.x, dd.y, dd.z};
+            const float rad[3] = {dc.x, dc.y, dc.z};
+            apply_light(q, Ld, rad, Lo);
+        }
+        const uint32_t x = tx * 32 + (pix & 31u), y = ty * 32 + (pix >> 5);
+        const size_t px = (size_t)y * a.W + x;
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+            a.out[3 * px + k] = a.mode == VREN_CS_SHADE_COLOR ? powf(0.03f * q.alb[k] + Lo[k], 1.0f / 2.2f) : Lo[k];
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// Adjoint, step 1: per-slot partials
+// ------------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(kTileThreads) shade_backward_slots_kernel(ShadeArgs a, const float* __restrict__ grad,
+                                                                            float* __restrict__ slot_grad,
+                                                                            uint32_t n_slots)
+{
+    extern __shared__ float4 s_dyn[];
+    __shared__ uint32_t s_misc[16];
+    Stage S = stage_layout(s_dyn);
+    const uint32_t TX = (a.W + 31) / 32;
+    const uint32_t tx = blockIdx.x % TX, ty = blockIdx.x / TX;
+    if (!stage_tile(a, grad, tx, ty, S, s_misc)) return;
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const uint32_t nc = S.nc, cmin = S.cmin, cmax = cmin + nc - 1;
+    // aux[c] = first slot of cluster c (list offsets); aux[nc] = end of the tile's slots
+    for (uint32_t c = tid; c <= nc; c += kTileThreads)
+        S.aux[c] = c < nc ? a.lists.offsets[cmin + c] : a.lists.offsets[cmax] + a.lists.counts[cmax];
+    __syncthreads();
+    const uint32_t s_begin = S.aux[0];
+    uint32_t s_end = S.aux[nc];
     if (s_end > n_slots) {  // the caller's assignment count does not cover these lists
         if (tid == 0) VREN_RECORD_ERROR(VREN_ERR_CAPACITY);
         s_end = n_slots;
     }
-
-    for (uint32_t s = s_begin + warp; s < s_end; s += kBwdThreads / 32) {
-        // cluster owning slot s: last c with s_coff[c] <= s
-        uint32_t lo = 0, hi = nc - 1;
+    for (uint32_t s = s_begin + warp; s < s_end; s += kTileThreads / 32) {
+        uint32_t lo = 0, hi = nc - 1;  // cluster owning slot s: last c with aux[c] <= s
         while (lo < hi) {
             const uint32_t mid = (lo + hi + 1) >> 1;
-            if (s_coff[mid] <= s) lo = mid;
+            if (S.aux[mid] <= s) lo = mid;
             else hi = mid - 1;
         }
-        const uint32_t cref = cmin + lo;
+        const uint32_t c = lo;
         const uint32_t l = a.lists.indices[s];
         const float4 lp = a.lpos[l], lc = a.lights[l];
+        const uint32_t b = S.cstart[c], n = S.cstart[c + 1] - b;
         float g7[7] = {0, 0, 0, 0, 0, 0, 0};
-        for (uint32_t i = lane; i < 1024; i += 32) {
-            const PxRec& rec = s_px[i];
-            if (__float_as_uint(rec.p_ref.w) != cref) continue;
+        for (uint32_t j = lane; j < n; j += 32) {
+            const PxRec& rec = S.px[S.order[b + j]];
             Px q;
-            q.p[0] = rec.p_ref.x; q.p[1] = rec.p_ref.y; q.p[2] = rec.p_ref.z;
-            q.N[0] = rec.n_rough.x; q.N[1] = rec.n_rough.y; q.N[2] = rec.n_rough.z; q.rough = rec.n_rough.w;
-            q.V[0] = rec.v_metal.x; q.V[1] = rec.v_metal.y; q.V[2] = rec.v_metal.z; q.metal = rec.v_metal.w;
-            q.alb[0] = rec.alb_nv.x; q.alb[1] = rec.alb_nv.y; q.alb[2] = rec.alb_nv.z; q.NdotV = rec.alb_nv.w;
-            q.omn2 = rec.g.w;
+            rec_to_px(rec, q);
             const float gin[3] = {rec.g.x, rec.g.y, rec.g.z};
             pair_backward(q, lp, lc, a.falloff, gin, g7);
         }
 #pragma unroll
-        for (int j = 0; j < 7; ++j)
+        for (int k = 0; k < 7; ++k)
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) g7[j] += __shfl_xor_sync(0xFFFFFFFFu, g7[j], o);
+            for (int o = 16; o > 0; o >>= 1) g7[k] += __shfl_xor_sync(0xFFFFFFFFu, g7[k], o);
         if (lane == 0) {
             float4* dst = reinterpret_cast<float4*>(slot_grad + 8 * (size_t)s);
             dst[0] = make_float4(g7[0], g7[1], g7[2], g7[3]);
@@ -515,8 +752,10 @@ extern "C" int vren_cs_shade(vren_stream_t s, const vren_cs_frame* frame, uint32
     a.falloff = falloff;
     a.mode = output_mode;
     a.out = out_rgb;
-    dim3 grid((width + 31) / 32, (height + 7) / 8);
-    shade_forward_kernel<<<grid, 256, 0, as_stream(s)>>>(a);
+    const uint32_t tiles = ((width + 31) / 32) * ((height + 31) / 32);
+    VREN_CUDA_TRY(cudaFuncSetAttribute(shade_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)kStageBytes));
+    shade_forward_kernel<<<tiles, kTileThreads, kStageBytes, as_stream(s)>>>(a);
     VREN_LAUNCH_CHECK();
     return VREN_OK;
 }
@@ -549,11 +788,11 @@ extern "C" int vren_cs_shade_backward(vren_stream_t s, const vren_cs_frame* fram
     const uint32_t kb = light_key_bits(light_count);
     VREN_CUDA_TRY(cudaMemsetAsync(slot_grad, 0, (size_t)(assignments ? assignments : 1) * 32, st));
     const uint32_t tiles = ((width + 31) / 32) * ((height + 31) / 32);
-    const size_t smem = 1024 * sizeof(PxRec);
     VREN_CUDA_TRY(cudaFuncSetAttribute(shade_backward_slots_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem));
+                                       (int)kStageBytes));
     if (assignments > 0) {
-        shade_backward_slots_kernel<<<tiles, kBwdThreads, smem, st>>>(a, grad_radiance, slot_grad, assignments);
+        shade_backward_slots_kernel<<<tiles, kTileThreads, kStageBytes, st>>>(a, grad_radiance, slot_grad,
+                                                                               assignments);
         VREN_LAUNCH_CHECK();
         uint32_t g = (assignments + 255) / 256;
         if (g > 4096) g = 4096;
