@@ -46,10 +46,12 @@ struct ShadeArgs {
     float* out;
 };
 
+// Per-pixel shading state: position (p + plo), geometry, and the terms of pbr_apply_light that
+// depend on the pixel alone.
 struct Px {
-    float p[3], plo[3], N[3], V[3], alb[3];
-    float rough, metal, NdotV;
-    float omn2;  // 1 - |N|^2
+    float p[3], plo[3], N[3], V[3];
+    float a2, k, k1, omn2, NdotV, ggxV, nv4;
+    float F0[3], omF0[3], kdiff[3];  // Fresnel F0, 1 - F0, (1 - metallic) albedo / PI
 };
 
 __device__ __forceinline__ float dot3(const float* a, const float* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
@@ -60,6 +62,27 @@ __device__ __forceinline__ void cross3(const float* a, const float* b, float* c)
     c[0] = fmaf(a[1], b[2], -(a[2] * b[1]));
     c[1] = fmaf(a[2], b[0], -(a[0] * b[2]));
     c[2] = fmaf(a[0], b[1], -(a[1] * b[0]));
+}
+
+// Hardware approximations (PTX rcp/rsqrt/sqrt .approx, about one ulp): the shading is compared with
+// an FP64 evaluation to 1e-5..1e-4, not bit for bit.
+__device__ __forceinline__ float rcp_a(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float rsqrt_a(float x)
+{
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float sqrt_a(float x)
+{
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -176,17 +199,27 @@ __device__ __forceinline__ float one_minus_norm2(const float* n)
     return __fsub_rn(__fsub_rn(1.0f, hi), lo);
 }
 
-// GGX denominator D = NdotH^2 (a2 - 1) + 1 (pbr.glsl:24-35) for NdotH = max(N.H, 0), H = hv / |hv|.
-// Written as a2 h^2 + (1 - h^2) with Lagrange's identity
-//     1 - (N.H)^2 = ((1 - |N|^2) |hv|^2 + |N x hv|^2) / |hv|^2,
-// whose terms stay accurate near the specular peak, where 1 - (N.H)^2 computed from a rounded N.H
-// would cancel (a2 = roughness^2 can be 0.0025, so D's relative error there would be ~1e-4).
-__device__ __forceinline__ float ggx_den(const float* N, const float* hv, float nhu, float hl2, float omn2, float a2)
+// View vector and the pixel-only terms, from p + plo, N, albedo, roughness and metallic.
+__device__ __forceinline__ void px_terms(Px& q, const float* eye, const float alb[3], float rough, float metal)
 {
-    if (!(nhu > 0.0f)) return 1.0f;
-    float c[3];
-    cross3(N, hv, c);
-    return (a2 * nhu * nhu + fmaf(hl2, omn2, dot3(c, c))) / hl2;
+    const float e[3] = {(eye[0] - q.p[0]) - q.plo[0], (eye[1] - q.p[1]) - q.plo[1], (eye[2] - q.p[2]) - q.plo[2]};
+    const float le = sqrtf(dot3(e, e));
+#pragma unroll
+    for (int c = 0; c < 3; ++c) q.V[c] = e[c] / le;
+    q.a2 = rough * rough;
+    q.k = rough;  // pbr.glsl:14-22 uses k = roughness
+    q.k1 = 1.0f - rough;
+    q.omn2 = one_minus_norm2(q.N);
+    q.NdotV = fmaxf(dot3(q.N, q.V), 0.0f);
+    q.ggxV = q.NdotV / fmaf(q.NdotV, q.k1, q.k);
+    q.nv4 = 4.0f * q.NdotV;
+    const float m1 = 1.0f - metal;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        q.F0[c] = fmaf(alb[c], metal, 0.04f * m1);
+        q.omF0[c] = 1.0f - q.F0[c];
+        q.kdiff[c] = m1 * alb[c] / kPi;
+    }
 }
 
 // Light offset d = p - light position with the low part of p folded in.
@@ -197,66 +230,55 @@ __device__ __forceinline__ void light_offset(const Px& q, float4 lp, float d[3])
     d[2] = (q.p[2] - lp.z) + q.plo[2];
 }
 
-// Per-pixel record staged in shared memory (96 bytes).
-struct PxRec {
-    float4 p_ref;     // p.xyz, cluster reference (bits; 0xFFFFFFFF = not shaded)
-    float4 n_rough;   // N.xyz, roughness
-    float4 v_metal;   // V.xyz, metallic
-    float4 alb_nv;    // albedo.xyz, NdotV
-    float4 g;         // upstream gradient, 1 - |N|^2
-    float4 plo;       // low part of p
-};
-
-__device__ __forceinline__ void rec_to_px(const PxRec& rec, Px& q)
+// GGX denominator D = NdotH^2 (a2 - 1) + 1 (pbr.glsl:24-35) for NdotH = max(N.H, 0), H = hv / |hv|,
+// given nhu = N.hv and rhl = 1 / |hv|.  Written as a2 h^2 + (1 - h^2) with Lagrange's identity
+//     1 - (N.H)^2 = ((1 - |N|^2) |hv|^2 + |N x hv|^2) / |hv|^2,
+// whose terms stay accurate near the specular peak, where 1 - (N.H)^2 computed from a rounded N.H
+// would cancel (a2 = roughness^2 can be 0.0025, so D's relative error there would be ~1e-4).
+__device__ __forceinline__ float ggx_den(const Px& q, const float* hv, float nhu, float hl2, float rhl)
 {
-    q.p[0] = rec.p_ref.x; q.p[1] = rec.p_ref.y; q.p[2] = rec.p_ref.z;
-    q.plo[0] = rec.plo.x; q.plo[1] = rec.plo.y; q.plo[2] = rec.plo.z;
-    q.N[0] = rec.n_rough.x; q.N[1] = rec.n_rough.y; q.N[2] = rec.n_rough.z; q.rough = rec.n_rough.w;
-    q.V[0] = rec.v_metal.x; q.V[1] = rec.v_metal.y; q.V[2] = rec.v_metal.z; q.metal = rec.v_metal.w;
-    q.alb[0] = rec.alb_nv.x; q.alb[1] = rec.alb_nv.y; q.alb[2] = rec.alb_nv.z; q.NdotV = rec.alb_nv.w;
-    q.omn2 = rec.g.w;
+    if (!(nhu > 0.0f)) return 1.0f;
+    float c[3];
+    cross3(q.N, hv, c);
+    return (q.a2 * nhu * nhu + fmaf(hl2, q.omn2, dot3(c, c))) * (rhl * rhl);
 }
 
 // pbr_apply_light (pbr.glsl:184-215) for light direction L (from the light towards the point) and
 // radiance; accumulates into out.
-__device__ __forceinline__ void apply_light(const Px& q, const float L[3], const float rad[3], float out[3])
+__device__ __forceinline__ void brdf_accumulate(const Px& q, const float L[3], const float rad[3], float out[3])
 {
-    float hv[3] = {q.V[0] - L[0], q.V[1] - L[1], q.V[2] - L[2]};
+    const float hv[3] = {q.V[0] - L[0], q.V[1] - L[1], q.V[2] - L[2]};
     const float hl2 = dot3(hv, hv);
-    const float hl = sqrtf(hl2);
-    const float H[3] = {hv[0] / hl, hv[1] / hl, hv[2] / hl};
-    const float a2 = q.rough * q.rough;
-    const float D = ggx_den(q.N, hv, dot3(q.N, hv), hl2, q.omn2, a2);
-    const float NDF = a2 / (kPi * D * D);
-    const float k = q.rough;
-    const float nl = -dot3(q.N, L);
-    const float NdotL = fmaxf(nl, 0.0f);
-    const float ggxV = q.NdotV / (q.NdotV * (1.0f - k) + k);
-    const float ggxL = NdotL / (NdotL * (1.0f - k) + k);
-    const float G = ggxV * ggxL;
+    const float rhl = rsqrt_a(hl2);
+    const float H[3] = {hv[0] * rhl, hv[1] * rhl, hv[2] * rhl};
+    const float D = ggx_den(q, hv, dot3(q.N, hv), hl2, rhl);
+    const float NDF = q.a2 * rcp_a(kPi * D * D);
+    const float NdotL = fmaxf(-dot3(q.N, L), 0.0f);
+    const float G = q.ggxV * NdotL * rcp_a(fmaf(NdotL, q.k1, q.k));
     const float HdotV = fmaxf(dot3(H, q.V), 0.0f);
     const float x = 1.0f - HdotV;
-    const float f5 = x * x * x * x * x;
-    const float spec = NDF * G / (4.0f * q.NdotV * NdotL + 0.0001f);
+    const float x2 = x * x;
+    const float f5 = x2 * x2 * x;
+    const float spec = NDF * G * rcp_a(fmaf(q.nv4, NdotL, 0.0001f));
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        const float F0 = 0.04f * (1.0f - q.metal) + q.alb[c] * q.metal;
-        const float F = F0 + (1.0f - F0) * f5;
-        const float kD = (1.0f - F) * (1.0f - q.metal);
-        out[c] += fmaxf((kD * q.alb[c] / kPi + F * spec) * rad[c] * NdotL, 0.0f);
+        const float F = fmaf(q.omF0[c], f5, q.F0[c]);
+        const float B = fmaf(1.0f - F, q.kdiff[c], F * spec);
+        out[c] += fmaxf(B * rad[c] * NdotL, 0.0f);
     }
 }
 
-__device__ __forceinline__ float falloff_value(int mode, float dist, float r)
+// Attenuation: reference 1 - min(d/r, 1)^1.5 (pbr.glsl:231) or windowed inverse square.
+__device__ __forceinline__ float falloff_value(int mode, float dist, float dd, float rr)
 {
+    const float t = dist * rr;
     if (mode == VREN_CS_FALLOFF_REF) {
-        const float u = fminf(dist / r, 1.0f);
-        return 1.0f - u * sqrtf(u);
+        const float u = fminf(t, 1.0f);
+        return 1.0f - u * sqrt_a(u);
     }
-    const float t = dist / r;
     const float t2 = t * t;
     const float w = fminf(fmaxf(1.0f - t2 * t2, 0.0f), 1.0f);
-    return w * w / (dist * dist + 1.0f);
+    return w * w * rcp_a(dd + 1.0f);
 }
 
 // pbr_apply_point_light (pbr.glsl:218-232) for one light.
@@ -264,11 +286,12 @@ __device__ __forceinline__ void point_light_fwd(const Px& q, float4 lp, float4 l
 {
     float d[3];
     light_offset(q, lp, d);
-    const float dist = sqrtf(dot3(d, d));
-    const float Ld[3] = {d[0] / dist, d[1] / dist, d[2] / dist};
-    const float att = falloff_value(falloff, dist, lc.w);
+    const float dd = dot3(d, d);
+    const float rdist = rsqrt_a(dd);
+    const float Ld[3] = {d[0] * rdist, d[1] * rdist, d[2] * rdist};
+    const float att = falloff_value(falloff, dd * rdist, dd, rcp_a(lc.w));
     const float rad[3] = {lc.x * att, lc.y * att, lc.z * att};
-    apply_light(q, Ld, rad, out);
+    brdf_accumulate(q, Ld, rad, out);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -278,78 +301,75 @@ __device__ __forceinline__ void point_light_fwd(const Px& q, float4 lp, float4 l
 __device__ __forceinline__ void pair_backward(const Px& q, float4 lp, float4 lc, int falloff, const float gin[3],
                                               float g7[7])
 {
-    const float r = lc.w;
+    const float rr = rcp_a(lc.w);
     float d[3];
     light_offset(q, lp, d);
     const float dd = dot3(d, d);
-    const float dist = sqrtf(dd);
-    const float L[3] = {d[0] / dist, d[1] / dist, d[2] / dist};
-    const float t = dist / r;
+    const float rdist = rsqrt_a(dd);
+    const float dist = dd * rdist;
+    const float L[3] = {d[0] * rdist, d[1] * rdist, d[2] * rdist};
+    const float t = dist * rr;
     float att, datt_dt, datt_ddist_direct = 0.0f;
     if (falloff == VREN_CS_FALLOFF_REF) {
         const float u = fminf(t, 1.0f);
-        att = 1.0f - u * sqrtf(u);
-        datt_dt = t < 1.0f ? -1.5f * sqrtf(t) : 0.0f;
+        const float su = sqrt_a(u);
+        att = 1.0f - u * su;
+        datt_dt = t < 1.0f ? -1.5f * su : 0.0f;
     } else {
         const float t2 = t * t;
         const float wr = 1.0f - t2 * t2;
         const float w = fminf(fmaxf(wr, 0.0f), 1.0f);
-        const float den = dd + 1.0f;
-        att = w * w / den;
+        const float rden = rcp_a(dd + 1.0f);
+        att = w * w * rden;
         const float dw_dt = (wr > 0.0f && wr < 1.0f) ? -4.0f * t2 * t : 0.0f;
-        datt_dt = 2.0f * w / den * dw_dt;
-        datt_ddist_direct = -w * w * 2.0f * dist / (den * den);
+        datt_dt = 2.0f * w * rden * dw_dt;
+        datt_ddist_direct = -w * w * 2.0f * dist * rden * rden;
     }
     const float col[3] = {lc.x, lc.y, lc.z};
 
-    float hv[3] = {q.V[0] - L[0], q.V[1] - L[1], q.V[2] - L[2]};
+    const float hv[3] = {q.V[0] - L[0], q.V[1] - L[1], q.V[2] - L[2]};
     const float hl2 = dot3(hv, hv);
-    const float hl = sqrtf(hl2);
-    const float H[3] = {hv[0] / hl, hv[1] / hl, hv[2] / hl};
-    const float a2 = q.rough * q.rough;
+    const float rhl = rsqrt_a(hl2);
+    const float H[3] = {hv[0] * rhl, hv[1] * rhl, hv[2] * rhl};
     const float nhu = dot3(q.N, hv);  // |hv| (N.H)
-    const float NdotH = fmaxf(nhu / hl, 0.0f);
-    const float D = ggx_den(q.N, hv, nhu, hl2, q.omn2, a2);
-    const float NDF = a2 / (kPi * D * D);
-    const float k = q.rough;
+    const float NdotH = fmaxf(nhu * rhl, 0.0f);
+    const float D = ggx_den(q, hv, nhu, hl2, rhl);
+    const float rD = rcp_a(D);
+    const float NDF = q.a2 * (rD * rD) * (1.0f / kPi);
     const float nl_raw = -dot3(q.N, L);
     const float NdotL = fmaxf(nl_raw, 0.0f);
-    const float ggxV = q.NdotV / (q.NdotV * (1.0f - k) + k);
-    const float dl = NdotL * (1.0f - k) + k;
-    const float ggxL = NdotL / dl;
-    const float G = ggxV * ggxL;
+    const float rdl = rcp_a(fmaf(NdotL, q.k1, q.k));
+    const float G = q.ggxV * NdotL * rdl;
     const float hvr = dot3(H, q.V);
     const float HdotV = fmaxf(hvr, 0.0f);
     const float x = 1.0f - HdotV;
-    const float x4 = x * x * x * x;
+    const float x2 = x * x;
+    const float x4 = x2 * x2;
     const float f5 = x4 * x;
-    const float sden = 4.0f * q.NdotV * NdotL + 0.0001f;
-    const float spec = NDF * G / sden;
+    const float rs = rcp_a(fmaf(q.nv4, NdotL, 0.0001f));
+    const float spec = NDF * G * rs;
 
+    const float an = att * NdotL;
     float gatt = 0.0f, gNdotL = 0.0f, gspec = 0.0f, gf5 = 0.0f;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        const float F0 = 0.04f * (1.0f - q.metal) + q.alb[c] * q.metal;
-        const float F = F0 + (1.0f - F0) * f5;
-        const float kD = (1.0f - F) * (1.0f - q.metal);
-        const float B = kD * q.alb[c] / kPi + F * spec;
-        const float val = B * col[c] * att * NdotL;
-        const float gv = val > 0.0f ? gin[c] : 0.0f;
-        const float gB = gv * col[c] * att * NdotL;
-        g7[3 + c] += gv * B * att * NdotL;  // colour
-        gatt += gv * B * col[c] * NdotL;
-        gNdotL += gv * B * col[c] * att;
-        const float gF = gB * (spec - (1.0f - q.metal) * q.alb[c] / kPi);
+        const float F = fmaf(q.omF0[c], f5, q.F0[c]);
+        const float B = fmaf(1.0f - F, q.kdiff[c], F * spec);
+        const float gv = B * col[c] * an > 0.0f ? gin[c] : 0.0f;
+        const float gvB = gv * B;
+        const float gB = gv * col[c] * an;
+        g7[3 + c] += gvB * an;  // colour
+        gatt += gvB * col[c] * NdotL;
+        gNdotL += gvB * col[c] * att;
         gspec += gB * F;
-        gf5 += gF * (1.0f - F0);
+        gf5 += gB * (spec - q.kdiff[c]) * q.omF0[c];
     }
-    const float gHdotV = -gf5 * 5.0f * x4;
-    const float gNDF = gspec * G / sden;
-    const float gG = gspec * NDF / sden;
-    const float gsden = -gspec * NDF * G / (sden * sden);
-    gNdotL += gsden * 4.0f * q.NdotV;
-    gNdotL += gG * ggxV * k / (dl * dl);
-    const float gNdotH = gNDF * (-4.0f * a2 * NdotH * (a2 - 1.0f) / (kPi * D * D * D));
+    const float gHdotV = -5.0f * gf5 * x4;
+    const float gNDF = gspec * G * rs;
+    const float gG = gspec * NDF * rs;
+    gNdotL += -gspec * spec * rs * q.nv4;             // through the specular denominator
+    gNdotL += gG * q.ggxV * q.k * (rdl * rdl);        // d(NdotL / (NdotL (1 - k) + k))
+    const float gNdotH = gNDF * (-4.0f * (q.a2 - 1.0f) * NdotH) * NDF * rD;
     const float gnl = nl_raw > 0.0f ? gNdotL : 0.0f;
     const float gnh = nhu > 0.0f ? gNdotH : 0.0f;
     const float ghv = hvr > 0.0f ? gHdotV : 0.0f;
@@ -358,54 +378,90 @@ __device__ __forceinline__ void pair_backward(const Px& q, float4 lp, float4 lc,
     float nxh[3], tri[3];
     cross3(q.N, hv, nxh);
     cross3(hv, nxh, tri);
-    const float sn = gnh / (hl2 * hl), sv = ghv / hl;
+    const float sn = gnh * rhl * rhl * rhl, sv = ghv * rhl;
     float gL[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) gL[c] = -gnl * q.N[c] - sn * tri[c] - sv * (q.V[c] - H[c] * hvr);
     // attenuation: t = dist / r
     const float gt = gatt * datt_dt;
-    const float gdist = gatt * datt_ddist_direct + gt / r;
-    g7[6] += -gt * dist / (r * r);  // radius
+    const float gdist = gatt * datt_ddist_direct + gt * rr;
+    g7[6] += -gt * dist * rr * rr;  // radius
     const float gLL = dot3(gL, L);
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        const float gd = (gL[c] - L[c] * gLL) / dist + gdist * L[c];
+        const float gd = (gL[c] - L[c] * gLL) * rdist + gdist * L[c];
         g7[c] += -gd;  // d = p - light position
+    }
+}
+
+// Per-pixel record staged in shared memory by the adjoint (96 bytes).
+struct PxRec {
+    float4 p_ref;     // p.xyz, cluster reference (bits; 0xFFFFFFFF = not shaded)
+    float4 n_rough;   // N.xyz, roughness
+    float4 v_metal;   // V.xyz, metallic
+    float4 alb_nv;    // albedo.xyz, NdotV
+    float4 g;         // upstream gradient, 1 - |N|^2
+    float4 plo;       // low part of p, ggxV
+};
+
+__device__ __forceinline__ void rec_to_px(const PxRec& rec, Px& q)
+{
+    q.p[0] = rec.p_ref.x; q.p[1] = rec.p_ref.y; q.p[2] = rec.p_ref.z;
+    q.plo[0] = rec.plo.x; q.plo[1] = rec.plo.y; q.plo[2] = rec.plo.z;
+    q.N[0] = rec.n_rough.x; q.N[1] = rec.n_rough.y; q.N[2] = rec.n_rough.z;
+    q.V[0] = rec.v_metal.x; q.V[1] = rec.v_metal.y; q.V[2] = rec.v_metal.z;
+    const float rough = rec.n_rough.w, metal = rec.v_metal.w;
+    q.a2 = rough * rough;
+    q.k = rough;
+    q.k1 = 1.0f - rough;
+    q.omn2 = rec.g.w;
+    q.NdotV = rec.alb_nv.w;
+    q.ggxV = rec.plo.w;
+    q.nv4 = 4.0f * q.NdotV;
+    const float m1 = 1.0f - metal;
+    const float alb[3] = {rec.alb_nv.x, rec.alb_nv.y, rec.alb_nv.z};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        q.F0[c] = fmaf(alb[c], metal, 0.04f * m1);
+        q.omF0[c] = 1.0f - q.F0[c];
+        q.kdiff[c] = m1 * alb[c] * (1.0f / kPi);
     }
 }
 
 // ------------------------------------------------------------------------------------------------
 // Tile staging shared by both passes.  Dynamic shared memory layout:
-//   PxRec px[1024] | uint32 cstart[1025] | uint32 aux[1025] | uint16 lc[1024] | uint16 order[1024]
-// cstart[c] = first position in order[] of local cluster c (packed with the running task count in
-// the forward pass); order[] lists the tile's shaded pixels grouped by cluster, in pixel order.
+//   uint32 cstart[1025] | uint32 aux[1025] | uint16 lc[1024] | uint16 order[1024] | PxRec px[1024]
+// (the last only for the adjoint).  cstart[c] = first position in order[] of local cluster c;
+// order[] lists the tile's shaded pixels grouped by cluster, in pixel order.
 // ------------------------------------------------------------------------------------------------
 constexpr int kTileThreads = 256;
 constexpr uint32_t kNoCluster = 0xFFFFu;
-constexpr size_t kStageBytes = 1024 * sizeof(PxRec) + 2 * 1025 * 4 + 2 * 1024 * 2;
+constexpr size_t kGroupBytes = (2 * 1025 * 4 + 2 * 1024 * 2 + 15) / 16 * 16;
+constexpr size_t kStageBytes = kGroupBytes + 1024 * sizeof(PxRec);
 
 struct Stage {
-    PxRec* px;
     uint32_t* cstart;
     uint32_t* aux;
     uint16_t* lc;
     uint16_t* order;
+    PxRec* px;
     uint32_t cmin, nc;
 };
 
 __device__ __forceinline__ Stage stage_layout(float4* dyn)
 {
     Stage S;
-    S.px = reinterpret_cast<PxRec*>(dyn);
-    S.cstart = reinterpret_cast<uint32_t*>(S.px + 1024);
+    char* base = reinterpret_cast<char*>(dyn);
+    S.cstart = reinterpret_cast<uint32_t*>(base);
     S.aux = S.cstart + 1025;
     S.lc = reinterpret_cast<uint16_t*>(S.aux + 1025);
     S.order = S.lc + 1024;
+    S.px = reinterpret_cast<PxRec*>(base + kGroupBytes);
     S.cmin = S.nc = 0;
     return S;
 }
 
-// Exclusive scan of v[0, n) in place (n <= 1025), all threads of the CTA; returns the total.
+// Exclusive scan of v[0, n) in place (n <= 1280), all threads of the CTA; returns the total.
 __device__ __forceinline__ uint32_t block_scan_1025(uint32_t* v, uint32_t n, uint32_t* s_warp)
 {
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
@@ -442,8 +498,9 @@ __device__ __forceinline__ uint32_t block_scan_1025(uint32_t* v, uint32_t n, uin
     return total;
 }
 
-// Stages tile (tx, ty) and groups its shaded pixels by cluster.  Returns false (uniformly) when the
-// tile has no shaded pixel.  A non-null grad loads the upstream gradient as well.
+// Groups tile (tx, ty)'s shaded pixels by cluster; with RECORDS also stages their records (and the
+// upstream gradient).  Returns false (uniformly) when the tile has no shaded pixel.
+template <bool RECORDS>
 __device__ __forceinline__ bool stage_tile(const ShadeArgs& a, const float* __restrict__ grad, uint32_t tx, uint32_t ty,
                                            Stage& S, uint32_t* s_misc)
 {
@@ -458,37 +515,34 @@ __device__ __forceinline__ bool stage_tile(const ShadeArgs& a, const float* __re
     for (int k = 0; k < 4; ++k) {
         const uint32_t i = tid + k * kTileThreads;
         const uint32_t x = tx * 32 + (i & 31u), y = ty * 32 + (i >> 5);
-        PxRec rec;
         uint32_t ref = 0xFFFFFFFFu;
         Px q;
-        if (x < a.W && y < a.H && pixel_world(a.frame, x, y, a.W, a.H, a.g.depth[(size_t)y * a.W + x], q.p, q.plo)) {
+        const bool shaded =
+            x < a.W && y < a.H && pixel_world(a.frame, x, y, a.W, a.H, a.g.depth[(size_t)y * a.W + x], q.p, q.plo);
+        if (shaded) {
             const size_t px = (size_t)y * a.W + x;
-            const float* eye = a.frame->view.eye;
-            // eye - (p + plo)
-            const float e[3] = {(eye[0] - q.p[0]) - q.plo[0], (eye[1] - q.p[1]) - q.plo[1],
-                                (eye[2] - q.p[2]) - q.plo[2]};
-            const float le = sqrtf(dot3(e, e));
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                q.V[c] = e[c] / le;
-                q.N[c] = a.g.normals[3 * px + c];
-                q.alb[c] = a.g.albedo[3 * px + c];
-            }
             ref = a.lists.cluster_refs[px];
-            rec.p_ref = make_float4(q.p[0], q.p[1], q.p[2], __uint_as_float(ref));
-            rec.n_rough = make_float4(q.N[0], q.N[1], q.N[2], a.g.roughness[px]);
-            rec.v_metal = make_float4(q.V[0], q.V[1], q.V[2], a.g.metallic[px]);
-            rec.alb_nv = make_float4(q.alb[0], q.alb[1], q.alb[2], fmaxf(dot3(q.N, q.V), 0.0f));
-            const float om = one_minus_norm2(q.N);
-            rec.g = grad ? make_float4(grad[3 * px], grad[3 * px + 1], grad[3 * px + 2], om)
-                         : make_float4(0.0f, 0.0f, 0.0f, om);
-            rec.plo = make_float4(q.plo[0], q.plo[1], q.plo[2], 0.0f);
             cmin = min(cmin, ref);
             cmax = max(cmax, ref);
-        } else {
-            rec.p_ref = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(0xFFFFFFFFu));
+            if (RECORDS) {
+                float alb[3];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    q.N[c] = a.g.normals[3 * px + c];
+                    alb[c] = a.g.albedo[3 * px + c];
+                }
+                const float rough = a.g.roughness[px], metal = a.g.metallic[px];
+                px_terms(q, a.frame->view.eye, alb, rough, metal);
+                PxRec rec;
+                rec.p_ref = make_float4(q.p[0], q.p[1], q.p[2], __uint_as_float(ref));
+                rec.n_rough = make_float4(q.N[0], q.N[1], q.N[2], rough);
+                rec.v_metal = make_float4(q.V[0], q.V[1], q.V[2], metal);
+                rec.alb_nv = make_float4(alb[0], alb[1], alb[2], q.NdotV);
+                rec.g = make_float4(grad[3 * px], grad[3 * px + 1], grad[3 * px + 2], q.omn2);
+                rec.plo = make_float4(q.plo[0], q.plo[1], q.plo[2], q.ggxV);
+                S.px[i] = rec;
+            }
         }
-        S.px[i] = rec;
         refs[k] = ref;
     }
     cmin = __reduce_min_sync(0xFFFFFFFFu, cmin);
@@ -508,7 +562,10 @@ __device__ __forceinline__ bool stage_tile(const ShadeArgs& a, const float* __re
     }
     S.cmin = cmin;
     S.nc = nc;
-    for (uint32_t c = tid; c <= nc; c += kTileThreads) S.cstart[c] = 0u;
+    for (uint32_t c = tid; c <= nc; c += kTileThreads) {
+        S.cstart[c] = 0u;
+        S.aux[c] = 0u;
+    }
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
@@ -520,20 +577,16 @@ __device__ __forceinline__ bool stage_tile(const ShadeArgs& a, const float* __re
     __syncthreads();
     block_scan_1025(S.cstart, nc + 1, s_misc);
     // Stable grouping: warp 0 walks the 32 rows of pixels in order; peers of one cluster within a
-    // row are ranked by lane, and a per-cluster running count carries the earlier rows.
-    for (uint32_t c = tid; c < nc; c += kTileThreads) S.aux[c] = 0u;
-    __syncthreads();
+    // row are ranked by lane, and a per-cluster running count (aux) carries the earlier rows.
     if (warp == 0) {
         for (uint32_t row = 0; row < 32; ++row) {
             const uint32_t i = row * 32 + lane;
             const uint32_t l = S.lc[i];
             const uint32_t peers = __match_any_sync(0xFFFFFFFFu, l);
-            if (l != kNoCluster) {
-                const uint32_t rank = __popc(peers & lanemask_lt());
-                S.order[S.cstart[l] + S.aux[l] + rank] = (uint16_t)i;
-            }
+            const uint32_t before = peers & lanemask_lt();
+            if (l != kNoCluster) S.order[S.cstart[l] + S.aux[l] + __popc(before)] = (uint16_t)i;
             __syncwarp();
-            if (l != kNoCluster && (peers & lanemask_lt()) == 0u) S.aux[l] += __popc(peers);
+            if (l != kNoCluster && before == 0u) S.aux[l] += __popc(peers);
             __syncwarp();
         }
     }
@@ -551,7 +604,7 @@ __global__ void __launch_bounds__(kTileThreads) shade_forward_kernel(ShadeArgs a
     Stage S = stage_layout(s_dyn);
     const uint32_t TX = (a.W + 31) / 32;
     const uint32_t tx = blockIdx.x % TX, ty = blockIdx.x / TX;
-    if (!stage_tile(a, nullptr, tx, ty, S, s_misc)) return;
+    if (!stage_tile<false>(a, nullptr, tx, ty, S, s_misc)) return;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const uint32_t nc = S.nc;
     // tasks: (cluster, chunk of 32 of its pixels); aux[c] = first task of cluster c
@@ -559,6 +612,7 @@ __global__ void __launch_bounds__(kTileThreads) shade_forward_kernel(ShadeArgs a
         S.aux[c] = c < nc ? (S.cstart[c + 1] - S.cstart[c] + 31u) / 32u : 0u;
     __syncthreads();
     const uint32_t ntasks = block_scan_1025(S.aux, nc + 1, s_misc);
+    const float* eye = a.frame->view.eye;
     for (uint32_t task = warp; task < ntasks; task += kTileThreads / 32) {
         uint32_t lo = 0, hi = nc - 1;  // last cluster whose first task <= task
         while (lo < hi) {
@@ -568,33 +622,39 @@ __global__ void __launch_bounds__(kTileThreads) shade_forward_kernel(ShadeArgs a
         }
         const uint32_t c = lo;
         const uint32_t j = (task - S.aux[c]) * 32u + lane;
-        const uint32_t n = S.cstart[c + 1] - S.cstart[c];
-        const bool valid = j < n;
-        const uint32_t pix = valid ? S.order[S.cstart[c] + j] : 0u;
+        const bool valid = j < S.cstart[c + 1] - S.cstart[c];
+        const uint32_t pix = valid ? S.order[S.cstart[c] + j] : S.order[S.cstart[c]];
+        const uint32_t x = tx * 32 + (pix & 31u), y = ty * 32 + (pix >> 5);
+        const size_t px = (size_t)y * a.W + x;
         Px q;
-        rec_to_px(S.px[pix], q);
+        pixel_world(a.frame, x, y, a.W, a.H, a.g.depth[px], q.p, q.plo);
+        float alb[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            q.N[k] = a.g.normals[3 * px + k];
+            alb[k] = a.g.albedo[3 * px + k];
+        }
+        px_terms(q, eye, alb, a.g.roughness[px], a.g.metallic[px]);
         float Lo[3] = {0.0f, 0.0f, 0.0f};
         if (a.L) {
             const uint32_t cref = S.cmin + c;
-            const uint32_t cnt = a.lists.counts[cref], off = a.lists.offsets[cref];
+            const uint32_t cnt = a.lists.counts[cref];
+            const uint32_t* idx = a.lists.indices + a.lists.offsets[cref];
             for (uint32_t i = 0; i < cnt; ++i) {
-                const uint32_t l = a.lists.indices[off + i];
-                const float4 lp = a.lpos[l], lc = a.lights[l];
-                if (valid) point_light_fwd(q, lp, lc, a.falloff, Lo);
+                const uint32_t l = idx[i];
+                point_light_fwd(q, a.lpos[l], a.lights[l], a.falloff, Lo);
             }
         }
-        if (!valid) continue;
         for (uint32_t i = 0; i < a.ndir; ++i) {
             const float4 dd = a.dir[2 * i], dc = a.dir[2 * i + 1];
             const float Ld[3] = {dd.x, dd.y, dd.z};
             const float rad[3] = {dc.x, dc.y, dc.z};
-            apply_light(q, Ld, rad, Lo);
+            brdf_accumulate(q, Ld, rad, Lo);
         }
-        const uint32_t x = tx * 32 + (pix & 31u), y = ty * 32 + (pix >> 5);
-        const size_t px = (size_t)y * a.W + x;
+        if (!valid) continue;
 #pragma unroll
         for (int k = 0; k < 3; ++k)
-            a.out[3 * px + k] = a.mode == VREN_CS_SHADE_COLOR ? powf(0.03f * q.alb[k] + Lo[k], 1.0f / 2.2f) : Lo[k];
+            a.out[3 * px + k] = a.mode == VREN_CS_SHADE_COLOR ? powf(0.03f * alb[k] + Lo[k], 1.0f / 2.2f) : Lo[k];
     }
 }
 
@@ -610,7 +670,7 @@ __global__ void __launch_bounds__(kTileThreads) shade_backward_slots_kernel(Shad
     Stage S = stage_layout(s_dyn);
     const uint32_t TX = (a.W + 31) / 32;
     const uint32_t tx = blockIdx.x % TX, ty = blockIdx.x / TX;
-    if (!stage_tile(a, grad, tx, ty, S, s_misc)) return;
+    if (!stage_tile<true>(a, grad, tx, ty, S, s_misc)) return;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const uint32_t nc = S.nc, cmin = S.cmin, cmax = cmin + nc - 1;
     // aux[c] = first slot of cluster c (list offsets); aux[nc] = end of the tile's slots
@@ -753,9 +813,7 @@ extern "C" int vren_cs_shade(vren_stream_t s, const vren_cs_frame* frame, uint32
     a.mode = output_mode;
     a.out = out_rgb;
     const uint32_t tiles = ((width + 31) / 32) * ((height + 31) / 32);
-    VREN_CUDA_TRY(cudaFuncSetAttribute(shade_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)kStageBytes));
-    shade_forward_kernel<<<tiles, kTileThreads, kStageBytes, as_stream(s)>>>(a);
+    shade_forward_kernel<<<tiles, kTileThreads, kGroupBytes, as_stream(s)>>>(a);
     VREN_LAUNCH_CHECK();
     return VREN_OK;
 }
