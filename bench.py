@@ -37,6 +37,10 @@ SEED = 20240611
 RADIX_N = 1 << 20
 L2_FLUSH_BYTES = 256 << 20
 BYTES_PER_PX = 20  # depth 4 + normal 12 + cluster reference 4
+# DRAM bytes (read + write) of one find_unique launch at 1920x1080: one ncu capture at 3840x2160
+# (profiles/find_unique_3840x2160.md: 133.8 MB read + 18.0 MB written) scaled by the pixel count (1/4).
+FUC_TRAFFIC_BYTES = int((133.809152 + 17.965312) * 1e6 / 4)
+FUC_TRAFFIC_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum at 3840x2160, scaled by pixels to 1920x1080"
 
 
 def peaks():
@@ -295,7 +299,8 @@ def run_ours(args, rank: int, world: int):
             "gpu_launches": launches_per_frame * args.steps,
             "roofline": {"bound": "hbm", "kernel": "find_unique_kernel", "achieved": round(fuc_gbs, 1),
                          "peak": hbm_peak, "unit": "GB/s", "frac": round(fuc_gbs / hbm_peak, 4),
-                         "peak_kind": peak_kind, "traffic": None,
+                         "peak_kind": peak_kind, "traffic": FUC_TRAFFIC_BYTES,
+                         "traffic_source": FUC_TRAFFIC_SOURCE,
                          "algorithmic_bytes": fuc_bytes, "kernel_ms": round(fuc_ms, 5)},
             "radix_sort": radix,
             "batched_vs_plain": None,
