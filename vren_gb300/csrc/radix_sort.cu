@@ -213,9 +213,10 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_pass_kernel(
             uint32_t peers = __ballot_sync(0xFFFFFFFFu, valid);
 #pragma unroll
             for (int b = 0; b < DIGIT_BITS; ++b) {
-                const bool bit = (d >> b) & 1u;
-                const uint32_t m = __ballot_sync(0xFFFFFFFFu, bit);
-                peers &= bit ? m : ~m;
+                const uint32_t m = __ballot_sync(0xFFFFFFFFu, (d >> b) & 1u);
+                // keep the lanes whose bit b equals mine: m where my bit is 1, ~m where it is 0
+                const uint32_t mine = (uint32_t)((int32_t)(d << (31 - b)) >> 31);
+                peers &= ~(m ^ mine);
             }
             uint32_t before = 0;
             if (valid) before = s_warp_hist[warp][d];
@@ -248,25 +249,16 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_pass_kernel(
     }
     if (lane == 31) s_wsum[warp] = incl;
     __syncthreads();
+    // Tile-local digit offsets, and the first look-back read for digit d issued now: its latency
+    // overlaps the staging below, which needs only tile-local offsets.
+    uint32_t excl = 0, lb_word = 0, goff = 0;
     if (tid < (uint32_t)RADIX) {
         const uint32_t d = tid;
-        uint32_t excl = incl - count;
+        excl = incl - count;
         for (uint32_t w = 0; w < warp; ++w) excl += s_wsum[w];
         s_tile_excl[d] = excl;
-        // Decoupled look-back for digit d.
-        uint32_t prefix = 0;
-        if (tile != 0) {
-            int64_t t = (int64_t)tile - 1;
-            while (t >= 0) {
-                const uint32_t w = wait_for_flag(status + (size_t)t * RADIX + d, wait_limit, spin,
-                                                 [] { VREN_RECORD_ERROR(VREN_ERR_TIMEOUT); });
-                prefix += w & kValueMask;
-                if (w & kFlagPrefix) break;
-                --t;
-            }
-            st_relaxed_u32(status + (size_t)tile * RADIX + d, kFlagPrefix | (prefix + count));
-        }
-        s_delta[d] = (int32_t)(ld_relaxed_u32(scratch + kOffsOffset + pass * kMaxRadix + d) + prefix) - (int32_t)excl;
+        if (tile != 0) lb_word = ld_relaxed_u32(status + (size_t)(tile - 1) * RADIX + d);
+        goff = ld_relaxed_u32(scratch + kOffsOffset + pass * kMaxRadix + d);
     }
     __syncthreads();
 
@@ -279,6 +271,27 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_pass_kernel(
             s_keys[p] = key[j];
             if (MODE == kPairs) s_vals[p] = val[j];
         }
+    }
+
+    // Decoupled look-back for digit d (thread d), starting from the word read before staging.
+    if (tid < (uint32_t)RADIX) {
+        const uint32_t d = tid;
+        uint32_t prefix = 0;
+        if (tile != 0) {
+            int64_t t = (int64_t)tile - 1;
+            uint32_t w = lb_word;
+            while (true) {
+                if (!(w & (3u << kFlagShift)))
+                    w = wait_for_flag(status + (size_t)t * RADIX + d, wait_limit, spin,
+                                      [] { VREN_RECORD_ERROR(VREN_ERR_TIMEOUT); });
+                prefix += w & kValueMask;
+                if ((w & kFlagPrefix) || t == 0) break;
+                --t;
+                w = ld_relaxed_u32(status + (size_t)t * RADIX + d);
+            }
+            st_relaxed_u32(status + (size_t)tile * RADIX + d, kFlagPrefix | (prefix + count));
+        }
+        s_delta[d] = (int32_t)(goff + prefix) - (int32_t)excl;
     }
     __syncthreads();
 
