@@ -392,6 +392,57 @@ int vren_cs_cluster(vren_cluster_and_shade* cs, vren_stream_t s, const vren_cs_v
                     const float* light_positions, const float* point_lights, uint32_t light_count);
 int vren_cs_get_outputs(const vren_cluster_and_shade* cs, vren_cs_outputs* out);
 
+/* ------------------------------------------------------------------------------------------------
+ * Batched cluster assignment (no counterpart in the reference, which runs one frame per
+ * cluster_and_shade call).  Many independent frames - each with its own camera, resolution,
+ * G-buffer and light set - go through one fixed kernel sequence (light view transform, Morton
+ * codes, one stable sort of all frames' lights keyed by (frame, code), leaves and BVH levels,
+ * unique clusters over all frames' tiles, traversal count, one scan, traversal write), replayed as
+ * one CUDA graph.  Every frame's outputs are bit-identical to vren_cs_cluster on the same inputs
+ * with the same morton bits (15 only; the 30-bit extension is per-frame only).
+ * ------------------------------------------------------------------------------------------------ */
+typedef struct vren_cs_batch vren_cs_batch;
+
+typedef struct vren_cs_batch_frame {
+    vren_cs_view view;
+    uint32_t width, height;       /* <= 8192 each */
+    uint32_t light_count;         /* <= 2^20 */
+    int32_t offscreen;            /* VREN_CS_OFFSCREEN_* */
+    const float* depth;           /* device: float[W*H] NDC depth */
+    const float* normals;         /* device: float[3*W*H] */
+    const float* light_positions; /* device: vec4[L], 16-byte aligned (null when L == 0) */
+    const float* point_lights;    /* device: {rgb, radius}[L], 16-byte aligned */
+} vren_cs_batch_frame;
+
+typedef struct vren_cs_batch_options {
+    uint32_t sort_digit_bits; /* 4, 6 or 8: digit width of the combined light sort */
+    uint32_t radix_items;     /* radix tile variant (VREN_TUNE_RADIX_ITEMS) */
+    uint32_t scan_slices;     /* scan tile variant (VREN_TUNE_SCAN_SLICES): 4 or 8 */
+    uint32_t assign_warps;    /* warps per CTA of the traversal kernels (1..8) */
+    uint32_t use_graph;       /* capture/replay one CUDA graph per batch shape (non-default streams) */
+} vren_cs_batch_options;
+
+int vren_cs_batch_create(vren_cs_batch** out);
+void vren_cs_batch_destroy(vren_cs_batch* b);
+/* Sizes the batch's device arena for these frames (allocates; call outside stream capture).
+ * max_assignments bounds the light-index entries of all frames together. */
+int vren_cs_batch_reserve(vren_cs_batch* b, const vren_cs_batch_frame* frames, uint32_t count,
+                          uint64_t max_assignments);
+int vren_cs_batch_set_options(vren_cs_batch* b, const vren_cs_batch_options* options);
+int vren_cs_batch_get_options(const vren_cs_batch* b, vren_cs_batch_options* options);
+/* Enqueues the batch on stream s (VREN_ERR_CAPACITY when it exceeds the reserved arena).  The
+ * radix and scan tile variants of the options are applied to this batch's launches only. */
+int vren_cs_batch_run(vren_cs_batch* b, vren_stream_t s, const vren_cs_batch_frame* frames, uint32_t count);
+/* Times candidate option sets on these frames (digit bits x radix tile x scan tile x traversal
+ * warps), keeps the fastest, and caches it per shape bucket (frame count, log2 of the total pixels
+ * and of the total lights): a bucket seen before returns its cached choice without measuring.
+ * Synchronizes s.  The chosen options are applied to the batch and written to *chosen. */
+int vren_cs_batch_autotune(vren_cs_batch* b, vren_stream_t s, const vren_cs_batch_frame* frames, uint32_t count,
+                           uint32_t reps, vren_cs_batch_options* chosen);
+/* Device pointers of frame f's outputs from the last run (synchronizes s to read the per-frame
+ * bases; offsets are frame-local and indices points at the frame's first index). */
+int vren_cs_batch_frame_outputs(vren_cs_batch* b, vren_stream_t s, uint32_t f, vren_cs_outputs* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -120,5 +120,13 @@ PROTOTYPES_CS: dict[str, tuple] = {
     "vren_cs_shade": (i32, [vp, vp, u32, u32, vp, vp, vp, vp, u32, vp, u32, i32, i32, vp]),
     "vren_cs_shade_backward_scratch_bytes": (sz, [u32, u32]),
     "vren_cs_shade_backward": (i32, [vp, vp, u32, u32, vp, vp, u32, vp, vp, u32, i32, vp, vp, vp, vp, vp]),
+    "vren_cs_batch_create": (i32, [C.POINTER(vp)]),
+    "vren_cs_batch_destroy": (None, [vp]),
+    "vren_cs_batch_reserve": (i32, [vp, vp, u32, C.c_uint64]),
+    "vren_cs_batch_set_options": (i32, [vp, vp]),
+    "vren_cs_batch_get_options": (i32, [vp, vp]),
+    "vren_cs_batch_run": (i32, [vp, vp, vp, u32]),
+    "vren_cs_batch_autotune": (i32, [vp, vp, vp, u32, u32, vp]),
+    "vren_cs_batch_frame_outputs": (i32, [vp, vp, u32, vp]),
 }
 PROTOTYPES.update(PROTOTYPES_CS)

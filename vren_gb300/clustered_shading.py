@@ -174,6 +174,85 @@ class cluster_and_shade:
         return o
 
 
+class BatchFrame(C.Structure):
+    _fields_ = [("view", View), ("width", C.c_uint32), ("height", C.c_uint32), ("light_count", C.c_uint32),
+                ("offscreen", C.c_int32), ("depth", C.c_void_p), ("normals", C.c_void_p),
+                ("light_positions", C.c_void_p), ("point_lights", C.c_void_p)]
+
+
+class BatchOptions(C.Structure):
+    _fields_ = [("sort_digit_bits", C.c_uint32), ("radix_items", C.c_uint32), ("scan_slices", C.c_uint32),
+                ("assign_warps", C.c_uint32), ("use_graph", C.c_uint32)]
+
+    def as_dict(self) -> dict:
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
+
+
+class cluster_batch:
+    """Batched cluster assignment over many frames (one graph per batch shape).  Frames are
+    (view, width, height, depth, normals, positions, lights, light_count[, offscreen]) tuples of
+    device tensors; each frame's outputs are bit-identical to cluster_and_shade.cluster."""
+
+    def __init__(self):
+        h = C.c_void_p()
+        check(lib().vren_cs_batch_create(C.byref(h)), "cs_batch_create")
+        self._h = h
+        self._frames = None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().vren_cs_batch_destroy(h)
+            self._h = None
+
+    @staticmethod
+    def _pack(frames):
+        arr = (BatchFrame * len(frames))()
+        keep = []
+        for i, f in enumerate(frames):
+            view, w, h, depth, normals, pos, lights, L = f[:8]
+            off = f[8] if len(f) > 8 else "wrap"
+            arr[i].view = view
+            arr[i].width, arr[i].height, arr[i].light_count = w, h, L
+            arr[i].offscreen = OFFSCREEN[off]
+            arr[i].depth, arr[i].normals = _ptr(depth), _ptr(normals)
+            arr[i].light_positions = _ptr(pos) if (pos is not None and L) else None
+            arr[i].point_lights = _ptr(lights) if (lights is not None and L) else None
+            keep.append(f)
+        return arr, keep
+
+    def reserve(self, frames, max_assignments: int):
+        arr, _ = self._pack(frames)
+        check(lib().vren_cs_batch_reserve(self._h, arr, len(frames), max_assignments), "cs_batch_reserve")
+
+    def set_options(self, sort_digit_bits=8, radix_items=0, scan_slices=8, assign_warps=8, use_graph=True):
+        o = BatchOptions(sort_digit_bits, radix_items, scan_slices, assign_warps, 1 if use_graph else 0)
+        check(lib().vren_cs_batch_set_options(self._h, C.byref(o)), "cs_batch_set_options")
+
+    def options(self) -> dict:
+        o = BatchOptions()
+        check(lib().vren_cs_batch_get_options(self._h, C.byref(o)), "cs_batch_get_options")
+        return o.as_dict()
+
+    def run(self, stream, frames):
+        arr, keep = self._pack(frames)
+        self._frames = (arr, keep)
+        check(lib().vren_cs_batch_run(self._h, _stream(stream), arr, len(frames)), "cs_batch_run")
+
+    def autotune(self, stream, frames, reps: int = 3) -> dict:
+        arr, keep = self._pack(frames)
+        self._frames = (arr, keep)
+        o = BatchOptions()
+        check(lib().vren_cs_batch_autotune(self._h, _stream(stream), arr, len(frames), reps, C.byref(o)),
+              "cs_batch_autotune")
+        return o.as_dict()
+
+    def frame_outputs(self, stream, f: int) -> Outputs:
+        o = Outputs()
+        check(lib().vren_cs_batch_frame_outputs(self._h, _stream(stream), f, C.byref(o)), "cs_batch_frame_outputs")
+        return o
+
+
 _CUDART = None
 
 

@@ -26,27 +26,7 @@ __global__ void __launch_bounds__(1024) build_bvh_kernel(vren_bvh_node* __restri
                                                          int two_levels)
 {
     __shared__ NodeF s_parent[32];
-    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-    const uint32_t local = blockIdx.x * 1024u + tid;
-    const bool present = local < count;
-    NodeF c{};
-    if (present) c = load_node(bvh, src_off + local);
-    const uint32_t parent_local = local >> 5;
-    NodeF p = warp_parent(c, present, src_off + (parent_local << 5));
-    if (lane == 0 && present) {
-        store_node(bvh, dst1_off + parent_local, p);
-        if (two_levels) s_parent[warp] = p;
-    }
-    if (!two_levels) return;
-    __syncthreads();
-    if (warp == 0) {
-        const uint32_t gp_local = blockIdx.x;
-        const uint32_t parents_here = (count >> 5) - blockIdx.x * 32u < 32u ? (count >> 5) - blockIdx.x * 32u : 32u;
-        const bool pres = lane < parents_here;
-        NodeF q = pres ? s_parent[lane] : NodeF{};
-        NodeF g = warp_parent(q, pres, dst1_off + (gp_local << 5));
-        if (lane == 0) store_node(bvh, dst2_off + gp_local, g);
-    }
+    bvh_levels_block(bvh, blockIdx.x, src_off, count, dst1_off, dst2_off, two_levels != 0, s_parent);
 }
 
 }  // namespace vren_gb300

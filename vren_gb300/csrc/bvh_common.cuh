@@ -58,4 +58,34 @@ __device__ __forceinline__ void store_node(vren_bvh_node* b, uint32_t i, const N
     p[1] = make_float4(n.mx[0], n.mx[1], n.mx[2], __uint_as_float(n.pad));
 }
 
+// One CTA of up to 1024 threads turns nodes [src_off + 1024 block, + 1024) of a level of `count`
+// nodes into their parents at dst1_off and, when two_levels, the CTA's 32 parents into their parent
+// at dst2_off + block.
+__device__ __forceinline__ void bvh_levels_block(vren_bvh_node* __restrict__ bvh, uint32_t block, uint32_t src_off,
+                                                 uint32_t count, uint32_t dst1_off, uint32_t dst2_off, bool two_levels,
+                                                 NodeF* s_parent)
+{
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const uint32_t local = block * 1024u + tid;
+    const bool present = local < count;
+    NodeF c{};
+    if (present) c = load_node(bvh, src_off + local);
+    const uint32_t parent_local = local >> 5;
+    NodeF p = warp_parent(c, present, src_off + (parent_local << 5));
+    if (lane == 0 && present) {
+        store_node(bvh, dst1_off + parent_local, p);
+        if (two_levels) s_parent[warp] = p;
+    }
+    if (!two_levels) return;
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t gp_local = block;
+        const uint32_t parents_here = (count >> 5) - block * 32u < 32u ? (count >> 5) - block * 32u : 32u;
+        const bool pres = lane < parents_here;
+        NodeF q = pres ? s_parent[lane] : NodeF{};
+        NodeF g = warp_parent(q, pres, dst1_off + (gp_local << 5));
+        if (lane == 0) store_node(bvh, dst2_off + gp_local, g);
+    }
+}
+
 }  // namespace vren_gb300

@@ -8,161 +8,17 @@
 // every key, list and index bit for bit.
 #include "common.cuh"
 #include "internal.h"
-#include "bvh_common.cuh"
 
 #include <cmath>
 #include <cstring>
 
 namespace vren_gb300 {
-
 VREN_DEFINE_ERROR_WORD(cs)
+}  // namespace vren_gb300
 
-// ================================================================================================
-// Canonical float helpers
-// ================================================================================================
-// out[r] = ((m[0][r]*x + m[1][r]*y) + m[2][r]*z) + m[3][r]*w, m column-major.
-__device__ __forceinline__ float mv_row(const float* m, int r, float x, float y, float z, float w)
-{
-    return fadd(fadd(fadd(fmul(m[r], x), fmul(m[4 + r], y)), fmul(m[8 + r], z)), fmul(m[12 + r], w));
-}
+#include "cs_device.cuh"
 
-__device__ __forceinline__ float glsl_min(float x, float y) { return y < x ? y : x; }
-__device__ __forceinline__ float glsl_max(float x, float y) { return x < y ? y : x; }
-
-// clustered_shading.glsl:128-164.  The reference walks the three axes with t_i = sign(n_i) / n_i
-// (= |rcp_rn(n_i)|, NaN for a zero or NaN component) and keeps the first strictly smaller t below
-// 1e35; the cube face and the 3x3 cell on it follow from that axis and t.  Here with one correctly
-// rounded reciprocal instead of three: rcp_rn is monotone non-increasing in |n|, so the smallest t
-// over the usable components is rcp_rn(max |n_i|), and the first component whose t rounds to that
-// value is the largest |n_i| or an earlier one within rounding of it (tested exactly, only when it is
-// that close).  x / 2 and x * 0.5 are the same correctly rounded value.
-__device__ __forceinline__ uint32_t discretize_normal(float nx, float ny, float nz)
-{
-    if (nx == 0.0f && ny == 0.0f && nz == 0.0f) return 0xFFFFFFFFu;
-    const float ax = fabsf(nx), ay = fabsf(ny), az = fabsf(nz);
-    const float M = fmaxf(fmaxf(ax, ay), az);  // NaN components drop out
-    float min_t = 1e35f;
-    uint32_t axis = 0, face = 0;
-    if (M > 0.0f) {
-        const float t = __frcp_rn(M);
-        if (t < 1e35f) {
-            // a < M rounds to the same reciprocal only within 2^-21 relative of M
-            const float close = fmul(M, 0.9999f);
-            if (ax == M || (ax >= close && __frcp_rn(ax) == t)) axis = 0;
-            else if (ay == M || (ay >= close && __frcp_rn(ay) == t)) axis = 1;
-            else axis = 2;
-            const float na = axis == 0 ? nx : (axis == 1 ? ny : nz);
-            min_t = t;
-            face = (na > 0.0f ? 1u : 0u) * 3u + axis;
-        }
-    }
-    const float n1 = axis == 0 ? ny : (axis == 1 ? nz : nx);
-    const float n2 = axis == 0 ? nz : (axis == 1 ? nx : ny);
-    const float u = fmul(n1, min_t);
-    const float w = fmul(n2, min_t);
-    const uint32_t du = floor_to_u32(fmul(fmul(fadd(u, 1.0f), 0.5f), 3.0f));
-    const uint32_t dw = floor_to_u32(fmul(fmul(fadd(w, 1.0f), 0.5f), 3.0f));
-    return (face * 9u + du * 3u + dw) & 0x3Fu;
-}
-
-// Largest k in [lo, hi] with bound[k] <= z, given bound[lo] <= z; bound is non-decreasing.
-__device__ __forceinline__ uint32_t slice_search(float z, const float* __restrict__ bound, uint32_t lo, uint32_t hi)
-{
-    while (lo < hi) {
-        const uint32_t mid = (lo + hi + 1u) >> 1;
-        if (__ldg(bound + mid) <= z) lo = mid;
-        else hi = mid - 1u;
-    }
-    return lo;
-}
-
-// Largest k in [0, kmax] with bound[k] <= z (0 if none) for a non-decreasing, geometric table (bound[k] = bound[0] * r^k up to rounding, as both slicing modes
-// build it): a logarithmic estimate, then at most two steps each way against the table before a
-// binary search takes over, so the table alone decides the result.  inv_log2_r = 1 / log2(r).
-__device__ __forceinline__ uint32_t slice_of_geometric(float z, const float* __restrict__ bound, uint32_t kmax, float b0,
-                                                      float inv_log2_r)
-{
-    if (!(b0 <= z)) return 0u;
-    if (kmax == 0u) return 0u;
-    const float e = __log2f(__fdividef(z, b0)) * inv_log2_r;
-    uint32_t k = e >= (float)kmax ? kmax : (e > 0.0f ? (uint32_t)e : 0u);
-    if (__ldg(bound + k) <= z) {
-        if (k < kmax && __ldg(bound + k + 1u) <= z) {
-            ++k;
-            if (k < kmax && __ldg(bound + k + 1u) <= z) k = slice_search(z, bound, k + 1u, kmax);
-        }
-    } else {
-        // bound[0] <= z < bound[k], so k >= 1
-        --k;
-        if (!(__ldg(bound + k) <= z)) {
-            --k;
-            if (!(__ldg(bound + k) <= z)) k = slice_search(z, bound, 0u, k - 1u);
-        }
-    }
-    return k;
-}
-
-struct Box {
-    float mn[3], mx[3];
-};
-
-// clustered_shading.glsl:193-231 (cluster_min / cluster_max in view space).
-__device__ __forceinline__ Box cluster_box(uint32_t key, const vren_cs_frame* __restrict__ F)
-{
-    const uint32_t ci = key & 0xFFu, cj = (key >> 8) & 0xFFu, ck = (key >> 16) & 0x3FFu;
-    const float TX = (float)F->tiles_x, TY = (float)F->tiles_y;
-    const float x0 = fdiv((float)ci, TX), y0 = fdiv((float)cj, TY);
-    const float x1 = fdiv((float)(ci + 1u), TX), y1 = fdiv((float)(cj + 1u), TY);
-    const float ax = fsub(fmul(x0, 2.0f), 1.0f), ay = fsub(fmul(fsub(1.0f, y0), 2.0f), 1.0f);
-    const float bx = fsub(fmul(x1, 2.0f), 1.0f), by = fsub(fmul(fsub(1.0f, y1), 2.0f), 1.0f);
-    const float* ip = F->view.inv_proj;
-    float va[4], vb[4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-        va[r] = mv_row(ip, r, ax, ay, 0.0f, 1.0f);
-        vb[r] = mv_row(ip, r, bx, by, 0.0f, 1.0f);
-    }
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        va[c] = fdiv(va[c], va[3]);
-        vb[c] = fdiv(vb[c], vb[3]);
-    }
-    const float la = fsqrt(fadd(fadd(fmul(va[0], va[0]), fmul(va[1], va[1])), fmul(va[2], va[2])));
-    const float lb = fsqrt(fadd(fadd(fmul(vb[0], vb[0]), fmul(vb[1], vb[1])), fmul(vb[2], vb[2])));
-    float d1[3], d2[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        d1[c] = fdiv(va[c], la);
-        d2[c] = fdiv(vb[c], lb);
-    }
-    const float s1 = fdiv(F->slice_near[ck], d1[2]);
-    const float s2 = fdiv(F->slice_far[ck], d2[2]);
-    Box b;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        b.mn[c] = fmul(s1, d1[c]);
-        b.mx[c] = fmul(s2, d2[c]);
-    }
-    return b;
-}
-
-// assign_lights.comp:84-94
-__device__ __forceinline__ bool test_aabb_aabb(const Box& c, const NodeF& n)
-{
-    return c.mx[0] >= n.mn[0] && c.mn[0] <= n.mx[0] && c.mx[1] >= n.mn[1] && c.mn[1] <= n.mx[1] &&
-           c.mx[2] >= n.mn[2] && c.mn[2] <= n.mx[2];
-}
-
-// assign_lights.comp:97-102
-__device__ __forceinline__ bool test_sphere_aabb(float ox, float oy, float oz, float r, const Box& c)
-{
-    const float o[3] = {ox, oy, oz};
-    float d[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) d[k] = fsub(glsl_max(c.mn[k], glsl_min(o[k], c.mx[k])), o[k]);
-    const float len = fsqrt(fadd(fadd(fmul(d[0], d[0]), fmul(d[1], d[1])), fmul(d[2], d[2])));
-    return len < r;
-}
+namespace vren_gb300 {
 
 // ================================================================================================
 // construct_point_light_bvh
@@ -202,12 +58,7 @@ __global__ void __launch_bounds__(kLbvhThreads) lbvh_transform_kernel(
     for (int k = 0; k < kLbvhPerThread; ++k) {
         const uint32_t i = blockIdx.x * kLbvhPerCta + k * kLbvhThreads + tid;
         if (i < L) {
-            const float4 p = positions[i];
-            float4 v;
-            v.x = mv_row(V, 0, p.x, p.y, p.z, 1.0f);
-            v.y = mv_row(V, 1, p.x, p.y, p.z, 1.0f);
-            v.z = mv_row(V, 2, p.x, p.y, p.z, 1.0f);
-            v.w = mv_row(V, 3, p.x, p.y, p.z, 1.0f);
+            const float4 v = light_to_view(V, positions[i]);
             view_pos[i] = v;
             const float c[3] = {v.x, v.y, v.z};
 #pragma unroll
@@ -268,61 +119,16 @@ __global__ void lbvh_morton_kernel(const float4* __restrict__ view_pos, uint32_t
         mn[a] = unkey(scratch[8 + a]);
         mx[a] = unkey(scratch[11 + a]);
     }
-    const float scale = (float)(1u << bits);
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < L; i += gridDim.x * blockDim.x) {
-        const float4 v = view_pos[i];
-        const float c[3] = {v.x, v.y, v.z};
-        uint32_t q[3];
-#pragma unroll
-        for (int a = 0; a < 3; ++a) q[a] = floor_to_u32(fmul(fdiv(fsub(c[a], mn[a]), fsub(mx[a], mn[a])), scale));
-        uint32_t code = 0;
-        for (uint32_t b = 0; b < bits; ++b) {
-            code |= ((q[0] >> b) & 1u) << (b * 3u);
-            code |= ((q[1] >> b) & 1u) << (b * 3u + 1u);
-            code |= ((q[2] >> b) & 1u) << (b * 3u + 2u);
-        }
-        pairs[i] = make_uint2(code, i);
-    }
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < L; i += gridDim.x * blockDim.x)
+        pairs[i] = make_uint2(morton_code(view_pos[i], mn, mx, bits), i);
 }
 
-// init_light_array_bvh.comp:117-139 fused with the first one or two BuildBVH levels.
 __global__ void __launch_bounds__(1024) lbvh_leaves_kernel(
     const uint2* __restrict__ light_index, const float4* __restrict__ view_pos, const float4* __restrict__ lights,
-    uint32_t L, uint32_t P, vren_bvh_node* __restrict__ bvh, float4* __restrict__ spheres, int two_levels)
+    uint32_t L, uint32_t P, vren_bvh_node* __restrict__ bvh, float4* __restrict__ spheres)
 {
     __shared__ NodeF s_parent[32];
-    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-    const uint32_t i = blockIdx.x * blockDim.x + tid;
-    NodeF leaf;
-    float4 sph;
-    if (i < L) {
-        const uint32_t li = light_index[i].y;
-        const float4 o = view_pos[li];
-        const float r = lights[li].w;
-        leaf.mn[0] = fsub(o.x, r); leaf.mn[1] = fsub(o.y, r); leaf.mn[2] = fsub(o.z, r);
-        leaf.mx[0] = fadd(o.x, r); leaf.mx[1] = fadd(o.y, r); leaf.mx[2] = fadd(o.z, r);
-        leaf.next = VREN_BVH_LEAF_NODE;
-        sph = make_float4(o.x, o.y, o.z, fdiv(fsub(leaf.mx[0], leaf.mn[0]), 2.0f));
-    } else {
-        leaf.mn[0] = leaf.mn[1] = leaf.mn[2] = __int_as_float(0x7F800000);
-        leaf.mx[0] = leaf.mx[1] = leaf.mx[2] = __int_as_float(0xFF800000);
-        leaf.next = VREN_BVH_INVALID_NODE;
-        sph = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
-    }
-    leaf.pad = 0u;
-    store_node(bvh, i, leaf);
-    if (spheres) spheres[i] = sph;
-    const NodeF p = warp_parent(leaf, true, i & ~31u);
-    if (lane == 0) {
-        store_node(bvh, P + (i >> 5), p);
-        if (two_levels) s_parent[warp] = p;
-    }
-    if (!two_levels) return;
-    __syncthreads();
-    if (warp == 0) {
-        const NodeF g = warp_parent(s_parent[lane], true, P + blockIdx.x * 32u);
-        if (lane == 0) store_node(bvh, P + P / 32u + blockIdx.x, g);
-    }
+    light_leaves_block(blockIdx.x, blockDim.x, L, P, light_index, view_pos, lights, bvh, spheres, s_parent);
 }
 
 static int construct_light_bvh(cudaStream_t st, const float* positions, const float* lights, uint32_t L,
@@ -352,10 +158,9 @@ static int construct_light_bvh(cudaStream_t st, const float* positions, const fl
 
     const uint32_t P = vren_calc_bvh_padded_leaf_count(L);
     const uint32_t threads = P < 1024 ? P : 1024;
-    const int two = P >= 1024 ? 1 : 0;
     lbvh_leaves_kernel<<<P / threads, threads, 0, st>>>(
         reinterpret_cast<const uint2*>(light_index), reinterpret_cast<const float4*>(view_pos),
-        reinterpret_cast<const float4*>(lights), L, P, bvh, reinterpret_cast<float4*>(spheres), two);
+        reinterpret_cast<const float4*>(lights), L, P, bvh, reinterpret_cast<float4*>(spheres));
     VREN_LAUNCH_CHECK();
     if (P >= 32768) return build_bvh_levels(st, bvh, P + P / 32u, P / 1024u);
     return VREN_OK;
@@ -364,253 +169,26 @@ static int construct_light_bvh(cudaStream_t st, const float* positions, const fl
 // ================================================================================================
 // find_unique_cluster_list
 // ================================================================================================
-constexpr int kFucThreads = 256;
-constexpr uint32_t kFucHeaderWords = 4;  // start ticket, done ticket, epoch, unused
-
-__device__ __forceinline__ uint64_t make_status(uint32_t epoch, uint32_t flag, uint32_t value)
+__global__ void __launch_bounds__(kFucThreads, 6) find_unique_kernel(FucFrame fr, uint32_t* __restrict__ scratch,
+                                                                    uint32_t wait_limit, uint32_t spin)
 {
-    return ((uint64_t)((epoch << 2) | flag) << 32) | value;
-}
-
-// One CTA per 32x32 tile (find_unique_clusters.comp:46-120).  The reference sorts the tile's 1024
-// (key, pixel) pairs with a 55-stage bitonic network; here the 16 varying key bits (slice and
-// normal; the tile coordinates are constant inside a tile) index a 65536-bit set in shared
-// memory, so the sorted unique keys and every pixel's rank fall out of a popcount prefix.  A
-// 2048-bit occupancy mask records which words of the set are non-zero, so the prefix visits only
-// those (a tile holds a handful of distinct keys).  Thread t owns a strip of four horizontally
-// adjacent pixels (row t / 8, columns 4 (t % 8) .. + 3), read with 128-bit loads when the row is
-// 16-byte aligned; along a strip a pixel whose depth (normal) bits equal its left neighbour's
-// reuses that neighbour's slice (normal bin), and only the first pixel of each run of equal
-// sub-keys along a row touches the set.  Tiles are ordered by a dynamic ticket; decoupled
-// look-back over the tiles gives each tile's offset in the key list (row-major tile order).
-__global__ void __launch_bounds__(kFucThreads, 6) find_unique_kernel(
-    const float* __restrict__ depth, const float* __restrict__ normals, uint32_t W, uint32_t H,
-    const vren_cs_frame* __restrict__ F, uint32_t* __restrict__ keys, uint32_t key_cap,
-    uint32_t* __restrict__ key_count, uint32_t* __restrict__ refs, uint32_t* __restrict__ scratch,
-    uint32_t num_tiles, uint32_t wait_limit, uint32_t spin, int vec)
-{
-    __shared__ __align__(16) uint32_t s_bits[2048];
-    __shared__ uint32_t s_prefix[2048];
-    __shared__ uint32_t s_used[64];  // bit w: word w of s_bits is non-zero
-    __shared__ uint32_t s_tile, s_epoch, s_offset;
-
-    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    __shared__ FucSmem sm;
+    __shared__ uint32_t s_tile, s_epoch;
+    const uint32_t tid = threadIdx.x;
     if (tid == 0) {
         s_tile = atomicAdd(scratch + 0, 1u);
         s_epoch = ld_relaxed_u32(scratch + 2) & 0x3FFFFFFFu;
     }
-    reinterpret_cast<uint4*>(s_bits)[tid] = make_uint4(0u, 0u, 0u, 0u);
-    reinterpret_cast<uint4*>(s_bits)[tid + kFucThreads] = make_uint4(0u, 0u, 0u, 0u);
-    if (tid < 64) s_used[tid] = 0u;
+    reinterpret_cast<uint4*>(sm.bits)[tid] = make_uint4(0u, 0u, 0u, 0u);
+    reinterpret_cast<uint4*>(sm.bits)[tid + kFucThreads] = make_uint4(0u, 0u, 0u, 0u);
+    if (tid < 64) sm.used[tid] = 0u;
     __syncthreads();
-    const uint32_t tile = s_tile, epoch = s_epoch;
-    const uint32_t TX = (W + 31) / 32;
-    const uint32_t tx = tile % TX, ty = tile / TX;
-    const uint32_t kmax = F->max_slice;
-    const bool skip_offscreen = F->offscreen == VREN_CS_OFFSCREEN_SKIP;
-    const float* ip = F->view.inv_proj;
-    const float m2[4] = {ip[2], ip[6], ip[10], ip[14]};
-    const float m3[4] = {ip[3], ip[7], ip[11], ip[15]};
-    const float fW = (float)W, fH = (float)H;
-    // For a perspective projection the z and w rows of its inverse have exact zeros in the x and y
-    // columns and non-zero last coefficients.  Then X and Y only contribute signed zeros to a partial
-    // sum that is either non-zero already or followed by the non-zero last term, so skipping them
-    // leaves every bit of vz and vw unchanged (and the slice depends on the depth alone).
-    const bool xy_free = m2[0] == 0.0f && m2[1] == 0.0f && m3[0] == 0.0f && m3[1] == 0.0f && m2[3] != 0.0f &&
-                         m3[3] != 0.0f;
-    const float* bound = F->slice_near;
-    const float b0 = __ldg(bound);
-    const float inv_log2_r = kmax ? __frcp_rn(__log2f(__fdividef(__ldg(bound + 1), b0))) : 0.0f;
-
-    const uint32_t row = tid >> 3, strip = tid & 7u;
-    const uint32_t gy = ty * 32u + row, gx0 = tx * 32u + strip * 4u;
-    const bool full = vec && gy < H && gx0 + 3u < W;  // whole strip on screen, 16-byte aligned
-    float D[4], N[4][3];
-    bool on[4];
-    if (full) {
-        const size_t px0 = (size_t)gy * W + gx0;
-        const float4 d4 = __ldg(reinterpret_cast<const float4*>(depth + px0));
-        const float4* np = reinterpret_cast<const float4*>(normals + 3 * px0);
-        const float4 a = __ldg(np), b = __ldg(np + 1), c = __ldg(np + 2);
-        D[0] = d4.x; D[1] = d4.y; D[2] = d4.z; D[3] = d4.w;
-        N[0][0] = a.x; N[0][1] = a.y; N[0][2] = a.z;
-        N[1][0] = a.w; N[1][1] = b.x; N[1][2] = b.y;
-        N[2][0] = b.z; N[2][1] = b.w; N[2][2] = c.x;
-        N[3][0] = c.y; N[3][1] = c.z; N[3][2] = c.w;
-#pragma unroll
-        for (int j = 0; j < 4; ++j) on[j] = true;
-    } else {
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const uint32_t gx = gx0 + j;
-            on[j] = !(skip_offscreen && (gx >= W || gy >= H));
-            // texel (x mod W, y mod H); a tile overhangs the image by less than 32 pixels
-            const uint32_t xw = gx < W ? gx : gx % W, yw = gy < H ? gy : gy % H;
-            const size_t px = (size_t)yw * W + xw;
-            D[j] = on[j] ? __ldg(depth + px) : 0.0f;
-#pragma unroll
-            for (int c = 0; c < 3; ++c) N[j][c] = on[j] ? __ldg(normals + 3 * px + c) : 0.0f;
-        }
-    }
-
-    uint32_t sub[4], k = 0, nd = 0;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        const bool same_d = j > 0 && xy_free && __float_as_uint(D[j]) == __float_as_uint(D[j - 1]);
-        if (!same_d) {
-            float vz, vw;
-            if (xy_free) {
-                vz = fadd(fmul(m2[2], D[j]), m2[3]);
-                vw = fadd(fmul(m3[2], D[j]), m3[3]);
-            } else {
-                const float fx = fdiv((float)(gx0 + j), fW), fy = fdiv((float)gy, fH);
-                const float X = fsub(fmul(fx, 2.0f), 1.0f), Y = fsub(fmul(fsub(1.0f, fy), 2.0f), 1.0f);
-                vz = fadd(fadd(fadd(fmul(m2[0], X), fmul(m2[1], Y)), fmul(m2[2], D[j])), fmul(m2[3], 1.0f));
-                vw = fadd(fadd(fadd(fmul(m3[0], X), fmul(m3[1], Y)), fmul(m3[2], D[j])), fmul(m3[3], 1.0f));
-            }
-            k = slice_of_geometric(fdiv(vz, vw), bound, kmax, b0, inv_log2_r);
-        }
-        const bool same_n = j > 0 && __float_as_uint(N[j][0]) == __float_as_uint(N[j - 1][0]) &&
-                            __float_as_uint(N[j][1]) == __float_as_uint(N[j - 1][1]) &&
-                            __float_as_uint(N[j][2]) == __float_as_uint(N[j - 1][2]);
-        if (!same_n) nd = discretize_normal(N[j][0], N[j][1], N[j][2]);
-        sub[j] = on[j] ? (((k & 0x3FFu) | (nd << 10)) & 0xFFFFu) : 0xFFFFFFFFu;
-    }
-    // One set insert per run of equal sub-keys along the row (lane - 1 holds the strip to the left).
-    const uint32_t left3 = __shfl_up_sync(0xFFFFFFFFu, sub[3], 1);
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        const uint32_t left = j ? sub[j - 1] : (strip ? left3 : 0xFFFFFFFFu);
-        if (on[j] && sub[j] != left) {
-            const uint32_t w = sub[j] >> 5;
-            if (atomicOr(&s_bits[w], 1u << (sub[j] & 31u)) == 0u) atomicOr(&s_used[w >> 5], 1u << (w & 31u));
-        }
-    }
-    __syncthreads();
-
-    if (warp == 0) {
-        // Lane l owns words [64 l, 64 l + 64): unique counts, exclusive scan, per-word prefixes.
-        const uint32_t u0 = s_used[2 * lane], u1 = s_used[2 * lane + 1];
-        uint32_t cnt = 0;
-        for (uint32_t m = u0; m; m &= m - 1u) cnt += __popc(s_bits[64u * lane + __ffs(m) - 1u]);
-        for (uint32_t m = u1; m; m &= m - 1u) cnt += __popc(s_bits[64u * lane + 32u + __ffs(m) - 1u]);
-        uint32_t incl = cnt;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, d);
-            if (lane >= (uint32_t)d) incl += y;
-        }
-        const uint32_t excl = incl - cnt;
-        const uint32_t tile_unique = __shfl_sync(0xFFFFFFFFu, incl, 31);
-        {
-            uint32_t run = excl;
-            for (uint32_t m = u0; m; m &= m - 1u) {
-                const uint32_t w = 64u * lane + __ffs(m) - 1u;
-                s_prefix[w] = run;
-                run += __popc(s_bits[w]);
-            }
-            for (uint32_t m = u1; m; m &= m - 1u) {
-                const uint32_t w = 64u * lane + 32u + __ffs(m) - 1u;
-                s_prefix[w] = run;
-                run += __popc(s_bits[w]);
-            }
-        }
-
-        // Decoupled look-back over tiles for this tile's offset.
-        uint64_t* status = reinterpret_cast<uint64_t*>(scratch + kFucHeaderWords);
-        uint32_t prefix = 0;
-        if (tile == 0) {
-            if (lane == 0) st_relaxed_u64(status, make_status(epoch, 2u, tile_unique));
-        } else {
-            if (lane == 0) st_relaxed_u64(status + tile, make_status(epoch, 1u, tile_unique));
-            int64_t pos = (int64_t)tile - 1;
-            bool timed_out = false;
-            while (true) {
-                const int64_t idx = pos - lane;
-                uint32_t flag = 2u, val = 0u;
-                if (idx >= 0) {
-                    uint32_t ns = 32;
-                    for (uint32_t round = 0;; ++round) {
-                        const uint64_t w = ld_relaxed_u64(status + idx);
-                        const uint32_t hi = (uint32_t)(w >> 32);
-                        if ((hi >> 2) == epoch && (hi & 3u) != 0) {
-                            flag = hi & 3u;
-                            val = (uint32_t)w;
-                            break;
-                        }
-                        if (round >= wait_limit) {
-                            timed_out = true;
-                            break;
-                        }
-                        if (round >= spin) {
-                            __nanosleep(ns);
-                            if (ns < 512) ns <<= 1;
-                        }
-                    }
-                }
-                const uint32_t pm = __ballot_sync(0xFFFFFFFFu, flag == 2u);
-                const uint32_t stop = pm ? (uint32_t)(__ffs(pm) - 1) : 31u;
-                uint32_t contrib = lane <= stop ? val : 0u;
-#pragma unroll
-                for (int d = 16; d > 0; d >>= 1) contrib += __shfl_xor_sync(0xFFFFFFFFu, contrib, d);
-                prefix += contrib;
-                if (pm) break;
-                pos -= 32;
-            }
-            if (__any_sync(0xFFFFFFFFu, timed_out) && lane == 0) VREN_RECORD_ERROR(VREN_ERR_TIMEOUT);
-            if (lane == 0) st_relaxed_u64(status + tile, make_status(epoch, 2u, prefix + tile_unique));
-        }
-        if (lane == 0) {
-            s_offset = prefix;
-            if (tile == num_tiles - 1) {
-                const uint32_t total = prefix + tile_unique;
-                *key_count = total < key_cap ? total : key_cap;
-                if (total > key_cap) VREN_RECORD_ERROR(VREN_ERR_CAPACITY);
-            }
-        }
-
-        // Keys, ascending: word w bit b is the sub-key 32 w + b.
-        const uint32_t low = ((ty & 0xFFu) << 8) | (tx & 0xFFu);
-        uint32_t pos = prefix + excl;
-        for (int h = 0; h < 2; ++h) {
-            for (uint32_t m = h ? u1 : u0; m; m &= m - 1u) {
-                const uint32_t w = 64u * lane + 32u * h + __ffs(m) - 1u;
-                for (uint32_t bits = s_bits[w]; bits; bits &= bits - 1u) {
-                    if (pos < key_cap) keys[pos] = ((w * 32u + __ffs(bits) - 1u) << 16) | low;
-                    ++pos;
-                }
-            }
-        }
-    }
-    __syncthreads();
-    const uint32_t off = s_offset;
-
-    // Per-pixel references (only on-screen pixels; the reference's imageStore drops the rest).
-    uint32_t r[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        const uint32_t sj = sub[j];
-        if (j > 0 && sj == sub[j - 1]) {
-            r[j] = r[j - 1];
-        } else if (sj != 0xFFFFFFFFu) {
-            const uint32_t w = sj >> 5;
-            r[j] = off + s_prefix[w] + __popc(s_bits[w] & ((1u << (sj & 31u)) - 1u));
-        } else {
-            r[j] = 0u;
-        }
-    }
-    if (full) {
-        *reinterpret_cast<uint4*>(refs + (size_t)gy * W + gx0) = make_uint4(r[0], r[1], r[2], r[3]);
-    } else if (gy < H) {
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-            if (gx0 + j < W) refs[(size_t)gy * W + gx0 + j] = r[j];
-    }
-
+    const uint32_t epoch = s_epoch;
+    find_unique_tile(fr, s_tile, epoch, wait_limit, spin, sm);
     if (tid == 0) {
         __threadfence();
         const uint32_t done = atomicAdd(scratch + 1, 1u);
-        if (done == num_tiles - 1) {
+        if (done == fr.num_tiles - 1) {
             scratch[0] = 0u;
             scratch[1] = 0u;
             scratch[2] = (epoch + 1u) & 0x3FFFFFFFu;
@@ -625,9 +203,9 @@ static int launch_find_unique(cudaStream_t st, const float* depth, const float* 
     const uint32_t tiles = ((W + 31) / 32) * ((H + 31) / 32);
     const int vec = (W % 4u == 0u) && ((uintptr_t)depth % 16u == 0u) && ((uintptr_t)normals % 16u == 0u) &&
                     ((uintptr_t)refs % 16u == 0u);
-    find_unique_kernel<<<tiles, kFucThreads, 0, st>>>(depth, normals, W, H, frame, keys, key_cap, key_count, refs,
-                                                      scratch, tiles, g_wait_limit,
-                                                      (uint32_t)tuning(VREN_TUNE_SPIN_POLLS), vec);
+    const FucFrame fr{depth, normals, W, H, frame, keys, key_cap, key_count, refs,
+                      reinterpret_cast<uint64_t*>(scratch + kFucHeaderWords), tiles, vec};
+    find_unique_kernel<<<tiles, kFucThreads, 0, st>>>(fr, scratch, g_wait_limit, (uint32_t)tuning(VREN_TUNE_SPIN_POLLS));
     VREN_LAUNCH_CHECK();
     return VREN_OK;
 }
@@ -635,71 +213,6 @@ static int launch_find_unique(cudaStream_t st, const float* depth, const float* 
 // ================================================================================================
 // assign_lights
 // ================================================================================================
-struct LevelBase {
-    uint32_t base[8];  // first node of each traversal level (0 = the root's children)
-};
-
-struct AssignArgs {
-    const uint32_t* keys;
-    const uint32_t* key_count;
-    uint32_t key_cap;
-    const vren_cs_frame* frame;
-    const vren_bvh_node* bvh;
-    const uint2* light_index;
-    const float4* view_pos;
-    const float4* spheres;
-    uint32_t* counts;
-    const uint32_t* offsets;
-    uint32_t* indices;
-    uint32_t index_cap;
-};
-
-// The reference walks the 32-ary tree with an explicit state machine over per-level overlap
-// masks (assign_lights.comp:142-240): ENTERING tests the 32 nodes of a group with one ballot,
-// ADVANCE clears the lowest set bit and descends into the next overlapping child.  The same
-// depth-first order, written as a recursion over compile-time levels: the masks stay in
-// registers and the group address is built incrementally (assign_lights.comp:108-119).
-template <int LEVEL, int LC, bool WRITE, bool SPHERES>
-__device__ __forceinline__ void visit(const AssignArgs& a, const LevelBase& lb, const Box& box, uint32_t rel,
-                                      uint32_t lane, uint32_t& acc, uint32_t out_base)
-{
-    const uint32_t addr = lb.base[LEVEL] + rel;
-    if constexpr (LEVEL == LC - 1) {
-        bool hit = false;
-        uint32_t li = 0;
-        if constexpr (SPHERES) {
-            const float4 s = __ldg(a.spheres + addr + lane);
-            hit = test_sphere_aabb(s.x, s.y, s.z, s.w, box);
-            if (WRITE && hit) li = __ldg(&a.light_index[addr + lane].y);
-        } else {
-            const NodeF n = load_node(a.bvh, addr + lane);
-            if (n.next != VREN_BVH_INVALID_NODE) {
-                li = a.light_index[addr + lane].y;
-                const float4 o = a.view_pos[li];
-                hit = test_sphere_aabb(o.x, o.y, o.z, fdiv(fsub(n.mx[0], n.mn[0]), 2.0f), box);
-            }
-        }
-        const uint32_t mask = __ballot_sync(0xFFFFFFFFu, hit);
-        if (WRITE && hit) {
-            // assign_lights.comp:229: lanes of a group are written in descending order
-            const uint32_t slot = __popc(mask & ~lanemask_lt()) - 1u;
-            const uint32_t pos = out_base + acc + slot;
-            if (pos < a.index_cap) a.indices[pos] = li;
-            else VREN_RECORD_ERROR(VREN_ERR_CAPACITY);
-        }
-        acc += __popc(mask);
-    } else {
-        const NodeF n = load_node(a.bvh, addr + lane);
-        const bool hit = n.next != VREN_BVH_INVALID_NODE && test_aabb_aabb(box, n);
-        uint32_t mask = __ballot_sync(0xFFFFFFFFu, hit);
-        while (mask) {
-            const uint32_t ch = __ffs(mask) - 1;
-            mask &= mask - 1u;
-            visit<LEVEL + 1, LC, WRITE, SPHERES>(a, lb, box, 32u * (rel + ch), lane, acc, out_base);
-        }
-    }
-}
-
 template <int LC, bool WRITE, bool SPHERES>
 __global__ void __launch_bounds__(256) assign_kernel(AssignArgs a, LevelBase lb)
 {
@@ -710,10 +223,7 @@ __global__ void __launch_bounds__(256) assign_kernel(AssignArgs a, LevelBase lb)
     uint32_t U = *a.key_count;
     if (U > a.key_cap) U = a.key_cap;
     for (uint32_t c = gw; c < U; c += nw) {
-        const Box box = cluster_box(a.keys[c], a.frame);
-        uint32_t acc = 0;
-        const uint32_t out_base = WRITE ? a.offsets[c] : 0u;
-        visit<0, LC, WRITE, SPHERES>(a, lb, box, 0u, lane, acc, out_base);
+        const uint32_t acc = assign_cluster<LC, WRITE, SPHERES>(a, lb, a.keys[c], WRITE ? a.offsets[c] : 0u, lane);
         if (!WRITE && lane == 0) a.counts[c] = acc;
     }
 }
@@ -753,16 +263,9 @@ static int assign_lights(cudaStream_t st, const uint32_t* keys, const uint32_t* 
         VREN_LAUNCH_CHECK();
         return VREN_OK;
     }
-    const uint32_t lc = vren_calc_bvh_level_count(L);
-    if (lc < 1 || lc > 6) return VREN_ERR_ARG;
     LevelBase lb{};
-    const uint32_t root = vren_calc_bvh_root_index(L);
-    uint64_t sub = 0, pw = 32;
-    for (uint32_t l = 0; l < lc; ++l) {
-        sub += pw;
-        pw *= 32;
-        lb.base[l] = (uint32_t)((uint64_t)root - sub);
-    }
+    const uint32_t lc = traversal_levels(L, lb);
+    if (lc < 1 || lc > 6) return VREN_ERR_ARG;
     AssignArgs a{keys, key_count, key_cap, frame, bvh, reinterpret_cast<const uint2*>(light_index),
                  reinterpret_cast<const float4*>(view_pos), reinterpret_cast<const float4*>(spheres),
                  counts, offsets, indices, index_cap};
