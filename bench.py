@@ -259,6 +259,7 @@ def run_ours(args, rank: int, world: int):
     radix = radix_bench(args, dev, stream, flush, radix_keys, hbm_peak)
     sweep = None if args.quick else primitive_sweep(args, dev, stream, flush, hbm_peak)
     shade = shade_bench(args, dev, stream, flush, ctx)
+    batched = None if args.quick else batched_vs_plain(args, dev, stream, flush)
 
     clocks.__exit__(None, None, None)
     clk = clocks.summary()
@@ -303,7 +304,7 @@ def run_ours(args, rank: int, world: int):
                          "traffic_source": FUC_TRAFFIC_SOURCE,
                          "algorithmic_bytes": fuc_bytes, "kernel_ms": round(fuc_ms, 5)},
             "radix_sort": radix,
-            "batched_vs_plain": None,
+            "batched_vs_plain": batched,
             "primitive_sweep": sweep,
             "shade": shade,
             "cpu_baseline": cpu,
@@ -461,6 +462,83 @@ def shade_bench(args, dev, stream, flush, ctx):
         "backward_tflops": round(SHADE_BWD_FLOPS_PER_PAIR * pairs / (ms_b * 1e-3) / 1e12, 3),
         "flops_per_pair": {"forward": SHADE_FWD_FLOPS_PER_PAIR, "backward": SHADE_BWD_FLOPS_PER_PAIR},
         "finite": ok,
+    }
+
+
+BATCH_FRAMES = 64
+BATCH_RES = [(640, 360), (1280, 720), (1920, 1080), (2560, 1440)]
+
+
+def batch_specs(seed: int = SEED + 4000):
+    """64 frames: resolution uniform over BATCH_RES, light count log-uniform in [1024, 65536]."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for k in range(BATCH_FRAMES):
+        w, h = BATCH_RES[int(rng.integers(0, len(BATCH_RES)))]
+        L = int(round(float(np.exp(rng.uniform(np.log(1024.0), np.log(65536.0))))))
+        specs.append((w, h, L))
+    return specs
+
+
+def batched_vs_plain(args, dev, stream, flush):
+    """Frames per second of the batched form (one graph for all 64 frames, autotuned) against the
+    plain per-frame form (64 cluster_and_shade calls, each a replay of its own captured graph), on
+    the same inputs; every frame's outputs are compared bit for bit."""
+    import torch
+
+    import vren_gb300.clustered_shading as cs
+    import vren_gb300.scene as scene
+
+    specs = batch_specs()
+    frames, plain = [], []
+    for k, (w, h, L) in enumerate(specs):
+        view = cs.view_from_camera(cs.scene_camera(w, h), "ref")
+        depth, normals = scene.depth_planes(SEED + 5000 + k, w, h, planes=64)
+        pos, lights = scene.lights(SEED + 6000 + k, L, w, h)
+        t = lambda a: torch.from_numpy(a).to(dev)
+        frames.append((view, w, h, t(depth), t(normals), t(pos), t(lights), L))
+        plain.append(cs.cluster_and_shade(w, h, L, 1 << 22))
+    torch.cuda.synchronize()
+
+    def run_plain():
+        for ctx, (view, w, h, d, n, p, l, L) in zip(plain, frames):
+            ctx.cluster(stream, view, w, h, d, n, p, l, L)
+
+    batch = cs.cluster_batch()
+    batch.reserve(frames, 1 << 26)
+    with torch.cuda.stream(stream):
+        chosen = batch.autotune(stream, frames, reps=2)
+    steps = max(3, args.steps // 2)
+    with torch.cuda.stream(stream):
+        ms_plain = time_events(stream, run_plain, 3, steps, flush)
+        ms_batch = time_events(stream, lambda: batch.run(stream, frames), 3, steps, flush)
+    # bit-exactness of every frame (outputs of the last run of each arm)
+    exact = True
+    for f, (ctx, fr) in enumerate(zip(plain, frames)):
+        a, b = ctx.outputs(), batch.frame_outputs(stream, f)
+        ua, ub = int(cs.read_device(a.key_count, 1)[0]), int(cs.read_device(b.key_count, 1)[0])
+        ta, tb = int(cs.read_device(a.total, 1)[0]), int(cs.read_device(b.total, 1)[0])
+        same = ua == ub and ta == tb
+        for name, cnt in (("cluster_keys", ua), ("cluster_refs", fr[1] * fr[2]), ("counts", ua), ("offsets", ua),
+                          ("indices", ta)):
+            if not same:
+                break
+            same = np.array_equal(cs.read_device(getattr(a, name), cnt), cs.read_device(getattr(b, name), cnt))
+        exact = exact and same
+    total_px = sum(w * h for w, h, _ in specs)
+    total_l = sum(L for _, _, L in specs)
+    return {
+        "workload": f"{BATCH_FRAMES} frames, resolution uniform over {BATCH_RES}, lights log-uniform in [1024, 65536], "
+                    "cluster assignment (light BVH + unique clusters + light lists) per frame",
+        "total_pixels": total_px, "total_lights": total_l,
+        "plain_ms": round(ms_plain, 4), "batched_ms": round(ms_batch, 4),
+        "plain_frames_per_s": round(BATCH_FRAMES / (ms_plain * 1e-3), 1),
+        "batched_frames_per_s": round(BATCH_FRAMES / (ms_batch * 1e-3), 1),
+        "speedup": round(ms_plain / ms_batch, 3),
+        "bit_exact_all_frames": bool(exact),
+        "autotuned_options": chosen,
+        "plain": "64 vren_cs_cluster calls, each replaying its own captured graph",
+        "l2": "flushed before each timed step",
     }
 
 

@@ -284,7 +284,9 @@ int vren_cs_construct_light_bvh(vren_stream_t s, const float* light_positions, c
 
 /* find_unique_cluster_list (clustered_shading.cpp:363-448, find_unique_clusters.comp:46-120).
  * key_count receives the number of keys written (the reference's dispatch_params.x); a list longer
- * than key_capacity is truncated and VREN_ERR_CAPACITY recorded.  tiles_x*tiles_y*1024 keys always fit. */
+ * than key_capacity is truncated and VREN_ERR_CAPACITY recorded.  tiles_x*tiles_y*1024 keys always fit.
+ * The scratch holds every tile's sorted keys, key count and offset (about 4 KiB per tile; no
+ * initialisation needed); calls sharing a scratch must not overlap. */
 size_t vren_cs_unique_clusters_scratch_bytes(uint32_t width, uint32_t height);
 int vren_cs_find_unique_clusters(vren_stream_t s, const float* depth, const float* normals, uint32_t width,
                                  uint32_t height, const vren_cs_frame* frame, uint32_t* cluster_keys,

@@ -11,7 +11,9 @@
 //               is exactly the per-frame stable sort by code
 //   leaves      1024-leaf blocks of every frame's padded leaf range (+ first two BVH levels)
 //   levels      one CTA per frame with >= 32768 padded leaves (the remaining one or two levels)
-//   unique      every frame's 32x32 tiles under one ticket; look-back chains per frame
+//   unique      every frame's 32x32 tiles, independent of each other
+//   tile scan   one CTA per frame: tile counts -> tile offsets
+//   fixup       tile offsets into the references, keys into each frame's dense list
 //   bases       per-frame cluster counts -> dense cluster numbering over the batch
 //   count       traversal over all clusters of all frames (warp per cluster)
 //   scan        one exclusive scan of the dense counts
@@ -203,49 +205,52 @@ __global__ void __launch_bounds__(1024) batch_levels_kernel(const BatchDesc* __r
 // ------------------------------------------------------------------------------------------------
 // Unique clusters over all frames' tiles
 // ------------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(kFucThreads, 6) batch_find_unique_kernel(
-    const BatchDesc* __restrict__ d, const uint32_t* __restrict__ tile_prefix, uint32_t n, uint32_t total_tiles,
-    uint32_t* __restrict__ keys, uint32_t* __restrict__ key_counts, uint32_t* __restrict__ refs,
-    uint32_t* __restrict__ scratch, uint32_t wait_limit, uint32_t spin)
+struct BatchFuc {
+    const BatchDesc* d;
+    const uint32_t* tile_prefix;
+    uint32_t n;
+    uint32_t* keys;
+    uint32_t* key_counts;
+    uint32_t* refs;
+    uint32_t* tile_keys;
+    uint32_t* tile_count;
+    uint32_t* tile_offset;
+};
+
+__device__ __forceinline__ FucFrame batch_fuc_frame(const BatchFuc& b, uint32_t f)
+{
+    const BatchDesc& fd = b.d[f];
+    const uint32_t t0 = b.tile_prefix[f];
+    return FucFrame{fd.depth,         fd.normals,          fd.W,          fd.H,
+                    fd.frame,         b.keys + fd.key_base, fd.tiles * 1024u,
+                    b.key_counts + f, b.refs + fd.pixel_base, b.tile_keys + (size_t)t0 * 1024u,
+                    b.tile_count + t0, b.tile_offset + t0, fd.tiles, fd.vec};
+}
+
+// Every frame's tiles.
+__global__ void __launch_bounds__(kFucThreads, 6) batch_find_unique_kernel(BatchFuc b)
 {
     __shared__ FucSmem sm;
-    __shared__ uint32_t s_ticket, s_epoch;
     const uint32_t tid = threadIdx.x;
-    if (tid == 0) {
-        s_ticket = atomicAdd(scratch + 0, 1u);
-        s_epoch = ld_relaxed_u32(scratch + 2) & 0x3FFFFFFFu;
-    }
     reinterpret_cast<uint4*>(sm.bits)[tid] = make_uint4(0u, 0u, 0u, 0u);
     reinterpret_cast<uint4*>(sm.bits)[tid + kFucThreads] = make_uint4(0u, 0u, 0u, 0u);
     if (tid < 64) sm.used[tid] = 0u;
     __syncthreads();
-    const uint32_t ticket = s_ticket, epoch = s_epoch;
-    // Tickets are handed out in order and a tile looks back only at earlier tiles of its own frame,
-    // which hold earlier tickets.
-    const uint32_t f = frame_of(tile_prefix, n, ticket);
-    const BatchDesc& fd = d[f];
-    const FucFrame fr{fd.depth,
-                      fd.normals,
-                      fd.W,
-                      fd.H,
-                      fd.frame,
-                      keys + fd.key_base,
-                      fd.tiles * 1024u,
-                      key_counts + f,
-                      refs + fd.pixel_base,
-                      reinterpret_cast<uint64_t*>(scratch + kFucHeaderWords) + tile_prefix[f],
-                      fd.tiles,
-                      fd.vec};
-    find_unique_tile(fr, ticket - tile_prefix[f], epoch, wait_limit, spin, sm);
-    if (tid == 0) {
-        __threadfence();
-        const uint32_t done = atomicAdd(scratch + 1, 1u);
-        if (done == total_tiles - 1) {
-            scratch[0] = 0u;
-            scratch[1] = 0u;
-            scratch[2] = (epoch + 1u) & 0x3FFFFFFFu;
-        }
-    }
+    const uint32_t f = frame_of(b.tile_prefix, b.n, blockIdx.x);
+    find_unique_tile(batch_fuc_frame(b, f), blockIdx.x - b.tile_prefix[f], sm);
+}
+
+// One CTA per frame: its tile counts into offsets.
+__global__ void __launch_bounds__(kFucScanThreads) batch_find_unique_scan_kernel(BatchFuc b)
+{
+    __shared__ uint32_t s_warp[kFucScanThreads / 32];
+    find_unique_scan(batch_fuc_frame(b, blockIdx.x), s_warp);
+}
+
+__global__ void __launch_bounds__(kFucThreads) batch_find_unique_fixup_kernel(BatchFuc b)
+{
+    const uint32_t f = frame_of(b.tile_prefix, b.n, blockIdx.x);
+    find_unique_fixup(batch_fuc_frame(b, f), blockIdx.x - b.tile_prefix[f]);
 }
 
 // Dense cluster numbering: base[f] = sum of the unique-cluster counts of frames < f; base[n] = total.
@@ -385,7 +390,9 @@ struct vren_cs_batch {
     uint32_t* fticket = nullptr;
     vren_bvh_node* bvh = nullptr;
     float4* spheres = nullptr;
-    uint32_t* fuc_scratch = nullptr;
+    uint32_t* tile_count = nullptr;
+    uint32_t* tile_offset = nullptr;
+    uint32_t* tile_keys = nullptr;
     uint32_t* keys = nullptr;
     uint32_t* key_counts = nullptr;
     uint32_t* refs = nullptr;
@@ -569,9 +576,13 @@ int enqueue_batch(vren_cs_batch* b, cudaStream_t st)
         batch_levels_kernel<<<n, 1024, 0, st>>>(b->desc, b->bvh);
         VREN_LAUNCH_CHECK();
     }
-    batch_find_unique_kernel<<<b->total_tiles, kFucThreads, 0, st>>>(
-        b->desc, tile_prefix, n, b->total_tiles, b->keys, b->key_counts, b->refs, b->fuc_scratch, g_wait_limit,
-        (uint32_t)tuning(VREN_TUNE_SPIN_POLLS));
+    const BatchFuc bf{b->desc, tile_prefix, n, b->keys, b->key_counts, b->refs, b->tile_keys, b->tile_count,
+                      b->tile_offset};
+    batch_find_unique_kernel<<<b->total_tiles, kFucThreads, 0, st>>>(bf);
+    VREN_LAUNCH_CHECK();
+    batch_find_unique_scan_kernel<<<n, kFucScanThreads, 0, st>>>(bf);
+    VREN_LAUNCH_CHECK();
+    batch_find_unique_fixup_kernel<<<b->total_tiles, kFucThreads, 0, st>>>(bf);
     VREN_LAUNCH_CHECK();
     batch_bases_kernel<<<1, 1024, 0, st>>>(b->desc, n, b->key_counts, b->base);
     VREN_LAUNCH_CHECK();
@@ -675,7 +686,9 @@ extern "C" int vren_cs_batch_reserve(vren_cs_batch* b, const vren_cs_batch_frame
     const size_t o_ftk = carve((size_t)F * 4);
     const size_t o_bvh = carve((size_t)(s.bvh ? s.bvh : 1) * sizeof(vren_bvh_node));
     const size_t o_sph = carve((size_t)(s.spheres ? s.spheres : 1) * 16);
-    const size_t o_fuc = carve((size_t)kFucHeaderWords * 4 + (size_t)(s.tiles ? s.tiles : 1) * 8);
+    const size_t o_tcount = carve((size_t)(s.tiles ? s.tiles : 1) * 4);
+    const size_t o_toff = carve((size_t)(s.tiles ? s.tiles : 1) * 4);
+    const size_t o_tkeys = carve((size_t)(s.tiles ? s.tiles : 1) * 4096);
     const size_t o_keys = carve(Kb * 4);
     const size_t o_kc = carve((size_t)F * 4);
     const size_t o_refs = carve((s.pixels ? s.pixels : 1) * 4);
@@ -715,7 +728,9 @@ extern "C" int vren_cs_batch_reserve(vren_cs_batch* b, const vren_cs_batch_frame
     b->fticket = reinterpret_cast<uint32_t*>(a + o_ftk);
     b->bvh = reinterpret_cast<vren_bvh_node*>(a + o_bvh);
     b->spheres = reinterpret_cast<float4*>(a + o_sph);
-    b->fuc_scratch = reinterpret_cast<uint32_t*>(a + o_fuc);
+    b->tile_count = reinterpret_cast<uint32_t*>(a + o_tcount);
+    b->tile_offset = reinterpret_cast<uint32_t*>(a + o_toff);
+    b->tile_keys = reinterpret_cast<uint32_t*>(a + o_tkeys);
     b->keys = reinterpret_cast<uint32_t*>(a + o_keys);
     b->key_counts = reinterpret_cast<uint32_t*>(a + o_kc);
     b->refs = reinterpret_cast<uint32_t*>(a + o_refs);

@@ -169,32 +169,31 @@ static int construct_light_bvh(cudaStream_t st, const float* positions, const fl
 // ================================================================================================
 // find_unique_cluster_list
 // ================================================================================================
-__global__ void __launch_bounds__(kFucThreads, 6) find_unique_kernel(FucFrame fr, uint32_t* __restrict__ scratch,
-                                                                    uint32_t wait_limit, uint32_t spin)
+__global__ void __launch_bounds__(kFucThreads, 6) find_unique_kernel(FucFrame fr)
 {
     __shared__ FucSmem sm;
-    __shared__ uint32_t s_tile, s_epoch;
     const uint32_t tid = threadIdx.x;
-    if (tid == 0) {
-        s_tile = atomicAdd(scratch + 0, 1u);
-        s_epoch = ld_relaxed_u32(scratch + 2) & 0x3FFFFFFFu;
-    }
     reinterpret_cast<uint4*>(sm.bits)[tid] = make_uint4(0u, 0u, 0u, 0u);
     reinterpret_cast<uint4*>(sm.bits)[tid + kFucThreads] = make_uint4(0u, 0u, 0u, 0u);
     if (tid < 64) sm.used[tid] = 0u;
     __syncthreads();
-    const uint32_t epoch = s_epoch;
-    find_unique_tile(fr, s_tile, epoch, wait_limit, spin, sm);
-    if (tid == 0) {
-        __threadfence();
-        const uint32_t done = atomicAdd(scratch + 1, 1u);
-        if (done == fr.num_tiles - 1) {
-            scratch[0] = 0u;
-            scratch[1] = 0u;
-            scratch[2] = (epoch + 1u) & 0x3FFFFFFFu;
-        }
-    }
+    find_unique_tile(fr, blockIdx.x, sm);
 }
+
+__global__ void __launch_bounds__(kFucScanThreads) find_unique_scan_kernel(FucFrame fr)
+{
+    __shared__ uint32_t s_warp[kFucScanThreads / 32];
+    find_unique_scan(fr, s_warp);
+}
+
+__global__ void __launch_bounds__(kFucThreads) find_unique_fixup_kernel(FucFrame fr)
+{
+    find_unique_fixup(fr, blockIdx.x);
+}
+
+// Scratch of find_unique_cluster_list for T tiles (uint32 words): tile counts [T], tile offsets [T],
+// then (16-byte aligned) the tiles' key slots [T][1024].
+static size_t fuc_keys_offset_words(uint32_t T) { return (2ull * T + 3) / 4 * 4; }
 
 static int launch_find_unique(cudaStream_t st, const float* depth, const float* normals, uint32_t W, uint32_t H,
                               const vren_cs_frame* frame, uint32_t* keys, uint32_t key_cap, uint32_t* key_count,
@@ -204,8 +203,12 @@ static int launch_find_unique(cudaStream_t st, const float* depth, const float* 
     const int vec = (W % 4u == 0u) && ((uintptr_t)depth % 16u == 0u) && ((uintptr_t)normals % 16u == 0u) &&
                     ((uintptr_t)refs % 16u == 0u);
     const FucFrame fr{depth, normals, W, H, frame, keys, key_cap, key_count, refs,
-                      reinterpret_cast<uint64_t*>(scratch + kFucHeaderWords), tiles, vec};
-    find_unique_kernel<<<tiles, kFucThreads, 0, st>>>(fr, scratch, g_wait_limit, (uint32_t)tuning(VREN_TUNE_SPIN_POLLS));
+                      scratch + fuc_keys_offset_words(tiles), scratch, scratch + tiles, tiles, vec};
+    find_unique_kernel<<<tiles, kFucThreads, 0, st>>>(fr);
+    VREN_LAUNCH_CHECK();
+    find_unique_scan_kernel<<<1, kFucScanThreads, 0, st>>>(fr);
+    VREN_LAUNCH_CHECK();
+    find_unique_fixup_kernel<<<tiles, kFucThreads, 0, st>>>(fr);
     VREN_LAUNCH_CHECK();
     return VREN_OK;
 }
@@ -477,7 +480,7 @@ extern "C" int vren_cs_construct_light_bvh(vren_stream_t s, const float* light_p
 extern "C" size_t vren_cs_unique_clusters_scratch_bytes(uint32_t width, uint32_t height)
 {
     const uint64_t tiles = (uint64_t)((width + 31) / 32) * ((height + 31) / 32);
-    return (size_t)(kFucHeaderWords * 4 + tiles * 8);
+    return (size_t)((fuc_keys_offset_words((uint32_t)tiles) + tiles * 1024u) * 4);
 }
 
 extern "C" int vren_cs_find_unique_clusters(vren_stream_t s, const float* depth, const float* normals, uint32_t width,

@@ -240,29 +240,28 @@ __device__ __forceinline__ void light_leaves_block(uint32_t chunk, uint32_t thre
 // find_unique_cluster_list body
 // ================================================================================================
 constexpr int kFucThreads = 256;
-constexpr uint32_t kFucHeaderWords = 4;  // start ticket, done ticket, epoch, unused
 
-__device__ __forceinline__ uint64_t make_status(uint32_t epoch, uint32_t flag, uint32_t value)
-{
-    return ((uint64_t)((epoch << 2) | flag) << 32) | value;
-}
-
-// One CTA per 32x32 tile (find_unique_clusters.comp:46-120).  The reference sorts the tile's 1024
-// (key, pixel) pairs with a 55-stage bitonic network; here the 16 varying key bits (slice and
-// normal; the tile coordinates are constant inside a tile) index a 65536-bit set in shared
-// memory, so the sorted unique keys and every pixel's rank fall out of a popcount prefix.  A
-// 2048-bit occupancy mask records which words of the set are non-zero, so the prefix visits only
-// those (a tile holds a handful of distinct keys).  Thread t owns a strip of four horizontally
-// adjacent pixels (row t / 8, columns 4 (t % 8) .. + 3), read with 128-bit loads when the row is
-// 16-byte aligned; along a strip a pixel whose depth (normal) bits equal its left neighbour's
-// reuses that neighbour's slice (normal bin), and only the first pixel of each run of equal
-// sub-keys along a row touches the set.  Tiles are ordered by a dynamic ticket; decoupled
-// look-back over the tiles gives each tile's offset in the key list (row-major tile order).
+// find_unique_cluster_list in two kernels, with no dependency between the tiles of the first:
+//
+// 1. One CTA per 32x32 tile (find_unique_clusters.comp:46-120).  The reference sorts the tile's 1024
+//    (key, pixel) pairs with a 55-stage bitonic network; here the 16 varying key bits (slice and
+//    normal; the tile coordinates are constant inside a tile) index a 65536-bit set in shared
+//    memory, so the sorted unique keys and every pixel's rank fall out of a popcount prefix.  A
+//    2048-bit occupancy mask records which words of the set are non-zero, so the prefix visits only
+//    those (a tile holds a handful of distinct keys), and every warp computes it for itself, so only
+//    one barrier separates the set inserts from the outputs.  Thread t owns a strip of four
+//    horizontally adjacent pixels (row t / 8, columns 4 (t % 8) .. + 3), read with 128-bit loads when
+//    the row is 16-byte aligned; along a strip a pixel whose depth (normal) bits equal its left
+//    neighbour's reuses that neighbour's slice (normal bin), and only the first pixel of each run of
+//    equal sub-keys along a row touches the set.  The tile writes its pixels' tile-local ranks into
+//    the reference buffer, its sorted keys into its own 1024-entry slot and its key count.
+// 2. One CTA scans the tile counts into tile offsets (row-major tile order) and the key count.
+// 3. One CTA per tile adds the tile's offset to its references (still in L2) and copies its keys to
+//    their place in the dense key list.
 struct FucSmem {
     __align__(16) uint32_t bits[2048];
     uint32_t prefix[2048];
     uint32_t used[64];  // bit w: word w of bits is non-zero
-    uint32_t offset;
 };
 
 // Where one frame's find_unique_cluster_list reads and writes.
@@ -275,22 +274,21 @@ struct FucFrame {
     uint32_t key_cap;
     uint32_t* key_count;
     uint32_t* refs;
-    uint64_t* status;  // the frame's tile status words
+    uint32_t* tile_keys;    // [num_tiles][1024]: each tile's sorted keys
+    uint32_t* tile_count;   // [num_tiles]: unique keys per tile
+    uint32_t* tile_offset;  // [num_tiles]: exclusive prefix of tile_count
     uint32_t num_tiles;
-    int vec;  // 128-bit loads allowed (W % 4 == 0, 16-byte aligned depth, normals, refs)
+    int vec;  // 128-bit accesses allowed (W % 4 == 0, 16-byte aligned depth, normals, refs)
 };
 
-// Tile `tile` of frame `fr`, all threads of the CTA; sm.bits and sm.used must be zero (and
-// synchronised) on entry.
-__device__ __forceinline__ void find_unique_tile(const FucFrame& fr, uint32_t tile, uint32_t epoch, uint32_t wait_limit,
-                                                 uint32_t spin, FucSmem& sm)
+// Stage 1 for tile `tile` of frame `fr`, all threads of the CTA; sm.bits and sm.used must be zero
+// (and synchronised) on entry.
+__device__ __forceinline__ void find_unique_tile(const FucFrame& fr, uint32_t tile, FucSmem& sm)
 {
     const float* __restrict__ depth = fr.depth;
     const float* __restrict__ normals = fr.normals;
-    const uint32_t W = fr.W, H = fr.H, key_cap = fr.key_cap, num_tiles = fr.num_tiles;
+    const uint32_t W = fr.W, H = fr.H;
     const vren_cs_frame* __restrict__ F = fr.F;
-    uint32_t* __restrict__ keys = fr.keys;
-    uint32_t* __restrict__ key_count = fr.key_count;
     uint32_t* __restrict__ refs = fr.refs;
     const int vec = fr.vec;
     uint32_t* s_bits = sm.bits;
@@ -381,104 +379,49 @@ __device__ __forceinline__ void find_unique_tile(const FucFrame& fr, uint32_t ti
     }
     __syncthreads();
 
+    // Every warp: lane l owns words [64 l, 64 l + 64); unique counts, exclusive scan over the lanes,
+    // per-word prefixes (all warps store the same values).
+    const uint32_t u0 = s_used[2 * lane], u1 = s_used[2 * lane + 1];
+    uint32_t cnt = 0;
+    for (uint32_t m = u0; m; m &= m - 1u) cnt += __popc(s_bits[64u * lane + __ffs(m) - 1u]);
+    for (uint32_t m = u1; m; m &= m - 1u) cnt += __popc(s_bits[64u * lane + 32u + __ffs(m) - 1u]);
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+        if (lane >= (uint32_t)d) incl += y;
+    }
+    const uint32_t excl = incl - cnt;
+    {
+        uint32_t run = excl;
+        for (uint32_t m = u0; m; m &= m - 1u) {
+            const uint32_t w = 64u * lane + __ffs(m) - 1u;
+            s_prefix[w] = run;
+            run += __popc(s_bits[w]);
+        }
+        for (uint32_t m = u1; m; m &= m - 1u) {
+            const uint32_t w = 64u * lane + 32u + __ffs(m) - 1u;
+            s_prefix[w] = run;
+            run += __popc(s_bits[w]);
+        }
+    }
+    __syncwarp();
     if (warp == 0) {
-        // Lane l owns words [64 l, 64 l + 64): unique counts, exclusive scan, per-word prefixes.
-        const uint32_t u0 = s_used[2 * lane], u1 = s_used[2 * lane + 1];
-        uint32_t cnt = 0;
-        for (uint32_t m = u0; m; m &= m - 1u) cnt += __popc(s_bits[64u * lane + __ffs(m) - 1u]);
-        for (uint32_t m = u1; m; m &= m - 1u) cnt += __popc(s_bits[64u * lane + 32u + __ffs(m) - 1u]);
-        uint32_t incl = cnt;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, d);
-            if (lane >= (uint32_t)d) incl += y;
-        }
-        const uint32_t excl = incl - cnt;
-        const uint32_t tile_unique = __shfl_sync(0xFFFFFFFFu, incl, 31);
-        {
-            uint32_t run = excl;
-            for (uint32_t m = u0; m; m &= m - 1u) {
-                const uint32_t w = 64u * lane + __ffs(m) - 1u;
-                s_prefix[w] = run;
-                run += __popc(s_bits[w]);
-            }
-            for (uint32_t m = u1; m; m &= m - 1u) {
-                const uint32_t w = 64u * lane + 32u + __ffs(m) - 1u;
-                s_prefix[w] = run;
-                run += __popc(s_bits[w]);
-            }
-        }
-
-        // Decoupled look-back over tiles for this tile's offset.
-        uint64_t* status = fr.status;
-        uint32_t prefix = 0;
-        if (tile == 0) {
-            if (lane == 0) st_relaxed_u64(status, make_status(epoch, 2u, tile_unique));
-        } else {
-            if (lane == 0) st_relaxed_u64(status + tile, make_status(epoch, 1u, tile_unique));
-            int64_t pos = (int64_t)tile - 1;
-            bool timed_out = false;
-            while (true) {
-                const int64_t idx = pos - lane;
-                uint32_t flag = 2u, val = 0u;
-                if (idx >= 0) {
-                    uint32_t ns = 32;
-                    for (uint32_t round = 0;; ++round) {
-                        const uint64_t w = ld_relaxed_u64(status + idx);
-                        const uint32_t hi = (uint32_t)(w >> 32);
-                        if ((hi >> 2) == epoch && (hi & 3u) != 0) {
-                            flag = hi & 3u;
-                            val = (uint32_t)w;
-                            break;
-                        }
-                        if (round >= wait_limit) {
-                            timed_out = true;
-                            break;
-                        }
-                        if (round >= spin) {
-                            __nanosleep(ns);
-                            if (ns < 512) ns <<= 1;
-                        }
-                    }
-                }
-                const uint32_t pm = __ballot_sync(0xFFFFFFFFu, flag == 2u);
-                const uint32_t stop = pm ? (uint32_t)(__ffs(pm) - 1) : 31u;
-                uint32_t contrib = lane <= stop ? val : 0u;
-#pragma unroll
-                for (int d = 16; d > 0; d >>= 1) contrib += __shfl_xor_sync(0xFFFFFFFFu, contrib, d);
-                prefix += contrib;
-                if (pm) break;
-                pos -= 32;
-            }
-            if (__any_sync(0xFFFFFFFFu, timed_out) && lane == 0) VREN_RECORD_ERROR(VREN_ERR_TIMEOUT);
-            if (lane == 0) st_relaxed_u64(status + tile, make_status(epoch, 2u, prefix + tile_unique));
-        }
-        if (lane == 0) {
-            sm.offset = prefix;
-            if (tile == num_tiles - 1) {
-                const uint32_t total = prefix + tile_unique;
-                *key_count = total < key_cap ? total : key_cap;
-                if (total > key_cap) VREN_RECORD_ERROR(VREN_ERR_CAPACITY);
-            }
-        }
-
-        // Keys, ascending: word w bit b is the sub-key 32 w + b.
+        // the tile's keys, ascending (word w bit b is the sub-key 32 w + b), and their count
         const uint32_t low = ((ty & 0xFFu) << 8) | (tx & 0xFFu);
-        uint32_t pos = prefix + excl;
+        uint32_t* out = fr.tile_keys + (size_t)tile * 1024u;
+        uint32_t pos = excl;
         for (int h = 0; h < 2; ++h) {
             for (uint32_t m = h ? u1 : u0; m; m &= m - 1u) {
                 const uint32_t w = 64u * lane + 32u * h + __ffs(m) - 1u;
-                for (uint32_t bits = s_bits[w]; bits; bits &= bits - 1u) {
-                    if (pos < key_cap) keys[pos] = ((w * 32u + __ffs(bits) - 1u) << 16) | low;
-                    ++pos;
-                }
+                for (uint32_t bits = s_bits[w]; bits; bits &= bits - 1u) out[pos++] = ((w * 32u + __ffs(bits) - 1u) << 16) | low;
             }
         }
+        if (lane == 31) fr.tile_count[tile] = incl;
     }
-    __syncthreads();
-    const uint32_t off = sm.offset;
 
-    // Per-pixel references (only on-screen pixels; the reference's imageStore drops the rest).
+    // Tile-local ranks into the reference buffer (only on-screen pixels: the reference's imageStore
+    // drops the rest).
     uint32_t r[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
@@ -487,7 +430,7 @@ __device__ __forceinline__ void find_unique_tile(const FucFrame& fr, uint32_t ti
             r[j] = r[j - 1];
         } else if (sj != 0xFFFFFFFFu) {
             const uint32_t w = sj >> 5;
-            r[j] = off + s_prefix[w] + __popc(s_bits[w] & ((1u << (sj & 31u)) - 1u));
+            r[j] = s_prefix[w] + __popc(s_bits[w] & ((1u << (sj & 31u)) - 1u));
         } else {
             r[j] = 0u;
         }
@@ -500,6 +443,65 @@ __device__ __forceinline__ void find_unique_tile(const FucFrame& fr, uint32_t ti
             if (gx0 + j < W) refs[(size_t)gy * W + gx0 + j] = r[j];
     }
 
+}
+
+// Between the stages: one CTA of kFucScanThreads scans the frame's tile counts into offsets and
+// writes the key count.
+constexpr int kFucScanThreads = 1024;
+__device__ __forceinline__ void find_unique_scan(const FucFrame& fr, uint32_t* s_warp)
+{
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const uint32_t T = fr.num_tiles;
+    const uint32_t per = (T + kFucScanThreads - 1) / kFucScanThreads;
+    const uint32_t b0 = tid * per, e0 = b0 + per < T ? b0 + per : T;
+    uint32_t sum = 0;
+    for (uint32_t t = b0; t < e0; ++t) sum += fr.tile_count[t];
+    uint32_t incl = sum;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+        if (lane >= (uint32_t)d) incl += y;
+    }
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    uint32_t before = incl - sum, total = 0;
+#pragma unroll
+    for (int w = 0; w < kFucScanThreads / 32; ++w) {
+        if (w < (int)warp) before += s_warp[w];
+        total += s_warp[w];
+    }
+    for (uint32_t t = b0; t < e0; ++t) {
+        fr.tile_offset[t] = before;
+        before += fr.tile_count[t];
+    }
+    if (tid == 0) {
+        *fr.key_count = total < fr.key_cap ? total : fr.key_cap;
+        if (total > fr.key_cap) VREN_RECORD_ERROR(VREN_ERR_CAPACITY);
+    }
+}
+
+// Stage 2 for tile `tile`: references += tile offset, keys to their place in the dense list.
+__device__ __forceinline__ void find_unique_fixup(const FucFrame& fr, uint32_t tile)
+{
+    const uint32_t tid = threadIdx.x;
+    const uint32_t off = fr.tile_offset[tile], n = fr.tile_count[tile];
+    const uint32_t* src = fr.tile_keys + (size_t)tile * 1024u;
+    for (uint32_t j = tid; j < n; j += kFucThreads)
+        if (off + j < fr.key_cap) fr.keys[off + j] = src[j];
+    const uint32_t W = fr.W, H = fr.H, TX = (W + 31) / 32;
+    const uint32_t tx = tile % TX, ty = tile / TX;
+    const uint32_t gy = ty * 32u + (tid >> 3), gx0 = tx * 32u + (tid & 7u) * 4u;
+    if (gy >= H) return;
+    uint32_t* row = fr.refs + (size_t)gy * W;
+    if (fr.vec && gx0 + 3u < W) {
+        uint4 v = *reinterpret_cast<uint4*>(row + gx0);
+        v.x += off; v.y += off; v.z += off; v.w += off;
+        *reinterpret_cast<uint4*>(row + gx0) = v;
+    } else {
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (gx0 + j < W) row[gx0 + j] += off;
+    }
 }
 
 // ================================================================================================
