@@ -143,6 +143,18 @@ def test_find_unique_clusters_special_normals(cuda):
     assert np.array_equal(u32(refs), erefs)
 
 
+def test_find_unique_clusters_many_tiles(cuda):
+    """More than 16,384 tiles (the tile-count scan runs in several chunks)."""
+    W, H = 4160, 4144  # 130 x 130 tiles
+    view = make_view(W, H)
+    depth, normals = scene.depth_planes(99, W, H)
+    _, keys, kc, refs = run_unique(cuda, depth, normals, W, H, view)
+    ekeys, erefs = oracle.cs_find_unique_clusters(depth, normals, W, H, view, 0)
+    U = int(u32(kc)[0])
+    assert U == len(ekeys) and np.array_equal(u32(keys)[:U], ekeys)
+    assert np.array_equal(u32(refs), erefs)
+
+
 @pytest.mark.parametrize("slicing", ["ref", "fixed32"])
 def test_find_unique_clusters_adversarial(cuda, slicing):
     """Depths at and one or two ulps either side of every slice boundary (the slice estimate must be

@@ -446,37 +446,48 @@ __device__ __forceinline__ void find_unique_tile(const FucFrame& fr, uint32_t ti
 }
 
 // Between the stages: one CTA of kFucScanThreads scans the frame's tile counts into offsets and
-// writes the key count.
+// writes the key count.  Thread t owns 16 consecutive counts of each 16384-tile chunk (unrolled
+// loads, all in flight); chunks carry their running total.
 constexpr int kFucScanThreads = 1024;
+constexpr uint32_t kFucScanPer = 16;
 __device__ __forceinline__ void find_unique_scan(const FucFrame& fr, uint32_t* s_warp)
 {
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const uint32_t T = fr.num_tiles;
-    const uint32_t per = (T + kFucScanThreads - 1) / kFucScanThreads;
-    const uint32_t b0 = tid * per, e0 = b0 + per < T ? b0 + per : T;
-    uint32_t sum = 0;
-    for (uint32_t t = b0; t < e0; ++t) sum += fr.tile_count[t];
-    uint32_t incl = sum;
+    uint32_t carry = 0;
+    for (uint32_t chunk = 0; chunk < T; chunk += kFucScanThreads * kFucScanPer) {
+        const uint32_t b0 = chunk + tid * kFucScanPer;
+        uint32_t v[kFucScanPer], sum = 0;
 #pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, d);
-        if (lane >= (uint32_t)d) incl += y;
-    }
-    if (lane == 31) s_warp[warp] = incl;
-    __syncthreads();
-    uint32_t before = incl - sum, total = 0;
+        for (uint32_t k = 0; k < kFucScanPer; ++k) {
+            v[k] = b0 + k < T ? fr.tile_count[b0 + k] : 0u;
+            sum += v[k];
+        }
+        uint32_t incl = sum;
 #pragma unroll
-    for (int w = 0; w < kFucScanThreads / 32; ++w) {
-        if (w < (int)warp) before += s_warp[w];
-        total += s_warp[w];
-    }
-    for (uint32_t t = b0; t < e0; ++t) {
-        fr.tile_offset[t] = before;
-        before += fr.tile_count[t];
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+            if (lane >= (uint32_t)d) incl += y;
+        }
+        __syncthreads();  // s_warp of the previous chunk has been read
+        if (lane == 31) s_warp[warp] = incl;
+        __syncthreads();
+        uint32_t before = carry + incl - sum, total = 0;
+#pragma unroll
+        for (int w = 0; w < kFucScanThreads / 32; ++w) {
+            if (w < (int)warp) before += s_warp[w];
+            total += s_warp[w];
+        }
+#pragma unroll
+        for (uint32_t k = 0; k < kFucScanPer; ++k) {
+            if (b0 + k < T) fr.tile_offset[b0 + k] = before;
+            before += v[k];
+        }
+        carry += total;
     }
     if (tid == 0) {
-        *fr.key_count = total < fr.key_cap ? total : fr.key_cap;
-        if (total > fr.key_cap) VREN_RECORD_ERROR(VREN_ERR_CAPACITY);
+        *fr.key_count = carry < fr.key_cap ? carry : fr.key_cap;
+        if (carry > fr.key_cap) VREN_RECORD_ERROR(VREN_ERR_CAPACITY);
     }
 }
 
