@@ -66,7 +66,8 @@ uint32_t vren_set_wait_limit(uint32_t rounds);
  *   VREN_TUNE_SCAN_SLICES  128-element slices per warp in a scan tile: 4 (4096/tile) or 8 (8192/tile)
  *   VREN_TUNE_SPIN_POLLS   look-back polls before a waiting thread starts to back off with nanosleep
  *   VREN_TUNE_RADIX_RANK   digit ranking in a sort pass: 0 = one ballot per digit bit,
- *                          1 = match.any + shared-memory atomic per peer group
+ *                          1 = match.any + shared-memory atomic per peer group,
+ *                          2 = match.any + counter update by the group's first lane
  *   VREN_TUNE_RADIX_ITEMS  keys per thread in a sort pass: 0 = 15/16 (3840/4096 per tile), 1 = 23/24 */
 enum { VREN_TUNE_SCAN_SLICES = 0, VREN_TUNE_SPIN_POLLS = 1, VREN_TUNE_RADIX_RANK = 2, VREN_TUNE_RADIX_ITEMS = 3,
        VREN_TUNE_COUNT = 4 };

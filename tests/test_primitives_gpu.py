@@ -323,7 +323,7 @@ def restore_tuning(native):
         native.vren_tuning_set(vg._lib.TUNE[k], v)
 
 
-@pytest.mark.parametrize("rank", [0, 1])
+@pytest.mark.parametrize("rank", [0, 1, 2])
 @pytest.mark.parametrize("items", [0, 1])
 @pytest.mark.parametrize("spin", [0, 64])
 def test_radix_variants_identical(cuda, restore_tuning, rank, items, spin):

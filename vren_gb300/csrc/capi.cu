@@ -69,7 +69,7 @@ extern "C" int vren_tuning_set(int knob, int value)
         if (value < 0 || value > (1 << 20)) return VREN_ERR_ARG;
         break;
     case VREN_TUNE_RADIX_RANK:
-        if (value != 0 && value != 1) return VREN_ERR_ARG;
+        if (value < 0 || value > 2) return VREN_ERR_ARG;
         break;
     case VREN_TUNE_RADIX_ITEMS:
         if (value != 0 && value != 1) return VREN_ERR_ARG;

@@ -138,35 +138,33 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_hist_kernel(
 }
 
 // ------------------------------------------------------------------------------------------------
-// One digit pass.  RANK 0: peers from one ballot per digit bit and per-warp counters updated by the
-// group's first lane; RANK 1: peers from match.any and one shared-memory atomic per peer group.
-// Both give the same (stable) ranks.  Keys/values are staged in dynamic shared memory.
+// One digit pass.  RANK 0: peers from one ballot per digit bit; RANK 1: peers from match.any and one
+// shared-memory atomic per peer group; RANK 2: peers from match.any, counters updated by the group's
+// first lane as in RANK 0.  All give the same (stable) ranks.  Keys/values are staged in dynamic
+// shared memory.  FULL tiles (all but the last) skip every per-item bounds test.
 // ------------------------------------------------------------------------------------------------
 template <int DIGIT_BITS, int ITEMS, int MODE, int RANK>
-__global__ void __launch_bounds__(kSortThreads) onesweep_pass_kernel(
-    const uint32_t* __restrict__ in_keys, const uint32_t* __restrict__ in_vals,
-    uint32_t* __restrict__ out_keys, uint32_t* __restrict__ out_vals,
-    uint32_t n, uint32_t pass, uint32_t shift, uint32_t width, uint32_t num_tiles,
-    uint32_t* __restrict__ scratch, uint32_t wait_limit, uint32_t spin)
+struct PassSmem {
+    static constexpr int RADIX = 1 << DIGIT_BITS;
+    uint32_t warp_hist[kSortWarps][RADIX];
+    uint32_t tile_excl[RADIX];
+    int32_t delta[RADIX];
+    uint32_t wsum[kSortWarps];
+};
+
+template <int DIGIT_BITS, int ITEMS, int MODE, int RANK, bool FULL>
+__device__ __forceinline__ void onesweep_pass_body(
+    const uint32_t* __restrict__ in_keys, const uint32_t* __restrict__ in_vals, uint32_t* __restrict__ out_keys,
+    uint32_t* __restrict__ out_vals, uint32_t n, uint32_t pass, uint32_t shift, uint32_t width, uint32_t num_tiles,
+    uint32_t* __restrict__ scratch, uint32_t wait_limit, uint32_t spin, uint32_t tile,
+    PassSmem<DIGIT_BITS, ITEMS, MODE, RANK>& sm, uint4* s_stage)
 {
     constexpr int RADIX = 1 << DIGIT_BITS;
     constexpr int TILE = kSortThreads * ITEMS;
     using Elem = typename std::conditional<MODE == kUvec2, uint2, uint32_t>::type;
-
-    extern __shared__ uint4 s_stage[];
     Elem* s_keys = reinterpret_cast<Elem*>(s_stage);
     uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_keys + TILE);
-    __shared__ uint32_t s_warp_hist[kSortWarps][RADIX];
-    __shared__ uint32_t s_tile_excl[RADIX];
-    __shared__ int32_t s_delta[RADIX];
-    __shared__ uint32_t s_wsum[kSortWarps];
-    __shared__ uint32_t s_tile;
-
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-    if (tid == 0) s_tile = atomicAdd(scratch + pass, 1u);
-    for (uint32_t i = tid; i < kSortWarps * RADIX; i += kSortThreads) (&s_warp_hist[0][0])[i] = 0u;
-    __syncthreads();
-    const uint32_t tile = s_tile;
 
     uint32_t* status = scratch + kStatusOffset + (size_t)(pass & 1u) * num_tiles * RADIX;
     uint32_t* status_next = scratch + kStatusOffset + (size_t)((pass + 1u) & 1u) * num_tiles * RADIX;
@@ -182,7 +180,7 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_pass_kernel(
         const uint32_t idx = warp_base + 32 * j + lane;
         key[j] = Elem{};
         val[j] = 0u;
-        if (idx < n) {
+        if (FULL || idx < n) {
             if (MODE == kUvec2) {
                 (reinterpret_cast<uint2*>(&key[j]))[0] = __ldcs(reinterpret_cast<const uint2*>(in_keys) + idx);
             } else {
@@ -196,7 +194,7 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_pass_kernel(
 #pragma unroll
     for (int j = 0; j < ITEMS; ++j) {
         const uint32_t idx = warp_base + 32 * j + lane;
-        const bool valid = idx < n;
+        const bool valid = FULL || idx < n;
         uint32_t k;
         if (MODE == kUvec2) k = (reinterpret_cast<uint2*>(&key[j]))->x;
         else k = *(reinterpret_cast<uint32_t*>(&key[j]));
@@ -206,24 +204,29 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_pass_kernel(
             const uint32_t peers = __match_any_sync(0xFFFFFFFFu, valid ? d : (0x10000u + lane));
             const uint32_t leader = __ffs(peers) - 1;
             uint32_t base = 0;
-            if (valid && lane == leader) base = atomicAdd(&s_warp_hist[warp][d], (uint32_t)__popc(peers));
+            if (valid && lane == leader) base = atomicAdd(&sm.warp_hist[warp][d], (uint32_t)__popc(peers));
             base = __shfl_sync(0xFFFFFFFFu, base, leader);
             pos[j] = valid ? (d | ((base + __popc(peers & lanemask_lt())) << 8)) : 0xFFFFFFFFu;
         } else {
-            uint32_t peers = __ballot_sync(0xFFFFFFFFu, valid);
+            uint32_t peers;
+            if (RANK == 2) {
+                peers = __match_any_sync(0xFFFFFFFFu, valid ? d : (0x10000u + lane));
+            } else {
+                peers = FULL ? 0xFFFFFFFFu : __ballot_sync(0xFFFFFFFFu, valid);
 #pragma unroll
-            for (int b = 0; b < DIGIT_BITS; ++b) {
-                const uint32_t m = __ballot_sync(0xFFFFFFFFu, (d >> b) & 1u);
-                // keep the lanes whose bit b equals mine: m where my bit is 1, ~m where it is 0
-                const uint32_t mine = (uint32_t)((int32_t)(d << (31 - b)) >> 31);
-                peers &= ~(m ^ mine);
+                for (int b = 0; b < DIGIT_BITS; ++b) {
+                    const uint32_t m = __ballot_sync(0xFFFFFFFFu, (d >> b) & 1u);
+                    // keep the lanes whose bit b equals mine: m where my bit is 1, ~m where it is 0
+                    const uint32_t mine = (uint32_t)((int32_t)(d << (31 - b)) >> 31);
+                    peers &= ~(m ^ mine);
+                }
             }
-            uint32_t before = 0;
-            if (valid) before = s_warp_hist[warp][d];
+            const uint32_t below = peers & lanemask_lt();
+            const uint32_t before = valid ? sm.warp_hist[warp][d] : 0u;
             __syncwarp();
-            if (valid && (peers & lanemask_lt()) == 0) s_warp_hist[warp][d] = before + __popc(peers);
+            if (valid && below == 0) sm.warp_hist[warp][d] = before + __popc(peers);
             __syncwarp();
-            pos[j] = valid ? (d | ((before + __popc(peers & lanemask_lt())) << 8)) : 0xFFFFFFFFu;
+            pos[j] = valid ? (d | ((before + __popc(below)) << 8)) : 0xFFFFFFFFu;
         }
     }
     __syncthreads();
@@ -234,8 +237,8 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_pass_kernel(
         const uint32_t d = tid;
 #pragma unroll
         for (int w = 0; w < kSortWarps; ++w) {
-            const uint32_t c = s_warp_hist[w][d];
-            s_warp_hist[w][d] = count;
+            const uint32_t c = sm.warp_hist[w][d];
+            sm.warp_hist[w][d] = count;
             count += c;
         }
         st_relaxed_u32(status + (size_t)tile * RADIX + d, (tile == 0 ? kFlagPrefix : kFlagAggregate) | count);
@@ -247,7 +250,7 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_pass_kernel(
         const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
         if (lane >= (uint32_t)o) incl += y;
     }
-    if (lane == 31) s_wsum[warp] = incl;
+    if (lane == 31) sm.wsum[warp] = incl;
     __syncthreads();
     // Tile-local digit offsets, and the first look-back read for digit d issued now: its latency
     // overlaps the staging below, which needs only tile-local offsets.
@@ -255,8 +258,8 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_pass_kernel(
     if (tid < (uint32_t)RADIX) {
         const uint32_t d = tid;
         excl = incl - count;
-        for (uint32_t w = 0; w < warp; ++w) excl += s_wsum[w];
-        s_tile_excl[d] = excl;
+        for (uint32_t w = 0; w < warp; ++w) excl += sm.wsum[w];
+        sm.tile_excl[d] = excl;
         if (tile != 0) lb_word = ld_relaxed_u32(status + (size_t)(tile - 1) * RADIX + d);
         goff = ld_relaxed_u32(scratch + kOffsOffset + pass * kMaxRadix + d);
     }
@@ -265,9 +268,9 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_pass_kernel(
     // Stage in digit order.
 #pragma unroll
     for (int j = 0; j < ITEMS; ++j) {
-        if (pos[j] != 0xFFFFFFFFu) {
+        if (FULL || pos[j] != 0xFFFFFFFFu) {
             const uint32_t d = pos[j] & 0xFFu;
-            const uint32_t p = s_tile_excl[d] + s_warp_hist[warp][d] + (pos[j] >> 8);
+            const uint32_t p = sm.tile_excl[d] + sm.warp_hist[warp][d] + (pos[j] >> 8);
             s_keys[p] = key[j];
             if (MODE == kPairs) s_vals[p] = val[j];
         }
@@ -291,31 +294,58 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_pass_kernel(
             }
             st_relaxed_u32(status + (size_t)tile * RADIX + d, kFlagPrefix | (prefix + count));
         }
-        s_delta[d] = (int32_t)(goff + prefix) - (int32_t)excl;
+        sm.delta[d] = (int32_t)(goff + prefix) - (int32_t)excl;
     }
     __syncthreads();
 
     // Write out: consecutive threads take consecutive staged elements.
-    const uint32_t tile_valid = (tile + 1) * TILE <= n ? TILE : n - tile * TILE;
+    const uint32_t tile_valid = FULL ? (uint32_t)TILE : ((tile + 1) * TILE <= n ? TILE : n - tile * TILE);
 #pragma unroll
     for (int j = 0; j < ITEMS; ++j) {
         const uint32_t p = j * kSortThreads + tid;
-        if (p < tile_valid) {
+        if (FULL || p < tile_valid) {
             const Elem e = s_keys[p];
             uint32_t k;
             if (MODE == kUvec2) k = (reinterpret_cast<const uint2*>(&e))->x;
             else k = *(reinterpret_cast<const uint32_t*>(&e));
             const uint32_t d = digit_of(k, shift, width);
-            const uint32_t dst = (uint32_t)((int32_t)p + s_delta[d]);
-            if (dst >= n) continue;  // only reachable after a timed-out look-back (error recorded)
-            if (MODE == kUvec2) {
-                reinterpret_cast<uint2*>(out_keys)[dst] = *(reinterpret_cast<const uint2*>(&e));
-            } else {
-                out_keys[dst] = k;
-                if (MODE == kPairs) out_vals[dst] = s_vals[p];
+            const uint32_t dst = (uint32_t)((int32_t)p + sm.delta[d]);
+            if (dst < n) {  // false only after a timed-out look-back (error recorded)
+                if (MODE == kUvec2) {
+                    reinterpret_cast<uint2*>(out_keys)[dst] = *(reinterpret_cast<const uint2*>(&e));
+                } else {
+                    out_keys[dst] = k;
+                    if (MODE == kPairs) out_vals[dst] = s_vals[p];
+                }
             }
         }
     }
+}
+
+template <int DIGIT_BITS, int ITEMS, int MODE, int RANK>
+__global__ void __launch_bounds__(kSortThreads, 4) onesweep_pass_kernel(
+    const uint32_t* __restrict__ in_keys, const uint32_t* __restrict__ in_vals,
+    uint32_t* __restrict__ out_keys, uint32_t* __restrict__ out_vals,
+    uint32_t n, uint32_t pass, uint32_t shift, uint32_t width, uint32_t num_tiles,
+    uint32_t* __restrict__ scratch, uint32_t wait_limit, uint32_t spin)
+{
+    constexpr int TILE = kSortThreads * ITEMS;
+    extern __shared__ uint4 s_stage[];
+    __shared__ PassSmem<DIGIT_BITS, ITEMS, MODE, RANK> sm;
+    __shared__ uint32_t s_tile;
+    const uint32_t tid = threadIdx.x;
+    if (tid == 0) s_tile = atomicAdd(scratch + pass, 1u);
+    for (uint32_t i = tid; i < kSortWarps * (1u << DIGIT_BITS); i += kSortThreads) (&sm.warp_hist[0][0])[i] = 0u;
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    if ((uint64_t)(tile + 1) * TILE <= n)
+        onesweep_pass_body<DIGIT_BITS, ITEMS, MODE, RANK, true>(in_keys, in_vals, out_keys, out_vals, n, pass, shift,
+                                                                width, num_tiles, scratch, wait_limit, spin, tile, sm,
+                                                                s_stage);
+    else
+        onesweep_pass_body<DIGIT_BITS, ITEMS, MODE, RANK, false>(in_keys, in_vals, out_keys, out_vals, n, pass, shift,
+                                                                 width, num_tiles, scratch, wait_limit, spin, tile, sm,
+                                                                 s_stage);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -384,7 +414,7 @@ static int run_passes(cudaStream_t st, const uint32_t* src_k, const uint32_t* sr
 {
     constexpr int RADIX = 1 << DB;
     const int variant = tuning(VREN_TUNE_RADIX_ITEMS) == 1 ? 1 : 0;
-    const int rank = tuning(VREN_TUNE_RADIX_RANK) == 1 ? 1 : 0;
+    const int rank = tuning(VREN_TUNE_RADIX_RANK);
     const uint32_t spin = (uint32_t)tuning(VREN_TUNE_SPIN_POLLS);
     const uint32_t tiles = (n + tile_of(DB, variant) - 1) / tile_of(DB, variant);
     const uint32_t status_tiles = tiles_for(n, DB);  // rows per status buffer (scratch layout)
@@ -403,12 +433,10 @@ static int run_passes(cudaStream_t st, const uint32_t* src_k, const uint32_t* sr
         uint32_t* ok = to_final ? dst_k : tmp_k;
         uint32_t* ov = to_final ? dst_v : tmp_v;
         int rc;
-        if (variant == 1)
-            rc = rank == 1 ? launch_pass<DB, MODE, 1, 1>(st, src_k, src_v, ok, ov, n, p, passes.shift[p], passes.width[p], tiles, scratch, spin)
-                           : launch_pass<DB, MODE, 1, 0>(st, src_k, src_v, ok, ov, n, p, passes.shift[p], passes.width[p], tiles, scratch, spin);
-        else
-            rc = rank == 1 ? launch_pass<DB, MODE, 0, 1>(st, src_k, src_v, ok, ov, n, p, passes.shift[p], passes.width[p], tiles, scratch, spin)
-                           : launch_pass<DB, MODE, 0, 0>(st, src_k, src_v, ok, ov, n, p, passes.shift[p], passes.width[p], tiles, scratch, spin);
+#define VREN_PASS(V, R) launch_pass<DB, MODE, V, R>(st, src_k, src_v, ok, ov, n, p, passes.shift[p], passes.width[p], tiles, scratch, spin)
+        if (variant == 1) rc = rank == 1 ? VREN_PASS(1, 1) : rank == 2 ? VREN_PASS(1, 2) : VREN_PASS(1, 0);
+        else rc = rank == 1 ? VREN_PASS(0, 1) : rank == 2 ? VREN_PASS(0, 2) : VREN_PASS(0, 0);
+#undef VREN_PASS
         if (rc != VREN_OK) return rc;
         src_k = ok;
         src_v = ov;
