@@ -82,6 +82,7 @@ __global__ void __launch_bounds__(256) batch_transform_kernel(const BatchDesc* _
                                                               float4* __restrict__ view_pos, uint32_t* __restrict__ part,
                                                               uint32_t* __restrict__ fmm, uint32_t* __restrict__ fticket)
 {
+    pdl_enter();
     __shared__ uint32_t s_keys[8][6];
     __shared__ bool s_last;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
@@ -151,6 +152,7 @@ __global__ void __launch_bounds__(256) batch_morton_kernel(const BatchDesc* __re
                                                            const float4* __restrict__ view_pos,
                                                            const uint32_t* __restrict__ fmm, uint2* __restrict__ pairs)
 {
+    pdl_enter();
     const uint32_t f = frame_of(chunk_prefix, n, blockIdx.x);
     const uint32_t chunk = blockIdx.x - chunk_prefix[f];
     const BatchDesc& fd = d[f];
@@ -176,6 +178,7 @@ __global__ void __launch_bounds__(1024) batch_leaves_kernel(const BatchDesc* __r
                                                             const float4* __restrict__ view_pos,
                                                             vren_bvh_node* __restrict__ bvh, float4* __restrict__ spheres)
 {
+    pdl_enter();
     __shared__ NodeF s_parent[32];
     const uint32_t f = frame_of(leaf_prefix, n, blockIdx.x);
     const uint32_t chunk = blockIdx.x - leaf_prefix[f];
@@ -193,6 +196,7 @@ __global__ void __launch_bounds__(1024) batch_leaves_kernel(const BatchDesc* __r
 __global__ void __launch_bounds__(1024) batch_levels_kernel(const BatchDesc* __restrict__ d,
                                                             vren_bvh_node* __restrict__ bvh)
 {
+    pdl_enter();
     __shared__ NodeF s_parent[32];
     const BatchDesc& fd = d[blockIdx.x];
     if (fd.L == 0 || fd.P < 32768u) return;
@@ -230,6 +234,7 @@ __device__ __forceinline__ FucFrame batch_fuc_frame(const BatchFuc& b, uint32_t 
 // Every frame's tiles.
 __global__ void __launch_bounds__(kFucThreads, 6) batch_find_unique_kernel(BatchFuc b)
 {
+    pdl_enter();
     __shared__ FucSmem sm;
     const uint32_t tid = threadIdx.x;
     reinterpret_cast<uint4*>(sm.bits)[tid] = make_uint4(0u, 0u, 0u, 0u);
@@ -243,12 +248,14 @@ __global__ void __launch_bounds__(kFucThreads, 6) batch_find_unique_kernel(Batch
 // One CTA per frame: its tile counts into offsets.
 __global__ void __launch_bounds__(kFucScanThreads) batch_find_unique_scan_kernel(BatchFuc b)
 {
+    pdl_enter();
     __shared__ uint32_t s_warp[kFucScanThreads / 32];
     find_unique_scan(batch_fuc_frame(b, blockIdx.x), s_warp);
 }
 
 __global__ void __launch_bounds__(kFucThreads) batch_find_unique_fixup_kernel(BatchFuc b)
 {
+    pdl_enter();
     const uint32_t f = frame_of(b.tile_prefix, b.n, blockIdx.x);
     find_unique_fixup(batch_fuc_frame(b, f), blockIdx.x - b.tile_prefix[f]);
 }
@@ -258,6 +265,7 @@ __global__ void __launch_bounds__(1024) batch_bases_kernel(const BatchDesc* __re
                                                            const uint32_t* __restrict__ key_counts,
                                                            uint32_t* __restrict__ base)
 {
+    pdl_enter();
     __shared__ uint32_t s_warp[32];
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     uint32_t u = 0;
@@ -317,6 +325,7 @@ __device__ __forceinline__ uint32_t batch_traverse(const AssignArgs& a, const Le
 template <bool WRITE>
 __global__ void __launch_bounds__(256) batch_assign_kernel(BatchAssign b)
 {
+    pdl_enter();
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t warps_per_cta = blockDim.x >> 5;
     const uint32_t gw = blockIdx.x * warps_per_cta + (threadIdx.x >> 5);
@@ -351,6 +360,7 @@ __global__ void batch_totals_kernel(uint32_t n, const uint32_t* __restrict__ bas
                                     const uint32_t* __restrict__ grand_total, uint32_t* __restrict__ index_base,
                                     uint32_t* __restrict__ totals)
 {
+    pdl_enter();
     const uint32_t clusters = base[n];
     for (uint32_t f = threadIdx.x; f < n; f += blockDim.x) {
         const uint32_t b0 = base[f], b1 = base[f + 1];
@@ -556,35 +566,36 @@ int stage_batch(vren_cs_batch* b, cudaStream_t st, const vren_cs_batch_frame* fr
 // The kernel sequence of one batch (capturable: no allocation, no host synchronisation).
 int enqueue_batch(vren_cs_batch* b, cudaStream_t st)
 {
+    const PdlScope pdl(1);  // consecutive kernels of the sequence overlap their launches
     const uint32_t n = b->n;
     const uint32_t* chunk_prefix = b->prefixes;
     const uint32_t* leaf_prefix = b->prefixes + (n + 1);
     const uint32_t* tile_prefix = b->prefixes + 2 * (n + 1);
     if (b->total_chunks > 0) {
-        batch_transform_kernel<<<b->total_chunks, 256, 0, st>>>(b->desc, chunk_prefix, n, b->view_pos, b->part, b->fmm,
+        launch_kernel(batch_transform_kernel, b->total_chunks, 256, 0, st, b->desc, chunk_prefix, n, b->view_pos, b->part, b->fmm,
                                                                 b->fticket);
         VREN_LAUNCH_CHECK();
-        batch_morton_kernel<<<b->total_chunks, 256, 0, st>>>(b->desc, chunk_prefix, n, b->view_pos, b->fmm, b->pairs);
+        launch_kernel(batch_morton_kernel, b->total_chunks, 256, 0, st, b->desc, chunk_prefix, n, b->view_pos, b->fmm, b->pairs);
         VREN_LAUNCH_CHECK();
         int rc = sort_uvec2(st, reinterpret_cast<const uint32_t*>(b->pairs), reinterpret_cast<uint32_t*>(b->light_index),
                             reinterpret_cast<uint32_t*>(b->sort_tmp), b->total_lights, 16u + b->frame_bits,
                             b->opt.sort_digit_bits, b->sort_scratch);
         if (rc != VREN_OK) return rc;
-        batch_leaves_kernel<<<b->total_leaf_blocks, 1024, 0, st>>>(b->desc, leaf_prefix, n, b->light_index,
+        launch_kernel(batch_leaves_kernel, b->total_leaf_blocks, 1024, 0, st, b->desc, leaf_prefix, n, b->light_index,
                                                                    b->view_pos, b->bvh, b->spheres);
         VREN_LAUNCH_CHECK();
-        batch_levels_kernel<<<n, 1024, 0, st>>>(b->desc, b->bvh);
+        launch_kernel(batch_levels_kernel, n, 1024, 0, st, b->desc, b->bvh);
         VREN_LAUNCH_CHECK();
     }
     const BatchFuc bf{b->desc, tile_prefix, n, b->keys, b->key_counts, b->refs, b->tile_keys, b->tile_count,
                       b->tile_offset};
-    batch_find_unique_kernel<<<b->total_tiles, kFucThreads, 0, st>>>(bf);
+    launch_kernel(batch_find_unique_kernel, b->total_tiles, kFucThreads, 0, st, bf);
     VREN_LAUNCH_CHECK();
-    batch_find_unique_scan_kernel<<<n, kFucScanThreads, 0, st>>>(bf);
+    launch_kernel(batch_find_unique_scan_kernel, n, kFucScanThreads, 0, st, bf);
     VREN_LAUNCH_CHECK();
-    batch_find_unique_fixup_kernel<<<b->total_tiles, kFucThreads, 0, st>>>(bf);
+    launch_kernel(batch_find_unique_fixup_kernel, b->total_tiles, kFucThreads, 0, st, bf);
     VREN_LAUNCH_CHECK();
-    batch_bases_kernel<<<1, 1024, 0, st>>>(b->desc, n, b->key_counts, b->base);
+    launch_kernel(batch_bases_kernel, 1, 1024, 0, st, b->desc, n, b->key_counts, b->base);
     VREN_LAUNCH_CHECK();
     BatchAssign a{b->desc, n, b->base, b->keys, b->counts, b->goff, b->offsets, b->indices,
                   (uint32_t)(b->cap_assign < 0xFFFFFFFFull ? b->cap_assign : 0xFFFFFFFFull),
@@ -592,14 +603,14 @@ int enqueue_batch(vren_cs_batch* b, cudaStream_t st)
     uint32_t warps = b->opt.assign_warps;
     if (warps < 1 || warps > 8) warps = 8;
     const dim3 block(32 * warps), grid(kNumSMsHint * (64 / warps));
-    batch_assign_kernel<false><<<grid, block, 0, st>>>(a);
+    launch_kernel(batch_assign_kernel<false>, grid, block, 0, st, a);
     VREN_LAUNCH_CHECK();
     int rc = scan_exclusive_u32(st, b->counts, b->goff, (uint32_t)b->total_keys, b->base + n, b->grand_total,
                                 b->scan_scratch);
     if (rc != VREN_OK) return rc;
-    batch_assign_kernel<true><<<grid, block, 0, st>>>(a);
+    launch_kernel(batch_assign_kernel<true>, grid, block, 0, st, a);
     VREN_LAUNCH_CHECK();
-    batch_totals_kernel<<<1, 256, 0, st>>>(n, b->base, b->goff, b->grand_total, b->index_base, b->totals);
+    launch_kernel(batch_totals_kernel, 1, 256, 0, st, n, b->base, b->goff, b->grand_total, b->index_base, b->totals);
     VREN_LAUNCH_CHECK();
     return VREN_OK;
 }

@@ -25,6 +25,7 @@ __global__ void __launch_bounds__(1024) build_bvh_kernel(vren_bvh_node* __restri
                                                          uint32_t count, uint32_t dst1_off, uint32_t dst2_off,
                                                          int two_levels)
 {
+    pdl_enter();
     __shared__ NodeF s_parent[32];
     bvh_levels_block(bvh, blockIdx.x, src_off, count, dst1_off, dst2_off, two_levels != 0, s_parent);
 }
@@ -87,12 +88,12 @@ int build_bvh_levels(cudaStream_t st, vren_bvh_node* bvh, uint32_t src, uint32_t
         const uint32_t dst1 = src + count;
         if (count >= 1024) {
             const uint32_t dst2 = dst1 + count / 32;
-            build_bvh_kernel<<<count / 1024, 1024, 0, st>>>(bvh, src, count, dst1, dst2, 1);
+            launch_kernel(build_bvh_kernel, count / 1024, 1024, 0, st, bvh, src, count, dst1, dst2, 1);
             VREN_LAUNCH_CHECK();
             src = dst1 + count / 32;
             count /= 1024;
         } else {
-            build_bvh_kernel<<<1, count, 0, st>>>(bvh, src, count, dst1, 0, 0);
+            launch_kernel(build_bvh_kernel, 1, count, 0, st, bvh, src, count, dst1, 0, 0);
             VREN_LAUNCH_CHECK();
             src = dst1;
             count /= 32;

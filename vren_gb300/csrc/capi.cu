@@ -49,6 +49,8 @@ extern "C" int vren_device_error(int clear)
 namespace vren_gb300 {
 // Kernel variant knobs (tile sizes, ranking method, polling policy), set by the autotuner or the
 // caller; every launcher reads its knob when it enqueues work.
+thread_local int g_pdl = 0;
+
 static int g_tuning[VREN_TUNE_COUNT] = {
     /* VREN_TUNE_SCAN_SLICES */ 8,
     /* VREN_TUNE_SPIN_POLLS */ 64,

@@ -49,6 +49,7 @@ __global__ void __launch_bounds__(kLbvhThreads) lbvh_transform_kernel(
     const float4* __restrict__ positions, uint32_t L, const vren_cs_frame* __restrict__ F,
     float4* __restrict__ view_pos, uint32_t* __restrict__ scratch)
 {
+    pdl_enter();
     __shared__ uint32_t s_keys[kLbvhThreads / 32][6];
     __shared__ bool s_last;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
@@ -113,6 +114,7 @@ __global__ void __launch_bounds__(kLbvhThreads) lbvh_transform_kernel(
 __global__ void lbvh_morton_kernel(const float4* __restrict__ view_pos, uint32_t L, const uint32_t* __restrict__ scratch,
                                    uint32_t bits, uint2* __restrict__ pairs)
 {
+    pdl_enter();
     float mn[3], mx[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -127,6 +129,7 @@ __global__ void __launch_bounds__(1024) lbvh_leaves_kernel(
     const uint2* __restrict__ light_index, const float4* __restrict__ view_pos, const float4* __restrict__ lights,
     uint32_t L, uint32_t P, vren_bvh_node* __restrict__ bvh, float4* __restrict__ spheres)
 {
+    pdl_enter();
     __shared__ NodeF s_parent[32];
     light_leaves_block(blockIdx.x, blockDim.x, L, P, light_index, view_pos, lights, bvh, spheres, s_parent);
 }
@@ -143,13 +146,13 @@ static int construct_light_bvh(cudaStream_t st, const float* positions, const fl
     uint32_t* tmp = reinterpret_cast<uint32_t*>(sc + lay.tmp);
     const uint32_t grid = (L + kLbvhPerCta - 1) / kLbvhPerCta;
 
-    lbvh_transform_kernel<<<grid, kLbvhThreads, 0, st>>>(reinterpret_cast<const float4*>(positions), L, frame,
+    launch_kernel(lbvh_transform_kernel, grid, kLbvhThreads, 0, st, reinterpret_cast<const float4*>(positions), L, frame,
                                                          reinterpret_cast<float4*>(view_pos), hdr);
     VREN_LAUNCH_CHECK();
     const uint32_t bits = morton_bits == 30 ? 10u : 5u;
     uint32_t mgrid = (L + 255) / 256;
     if (mgrid > 1024) mgrid = 1024;
-    lbvh_morton_kernel<<<mgrid, 256, 0, st>>>(reinterpret_cast<const float4*>(view_pos), L, hdr, bits, pairs);
+    launch_kernel(lbvh_morton_kernel, mgrid, 256, 0, st, reinterpret_cast<const float4*>(view_pos), L, hdr, bits, pairs);
     VREN_LAUNCH_CHECK();
     // bucket sort on the low 16 bits (bucket_sort.hpp:15-16); the 30-bit extension sorts 30 bits
     int rc = sort_uvec2(st, reinterpret_cast<const uint32_t*>(pairs), light_index, tmp, L, morton_bits == 30 ? 30 : 16,
@@ -158,7 +161,7 @@ static int construct_light_bvh(cudaStream_t st, const float* positions, const fl
 
     const uint32_t P = vren_calc_bvh_padded_leaf_count(L);
     const uint32_t threads = P < 1024 ? P : 1024;
-    lbvh_leaves_kernel<<<P / threads, threads, 0, st>>>(
+    launch_kernel(lbvh_leaves_kernel, P / threads, threads, 0, st, 
         reinterpret_cast<const uint2*>(light_index), reinterpret_cast<const float4*>(view_pos),
         reinterpret_cast<const float4*>(lights), L, P, bvh, reinterpret_cast<float4*>(spheres));
     VREN_LAUNCH_CHECK();
@@ -171,6 +174,7 @@ static int construct_light_bvh(cudaStream_t st, const float* positions, const fl
 // ================================================================================================
 __global__ void __launch_bounds__(kFucThreads, 6) find_unique_kernel(FucFrame fr)
 {
+    pdl_enter();
     __shared__ FucSmem sm;
     const uint32_t tid = threadIdx.x;
     reinterpret_cast<uint4*>(sm.bits)[tid] = make_uint4(0u, 0u, 0u, 0u);
@@ -182,12 +186,14 @@ __global__ void __launch_bounds__(kFucThreads, 6) find_unique_kernel(FucFrame fr
 
 __global__ void __launch_bounds__(kFucScanThreads) find_unique_scan_kernel(FucFrame fr)
 {
+    pdl_enter();
     __shared__ uint32_t s_warp[kFucScanThreads / 32];
     find_unique_scan(fr, s_warp);
 }
 
 __global__ void __launch_bounds__(kFucThreads) find_unique_fixup_kernel(FucFrame fr)
 {
+    pdl_enter();
     find_unique_fixup(fr, blockIdx.x);
 }
 
@@ -204,11 +210,11 @@ static int launch_find_unique(cudaStream_t st, const float* depth, const float* 
                     ((uintptr_t)refs % 16u == 0u);
     const FucFrame fr{depth, normals, W, H, frame, keys, key_cap, key_count, refs,
                       scratch + fuc_keys_offset_words(tiles), scratch, scratch + tiles, tiles, vec};
-    find_unique_kernel<<<tiles, kFucThreads, 0, st>>>(fr);
+    launch_kernel(find_unique_kernel, tiles, kFucThreads, 0, st, fr);
     VREN_LAUNCH_CHECK();
-    find_unique_scan_kernel<<<1, kFucScanThreads, 0, st>>>(fr);
+    launch_kernel(find_unique_scan_kernel, 1, kFucScanThreads, 0, st, fr);
     VREN_LAUNCH_CHECK();
-    find_unique_fixup_kernel<<<tiles, kFucThreads, 0, st>>>(fr);
+    launch_kernel(find_unique_fixup_kernel, tiles, kFucThreads, 0, st, fr);
     VREN_LAUNCH_CHECK();
     return VREN_OK;
 }
@@ -219,6 +225,7 @@ static int launch_find_unique(cudaStream_t st, const float* depth, const float* 
 template <int LC, bool WRITE, bool SPHERES>
 __global__ void __launch_bounds__(256) assign_kernel(AssignArgs a, LevelBase lb)
 {
+    pdl_enter();
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t warps_per_cta = blockDim.x >> 5;
     const uint32_t gw = blockIdx.x * warps_per_cta + (threadIdx.x >> 5);
@@ -234,6 +241,7 @@ __global__ void __launch_bounds__(256) assign_kernel(AssignArgs a, LevelBase lb)
 __global__ void zero_counts_kernel(const uint32_t* __restrict__ key_count, uint32_t key_cap, uint32_t* __restrict__ counts,
                                    uint32_t* __restrict__ offsets, uint32_t* __restrict__ total)
 {
+    pdl_enter();
     uint32_t U = *key_count;
     if (U > key_cap) U = key_cap;
     for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < U; c += gridDim.x * blockDim.x) {
@@ -247,12 +255,12 @@ template <bool WRITE, bool SPHERES>
 static void launch_assign(cudaStream_t st, uint32_t lc, dim3 grid, dim3 block, const AssignArgs& a, const LevelBase& lb)
 {
     switch (lc) {
-    case 1: assign_kernel<1, WRITE, SPHERES><<<grid, block, 0, st>>>(a, lb); break;
-    case 2: assign_kernel<2, WRITE, SPHERES><<<grid, block, 0, st>>>(a, lb); break;
-    case 3: assign_kernel<3, WRITE, SPHERES><<<grid, block, 0, st>>>(a, lb); break;
-    case 4: assign_kernel<4, WRITE, SPHERES><<<grid, block, 0, st>>>(a, lb); break;
-    case 5: assign_kernel<5, WRITE, SPHERES><<<grid, block, 0, st>>>(a, lb); break;
-    default: assign_kernel<6, WRITE, SPHERES><<<grid, block, 0, st>>>(a, lb); break;
+    case 1: launch_kernel(assign_kernel<1, WRITE, SPHERES>, grid, block, 0, st, a, lb); break;
+    case 2: launch_kernel(assign_kernel<2, WRITE, SPHERES>, grid, block, 0, st, a, lb); break;
+    case 3: launch_kernel(assign_kernel<3, WRITE, SPHERES>, grid, block, 0, st, a, lb); break;
+    case 4: launch_kernel(assign_kernel<4, WRITE, SPHERES>, grid, block, 0, st, a, lb); break;
+    case 5: launch_kernel(assign_kernel<5, WRITE, SPHERES>, grid, block, 0, st, a, lb); break;
+    default: launch_kernel(assign_kernel<6, WRITE, SPHERES>, grid, block, 0, st, a, lb); break;
     }
 }
 
@@ -262,7 +270,7 @@ static int assign_lights(cudaStream_t st, const uint32_t* keys, const uint32_t* 
                          uint32_t* indices, uint32_t index_cap, uint32_t* total, void* scratch, uint32_t warps_per_cta)
 {
     if (L == 0) {
-        zero_counts_kernel<<<256, 256, 0, st>>>(key_count, key_cap, counts, offsets, total);
+        launch_kernel(zero_counts_kernel, 256, 256, 0, st, key_count, key_cap, counts, offsets, total);
         VREN_LAUNCH_CHECK();
         return VREN_OK;
     }
@@ -554,6 +562,7 @@ size_t align256(size_t x) { return (x + 255) / 256 * 256; }
 int cs_enqueue(vren_cluster_and_shade* cs, cudaStream_t st, uint32_t W, uint32_t H, const float* depth,
                const float* normals, const float* positions, const float* lights, uint32_t L)
 {
+    const PdlScope pdl(1);  // consecutive kernels of the frame overlap their launches
     int rc = VREN_OK;
     if (L > 0) {
         rc = construct_light_bvh(st, positions, lights, L, cs->frame, cs->opt.morton_bits, cs->opt.sort_digit_bits,

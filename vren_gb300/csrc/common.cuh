@@ -27,6 +27,49 @@ constexpr uint32_t kDefaultWaitLimit = 1u << 21;
 inline cudaStream_t as_stream(vren_stream_t s) { return reinterpret_cast<cudaStream_t>(s); }
 
 // ------------------------------------------------------------------------------------------------
+// Programmatic dependent launch.  Inside the per-frame and batched clustering sequences every kernel
+// is launched with programmatic stream serialisation, so the next kernel's launch overlaps this one.
+// Each such kernel starts with pdl_enter(): griddepcontrol.wait blocks until the preceding grid has
+// completed and its memory is visible (so nothing is read or written early), then
+// launch_dependents lets the following grid be scheduled.  Launched without the attribute, both
+// instructions do nothing.
+// ------------------------------------------------------------------------------------------------
+__device__ __forceinline__ void pdl_enter()
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// Non-zero while a clustering sequence is being enqueued on this host thread (capi.cu).
+extern thread_local int g_pdl;
+
+struct PdlScope {
+    int prev;
+    explicit PdlScope(int on) : prev(g_pdl) { g_pdl = on; }
+    ~PdlScope() { g_pdl = prev; }
+};
+
+// kernel<<<grid, block, smem, st>>>(args...), with programmatic stream serialisation when g_pdl is set.
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_kernel(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                                 Args&&... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    if (g_pdl) {
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+    }
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<Args&&>(args)...);
+}
+
+// ------------------------------------------------------------------------------------------------
 // Device error word.  Each translation unit owns one (no relocatable device code is used);
 // VREN_DEFINE_ERROR_WORD(tag) defines it and a host accessor vren_internal_error_<tag>().
 // ------------------------------------------------------------------------------------------------

@@ -64,6 +64,7 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_hist_kernel(
     const uint32_t* __restrict__ keys, uint32_t n, PassInfo passes, uint32_t* __restrict__ scratch,
     uint32_t status_words)
 {
+    pdl_enter();
     __shared__ uint32_t s_hist[kMaxPasses * RADIX];
     const uint32_t tid = threadIdx.x;
     for (uint32_t i = tid; i < passes.count * RADIX; i += kSortThreads) s_hist[i] = 0u;
@@ -329,6 +330,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) onesweep_pass_kernel(
     uint32_t n, uint32_t pass, uint32_t shift, uint32_t width, uint32_t num_tiles,
     uint32_t* __restrict__ scratch, uint32_t wait_limit, uint32_t spin)
 {
+    pdl_enter();
     constexpr int TILE = kSortThreads * ITEMS;
     extern __shared__ uint4 s_stage[];
     __shared__ PassSmem<DIGIT_BITS, ITEMS, MODE, RANK> sm;
@@ -403,7 +405,8 @@ static int launch_pass(cudaStream_t st, const uint32_t* sk, const uint32_t* sv, 
     constexpr size_t smem = (size_t)kSortThreads * ITEMS * (elem + (MODE == kPairs ? 4 : 0));
     auto kern = onesweep_pass_kernel<DB, ITEMS, MODE, RANK>;
     VREN_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<tiles, kSortThreads, smem, st>>>(sk, sv, ok, ov, n, p, shift, width, tiles, scratch, g_wait_limit, spin);
+    VREN_CUDA_TRY(launch_kernel(kern, tiles, kSortThreads, smem, st, sk, sv, ok, ov, n, p, shift, width, tiles, scratch,
+                                g_wait_limit, spin));
     VREN_LAUNCH_CHECK();
     return VREN_OK;
 }
@@ -423,7 +426,7 @@ static int run_passes(cudaStream_t st, const uint32_t* src_k, const uint32_t* sr
     uint32_t hist_grid = (n / 4 + kSortThreads - 1) / kSortThreads;
     if (hist_grid > (uint32_t)kNumSMsHint * 4) hist_grid = kNumSMsHint * 4;
     if (hist_grid == 0) hist_grid = 1;
-    onesweep_hist_kernel<RADIX, MODE><<<hist_grid, kSortThreads, 0, st>>>(src_k, n, passes, scratch, tiles * RADIX);
+    launch_kernel(onesweep_hist_kernel<RADIX, MODE>, hist_grid, kSortThreads, 0, st, src_k, n, passes, scratch, tiles * RADIX);
     VREN_LAUNCH_CHECK();
 
     const uint32_t P = passes.count;

@@ -87,6 +87,7 @@ __global__ void __launch_bounds__(kScanThreads) exclusive_scan_kernel(
     uint32_t* __restrict__ scratch, uint32_t wait_limit, uint32_t spin, const uint32_t* __restrict__ n_dev,
     uint32_t* __restrict__ total_out)
 {
+    pdl_enter();
     constexpr int kSlices = SLICES;
     constexpr uint32_t kTile = SLICES * 128u * (kScanThreads / 32);
     __shared__ uint32_t s_tile;
@@ -286,10 +287,10 @@ static int scan_launch(cudaStream_t st, const uint32_t* in, uint32_t* out, uint3
     const uint32_t spin = (uint32_t)tuning(VREN_TUNE_SPIN_POLLS);
     uint32_t* sc = static_cast<uint32_t*>(scratch);
     if (slices == 8)
-        exclusive_scan_kernel<8><<<(uint32_t)total, kScanThreads, 0, st>>>(
+        launch_kernel(exclusive_scan_kernel<8>, (uint32_t)total, kScanThreads, 0, st, 
             in, out, n, tiles_per_seg ? tiles_per_seg : 1, (uint32_t)total, sc, g_wait_limit, spin, n_dev, total_out);
     else
-        exclusive_scan_kernel<4><<<(uint32_t)total, kScanThreads, 0, st>>>(
+        launch_kernel(exclusive_scan_kernel<4>, (uint32_t)total, kScanThreads, 0, st, 
             in, out, n, tiles_per_seg ? tiles_per_seg : 1, (uint32_t)total, sc, g_wait_limit, spin, n_dev, total_out);
     VREN_LAUNCH_CHECK();
     return VREN_OK;
@@ -394,7 +395,7 @@ extern "C" int vren_exclusive_scan_u32_noalloc(vren_stream_t s, uint32_t* data, 
     if (rc != VREN_OK) return rc;
     cudaStream_t st = as_stream(s);
     VREN_CUDA_TRY(cudaMemsetAsync(scratch, 0, (kScanHeaderWords + 2u * total) * sizeof(uint32_t), st));
-    exclusive_scan_kernel<4><<<total, kScanThreads, 0, st>>>(data, data, n, tiles_per_seg, total, scratch, g_wait_limit,
+    launch_kernel(exclusive_scan_kernel<4>, total, kScanThreads, 0, st, data, data, n, tiles_per_seg, total, scratch, g_wait_limit,
                                                              (uint32_t)tuning(VREN_TUNE_SPIN_POLLS), nullptr, nullptr);
     VREN_LAUNCH_CHECK();
     return VREN_OK;
