@@ -125,13 +125,168 @@ __global__ void lbvh_morton_kernel(const float4* __restrict__ view_pos, uint32_t
         pairs[i] = make_uint2(morton_code(view_pos[i], mn, mx, bits), i);
 }
 
+// Leaves and the two levels above them; with `done` (32768 <= P <= 2^20) the last CTA to finish also
+// builds the one or two levels up to the root.
 __global__ void __launch_bounds__(1024) lbvh_leaves_kernel(
     const uint2* __restrict__ light_index, const float4* __restrict__ view_pos, const float4* __restrict__ lights,
-    uint32_t L, uint32_t P, vren_bvh_node* __restrict__ bvh, float4* __restrict__ spheres)
+    uint32_t L, uint32_t P, vren_bvh_node* __restrict__ bvh, float4* __restrict__ spheres, uint32_t* __restrict__ done)
 {
     pdl_enter();
     __shared__ NodeF s_parent[32];
+    __shared__ bool s_last;
     light_leaves_block(blockIdx.x, blockDim.x, L, P, light_index, view_pos, lights, bvh, spheres, s_parent);
+    if (!done) return;
+    __syncthreads();
+    if (threadIdx.x == 0) {  // thread 0 wrote this CTA's level-2 node
+        __threadfence();
+        s_last = atomicAdd(done, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    const uint32_t src = P + P / 32u, count = P / 1024u;  // 32 or 1024 nodes
+    bvh_levels_block(bvh, 0, src, count, src + count, src + count + count / 32u, count >= 1024u, s_parent);
+    if (threadIdx.x == 0) *done = 0u;
+}
+
+// construct_point_light_bvh for L <= 16384 lights with 15-bit codes in one CTA: view transform and
+// min/max, Morton codes, and the stable sort by code as two 8-bit LSD passes over (code << 16 | index)
+// in shared memory (per-warp ballot ranking and digit counters, as in the multi-CTA onesweep passes;
+// warp w takes a contiguous run of indices, so equal codes keep index order).  Writes view_pos and
+// light_index exactly as the multi-kernel path does.
+constexpr uint32_t kSmallLights = 16384;
+constexpr int kSmallThreads = 1024;
+constexpr size_t kSmallSmem = (2 * kSmallLights + 32 * 256) * sizeof(uint32_t);
+
+__global__ void __launch_bounds__(kSmallThreads) lbvh_small_kernel(const float4* __restrict__ positions, uint32_t L,
+                                                                   const vren_cs_frame* __restrict__ F,
+                                                                   float4* __restrict__ view_pos,
+                                                                   uint2* __restrict__ light_index)
+{
+    pdl_enter();
+    extern __shared__ uint32_t s_dyn[];
+    uint32_t* A = s_dyn;                // keys (code << 16 | index), sorted result after two passes
+    uint32_t* B = A + kSmallLights;     // pass temporary
+    uint32_t* cnt = B + kSmallLights;   // [32 warps][256 digits]: counts, then scatter offsets
+    __shared__ uint32_t s_mm[32][6];
+    __shared__ uint32_t s_bound[6];
+    __shared__ uint32_t s_wsum[32];
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+
+    // view positions and their min/max (order-preserving keys)
+    const float* V = F->view.view;
+    uint32_t kmin[3] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu}, kmax[3] = {0u, 0u, 0u};
+    for (uint32_t i = tid; i < L; i += kSmallThreads) {
+        const float4 v = light_to_view(V, positions[i]);
+        view_pos[i] = v;
+        const float c[3] = {v.x, v.y, v.z};
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const uint32_t key = fkey(c[a]);
+            kmin[a] = key < kmin[a] ? key : kmin[a];
+            kmax[a] = key > kmax[a] ? key : kmax[a];
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        kmin[a] = __reduce_min_sync(0xFFFFFFFFu, kmin[a]);
+        kmax[a] = __reduce_max_sync(0xFFFFFFFFu, kmax[a]);
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            s_mm[warp][a] = kmin[a];
+            s_mm[warp][3 + a] = kmax[a];
+        }
+    }
+    __syncthreads();
+    if (tid < 6) {
+        uint32_t v = tid < 3 ? 0xFFFFFFFFu : 0u;
+        for (int w = 0; w < 32; ++w) {
+            const uint32_t x = s_mm[w][tid];
+            v = tid < 3 ? (x < v ? x : v) : (x > v ? x : v);
+        }
+        s_bound[tid] = v;
+    }
+    __syncthreads();
+    float mn[3], mx[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        mn[a] = unkey(s_bound[a]);
+        mx[a] = unkey(s_bound[3 + a]);
+    }
+    // Morton codes (each thread reads back the view positions it wrote)
+    for (uint32_t i = tid; i < L; i += kSmallThreads) A[i] = (morton_code(view_pos[i], mn, mx, 5u) << 16) | i;
+
+    // two stable 8-bit passes over bits 16..31
+    const uint32_t items = (L + kSmallThreads - 1) / kSmallThreads;  // <= 16
+    const uint32_t chunk = items * 32u;                               // indices per warp
+    for (uint32_t pass = 0; pass < 2; ++pass) {
+        const uint32_t* src = pass ? B : A;
+        uint32_t* dst = pass ? A : B;
+        const uint32_t shift = 16u + 8u * pass;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) cnt[tid * 8 + k] = 0u;
+        __syncthreads();
+        uint32_t rank[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            const uint32_t idx = warp * chunk + (uint32_t)j * 32u + lane;
+            const bool valid = (uint32_t)j < items && idx < L;
+            const uint32_t d = valid ? (src[idx] >> shift) & 0xFFu : 0u;
+            uint32_t peers = __ballot_sync(0xFFFFFFFFu, valid);
+#pragma unroll
+            for (int b = 0; b < 8; ++b) {
+                const uint32_t m = __ballot_sync(0xFFFFFFFFu, (d >> b) & 1u);
+                const uint32_t mine = (uint32_t)((int32_t)(d << (31 - b)) >> 31);
+                peers &= ~(m ^ mine);
+            }
+            const uint32_t below = peers & lanemask_lt();
+            const uint32_t before = valid ? cnt[warp * 256u + d] : 0u;
+            __syncwarp();
+            if (valid && below == 0) cnt[warp * 256u + d] = before + __popc(peers);
+            __syncwarp();
+            rank[j] = valid ? before + __popc(below) : 0xFFFFFFFFu;
+        }
+        __syncthreads();
+        // exclusive scan of the counts in (digit, warp) order: entry f = 8 tid + k is (d = f / 32, w = f % 32)
+        uint32_t c8[8], sum = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const uint32_t f = tid * 8u + (uint32_t)k;
+            c8[k] = cnt[(f & 31u) * 256u + (f >> 5)];
+            sum += c8[k];
+        }
+        uint32_t incl = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= (uint32_t)o) incl += y;
+        }
+        if (lane == 31) s_wsum[warp] = incl;
+        __syncthreads();
+        uint32_t base = incl - sum;
+        for (uint32_t w = 0; w < warp; ++w) base += s_wsum[w];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const uint32_t f = tid * 8u + (uint32_t)k;
+            cnt[(f & 31u) * 256u + (f >> 5)] = base;
+            base += c8[k];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            if (rank[j] != 0xFFFFFFFFu) {
+                const uint32_t k = src[warp * chunk + (uint32_t)j * 32u + lane];
+                dst[cnt[warp * 256u + ((k >> shift) & 0xFFu)] + rank[j]] = k;
+            }
+        }
+        __syncthreads();
+    }
+    for (uint32_t i = tid; i < L; i += kSmallThreads) {
+        const uint32_t k = A[i];
+        light_index[i] = make_uint2(k >> 16, k & 0xFFFFu);
+    }
 }
 
 static int construct_light_bvh(cudaStream_t st, const float* positions, const float* lights, uint32_t L,
@@ -142,30 +297,42 @@ static int construct_light_bvh(cudaStream_t st, const float* positions, const fl
     const LbvhLayout lay = lbvh_layout(L, morton_bits, digit_bits);
     char* sc = static_cast<char*>(scratch);
     uint32_t* hdr = reinterpret_cast<uint32_t*>(sc);
-    uint2* pairs = reinterpret_cast<uint2*>(sc + lay.pairs);
-    uint32_t* tmp = reinterpret_cast<uint32_t*>(sc + lay.tmp);
-    const uint32_t grid = (L + kLbvhPerCta - 1) / kLbvhPerCta;
-
-    launch_kernel(lbvh_transform_kernel, grid, kLbvhThreads, 0, st, reinterpret_cast<const float4*>(positions), L, frame,
-                                                         reinterpret_cast<float4*>(view_pos), hdr);
-    VREN_LAUNCH_CHECK();
-    const uint32_t bits = morton_bits == 30 ? 10u : 5u;
-    uint32_t mgrid = (L + 255) / 256;
-    if (mgrid > 1024) mgrid = 1024;
-    launch_kernel(lbvh_morton_kernel, mgrid, 256, 0, st, reinterpret_cast<const float4*>(view_pos), L, hdr, bits, pairs);
-    VREN_LAUNCH_CHECK();
-    // bucket sort on the low 16 bits (bucket_sort.hpp:15-16); the 30-bit extension sorts 30 bits
-    int rc = sort_uvec2(st, reinterpret_cast<const uint32_t*>(pairs), light_index, tmp, L, morton_bits == 30 ? 30 : 16,
-                        digit_bits, sc + lay.sort);
-    if (rc != VREN_OK) return rc;
-
+    if (morton_bits != 30 && L <= kSmallLights) {
+        static bool attr_set = false;  // the attribute is per function, set once
+        if (!attr_set) {
+            VREN_CUDA_TRY(cudaFuncSetAttribute(lbvh_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)kSmallSmem));
+            attr_set = true;
+        }
+        launch_kernel(lbvh_small_kernel, 1, kSmallThreads, kSmallSmem, st, reinterpret_cast<const float4*>(positions),
+                      L, frame, reinterpret_cast<float4*>(view_pos), reinterpret_cast<uint2*>(light_index));
+        VREN_LAUNCH_CHECK();
+    } else {
+        uint2* pairs = reinterpret_cast<uint2*>(sc + lay.pairs);
+        uint32_t* tmp = reinterpret_cast<uint32_t*>(sc + lay.tmp);
+        const uint32_t grid = (L + kLbvhPerCta - 1) / kLbvhPerCta;
+        launch_kernel(lbvh_transform_kernel, grid, kLbvhThreads, 0, st, reinterpret_cast<const float4*>(positions), L,
+                      frame, reinterpret_cast<float4*>(view_pos), hdr);
+        VREN_LAUNCH_CHECK();
+        const uint32_t bits = morton_bits == 30 ? 10u : 5u;
+        uint32_t mgrid = (L + 255) / 256;
+        if (mgrid > 1024) mgrid = 1024;
+        launch_kernel(lbvh_morton_kernel, mgrid, 256, 0, st, reinterpret_cast<const float4*>(view_pos), L, hdr, bits,
+                      pairs);
+        VREN_LAUNCH_CHECK();
+        // bucket sort on the low 16 bits (bucket_sort.hpp:15-16); the 30-bit extension sorts 30 bits
+        int rc = sort_uvec2(st, reinterpret_cast<const uint32_t*>(pairs), light_index, tmp, L,
+                            morton_bits == 30 ? 30 : 16, digit_bits, sc + lay.sort);
+        if (rc != VREN_OK) return rc;
+    }
     const uint32_t P = vren_calc_bvh_padded_leaf_count(L);
     const uint32_t threads = P < 1024 ? P : 1024;
-    launch_kernel(lbvh_leaves_kernel, P / threads, threads, 0, st, 
-        reinterpret_cast<const uint2*>(light_index), reinterpret_cast<const float4*>(view_pos),
-        reinterpret_cast<const float4*>(lights), L, P, bvh, reinterpret_cast<float4*>(spheres));
+    uint32_t* done = (P >= 32768u && P <= (1u << 20)) ? hdr + 1 : nullptr;
+    launch_kernel(lbvh_leaves_kernel, P / threads, threads, 0, st, reinterpret_cast<const uint2*>(light_index),
+                  reinterpret_cast<const float4*>(view_pos), reinterpret_cast<const float4*>(lights), L, P, bvh,
+                  reinterpret_cast<float4*>(spheres), done);
     VREN_LAUNCH_CHECK();
-    if (P >= 32768) return build_bvh_levels(st, bvh, P + P / 32u, P / 1024u);
+    if (P > (1u << 20)) return build_bvh_levels(st, bvh, P + P / 32u, P / 1024u);
     return VREN_OK;
 }
 
