@@ -61,7 +61,7 @@ def run_light_bvh(device, pos, li, L, view, W, H, morton_bits=15):
     return frame, vp, bvh, lidx, sph
 
 
-@pytest.mark.parametrize("L", [1, 5, 31, 32, 33, 1000, 1024, 1025, 16384, 40000])
+@pytest.mark.parametrize("L", [1, 5, 31, 32, 33, 1000, 1024, 1025, 2048, 2049, 16384, 40000])
 @pytest.mark.parametrize("morton_bits", [15, 30])
 def test_construct_light_bvh(cuda, L, morton_bits):
     W, H = 1920, 1080
@@ -81,11 +81,12 @@ def test_construct_light_bvh(cuda, L, morton_bits):
     assert np.all(s[L:, 3] == -1)
 
 
-def test_construct_light_bvh_duplicate_positions(cuda):
-    """Equal Morton codes (and a zero extent) exercise the stable tie order and the NaN path."""
+@pytest.mark.parametrize("L", [2000, 3000])
+def test_construct_light_bvh_duplicate_positions(cuda, L):
+    """Equal Morton codes (and a zero extent) exercise the stable tie order and the NaN path, in the
+    one-CTA path (2000 lights) and the multi-CTA one (3000)."""
     W, H = 640, 360
     view = make_view(W, H)
-    L = 3000
     pos = np.tile(np.array([1.0, 2.0, 30.0, 1.0], np.float32), L)
     pos[4 * 7: 4 * 7 + 3] = [5.0, -1.0, 60.0]
     li = np.tile(np.array([0.5, 0.5, 0.5, 2.0], np.float32), L)

@@ -149,12 +149,14 @@ __global__ void __launch_bounds__(1024) lbvh_leaves_kernel(
     if (threadIdx.x == 0) *done = 0u;
 }
 
-// construct_point_light_bvh for L <= 16384 lights with 15-bit codes in one CTA: view transform and
+// construct_point_light_bvh for few lights (up to kSmallPathLights, where the launches of the multi-CTA
+// path cost more than its work) with 15-bit codes in one CTA: view transform and
 // min/max, Morton codes, and the stable sort by code as two 8-bit LSD passes over (code << 16 | index)
 // in shared memory (per-warp ballot ranking and digit counters, as in the multi-CTA onesweep passes;
 // warp w takes a contiguous run of indices, so equal codes keep index order).  Writes view_pos and
 // light_index exactly as the multi-kernel path does.
-constexpr uint32_t kSmallLights = 16384;
+constexpr uint32_t kSmallLights = 16384;      // capacity of the kernel's shared-memory arrays
+constexpr uint32_t kSmallPathLights = 2048;   // measured: at 16384 lights the multi-CTA path is faster
 constexpr int kSmallThreads = 1024;
 constexpr size_t kSmallSmem = (2 * kSmallLights + 32 * 256) * sizeof(uint32_t);
 
@@ -297,7 +299,7 @@ static int construct_light_bvh(cudaStream_t st, const float* positions, const fl
     const LbvhLayout lay = lbvh_layout(L, morton_bits, digit_bits);
     char* sc = static_cast<char*>(scratch);
     uint32_t* hdr = reinterpret_cast<uint32_t*>(sc);
-    if (morton_bits != 30 && L <= kSmallLights) {
+    if (morton_bits != 30 && L <= kSmallPathLights) {
         static bool attr_set = false;  // the attribute is per function, set once
         if (!attr_set) {
             VREN_CUDA_TRY(cudaFuncSetAttribute(lbvh_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
