@@ -208,7 +208,9 @@ def run_ours(args, rank: int, world: int):
     fuc_bytes = BYTES_PER_PX * W * H
     fuc_gbs = fuc_bytes / (fuc_ms * 1e-3) / 1e9
 
-    # end to end through the public API from pinned host buffers
+    # end to end through the public API from pinned host buffers: vren_cs_cluster_host uploads the
+    # G-buffer and lights (the light BVH built while the G-buffer uploads) and downloads the cluster
+    # references during the light assignment; the light lists follow once their lengths are known.
     h_depth = torch.from_numpy(depth).pin_memory()
     h_norm = torch.from_numpy(normals).pin_memory()
     h_pos = torch.from_numpy(pos).pin_memory()
@@ -234,14 +236,9 @@ def run_ours(args, rank: int, world: int):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         with torch.cuda.stream(stream):
-            d_depth.copy_(h_depth, non_blocking=True)
-            d_norm.copy_(h_norm, non_blocking=True)
-            d_pos.copy_(h_pos, non_blocking=True)
-            d_light.copy_(h_light, non_blocking=True)
-            frame()
+            ctx.cluster_host(stream, view, W, H, h_depth, h_norm, h_pos, h_light, L, h_refs)
             d2h(h_small.data_ptr(), out.key_count, 4)
             d2h(h_small.data_ptr() + 4, out.total, 4)
-            d2h(h_refs.data_ptr(), out.cluster_refs, W * H * 4)
             stream.synchronize()
             u, tot = int(h_small[0]), int(h_small[1])
             base = h_lists.data_ptr()
@@ -254,6 +251,7 @@ def run_ours(args, rank: int, world: int):
             e2e_ms.append((time.perf_counter() - t0) * 1e3)
             d2h_total = 8 + W * H * 4 + u * 12 + tot * 4
     e2e = sum(e2e_ms) / len(e2e_ms)
+    e2e_refs_ok = bool(np.array_equal(h_refs.numpy(), cs.read_device(out.cluster_refs, W * H).view(np.int32)))
 
     # radix sort: 2^20 key/value pairs (config 1), plus sizes beyond L2
     radix = radix_bench(args, dev, stream, flush, radix_keys, hbm_peak)
@@ -296,7 +294,10 @@ def run_ours(args, rank: int, world: int):
                 "parallelism": f"replicas x{world} (frames are independent)",
             },
             "e2e": {"value": round(e2e, 4), "unit": "ms", "h2d_bytes_per_step": h2d_bytes,
-                    "d2h_bytes_per_step": d2h_total},
+                    "d2h_bytes_per_step": d2h_total,
+                    "path": "vren_cs_cluster_host from pinned buffers (uploads overlap the light BVH, reference "
+                            "download overlaps the assignment), then the light lists; host wall clock",
+                    "refs_match_device": e2e_refs_ok},
             "gpu_launches": launches_per_frame * args.steps,
             "roofline": {"bound": "hbm", "kernel": "find_unique_kernel", "achieved": round(fuc_gbs, 1),
                          "peak": hbm_peak, "unit": "GB/s", "frac": round(fuc_gbs / hbm_peak, 4),

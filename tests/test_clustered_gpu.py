@@ -338,3 +338,35 @@ def test_cluster_and_shade_context(cuda, use_graph):
             ctx.cluster(stream, view, W, H, *bufs, L)
         stream.synchronize()
         check_context_outputs(ctx, W, H, view, depth, normals, pos, li, L)
+
+
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_cluster_host_matches_device_path(cuda, use_graph):
+    """vren_cs_cluster_host (page-locked host inputs, overlapped uploads and reference download) gives
+    the same outputs as vren_cs_cluster on the same data."""
+    W, H, L = 640, 360, 3000
+    view = make_view(W, H)
+    depth, normals = scene.depth_planes(41, W, H)
+    pos, li = dense_lights(42, L)
+    stream = torch.cuda.Stream(device=cuda)
+    a = cs.cluster_and_shade(W, H, L, 1 << 22, use_graph=use_graph)
+    b = cs.cluster_and_shade(W, H, L, 1 << 22, use_graph=use_graph)
+    with torch.cuda.stream(stream):
+        a.cluster(stream, view, W, H, to_dev(depth, cuda), to_dev(normals, cuda), to_dev(pos, cuda), to_dev(li, cuda),
+                  L)
+    stream.synchronize()
+    hp = lambda x: torch.from_numpy(np.ascontiguousarray(x)).pin_memory()
+    h_refs = torch.zeros(W * H, dtype=torch.int32).pin_memory()
+    for _ in range(2):  # second call replays the captured graph
+        h_refs.zero_()
+        with torch.cuda.stream(stream):
+            b.cluster_host(stream, view, W, H, hp(depth), hp(normals), hp(pos), hp(li), L, h_refs)
+        stream.synchronize()
+        oa, ob = a.outputs(), b.outputs()
+        U = int(cs.read_device(oa.key_count, 1)[0])
+        tot = int(cs.read_device(oa.total, 1)[0])
+        assert U > 0 and tot > 0
+        assert int(cs.read_device(ob.key_count, 1)[0]) == U and int(cs.read_device(ob.total, 1)[0]) == tot
+        for name, n in (("cluster_keys", U), ("counts", U), ("offsets", U), ("indices", tot), ("cluster_refs", W * H)):
+            assert np.array_equal(cs.read_device(getattr(oa, name), n), cs.read_device(getattr(ob, name), n)), name
+        assert np.array_equal(h_refs.numpy().view(np.uint32), cs.read_device(oa.cluster_refs, W * H))

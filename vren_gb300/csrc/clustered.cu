@@ -723,6 +723,17 @@ struct vren_cluster_and_shade {
         cudaStream_t stream;
         vren_cs_options opt;
     } graph_key{};
+    // vren_cs_cluster_host: device copies of the host inputs, a second stream with its events, and
+    // the graph of the last host-input frame shape
+    char* inputs = nullptr;
+    float *in_depth = nullptr, *in_normals = nullptr, *in_pos = nullptr, *in_lights = nullptr;
+    cudaStream_t aux = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_bvh = nullptr, ev_fuc = nullptr, ev_join = nullptr;
+    cudaGraphExec_t host_graph = nullptr;
+    struct HostKey {
+        Key k;
+        void* refs_out;
+    } host_key{};
 };
 
 namespace {
@@ -822,6 +833,11 @@ extern "C" void vren_cs_destroy(vren_cluster_and_shade* cs)
 {
     if (!cs) return;
     if (cs->graph) cudaGraphExecDestroy(cs->graph);
+    if (cs->host_graph) cudaGraphExecDestroy(cs->host_graph);
+    if (cs->aux) cudaStreamDestroy(cs->aux);
+    for (cudaEvent_t e : {cs->ev_fork, cs->ev_bvh, cs->ev_fuc, cs->ev_join})
+        if (e) cudaEventDestroy(e);
+    cudaFree(cs->inputs);
     cudaFree(cs->arena);
     cudaFreeHost(cs->host_frame);
     delete cs;
@@ -838,19 +854,19 @@ extern "C" int vren_cs_set_options(vren_cluster_and_shade* cs, const vren_cs_opt
         cudaGraphExecDestroy(cs->graph);
         cs->graph = nullptr;
     }
+    if (cs->host_graph) {
+        cudaGraphExecDestroy(cs->host_graph);
+        cs->host_graph = nullptr;
+    }
     return VREN_OK;
 }
 
-extern "C" int vren_cs_cluster(vren_cluster_and_shade* cs, vren_stream_t s, const vren_cs_view* view, uint32_t width,
-                               uint32_t height, int offscreen, const float* depth, const float* normals,
-                               const float* light_positions, const float* point_lights, uint32_t light_count)
+namespace {
+// The frame block lives in device memory and is read by every kernel; it is re-uploaded (from pinned
+// memory, outside any captured graph) only when the camera or the frame shape changes.
+int refresh_frame(vren_cluster_and_shade* cs, cudaStream_t st, const vren_cs_view* view, uint32_t width,
+                  uint32_t height, int offscreen)
 {
-    if (!cs || !view || !depth || !normals) return VREN_ERR_ARG;
-    if (width > cs->max_w || height > cs->max_h || light_count > cs->max_lights) return VREN_ERR_CAPACITY;
-    if (light_count > 0 && (!light_positions || !point_lights)) return VREN_ERR_ARG;
-    cudaStream_t st = as_stream(s);
-    // The frame block lives in device memory and is read by every kernel; it is re-uploaded (from
-    // pinned memory, outside the captured graph) only when the camera or the frame shape changes.
     static thread_local vren_cs_frame fresh;
     int rc = vren_cs_frame_build(view, width, height, offscreen, &fresh);
     if (rc != VREN_OK) return rc;
@@ -860,6 +876,60 @@ extern "C" int vren_cs_cluster(vren_cluster_and_shade* cs, vren_stream_t s, cons
         VREN_CUDA_TRY(cudaMemcpyAsync(cs->frame, cs->host_frame, sizeof(vren_cs_frame), cudaMemcpyHostToDevice, st));
         cs->frame_valid = true;
     }
+    return VREN_OK;
+}
+
+// One frame from host buffers: the lights go up and their BVH is built on the second stream while the
+// depth and normals go up on `st`; the unique clusters run when those arrive, then the references go
+// down on the second stream while the light lists are assigned on `st`.
+int cs_enqueue_host(vren_cluster_and_shade* cs, cudaStream_t st, uint32_t W, uint32_t H, const float* depth,
+                    const float* normals, const float* positions, const float* lights, uint32_t L, uint32_t* refs_out)
+{
+    const PdlScope pdl(1);
+    cudaStream_t aux = cs->aux;
+    VREN_CUDA_TRY(cudaEventRecord(cs->ev_fork, st));
+    VREN_CUDA_TRY(cudaStreamWaitEvent(aux, cs->ev_fork, 0));
+    int rc = VREN_OK;
+    if (L > 0) {
+        VREN_CUDA_TRY(cudaMemcpyAsync(cs->in_pos, positions, (size_t)L * 16, cudaMemcpyHostToDevice, aux));
+        VREN_CUDA_TRY(cudaMemcpyAsync(cs->in_lights, lights, (size_t)L * 16, cudaMemcpyHostToDevice, aux));
+        rc = construct_light_bvh(aux, cs->in_pos, cs->in_lights, L, cs->frame, cs->opt.morton_bits,
+                                 cs->opt.sort_digit_bits, cs->view_pos, cs->bvh, cs->light_index, cs->spheres,
+                                 cs->lbvh_scratch);
+        if (rc != VREN_OK) return rc;
+    }
+    VREN_CUDA_TRY(cudaEventRecord(cs->ev_bvh, aux));
+    VREN_CUDA_TRY(cudaMemcpyAsync(cs->in_depth, depth, (size_t)W * H * 4, cudaMemcpyHostToDevice, st));
+    VREN_CUDA_TRY(cudaMemcpyAsync(cs->in_normals, normals, (size_t)W * H * 12, cudaMemcpyHostToDevice, st));
+    rc = launch_find_unique(st, cs->in_depth, cs->in_normals, W, H, cs->frame, cs->keys, cs->key_cap, cs->key_count,
+                            cs->refs, static_cast<uint32_t*>(cs->fuc_scratch));
+    if (rc != VREN_OK) return rc;
+    if (refs_out) {
+        VREN_CUDA_TRY(cudaEventRecord(cs->ev_fuc, st));
+        VREN_CUDA_TRY(cudaStreamWaitEvent(aux, cs->ev_fuc, 0));
+        VREN_CUDA_TRY(cudaMemcpyAsync(refs_out, cs->refs, (size_t)W * H * 4, cudaMemcpyDeviceToHost, aux));
+    }
+    VREN_CUDA_TRY(cudaStreamWaitEvent(st, cs->ev_bvh, 0));
+    rc = assign_lights(st, cs->keys, cs->key_count, cs->key_cap, cs->frame, cs->bvh, L, cs->light_index,
+                       cs->view_pos, cs->spheres, cs->counts, cs->offsets, cs->indices, cs->max_assign, cs->total,
+                       cs->assign_scratch, cs->opt.assign_warps);
+    if (rc != VREN_OK) return rc;
+    VREN_CUDA_TRY(cudaEventRecord(cs->ev_join, aux));
+    VREN_CUDA_TRY(cudaStreamWaitEvent(st, cs->ev_join, 0));
+    return VREN_OK;
+}
+}  // namespace
+
+extern "C" int vren_cs_cluster(vren_cluster_and_shade* cs, vren_stream_t s, const vren_cs_view* view, uint32_t width,
+                               uint32_t height, int offscreen, const float* depth, const float* normals,
+                               const float* light_positions, const float* point_lights, uint32_t light_count)
+{
+    if (!cs || !view || !depth || !normals) return VREN_ERR_ARG;
+    if (width > cs->max_w || height > cs->max_h || light_count > cs->max_lights) return VREN_ERR_CAPACITY;
+    if (light_count > 0 && (!light_positions || !point_lights)) return VREN_ERR_ARG;
+    cudaStream_t st = as_stream(s);
+    int rc = refresh_frame(cs, st, view, width, height, offscreen);
+    if (rc != VREN_OK) return rc;
     const vren_cluster_and_shade::Key key{width, height, light_count, (uint32_t)offscreen, depth, normals,
                                           light_positions, point_lights, st, cs->opt};
     const bool use_graph = cs->opt.use_graph && st != nullptr;
@@ -889,6 +959,72 @@ extern "C" int vren_cs_cluster(vren_cluster_and_shade* cs, vren_stream_t s, cons
     }
     cs->graph_key = key;
     VREN_CUDA_TRY(cudaGraphLaunch(cs->graph, st));
+    return VREN_OK;
+}
+
+extern "C" int vren_cs_cluster_host(vren_cluster_and_shade* cs, vren_stream_t s, const vren_cs_view* view,
+                                    uint32_t width, uint32_t height, int offscreen, const float* depth,
+                                    const float* normals, const float* light_positions, const float* point_lights,
+                                    uint32_t light_count, uint32_t* cluster_refs_out)
+{
+    if (!cs || !view || !depth || !normals) return VREN_ERR_ARG;
+    if (width > cs->max_w || height > cs->max_h || light_count > cs->max_lights) return VREN_ERR_CAPACITY;
+    if (light_count > 0 && (!light_positions || !point_lights)) return VREN_ERR_ARG;
+    cudaStream_t st = as_stream(s);
+    if (!cs->inputs) {  // first use: device copies of the inputs, the second stream and its events
+        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+        VREN_CUDA_TRY(cudaStreamIsCapturing(st, &cap));
+        if (cap != cudaStreamCaptureStatusNone) return VREN_ERR_STATE;
+        const size_t px = (size_t)cs->max_w * cs->max_h, Lb = cs->max_lights ? cs->max_lights : 1;
+        const size_t o_n = align256(px * 4), o_p = o_n + align256(px * 12), o_l = o_p + align256(Lb * 16);
+        const size_t bytes = o_l + align256(Lb * 16);
+        if (cudaMalloc(&cs->inputs, bytes) != cudaSuccess) {
+            cs->inputs = nullptr;
+            return VREN_ERR_CUDA;
+        }
+        cs->in_depth = reinterpret_cast<float*>(cs->inputs);
+        cs->in_normals = reinterpret_cast<float*>(cs->inputs + o_n);
+        cs->in_pos = reinterpret_cast<float*>(cs->inputs + o_p);
+        cs->in_lights = reinterpret_cast<float*>(cs->inputs + o_l);
+        VREN_CUDA_TRY(cudaStreamCreateWithFlags(&cs->aux, cudaStreamNonBlocking));
+        for (cudaEvent_t* e : {&cs->ev_fork, &cs->ev_bvh, &cs->ev_fuc, &cs->ev_join})
+            VREN_CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    }
+    int rc = refresh_frame(cs, st, view, width, height, offscreen);
+    if (rc != VREN_OK) return rc;
+    const vren_cluster_and_shade::HostKey key{{width, height, light_count, (uint32_t)offscreen, depth, normals,
+                                               light_positions, point_lights, st, cs->opt},
+                                              cluster_refs_out};
+    const bool use_graph = cs->opt.use_graph && st != nullptr;
+    if (!use_graph)
+        return cs_enqueue_host(cs, st, width, height, depth, normals, light_positions, point_lights, light_count,
+                               cluster_refs_out);
+    if (cs->host_graph && std::memcmp(&key, &cs->host_key, sizeof(key)) == 0) {
+        VREN_CUDA_TRY(cudaGraphLaunch(cs->host_graph, st));
+        return VREN_OK;
+    }
+    if (cs->host_graph) {
+        cudaGraphExecDestroy(cs->host_graph);
+        cs->host_graph = nullptr;
+    }
+    cudaGraph_t g;
+    VREN_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    rc = cs_enqueue_host(cs, st, width, height, depth, normals, light_positions, point_lights, light_count,
+                         cluster_refs_out);
+    cudaError_t e = cudaStreamEndCapture(st, &g);
+    if (rc != VREN_OK) {
+        if (e == cudaSuccess) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return VREN_ERR_CUDA;
+    e = cudaGraphInstantiate(&cs->host_graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        cs->host_graph = nullptr;
+        return VREN_ERR_CUDA;
+    }
+    cs->host_key = key;
+    VREN_CUDA_TRY(cudaGraphLaunch(cs->host_graph, st));
     return VREN_OK;
 }
 
