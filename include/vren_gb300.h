@@ -397,13 +397,16 @@ int vren_cs_get_outputs(const vren_cluster_and_shade* cs, vren_cs_outputs* out);
 /* vren_cs_cluster for a frame held in page-locked host memory (no counterpart in the reference, whose
  * G-buffer is rendered on the GPU).  The lights are uploaded and their BVH built on a second stream
  * of the context while the depth and normals upload; when cluster_refs_out (page-locked, W*H) is
- * given, the references are downloaded while the light lists are assigned.  The outputs are the same
- * as vren_cs_cluster's on the same data.  The first call allocates the context's input buffers and
- * must not be made during stream capture. */
+ * given, the references are downloaded while the light lists are assigned; when lists_out
+ * (page-locked) is given, the device writes [U, total, keys[U], counts[U], offsets[U], indices[total]]
+ * into it, cut at lists_capacity words (VREN_ERR_CAPACITY recorded).  The depth and normals upload in
+ * bands of tile rows, each band's tiles starting as soon as it arrives.  The outputs are the same as
+ * vren_cs_cluster's on the same data.  The first call allocates the context's input buffers and must
+ * not be made during stream capture. */
 int vren_cs_cluster_host(vren_cluster_and_shade* cs, vren_stream_t s, const vren_cs_view* view, uint32_t width,
                          uint32_t height, int offscreen, const float* depth, const float* normals,
                          const float* light_positions, const float* point_lights, uint32_t light_count,
-                         uint32_t* cluster_refs_out);
+                         uint32_t* cluster_refs_out, uint32_t* lists_out, uint64_t lists_capacity);
 
 /* ------------------------------------------------------------------------------------------------
  * Batched cluster assignment (no counterpart in the reference, which runs one frame per

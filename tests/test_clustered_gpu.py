@@ -357,10 +357,13 @@ def test_cluster_host_matches_device_path(cuda, use_graph):
     stream.synchronize()
     hp = lambda x: torch.from_numpy(np.ascontiguousarray(x)).pin_memory()
     h_refs = torch.zeros(W * H, dtype=torch.int32).pin_memory()
+    h_lists = torch.zeros(1 << 22, dtype=torch.int32).pin_memory()
+    ins = (hp(depth), hp(normals), hp(pos), hp(li))
     for _ in range(2):  # second call replays the captured graph
         h_refs.zero_()
+        h_lists.zero_()
         with torch.cuda.stream(stream):
-            b.cluster_host(stream, view, W, H, hp(depth), hp(normals), hp(pos), hp(li), L, h_refs)
+            b.cluster_host(stream, view, W, H, *ins, L, h_refs, h_lists)
         stream.synchronize()
         oa, ob = a.outputs(), b.outputs()
         U = int(cs.read_device(oa.key_count, 1)[0])
@@ -370,3 +373,8 @@ def test_cluster_host_matches_device_path(cuda, use_graph):
         for name, n in (("cluster_keys", U), ("counts", U), ("offsets", U), ("indices", tot), ("cluster_refs", W * H)):
             assert np.array_equal(cs.read_device(getattr(oa, name), n), cs.read_device(getattr(ob, name), n)), name
         assert np.array_equal(h_refs.numpy().view(np.uint32), cs.read_device(oa.cluster_refs, W * H))
+        hl = h_lists.numpy().view(np.uint32)
+        assert hl[0] == U and hl[1] == tot
+        for k, (name, n) in enumerate((("cluster_keys", U), ("counts", U), ("offsets", U))):
+            assert np.array_equal(hl[2 + k * U: 2 + (k + 1) * U], cs.read_device(getattr(oa, name), n)), name
+        assert np.array_equal(hl[2 + 3 * U: 2 + 3 * U + tot], cs.read_device(oa.indices, tot))

@@ -170,14 +170,18 @@ class cluster_and_shade:
 
     def cluster_host(self, stream, view: View, width: int, height: int, depth: torch.Tensor, normals: torch.Tensor,
                      positions: torch.Tensor | None, lights: torch.Tensor | None, light_count: int,
-                     refs_out: torch.Tensor | None = None, offscreen: str = "wrap"):
-        """The same frame from page-locked host tensors (uploads overlapped with the light BVH; the
-        references downloaded into refs_out while the light lists are assigned)."""
+                     refs_out: torch.Tensor | None = None, lists_out: torch.Tensor | None = None,
+                     offscreen: str = "wrap"):
+        """The same frame from page-locked host tensors (uploads overlapped with the light BVH and the
+        unique clusters; the references downloaded into refs_out while the light lists are assigned; the
+        lists written by the device into lists_out as [U, total, keys, counts, offsets, indices])."""
         check(lib().vren_cs_cluster_host(self._h, _stream(stream), C.byref(view), width, height, OFFSCREEN[offscreen],
                                          depth.data_ptr(), normals.data_ptr(),
                                          positions.data_ptr() if positions is not None else None,
                                          lights.data_ptr() if lights is not None else None, light_count,
-                                         refs_out.data_ptr() if refs_out is not None else None), "cs_cluster_host")
+                                         refs_out.data_ptr() if refs_out is not None else None,
+                                         lists_out.data_ptr() if lists_out is not None else None,
+                                         lists_out.numel() if lists_out is not None else 0), "cs_cluster_host")
 
     def outputs(self) -> Outputs:
         o = Outputs()

@@ -341,7 +341,7 @@ static int construct_light_bvh(cudaStream_t st, const float* positions, const fl
 // ================================================================================================
 // find_unique_cluster_list
 // ================================================================================================
-__global__ void __launch_bounds__(kFucThreads, 6) find_unique_kernel(FucFrame fr)
+__global__ void __launch_bounds__(kFucThreads, 6) find_unique_kernel(FucFrame fr, uint32_t tile_base)
 {
     pdl_enter();
     __shared__ FucSmem sm;
@@ -350,7 +350,7 @@ __global__ void __launch_bounds__(kFucThreads, 6) find_unique_kernel(FucFrame fr
     reinterpret_cast<uint4*>(sm.bits)[tid + kFucThreads] = make_uint4(0u, 0u, 0u, 0u);
     if (tid < 64) sm.used[tid] = 0u;
     __syncthreads();
-    find_unique_tile(fr, blockIdx.x, sm);
+    find_unique_tile(fr, tile_base + blockIdx.x, sm);
 }
 
 __global__ void __launch_bounds__(kFucScanThreads) find_unique_scan_kernel(FucFrame fr)
@@ -370,22 +370,75 @@ __global__ void __launch_bounds__(kFucThreads) find_unique_fixup_kernel(FucFrame
 // then (16-byte aligned) the tiles' key slots [T][1024].
 static size_t fuc_keys_offset_words(uint32_t T) { return (2ull * T + 3) / 4 * 4; }
 
-static int launch_find_unique(cudaStream_t st, const float* depth, const float* normals, uint32_t W, uint32_t H,
-                              const vren_cs_frame* frame, uint32_t* keys, uint32_t key_cap, uint32_t* key_count,
-                              uint32_t* refs, uint32_t* scratch)
+static FucFrame fuc_frame(const float* depth, const float* normals, uint32_t W, uint32_t H, const vren_cs_frame* frame,
+                          uint32_t* keys, uint32_t key_cap, uint32_t* key_count, uint32_t* refs, uint32_t* scratch)
 {
     const uint32_t tiles = ((W + 31) / 32) * ((H + 31) / 32);
     const int vec = (W % 4u == 0u) && ((uintptr_t)depth % 16u == 0u) && ((uintptr_t)normals % 16u == 0u) &&
                     ((uintptr_t)refs % 16u == 0u);
-    const FucFrame fr{depth, normals, W, H, frame, keys, key_cap, key_count, refs,
-                      scratch + fuc_keys_offset_words(tiles), scratch, scratch + tiles, tiles, vec};
-    launch_kernel(find_unique_kernel, tiles, kFucThreads, 0, st, fr);
-    VREN_LAUNCH_CHECK();
-    launch_kernel(find_unique_scan_kernel, 1, kFucScanThreads, 0, st, fr);
-    VREN_LAUNCH_CHECK();
-    launch_kernel(find_unique_fixup_kernel, tiles, kFucThreads, 0, st, fr);
+    return FucFrame{depth, normals, W, H, frame, keys, key_cap, key_count, refs,
+                    scratch + fuc_keys_offset_words(tiles), scratch, scratch + tiles, tiles, vec};
+}
+
+// Stage 1 over tiles [tile_begin, tile_begin + count).
+static int launch_find_unique_tiles(cudaStream_t st, const FucFrame& fr, uint32_t tile_begin, uint32_t count)
+{
+    if (count == 0) return VREN_OK;
+    launch_kernel(find_unique_kernel, count, kFucThreads, 0, st, fr, tile_begin);
     VREN_LAUNCH_CHECK();
     return VREN_OK;
+}
+
+// Stages 2 and 3 (after every tile).
+static int launch_find_unique_finish(cudaStream_t st, const FucFrame& fr)
+{
+    launch_kernel(find_unique_scan_kernel, 1, kFucScanThreads, 0, st, fr);
+    VREN_LAUNCH_CHECK();
+    launch_kernel(find_unique_fixup_kernel, fr.num_tiles, kFucThreads, 0, st, fr);
+    VREN_LAUNCH_CHECK();
+    return VREN_OK;
+}
+
+static int launch_find_unique(cudaStream_t st, const float* depth, const float* normals, uint32_t W, uint32_t H,
+                              const vren_cs_frame* frame, uint32_t* keys, uint32_t key_cap, uint32_t* key_count,
+                              uint32_t* refs, uint32_t* scratch)
+{
+    const FucFrame fr = fuc_frame(depth, normals, W, H, frame, keys, key_cap, key_count, refs, scratch);
+    const int rc = launch_find_unique_tiles(st, fr, 0, fr.num_tiles);
+    return rc != VREN_OK ? rc : launch_find_unique_finish(st, fr);
+}
+
+// The light lists of a frame copied into page-locked host memory by the device (no host round trip
+// for their lengths): out = [U, total, keys[U], counts[U], offsets[U], indices[total]], cut at cap
+// words (VREN_ERR_CAPACITY recorded when it does not fit).
+__global__ void lists_to_host_kernel(const uint32_t* __restrict__ key_count, uint32_t key_cap,
+                                     const uint32_t* __restrict__ total_p, const uint32_t* __restrict__ keys,
+                                     const uint32_t* __restrict__ counts, const uint32_t* __restrict__ offsets,
+                                     const uint32_t* __restrict__ indices, uint32_t* __restrict__ out, uint64_t cap)
+{
+    pdl_enter();
+    uint32_t U = *key_count;
+    U = U < key_cap ? U : key_cap;
+    const uint32_t total = *total_p;
+    const uint64_t need = 2ull + 3ull * U + total;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (cap >= 2) {
+            out[0] = U;
+            out[1] = total;
+        }
+        if (need > cap) VREN_RECORD_ERROR(VREN_ERR_CAPACITY);
+    }
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < 3ull * U + total; i += stride) {
+        const uint64_t o = 2 + i;
+        if (o >= cap) break;
+        uint32_t v;
+        if (i < U) v = keys[i];
+        else if (i < 2ull * U) v = counts[i - U];
+        else if (i < 3ull * U) v = offsets[i - 2ull * U];
+        else v = indices[i - 3ull * U];
+        out[o] = v;
+    }
 }
 
 // ================================================================================================
@@ -733,6 +786,8 @@ struct vren_cluster_and_shade {
     struct HostKey {
         Key k;
         void* refs_out;
+        void* lists_out;
+        uint64_t lists_cap;
     } host_key{};
 };
 
@@ -880,10 +935,12 @@ int refresh_frame(vren_cluster_and_shade* cs, cudaStream_t st, const vren_cs_vie
 }
 
 // One frame from host buffers: the lights go up and their BVH is built on the second stream while the
-// depth and normals go up on `st`; the unique clusters run when those arrive, then the references go
-// down on the second stream while the light lists are assigned on `st`.
+// depth and normals go up on `st` in bands of tile rows, each band's tiles processed as it arrives;
+// then the references go down on the second stream while the light lists are assigned on `st`, and
+// the lists are written into host memory by the device.
 int cs_enqueue_host(vren_cluster_and_shade* cs, cudaStream_t st, uint32_t W, uint32_t H, const float* depth,
-                    const float* normals, const float* positions, const float* lights, uint32_t L, uint32_t* refs_out)
+                    const float* normals, const float* positions, const float* lights, uint32_t L, uint32_t* refs_out,
+                    uint32_t* lists_out, uint64_t lists_cap)
 {
     const PdlScope pdl(1);
     cudaStream_t aux = cs->aux;
@@ -899,10 +956,23 @@ int cs_enqueue_host(vren_cluster_and_shade* cs, cudaStream_t st, uint32_t W, uin
         if (rc != VREN_OK) return rc;
     }
     VREN_CUDA_TRY(cudaEventRecord(cs->ev_bvh, aux));
-    VREN_CUDA_TRY(cudaMemcpyAsync(cs->in_depth, depth, (size_t)W * H * 4, cudaMemcpyHostToDevice, st));
-    VREN_CUDA_TRY(cudaMemcpyAsync(cs->in_normals, normals, (size_t)W * H * 12, cudaMemcpyHostToDevice, st));
-    rc = launch_find_unique(st, cs->in_depth, cs->in_normals, W, H, cs->frame, cs->keys, cs->key_cap, cs->key_count,
-                            cs->refs, static_cast<uint32_t*>(cs->fuc_scratch));
+    // G-buffer up in bands of tile rows, each band's tiles processed as soon as it has arrived (the last
+    // tile row may wrap to the first rows, which arrive first)
+    const FucFrame fr = fuc_frame(cs->in_depth, cs->in_normals, W, H, cs->frame, cs->keys, cs->key_cap,
+                                  cs->key_count, cs->refs, static_cast<uint32_t*>(cs->fuc_scratch));
+    const uint32_t TX = (W + 31) / 32, TY = (H + 31) / 32;
+    const uint32_t bands = TY < 4u ? TY : 4u, per = (TY + bands - 1) / bands;
+    for (uint32_t ty0 = 0; ty0 < TY; ty0 += per) {
+        const uint32_t ty1 = ty0 + per < TY ? ty0 + per : TY;
+        const size_t y0 = (size_t)ty0 * 32, y1 = (size_t)ty1 * 32 < H ? (size_t)ty1 * 32 : H;
+        VREN_CUDA_TRY(cudaMemcpyAsync(cs->in_depth + y0 * W, depth + y0 * W, (y1 - y0) * W * 4,
+                                      cudaMemcpyHostToDevice, st));
+        VREN_CUDA_TRY(cudaMemcpyAsync(cs->in_normals + 3 * y0 * W, normals + 3 * y0 * W, (y1 - y0) * W * 12,
+                                      cudaMemcpyHostToDevice, st));
+        rc = launch_find_unique_tiles(st, fr, ty0 * TX, (ty1 - ty0) * TX);
+        if (rc != VREN_OK) return rc;
+    }
+    rc = launch_find_unique_finish(st, fr);
     if (rc != VREN_OK) return rc;
     if (refs_out) {
         VREN_CUDA_TRY(cudaEventRecord(cs->ev_fuc, st));
@@ -914,6 +984,11 @@ int cs_enqueue_host(vren_cluster_and_shade* cs, cudaStream_t st, uint32_t W, uin
                        cs->view_pos, cs->spheres, cs->counts, cs->offsets, cs->indices, cs->max_assign, cs->total,
                        cs->assign_scratch, cs->opt.assign_warps);
     if (rc != VREN_OK) return rc;
+    if (lists_out) {
+        launch_kernel(lists_to_host_kernel, kNumSMsHint, 256, 0, st, cs->key_count, cs->key_cap, cs->total, cs->keys,
+                      cs->counts, cs->offsets, cs->indices, lists_out, lists_cap);
+        VREN_LAUNCH_CHECK();
+    }
     VREN_CUDA_TRY(cudaEventRecord(cs->ev_join, aux));
     VREN_CUDA_TRY(cudaStreamWaitEvent(st, cs->ev_join, 0));
     return VREN_OK;
@@ -965,7 +1040,8 @@ extern "C" int vren_cs_cluster(vren_cluster_and_shade* cs, vren_stream_t s, cons
 extern "C" int vren_cs_cluster_host(vren_cluster_and_shade* cs, vren_stream_t s, const vren_cs_view* view,
                                     uint32_t width, uint32_t height, int offscreen, const float* depth,
                                     const float* normals, const float* light_positions, const float* point_lights,
-                                    uint32_t light_count, uint32_t* cluster_refs_out)
+                                    uint32_t light_count, uint32_t* cluster_refs_out, uint32_t* lists_out,
+                                    uint64_t lists_capacity)
 {
     if (!cs || !view || !depth || !normals) return VREN_ERR_ARG;
     if (width > cs->max_w || height > cs->max_h || light_count > cs->max_lights) return VREN_ERR_CAPACITY;
@@ -994,11 +1070,11 @@ extern "C" int vren_cs_cluster_host(vren_cluster_and_shade* cs, vren_stream_t s,
     if (rc != VREN_OK) return rc;
     const vren_cluster_and_shade::HostKey key{{width, height, light_count, (uint32_t)offscreen, depth, normals,
                                                light_positions, point_lights, st, cs->opt},
-                                              cluster_refs_out};
+                                              cluster_refs_out, lists_out, lists_capacity};
     const bool use_graph = cs->opt.use_graph && st != nullptr;
     if (!use_graph)
         return cs_enqueue_host(cs, st, width, height, depth, normals, light_positions, point_lights, light_count,
-                               cluster_refs_out);
+                               cluster_refs_out, lists_out, lists_capacity);
     if (cs->host_graph && std::memcmp(&key, &cs->host_key, sizeof(key)) == 0) {
         VREN_CUDA_TRY(cudaGraphLaunch(cs->host_graph, st));
         return VREN_OK;
@@ -1010,7 +1086,7 @@ extern "C" int vren_cs_cluster_host(vren_cluster_and_shade* cs, vren_stream_t s,
     cudaGraph_t g;
     VREN_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     rc = cs_enqueue_host(cs, st, width, height, depth, normals, light_positions, point_lights, light_count,
-                         cluster_refs_out);
+                         cluster_refs_out, lists_out, lists_capacity);
     cudaError_t e = cudaStreamEndCapture(st, &g);
     if (rc != VREN_OK) {
         if (e == cudaSuccess) cudaGraphDestroy(g);
