@@ -780,8 +780,9 @@ struct vren_cluster_and_shade {
     // the graph of the last host-input frame shape
     char* inputs = nullptr;
     float *in_depth = nullptr, *in_normals = nullptr, *in_pos = nullptr, *in_lights = nullptr;
-    cudaStream_t aux = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_bvh = nullptr, ev_fuc = nullptr, ev_join = nullptr;
+    cudaStream_t aux = nullptr, up = nullptr;  // light BVH and downloads; G-buffer uploads
+    cudaEvent_t ev_fork = nullptr, ev_bvh = nullptr, ev_fuc = nullptr, ev_join = nullptr, ev_join_up = nullptr;
+    cudaEvent_t ev_band[4] = {nullptr, nullptr, nullptr, nullptr};
     cudaGraphExec_t host_graph = nullptr;
     struct HostKey {
         Key k;
@@ -890,7 +891,9 @@ extern "C" void vren_cs_destroy(vren_cluster_and_shade* cs)
     if (cs->graph) cudaGraphExecDestroy(cs->graph);
     if (cs->host_graph) cudaGraphExecDestroy(cs->host_graph);
     if (cs->aux) cudaStreamDestroy(cs->aux);
-    for (cudaEvent_t e : {cs->ev_fork, cs->ev_bvh, cs->ev_fuc, cs->ev_join})
+    if (cs->up) cudaStreamDestroy(cs->up);
+    for (cudaEvent_t e : {cs->ev_fork, cs->ev_bvh, cs->ev_fuc, cs->ev_join, cs->ev_join_up, cs->ev_band[0],
+                          cs->ev_band[1], cs->ev_band[2], cs->ev_band[3]})
         if (e) cudaEventDestroy(e);
     cudaFree(cs->inputs);
     cudaFree(cs->arena);
@@ -943,9 +946,10 @@ int cs_enqueue_host(vren_cluster_and_shade* cs, cudaStream_t st, uint32_t W, uin
                     uint32_t* lists_out, uint64_t lists_cap)
 {
     const PdlScope pdl(1);
-    cudaStream_t aux = cs->aux;
+    cudaStream_t aux = cs->aux, up = cs->up;
     VREN_CUDA_TRY(cudaEventRecord(cs->ev_fork, st));
     VREN_CUDA_TRY(cudaStreamWaitEvent(aux, cs->ev_fork, 0));
+    VREN_CUDA_TRY(cudaStreamWaitEvent(up, cs->ev_fork, 0));
     int rc = VREN_OK;
     if (L > 0) {
         VREN_CUDA_TRY(cudaMemcpyAsync(cs->in_pos, positions, (size_t)L * 16, cudaMemcpyHostToDevice, aux));
@@ -962,13 +966,21 @@ int cs_enqueue_host(vren_cluster_and_shade* cs, cudaStream_t st, uint32_t W, uin
                                   cs->key_count, cs->refs, static_cast<uint32_t*>(cs->fuc_scratch));
     const uint32_t TX = (W + 31) / 32, TY = (H + 31) / 32;
     const uint32_t bands = TY < 4u ? TY : 4u, per = (TY + bands - 1) / bands;
-    for (uint32_t ty0 = 0; ty0 < TY; ty0 += per) {
+    uint32_t band = 0;
+    for (uint32_t ty0 = 0; ty0 < TY; ty0 += per, ++band) {  // uploads on `up`, one event per band
         const uint32_t ty1 = ty0 + per < TY ? ty0 + per : TY;
         const size_t y0 = (size_t)ty0 * 32, y1 = (size_t)ty1 * 32 < H ? (size_t)ty1 * 32 : H;
         VREN_CUDA_TRY(cudaMemcpyAsync(cs->in_depth + y0 * W, depth + y0 * W, (y1 - y0) * W * 4,
-                                      cudaMemcpyHostToDevice, st));
+                                      cudaMemcpyHostToDevice, up));
         VREN_CUDA_TRY(cudaMemcpyAsync(cs->in_normals + 3 * y0 * W, normals + 3 * y0 * W, (y1 - y0) * W * 12,
-                                      cudaMemcpyHostToDevice, st));
+                                      cudaMemcpyHostToDevice, up));
+        VREN_CUDA_TRY(cudaEventRecord(cs->ev_band[band], up));
+    }
+    VREN_CUDA_TRY(cudaEventRecord(cs->ev_join_up, up));
+    band = 0;
+    for (uint32_t ty0 = 0; ty0 < TY; ty0 += per, ++band) {  // each band's tiles once it has arrived
+        const uint32_t ty1 = ty0 + per < TY ? ty0 + per : TY;
+        VREN_CUDA_TRY(cudaStreamWaitEvent(st, cs->ev_band[band], 0));
         rc = launch_find_unique_tiles(st, fr, ty0 * TX, (ty1 - ty0) * TX);
         if (rc != VREN_OK) return rc;
     }
@@ -991,6 +1003,7 @@ int cs_enqueue_host(vren_cluster_and_shade* cs, cudaStream_t st, uint32_t W, uin
     }
     VREN_CUDA_TRY(cudaEventRecord(cs->ev_join, aux));
     VREN_CUDA_TRY(cudaStreamWaitEvent(st, cs->ev_join, 0));
+    VREN_CUDA_TRY(cudaStreamWaitEvent(st, cs->ev_join_up, 0));
     return VREN_OK;
 }
 }  // namespace
@@ -1063,7 +1076,9 @@ extern "C" int vren_cs_cluster_host(vren_cluster_and_shade* cs, vren_stream_t s,
         cs->in_pos = reinterpret_cast<float*>(cs->inputs + o_p);
         cs->in_lights = reinterpret_cast<float*>(cs->inputs + o_l);
         VREN_CUDA_TRY(cudaStreamCreateWithFlags(&cs->aux, cudaStreamNonBlocking));
-        for (cudaEvent_t* e : {&cs->ev_fork, &cs->ev_bvh, &cs->ev_fuc, &cs->ev_join})
+        VREN_CUDA_TRY(cudaStreamCreateWithFlags(&cs->up, cudaStreamNonBlocking));
+        for (cudaEvent_t* e : {&cs->ev_fork, &cs->ev_bvh, &cs->ev_fuc, &cs->ev_join, &cs->ev_join_up, &cs->ev_band[0],
+                               &cs->ev_band[1], &cs->ev_band[2], &cs->ev_band[3]})
             VREN_CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     }
     int rc = refresh_frame(cs, st, view, width, height, offscreen);
