@@ -7,10 +7,10 @@
 // exclusive prefix by decoupled look-back over the preceding tiles of its segment, and writes
 // the exclusive sums with uint4 stores — 8 bytes of HBM traffic per element.
 //
-// Scratch layout (uint32 words): [0] start ticket, [1] unused, [2] epoch, [3] unused, then one
-// 64-bit status word per tile: [epoch:30 | flag:2 | value:32].  A one-thread kernel before each scan
-// resets the ticket and advances the epoch; status words from an earlier call carry an older epoch
-// and read as "not published", so the scratch needs no clearing between calls.
+// Scratch layout (uint32 words): [0] start ticket, [1] done ticket, [2] epoch, [3] unused,
+// then one 64-bit status word per tile: [epoch:30 | flag:2 | value:32].  Status words from an
+// earlier call carry an older epoch and read as "not published", so the scratch needs no
+// clearing between calls; the last CTA to finish resets the tickets and advances the epoch.
 // The scratch must be zero-filled before its first use (and again after VREN_ERR_TIMEOUT).
 #include "common.cuh"
 #include "internal.h"
@@ -205,17 +205,15 @@ __global__ void __launch_bounds__(kScanThreads, 4) exclusive_scan_kernel(
     }
 
 done:
-    (void)total_tiles;
-}
-
-// Runs before every scan: resets the tile ticket and advances the epoch, so no CTA of the scan has to
-// report its completion (status words of earlier calls carry an older epoch).
-__global__ void scan_prepare_kernel(uint32_t* __restrict__ scratch)
-{
-    pdl_enter();
-    if (threadIdx.x == 0) {
-        scratch[0] = 0u;
-        scratch[2] = (scratch[2] + 1u) & 0x3FFFFFFFu;
+    // The last CTA to finish resets the tickets and advances the epoch for the next call (every CTA
+    // has taken its ticket by then; the next kernel sees these words at the kernel boundary).
+    if (tid == 0) {
+        const uint32_t done = atomicAdd(scratch + 1, 1u);
+        if (done == total_tiles - 1) {
+            scratch[0] = 0u;
+            scratch[1] = 0u;
+            scratch[2] = (epoch + 1u) & 0x3FFFFFFFu;
+        }
     }
 }
 
@@ -288,8 +286,6 @@ static int scan_launch(cudaStream_t st, const uint32_t* in, uint32_t* out, uint3
     if (total > 0x7FFFFFFFull) return VREN_ERR_ARG;
     const uint32_t spin = (uint32_t)tuning(VREN_TUNE_SPIN_POLLS);
     uint32_t* sc = static_cast<uint32_t*>(scratch);
-    launch_kernel(scan_prepare_kernel, 1, 32, 0, st, sc);
-    VREN_LAUNCH_CHECK();
     if (slices == 8)
         launch_kernel(exclusive_scan_kernel<8>, (uint32_t)total, kScanThreads, 0, st, 
             in, out, n, tiles_per_seg ? tiles_per_seg : 1, (uint32_t)total, sc, g_wait_limit, spin, n_dev, total_out);
