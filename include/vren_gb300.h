@@ -68,9 +68,14 @@ uint32_t vren_set_wait_limit(uint32_t rounds);
  *   VREN_TUNE_RADIX_RANK   digit ranking in a sort pass: 0 = one ballot per digit bit,
  *                          1 = match.any + shared-memory atomic per peer group,
  *                          2 = match.any + counter update by the group's first lane
- *   VREN_TUNE_RADIX_ITEMS  keys per thread in a sort pass: 0 = 15/16 (3840/4096 per tile), 1 = 23/24 */
+ *   VREN_TUNE_RADIX_ITEMS  keys per thread in a sort pass: 0 = 15/16 (3840/4096 per tile), 1 = 23/24
+ *   VREN_TUNE_SCAN_STAGED  scan form: 0 = automatic (the persistent form from 2^20 elements when
+ *                          every tile starts 16-byte aligned, else tiles in registers), 1 = always
+ *                          one CTA per tile in registers, 2 = one CTA per tile staged in shared
+ *                          memory by bulk copies, 3 = persistent grid with a producer warp streaming
+ *                          tiles by bulk copies (2 and 3 whenever the alignment allows) */
 enum { VREN_TUNE_SCAN_SLICES = 0, VREN_TUNE_SPIN_POLLS = 1, VREN_TUNE_RADIX_RANK = 2, VREN_TUNE_RADIX_ITEMS = 3,
-       VREN_TUNE_COUNT = 4 };
+       VREN_TUNE_SCAN_STAGED = 4, VREN_TUNE_COUNT = 5 };
 int vren_tuning_set(int knob, int value);
 int vren_tuning_get(int knob);
 

@@ -354,13 +354,20 @@ def test_radix_variants_identical(cuda, restore_tuning, rank, items, spin):
 
 @pytest.mark.parametrize("slices", [4, 8])
 @pytest.mark.parametrize("spin", [0, 64, 4096])
-def test_scan_variants_identical(cuda, restore_tuning, slices, spin):
+@pytest.mark.parametrize("staged", [0, 1, 2, 3])
+def test_scan_variants_identical(cuda, restore_tuning, slices, spin, staged):
+    """Tiles in registers, tiles staged in shared memory by bulk copies (forced with staged=2,
+    automatic from 2^20 elements with staged=0) and the persistent warp-specialised grid (staged=3)
+    give the same sums: partial last tiles, aligned and unaligned segments, more tiles than resident
+    CTAs, calls alternating between the forms on one scratch."""
     lib = restore_tuning
     assert lib.vren_tuning_set(vg._lib.TUNE["scan_slices"], slices) == 0
     assert lib.vren_tuning_set(vg._lib.TUNE["spin_polls"], spin) == 0
-    rng = np.random.default_rng(slices + spin)
+    assert lib.vren_tuning_set(vg._lib.TUNE["scan_staged"], staged) == 0
+    rng = np.random.default_rng(slices + spin + 7 * staged)
     scan = vg.blelloch_scan()
-    for n, blocks in ((1, 1), (8191, 1), (8193, 3), ((1 << 22) + 5, 1)):
+    for n, blocks in ((1, 1), (8191, 1), (8193, 3), (8196, 3), (3 * 8192, 5), ((1 << 22) + 5, 1),
+                      ((1 << 20) + 4, 3), (1 << 24, 1)):
         x = rng.integers(0, 256, n * blocks).astype(np.uint32)
         buf = dev_u32(x, cuda)
         scan(None, buf, n, 0, blocks)
