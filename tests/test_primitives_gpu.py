@@ -89,6 +89,26 @@ def test_reduce_scalar_u32(cuda, op, n):
         assert host_u32(out)[0] == oracle.reduce_u32(op, x)
 
 
+@pytest.mark.parametrize("n", [(1 << 22) + 4099, 305 * 4096, 1 << 20, 4099])
+@pytest.mark.parametrize("form", [0, 1, 2, 3, 4, 5])
+def test_reduce_scalar_streaming_edges(cuda, restore_tuning, n, form):
+    """Every scalar reduce form (grid-stride loop, streaming stage shapes, automatic): extremes
+    planted in the last partial stage, the scalar tail (n mod 4) and the first element; more stages
+    than CTAs and CTAs with no stage."""
+    assert restore_tuning.vren_tuning_set(vg._lib.TUNE["reduce_form"], form) == 0
+    rng = np.random.default_rng(n)
+    x = rng.integers(100, 200, n).astype(np.uint32)
+    x[-1] = 3                     # tail element (n mod 4 != 0) or the last element of the last stage
+    x[max((n // 4096) * 4096 - 5, 1)] = 900
+    x[0] = 7
+    sc = vg.primitives.alloc_scratch(vg.primitives.reduce_scratch_bytes(n), cuda)
+    d = dev_u32(x, cuda)
+    for op in ("add", "min", "max"):
+        out = torch.zeros(1, dtype=torch.int32, device=cuda)
+        vg.reduce_scalar(None, op, d, out, sc)
+        assert host_u32(out)[0] == oracle.reduce_u32(op, x), op
+
+
 def test_reduce_scalar_u32_sum_wraps(cuda):
     n = 1 << 26
     x = torch.full((n,), 255, dtype=torch.int32, device=cuda)

@@ -11,9 +11,13 @@
 // VREN_OPERATION(s_data[b], s_data[a]) (reduce.comp:266), so float sums follow the same
 // pairwise tree and are bit-identical.
 //
-// Scalar form: a single pass over uint4-vectorised loads, block partials in scratch and a
-// last-block-done combine (no spinning, integer/total-order ops, exact in any order).
+// Scalar form: a single pass, block partials in scratch and a last-block-done combine (no
+// spinning, integer/total-order ops, exact in any order): a grid-stride loop of uint4 loads, four
+// in flight per thread.  Streaming forms that pull the input through shared-memory stages filled
+// by bulk copies (cp.async.bulk) are selectable; they measured slower on GB300.
 #include "common.cuh"
+#include "internal.h"
+#include "tma.cuh"
 
 #include <cfloat>
 
@@ -179,6 +183,47 @@ __device__ __forceinline__ uint32_t f32_from_order_key(uint32_t key)
 constexpr int kScalarThreads = 512;
 constexpr int kScalarVecPerThread = 4;  // uint4 loads in flight per thread per iteration
 
+// Block combine of every thread's `acc`, the block partial into scratch[1 + block], and the final
+// combine by the last block to finish (which also resets the ticket scratch[0]).
+template <int OP, bool FLOAT_KEYS, int THREADS>
+__device__ __forceinline__ void reduce_finish(uint32_t acc, uint32_t* __restrict__ out, uint32_t* __restrict__ scratch,
+                                              uint32_t* s_warp, bool* s_last)
+{
+    using Op = U32Op<OP>;
+    const uint32_t tid = threadIdx.x;
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) acc = Op::apply(acc, __shfl_xor_sync(0xFFFFFFFFu, acc, d));
+    if ((tid & 31) == 0) s_warp[tid >> 5] = acc;
+    __syncthreads();
+    if (tid < 32) {
+        uint32_t w = tid < THREADS / 32 ? s_warp[tid] : Op::identity();
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) w = Op::apply(w, __shfl_xor_sync(0xFFFFFFFFu, w, d));
+        if (tid == 0) {
+            st_relaxed_u32(scratch + 1 + blockIdx.x, w);
+            __threadfence();
+            const uint32_t ticket = atomicAdd(scratch, 1u);
+            *s_last = (ticket == gridDim.x - 1);
+        }
+    }
+    __syncthreads();
+    if (!*s_last) return;
+    __threadfence();
+    uint32_t total = Op::identity();
+    for (uint32_t b = tid; b < gridDim.x; b += THREADS) total = Op::apply(total, ld_relaxed_u32(scratch + 1 + b));
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) total = Op::apply(total, __shfl_xor_sync(0xFFFFFFFFu, total, d));
+    __syncthreads();
+    if ((tid & 31) == 0) s_warp[tid >> 5] = total;
+    __syncthreads();
+    if (tid == 0) {
+        uint32_t t = Op::identity();
+        for (int w = 0; w < THREADS / 32; ++w) t = Op::apply(t, s_warp[w]);
+        out[0] = FLOAT_KEYS ? f32_from_order_key(t) : t;
+        scratch[0] = 0u;
+    }
+}
+
 template <int OP, bool FLOAT_KEYS>
 __global__ void __launch_bounds__(kScalarThreads) reduce_scalar_kernel(
     const uint32_t* __restrict__ in, uint32_t n, uint32_t* __restrict__ out, uint32_t* __restrict__ scratch)
@@ -216,41 +261,142 @@ __global__ void __launch_bounds__(kScalarThreads) reduce_scalar_kernel(
     // Tail (n not a multiple of 4), handled by block 0.
     if (blockIdx.x == 0 && tid < (n & 3u)) fold(in[nvec * 4 + tid]);
 
-    // Block reduction.
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) acc = Op::apply(acc, __shfl_xor_sync(0xFFFFFFFFu, acc, d));
-    if ((tid & 31) == 0) s_warp[tid >> 5] = acc;
-    __syncthreads();
-    if (tid < 32) {
-        uint32_t w = tid < kScalarThreads / 32 ? s_warp[tid] : Op::identity();
-#pragma unroll
-        for (int d = 16; d > 0; d >>= 1) w = Op::apply(w, __shfl_xor_sync(0xFFFFFFFFu, w, d));
-        if (tid == 0) {
-            // scratch[0] = ticket, scratch[1 + b] = partial of block b.
-            st_relaxed_u32(scratch + 1 + blockIdx.x, w);
-            __threadfence();
-            uint32_t ticket = atomicAdd(scratch, 1u);
-            s_last = (ticket == gridDim.x - 1);
-        }
-    }
-    __syncthreads();
-    if (!s_last) return;
+    reduce_finish<OP, FLOAT_KEYS, kScalarThreads>(acc, out, scratch, s_warp, &s_last);
+}
 
-    // Last block: combine the partials and reset the ticket for the next call.
-    __threadfence();
-    uint32_t total = Op::identity();
-    for (uint32_t b = tid; b < gridDim.x; b += kScalarThreads) total = Op::apply(total, ld_relaxed_u32(scratch + 1 + b));
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) total = Op::apply(total, __shfl_xor_sync(0xFFFFFFFFu, total, d));
-    __syncthreads();
-    if ((tid & 31) == 0) s_warp[tid >> 5] = total;
-    __syncthreads();
-    if (tid == 0) {
-        uint32_t t = Op::identity();
-        for (int w = 0; w < kScalarThreads / 32; ++w) t = Op::apply(t, s_warp[w]);
-        out[0] = FLOAT_KEYS ? f32_from_order_key(t) : t;
-        scratch[0] = 0u;
+// Streaming form: each CTA pulls its share of the input through a ring of `stages` shared-memory
+// stages of `stage_vec` uint4, several in flight.  Warp 8 issues the bulk copies; each of the eight
+// consumer warps folds its eighth of a stage and releases it on the stage's `empty` barrier (count
+// 8), and the producer refills a stage once all eight have released it, so no CTA-wide barrier
+// sits between stages.  A CTA's stages are either one contiguous run or every grid-th stage.
+constexpr int kStreamConsumers = 256;
+constexpr int kStreamThreads = kStreamConsumers + 32;
+constexpr int kStreamMaxStages = 12;
+
+struct StreamShape {
+    uint32_t stage_vec;  // uint4 per stage (multiple of 256)
+    uint32_t stages;     // ring depth (<= kStreamMaxStages)
+    uint32_t per_sm;     // CTAs per SM the shape is sized for
+    uint32_t interleave; // 1: CTA b takes stages b, b + grid, ...; 0: one contiguous run
+};
+
+template <int OP, bool FLOAT_KEYS>
+__global__ void __launch_bounds__(kStreamThreads) reduce_stream_kernel(
+    const uint32_t* __restrict__ in, uint32_t n, uint32_t* __restrict__ out, uint32_t* __restrict__ scratch,
+    uint32_t wait_limit, StreamShape shape)
+{
+    using Op = U32Op<OP>;
+    extern __shared__ __align__(128) uint4 s_stage[];
+    __shared__ __align__(8) uint64_t s_full[kStreamMaxStages];
+    __shared__ __align__(8) uint64_t s_empty[kStreamMaxStages];
+    __shared__ uint32_t s_warp[kStreamThreads / 32];
+    __shared__ bool s_last;
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const uint32_t V = shape.stage_vec, S = shape.stages;
+    const uint32_t nvec = n / 4;
+    const uint32_t stages_total = (nvec + V - 1) / V;
+    uint32_t first, step, count;
+    if (shape.interleave) {
+        first = blockIdx.x;
+        step = gridDim.x;
+        count = first < stages_total ? (stages_total - first + step - 1) / step : 0u;
+    } else {
+        const uint32_t per = (stages_total + gridDim.x - 1) / gridDim.x;
+        first = min(blockIdx.x * per, stages_total);
+        step = 1;
+        count = min(first + per, stages_total) - first;
     }
+    const uint4* in4 = reinterpret_cast<const uint4*>(in);
+    if (tid == 0) {
+        for (uint32_t s = 0; s < S; ++s) {
+            mbar_init(&s_full[s], 1u);
+            mbar_init(&s_empty[s], kStreamConsumers / 32);
+        }
+        fence_barrier_init();
+    }
+    __syncthreads();
+
+    uint32_t acc = Op::identity();
+    auto fold = [&](uint32_t x) {
+        if (FLOAT_KEYS) x = f32_order_key(x);
+        acc = Op::apply(acc, x);
+    };
+    bool timed_out = false;
+    if (warp == kStreamConsumers / 32) {
+        if (lane == 0) {
+            for (uint32_t k = 0; k < count; ++k) {
+                const uint32_t s = k % S;
+                if (k >= S && !mbar_wait(&s_empty[s], ((k - S) / S) & 1u, wait_limit)) {
+                    timed_out = true;  // the consumers time out on `full` in turn
+                    break;
+                }
+                const uint32_t v0 = (first + k * step) * V;
+                const uint32_t nv = min(V, nvec - v0);
+                mbar_arrive_expect_tx(&s_full[s], nv * 16u);
+                bulk_load(s_stage + (size_t)s * V, in4 + v0, nv * 16u, &s_full[s]);
+            }
+        }
+    } else {
+        const uint32_t share = V / 8;  // uint4 per consumer warp per stage
+        for (uint32_t k = 0; k < count; ++k) {
+            const uint32_t s = k % S;
+            if (!__all_sync(0xFFFFFFFFu, mbar_wait(&s_full[s], (k / S) & 1u, wait_limit))) {
+                timed_out = true;
+                break;
+            }
+            const uint32_t nv = min(V, nvec - (first + k * step) * V);
+            const uint32_t base = warp * share;
+            const uint4* st = s_stage + (size_t)s * V + base;
+#pragma unroll 4
+            for (uint32_t idx = lane; idx < share; idx += 32) {
+                if (base + idx < nv) {
+                    const uint4 q = st[idx];
+                    fold(q.x); fold(q.y); fold(q.z); fold(q.w);
+                }
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&s_empty[s]);
+        }
+        if (blockIdx.x == 0 && tid < (n & 3u)) fold(in[nvec * 4 + tid]);
+    }
+    if (timed_out) VREN_RECORD_ERROR(VREN_ERR_TIMEOUT);
+    __syncthreads();
+    reduce_finish<OP, FLOAT_KEYS, kStreamThreads>(acc, out, scratch, s_warp, &s_last);
+}
+
+// Stream shapes selectable with VREN_TUNE_REDUCE_FORM (2..5).  Measured on GB300 (2^26 / 2^27
+// elements): 60-65 us / 104-111 us against 52 us / 93 us for the grid-stride loop of uint4 loads,
+// which is therefore the automatic choice at every size.
+constexpr StreamShape kStreamShapes[4] = {
+    {1024, 6, 2, 0},   // 16 KB x 6, two CTAs per SM, contiguous runs
+    {1024, 6, 2, 1},   // the same, interleaved stages
+    {2048, 6, 1, 1},   // 32 KB x 6, one CTA per SM, interleaved
+    {512, 12, 2, 1},   // 8 KB x 12, two CTAs per SM, interleaved
+};
+constexpr uint32_t kStreamMaxGrid = 2 * kNumSMsHint;
+
+static uint32_t stream_grid(uint32_t n, const StreamShape& sh)
+{
+    const uint32_t stages = (n / 4 + sh.stage_vec - 1) / sh.stage_vec;
+    const uint32_t cap = sh.per_sm * kNumSMsHint;
+    return stages < cap ? (stages ? stages : 1) : cap;
+}
+
+template <int OP, bool FLOAT_KEYS>
+static int launch_stream(cudaStream_t st, const uint32_t* in, uint32_t n, uint32_t* out, uint32_t* sc,
+                         const StreamShape& sh)
+{
+    static bool attr_set = false;  // per instantiation: the largest ring any shape uses
+    if (!attr_set) {
+        VREN_CUDA_TRY(cudaFuncSetAttribute(reduce_stream_kernel<OP, FLOAT_KEYS>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, 192 * 1024));
+        attr_set = true;
+    }
+    const size_t smem = (size_t)sh.stage_vec * sh.stages * sizeof(uint4);
+    reduce_stream_kernel<OP, FLOAT_KEYS><<<stream_grid(n, sh), kStreamThreads, smem, st>>>(in, n, out, sc,
+                                                                                         g_wait_limit, sh);
+    VREN_LAUNCH_CHECK();
+    return VREN_OK;
 }
 
 static uint32_t scalar_grid(uint32_t n)
@@ -269,6 +415,16 @@ static int reduce_scalar_dispatch(cudaStream_t st, int op, const uint32_t* in, u
 {
     uint32_t g = scalar_grid(n);
     uint32_t* sc = static_cast<uint32_t*>(scratch);
+    const int form = tuning(VREN_TUNE_REDUCE_FORM);
+    if (form >= 2 && n > 0) {
+        const StreamShape& sh = kStreamShapes[form - 2];
+        switch (op) {
+        case VREN_REDUCE_ADD: return launch_stream<VREN_REDUCE_ADD, FLOAT_KEYS>(st, in, n, out, sc, sh);
+        case VREN_REDUCE_MIN: return launch_stream<VREN_REDUCE_MIN, FLOAT_KEYS>(st, in, n, out, sc, sh);
+        case VREN_REDUCE_MAX: return launch_stream<VREN_REDUCE_MAX, FLOAT_KEYS>(st, in, n, out, sc, sh);
+        default: return VREN_ERR_ARG;
+        }
+    }
     switch (op) {
     case VREN_REDUCE_ADD: reduce_scalar_kernel<VREN_REDUCE_ADD, FLOAT_KEYS><<<g, kScalarThreads, 0, st>>>(in, n, out, sc); break;
     case VREN_REDUCE_MIN: reduce_scalar_kernel<VREN_REDUCE_MIN, FLOAT_KEYS><<<g, kScalarThreads, 0, st>>>(in, n, out, sc); break;
@@ -316,7 +472,9 @@ extern "C" int vren_reduce_tree_vec4(vren_stream_t s, int op, const float* in, u
 
 extern "C" size_t vren_reduce_scratch_bytes(uint32_t n)
 {
-    return (size_t)(1 + scalar_grid(n)) * sizeof(uint32_t);
+    // partials for the largest grid any form may use at this size
+    const uint32_t g = scalar_grid(n) > kStreamMaxGrid ? scalar_grid(n) : kStreamMaxGrid;
+    return (size_t)(1 + g) * sizeof(uint32_t);
 }
 
 extern "C" int vren_reduce_u32(vren_stream_t s, int op, const uint32_t* in, uint32_t n, uint32_t* out, void* scratch)
