@@ -206,6 +206,27 @@ uint32_t vren_calc_bvh_root_index(uint32_t leaf_count);         /* build_bvh.cpp
 uint32_t vren_calc_bvh_level_count(uint32_t leaf_count);        /* build_bvh.cpp:189-193 */
 int vren_build_bvh(vren_stream_t s, vren_bvh_node* bvh, uint32_t padded_leaf_count);
 
+/* Karras binary radix tree (extension beside the reference's 32-ary BuildBVH; T. Karras, "Maximizing
+ * Parallelism in the Construction of BVHs, Octrees, and k-d Trees", HPG 2012).  Built over n leaves
+ * already sorted by key: `sorted_pairs` = uvec2(key, payload)[n] in ascending key order (e.g. the
+ * light index of vren_cs_construct_light_bvh, keys = 15- or 30-bit Morton codes); equal keys are
+ * ordered by leaf position.  Node 0 is the root of the n - 1 internal nodes; a child index with
+ * VREN_LBVH_LEAF set names leaf position (index & ~VREN_LBVH_LEAF).  Leaf i's box is
+ * boxes[i >> box_shift] (box_shift 0: one box per leaf; 5 with boxes = level 1 of a 32-ary BVH: the
+ * box of the leaf's 32-leaf group), or an infinite box when boxes is NULL; internal boxes are unions
+ * in IEEE total order, so the tree is deterministic.  Scratch: vren_lbvh_scratch_bytes(n), no
+ * initialisation needed.  n <= 2^24; n < 2 writes nothing. */
+#define VREN_LBVH_LEAF 0x80000000u
+typedef struct vren_lbvh_node {
+    float min[3];
+    uint32_t left;
+    float max[3];
+    uint32_t right;
+} vren_lbvh_node;
+size_t vren_lbvh_scratch_bytes(uint32_t leaf_count);
+int vren_build_lbvh(vren_stream_t s, const uint32_t* sorted_pairs, uint32_t leaf_count, const vren_bvh_node* boxes,
+                    uint32_t box_shift, vren_lbvh_node* nodes, void* scratch);
+
 
 /* ------------------------------------------------------------------------------------------------
  * Clustered shading — vren::clustered_shading::{construct_point_light_bvh, find_unique_cluster_list,
@@ -315,6 +336,21 @@ int vren_cs_assign_lights(vren_stream_t s, const uint32_t* cluster_keys, const u
                           uint32_t light_count, const uint32_t* light_index, const float* view_positions,
                           const float* leaf_spheres, uint32_t* counts, uint32_t* offsets, uint32_t* indices,
                           uint32_t index_capacity, uint32_t* total, void* scratch);
+
+/* assign_lights through a Karras tree (extension): the same counts, offsets and index lists as
+ * vren_cs_assign_lights on the same light BVH, when `nodes` was built by vren_build_lbvh over the
+ * group boxes (boxes = the BVH's level 1, box_shift = 5; boxes = NULL for at most 32 lights).  The
+ * reference's traversal tests the boxes of a light's ancestors and then its sphere; its box test is
+ * monotone in box inclusion, so a light is assigned exactly when its 32-leaf group box and its sphere
+ * overlap the cluster box, which is what this traversal tests, one cluster per thread, writing each
+ * group's lights in the reference's order (groups ascending, lanes descending).  `bvh` supplies the
+ * leaf boxes (and with `leaf_spheres` NULL, the radii); the other arguments are vren_cs_assign_lights'. */
+int vren_cs_assign_lights_lbvh(vren_stream_t s, const uint32_t* cluster_keys, const uint32_t* key_count,
+                               uint32_t key_capacity, const vren_cs_frame* frame, const vren_lbvh_node* nodes,
+                               const vren_bvh_node* bvh, uint32_t light_count, const uint32_t* light_index,
+                               const float* view_positions, const float* leaf_spheres, uint32_t* counts,
+                               uint32_t* offsets, uint32_t* indices, uint32_t index_capacity, uint32_t* total,
+                               void* scratch);
 
 /* shade (clustered_shading.cpp:696-811, shade.comp:69-141, pbr.glsl:6-112): per on-screen pixel
  * whose view depth is below far - 0.001, Cook-Torrance/GGX over the lights of its cluster plus the

@@ -36,6 +36,8 @@ _PROTOS = {
     "oracle_cs_light_bvh": (None, [vp, vp, u32, vp, u32, vp, vp, vp]),
     "oracle_cs_find_unique_clusters": (u32, [vp, vp, u32, u32, vp, i32, vp, u32, vp, i32]),
     "oracle_cs_assign_lights": (u64, [vp, u32, u32, u32, vp, vp, u32, vp, vp, vp, vp, vp, u64, i32]),
+    "oracle_lbvh_build": (None, [vp, vp, u32, vp]),
+    "oracle_cs_assign_lights_lbvh": (u64, [vp, u32, u32, u32, vp, vp, vp, vp, u32, vp, vp, vp, vp, vp, u64, i32]),
     "oracle_cs_shade_f64": (None, [vp, u32, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, u32, i32, i32, vp, vp, i32]),
     "oracle_cs_shade_grad_f64": (None, [vp, u32, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, u32, i32, vp, vp, i32]),
     "oracle_cs_shade_light_loss_f64": (C.c_double, [vp, u32, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, u32, vp, i32, vp]),
@@ -194,6 +196,50 @@ def cs_assign_lights(keys, W: int, H: int, view, bvh, L: int, light_index, view_
                                           _p(np.ascontiguousarray(light_index, np.uint32)),
                                           _p(np.ascontiguousarray(view_pos, np.float32)), _p(counts), _p(offsets),
                                           _p(indices), cap, threads)
+    return counts[:U], offsets[:U], indices[: min(total, cap)].copy(), int(total)
+
+
+def lbvh_group_boxes(bvh, L: int) -> np.ndarray:
+    """Per leaf, the box the reference's traversal effectively tests: its 32-leaf group's AABB (level 1
+    of the 32-ary BVH), or an infinite box when L <= 32 (no box is tested then).  (L, 8) uint32."""
+    b = np.ascontiguousarray(bvh, np.uint32).reshape(-1, 8)
+    out = np.zeros((max(L, 1), 8), np.uint32)
+    if L <= 32:
+        f = out.view(np.float32)
+        f[:, 0:3] = -np.inf
+        f[:, 4:7] = np.inf
+    else:
+        P = 32
+        while P < L:
+            P *= 32
+        out[:L] = b[P + np.arange(L) // 32]
+    return out[:L]
+
+
+def lbvh_build(light_index, boxes, L: int) -> np.ndarray:
+    """Karras binary radix tree over the L sorted leaves with the given per-leaf boxes (vren_oracle.c):
+    (L - 1, 8) uint32 nodes [min xyz, left, max xyz, right] as raw words; leaf children carry bit 31."""
+    nodes = np.zeros((max(L - 1, 1), 8), np.uint32)
+    lib().oracle_lbvh_build(_p(np.ascontiguousarray(light_index, np.uint32)),
+                            _p(np.ascontiguousarray(boxes, np.uint32)), L, _p(nodes))
+    return nodes[: max(L - 1, 0)]
+
+
+def cs_assign_lights_lbvh(keys, W: int, H: int, view, nodes, boxes, bvh, L: int, light_index, view_pos,
+                          threads: int = 0, index_cap: int | None = None):
+    """assign_lights by the Karras tree built over `boxes`: lights whose box and sphere overlap."""
+    U = len(keys)
+    counts = np.zeros(max(U, 1), np.uint32)
+    offsets = np.zeros(max(U, 1), np.uint32)
+    cap = index_cap if index_cap is not None else 1 << 26
+    indices = np.zeros(cap, np.uint32)
+    nd = np.ascontiguousarray(nodes, np.uint32) if len(nodes) else np.zeros((1, 8), np.uint32)
+    total = lib().oracle_cs_assign_lights_lbvh(_p(np.ascontiguousarray(keys, np.uint32)), U, W, H, _view_ptr(view),
+                                               _p(nd), _p(np.ascontiguousarray(boxes, np.uint32)),
+                                               _p(np.ascontiguousarray(bvh, np.uint32)), L,
+                                               _p(np.ascontiguousarray(light_index, np.uint32)),
+                                               _p(np.ascontiguousarray(view_pos, np.float32)), _p(counts),
+                                               _p(offsets), _p(indices), cap, threads)
     return counts[:U], offsets[:U], indices[: min(total, cap)].copy(), int(total)
 
 

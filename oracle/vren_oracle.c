@@ -729,3 +729,154 @@ uint64_t oracle_cs_assign_lights(const uint32_t* keys, uint32_t U, uint32_t W, u
     }
     return total;
 }
+
+/* ================================================================================================
+ * Karras binary radix tree over the sorted light leaves — an extension beside the reference's 32-ary
+ * tree (no counterpart in the reference).  Restated from T. Karras, "Maximizing Parallelism in the
+ * Construction of BVHs, Octrees, and k-d Trees", HPG 2012, section 4 (Figure 4 pseudocode): keys are
+ * the sorted Morton codes augmented with the leaf position, so equal codes still give a unique
+ * order (delta = 32 + clz(i ^ j) for equal codes).  Internal node 0 is the root; a child index with
+ * ORACLE_LBVH_LEAF set names a leaf (a position in the sorted light order, i.e. a level-0 node of
+ * the 32-ary BVH, whose AABB it reuses).  Internal AABBs are unions in IEEE total order.
+ * ================================================================================================ */
+static int lbvh_delta(const uint32_t* light_index, int64_t n, int64_t i, int64_t j)
+{
+    if (j < 0 || j >= n) return -1;
+    const uint32_t a = light_index[2 * i], b = light_index[2 * j];
+    if (a != b) return __builtin_clz(a ^ b);
+    return 32 + __builtin_clz((uint32_t)i ^ (uint32_t)j);
+}
+
+static void lbvh_union(oracle_lbvh_node* nd, const float mn[3], const float mx[3], int first)
+{
+    for (int k = 0; k < 3; ++k) {
+        nd->min[k] = first ? mn[k] : fmin_total(nd->min[k], mn[k]);
+        nd->max[k] = first ? mx[k] : fmax_total(nd->max[k], mx[k]);
+    }
+}
+
+static void lbvh_refit(oracle_lbvh_node* nodes, const oracle_bvh_node* leaves, uint32_t node)
+{
+    oracle_lbvh_node* nd = &nodes[node];
+    const uint32_t ch[2] = {nd->left, nd->right};
+    for (int c = 0; c < 2; ++c) {
+        if (ch[c] & ORACLE_LBVH_LEAF) {
+            const oracle_bvh_node* lf = &leaves[ch[c] & ~ORACLE_LBVH_LEAF];
+            lbvh_union(nd, lf->min, lf->max, c == 0);
+        } else {
+            lbvh_refit(nodes, leaves, ch[c]);
+            lbvh_union(nd, nodes[ch[c]].min, nodes[ch[c]].max, c == 0);
+        }
+    }
+}
+
+void oracle_lbvh_build(const uint32_t* light_index, const oracle_bvh_node* leaves, uint32_t n,
+                       oracle_lbvh_node* nodes)
+{
+    for (int64_t i = 0; i + 1 < (int64_t)n; ++i) {
+        const int d = lbvh_delta(light_index, n, i, i + 1) - lbvh_delta(light_index, n, i, i - 1) >= 0 ? 1 : -1;
+        const int dmin = lbvh_delta(light_index, n, i, i - d);
+        int64_t lmax = 2;
+        while (lbvh_delta(light_index, n, i, i + lmax * d) > dmin) lmax *= 2;
+        int64_t l = 0;
+        for (int64_t t = lmax / 2; t >= 1; t /= 2)
+            if (lbvh_delta(light_index, n, i, i + (l + t) * d) > dmin) l += t;
+        const int64_t j = i + l * d;
+        const int dnode = lbvh_delta(light_index, n, i, j);
+        int64_t s = 0, t = l;
+        do {
+            t = (t + 1) / 2;
+            if (lbvh_delta(light_index, n, i, i + (s + t) * d) > dnode) s += t;
+        } while (t > 1);
+        const int64_t gamma = i + s * d + (d < 0 ? -1 : 0);
+        const int64_t lo = i < j ? i : j, hi = i < j ? j : i;
+        nodes[i].left = (uint32_t)gamma | (lo == gamma ? ORACLE_LBVH_LEAF : 0u);
+        nodes[i].right = (uint32_t)(gamma + 1) | (hi == gamma + 1 ? ORACLE_LBVH_LEAF : 0u);
+    }
+    if (n > 1) lbvh_refit(nodes, leaves, 0);
+}
+
+/* Lights of one cluster by the Karras tree: a light is assigned when its test box boxes[i] overlaps
+ * the cluster box and its sphere (view position, (max.x - min.x) / 2 of its leaf AABB) does too,
+ * written in the reference's order (leaf groups of 32 ascending, lanes of a group descending): the
+ * depth-first walk (left child first) meets leaves in ascending order and each group's hits are
+ * written back to front.  With boxes[i] = the AABB of leaf i's 32-leaf group (infinite when there are
+ * at most 32 lights) this is exactly the 32-ary traversal's rule: its box test is monotone in box
+ * inclusion, so a leaf under an overlapping group box has every ancestor overlapping, and the
+ * reference never tests the leaf's own box.  The tree must then be built over the same boxes so
+ * that its pruning is conservative. */
+static uint32_t lbvh_traverse(const caabb* c, const oracle_lbvh_node* nodes, const oracle_bvh_node* boxes,
+                              const oracle_bvh_node* leaves, uint32_t n, const uint32_t* light_index,
+                              const float* view_pos, uint32_t* out)
+{
+    uint32_t stack[128];
+    int sp = 0;
+    uint32_t cur = n == 1 ? ORACLE_LBVH_LEAF : 0u;
+    uint32_t acc = 0, written = 0, buf[32], grp = 0xFFFFFFFFu;
+    int nb = 0;
+    for (;;) {
+        int descend = 0;
+        if (cur & ORACLE_LBVH_LEAF) {
+            const uint32_t i = cur & ~ORACLE_LBVH_LEAF;
+            const oracle_bvh_node* lf = &leaves[i];
+            if (test_aabb_aabb(c, &boxes[i])) {
+                const uint32_t li = light_index[2 * i + 1];
+                const float o[3] = {view_pos[4 * li], view_pos[4 * li + 1], view_pos[4 * li + 2]};
+                if (test_sphere_aabb(o, (lf->max[0] - lf->min[0]) / 2.0f, c)) {
+                    if (out) {
+                        if ((i >> 5) != grp) {
+                            while (nb > 0) out[written++] = buf[--nb];
+                            grp = i >> 5;
+                        }
+                        buf[nb++] = li;
+                    }
+                    ++acc;
+                }
+            }
+        } else {
+            const oracle_lbvh_node* nd = &nodes[cur];
+            descend = c->mx[0] >= nd->min[0] && c->mn[0] <= nd->max[0] && c->mx[1] >= nd->min[1] &&
+                      c->mn[1] <= nd->max[1] && c->mx[2] >= nd->min[2] && c->mn[2] <= nd->max[2];
+            if (descend) {
+                stack[sp++] = nd->right;
+                cur = nd->left;
+            }
+        }
+        if (!descend) {
+            if (sp == 0) break;
+            cur = stack[--sp];
+        }
+    }
+    if (out)
+        while (nb > 0) out[written++] = buf[--nb];
+    return acc;
+}
+
+uint64_t oracle_cs_assign_lights_lbvh(const uint32_t* keys, uint32_t U, uint32_t W, uint32_t H,
+                                      const oracle_cs_view* v, const oracle_lbvh_node* nodes,
+                                      const oracle_bvh_node* boxes, const oracle_bvh_node* leaves, uint32_t L,
+                                      const uint32_t* light_index, const float* view_pos, uint32_t* counts,
+                                      uint32_t* offsets, uint32_t* indices, uint64_t index_cap, int threads)
+{
+    const uint32_t TX = (W + 31) / 32, TY = (H + 31) / 32;
+    if (L == 0) {
+        for (uint32_t c = 0; c < U; ++c) { counts[c] = 0; offsets[c] = 0; }
+        return 0;
+    }
+    float bnear[ORACLE_SLICES], bfar[ORACLE_SLICES];
+    oracle_cs_slice_table(v, TY, bnear, bfar);
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads(threads))
+    for (int64_t c = 0; c < (int64_t)U; ++c) {
+        caabb box = cluster_aabb(keys[c], TX, TY, v, bnear, bfar);
+        counts[c] = lbvh_traverse(&box, nodes, boxes, leaves, L, light_index, view_pos, NULL);
+    }
+    uint64_t total = 0;
+    for (uint32_t c = 0; c < U; ++c) { offsets[c] = (uint32_t)total; total += counts[c]; }
+    if (total > index_cap) return total;
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads(threads))
+    for (int64_t c = 0; c < (int64_t)U; ++c) {
+        caabb box = cluster_aabb(keys[c], TX, TY, v, bnear, bfar);
+        lbvh_traverse(&box, nodes, boxes, leaves, L, light_index, view_pos, indices + offsets[c]);
+    }
+    return total;
+}

@@ -105,6 +105,28 @@ uint64_t oracle_cs_assign_lights(const uint32_t* keys, uint32_t U, uint32_t W, u
                                  const float* view_pos, uint32_t* counts, uint32_t* offsets, uint32_t* indices,
                                  uint64_t index_cap, int threads);
 
+/* ---- Karras binary radix tree over the sorted light leaves (extension) ---- */
+#define ORACLE_LBVH_LEAF 0x80000000u
+typedef struct {
+    float min[3];
+    uint32_t left;   /* internal node index, or leaf position | ORACLE_LBVH_LEAF */
+    float max[3];
+    uint32_t right;
+} oracle_lbvh_node;
+
+/* n - 1 internal nodes (root = 0) over the n sorted leaves: light_index = uvec2(code, light)[n] in
+ * sorted order, boxes[i] = the box of leaf i (e.g. level 0 of the 32-ary BVH). */
+void oracle_lbvh_build(const uint32_t* light_index, const oracle_bvh_node* boxes, uint32_t n,
+                       oracle_lbvh_node* nodes);
+/* assign_lights by the Karras tree built over `boxes`: lights whose box and sphere (from `leaves`,
+ * the 32-ary level 0) overlap the cluster box, in the reference's list order.  Same return
+ * convention as oracle_cs_assign_lights. */
+uint64_t oracle_cs_assign_lights_lbvh(const uint32_t* keys, uint32_t U, uint32_t W, uint32_t H,
+                                      const oracle_cs_view* v, const oracle_lbvh_node* nodes,
+                                      const oracle_bvh_node* boxes, const oracle_bvh_node* leaves, uint32_t L,
+                                      const uint32_t* light_index, const float* view_pos, uint32_t* counts,
+                                      uint32_t* offsets, uint32_t* indices, uint64_t index_cap, int threads);
+
 /* ---- shading in FP64 (vren_oracle_shade.cpp): forward, forward-mode gradient, per-light loss ---- */
 void oracle_cs_shade_f64(const oracle_cs_view* v, uint32_t W, uint32_t H, const float* depth, const float* normals,
                          const float* albedo, const float* rough, const float* metal, const uint32_t* refs,

@@ -54,6 +54,8 @@ PROTOTYPES: dict[str, tuple] = {
     "vren_calc_bvh_root_index": (u32, [u32]),
     "vren_calc_bvh_level_count": (u32, [u32]),
     "vren_build_bvh": (i32, [vp, vp, u32]),
+    "vren_lbvh_scratch_bytes": (C.c_size_t, [u32]),
+    "vren_build_lbvh": (i32, [vp, vp, u32, vp, u32, vp, vp]),
 }
 
 _LIB: C.CDLL | None = None
@@ -112,6 +114,7 @@ PROTOTYPES_CS: dict[str, tuple] = {
     "vren_cs_find_unique_clusters": (i32, [vp, vp, vp, u32, u32, vp, vp, u32, vp, vp, vp]),
     "vren_cs_assign_lights_scratch_bytes": (sz, [u32]),
     "vren_cs_assign_lights": (i32, [vp, vp, vp, u32, vp, vp, u32, vp, vp, vp, vp, vp, vp, u32, vp, vp]),
+    "vren_cs_assign_lights_lbvh": (i32, [vp, vp, vp, u32, vp, vp, vp, u32, vp, vp, vp, vp, vp, vp, u32, vp, vp]),
     "vren_cs_create": (i32, [C.POINTER(vp), u32, u32, u32, u32]),
     "vren_cs_destroy": (None, [vp]),
     "vren_cs_set_options": (i32, [vp, vp]),

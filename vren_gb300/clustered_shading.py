@@ -141,6 +141,58 @@ class assign_lights:
             indices.numel() if indices is not None else 0, _ptr(total), _ptr(self._scratch)), "assign_lights")
 
 
+class build_lbvh:
+    """Karras binary radix tree over sorted leaves (extension; vren_build_lbvh).  `sorted_pairs` is a
+    uvec2(key, payload) tensor in key order; leaf i's box is boxes[i >> box_shift] (None: infinite).
+    Nodes: int32 tensor of (leaf_count - 1) * 8 words."""
+
+    def __init__(self):
+        self._scratch = None
+
+    @staticmethod
+    def group_boxes(bvh: torch.Tensor, light_count: int):
+        """(boxes, box_shift) giving each light its 32-leaf group box: level 1 of the 32-ary BVH, or
+        no boxes at all for at most 32 lights (the reference tests none then)."""
+        if light_count <= 32:
+            return None, 0
+        P = calc_bvh_padded_leaf_count(light_count)
+        return bvh[P * 8:], 5
+
+    def __call__(self, stream, sorted_pairs: torch.Tensor, leaf_count: int, boxes: torch.Tensor | None,
+                 box_shift: int, nodes: torch.Tensor):
+        need = int(lib().vren_lbvh_scratch_bytes(leaf_count))
+        if self._scratch is None or self._scratch.numel() * 4 < need:
+            self._scratch = alloc_scratch(need, sorted_pairs.device)
+        check(lib().vren_build_lbvh(_stream(stream), _ptr(sorted_pairs), leaf_count,
+                                    _ptr(boxes) if boxes is not None else None, box_shift, _ptr(nodes),
+                                    _ptr(self._scratch)), "build_lbvh")
+
+
+class assign_lights_lbvh:
+    """assign_lights through a Karras tree built over the group boxes (vren_cs_assign_lights_lbvh):
+    the same counts, offsets and lists as assign_lights."""
+
+    def __init__(self):
+        self._scratch = None
+
+    def __call__(self, stream, cluster_keys: torch.Tensor, key_count: torch.Tensor, frame_dev: torch.Tensor,
+                 nodes: torch.Tensor | None, bvh: torch.Tensor, light_count: int, light_index: torch.Tensor,
+                 view_positions: torch.Tensor, counts: torch.Tensor, offsets: torch.Tensor, indices: torch.Tensor,
+                 total: torch.Tensor, leaf_spheres: torch.Tensor | None = None):
+        cap = cluster_keys.numel()
+        need = int(lib().vren_cs_assign_lights_scratch_bytes(cap))
+        if self._scratch is None or self._scratch.numel() * 4 < need:
+            self._scratch = alloc_scratch(need, cluster_keys.device)
+        check(lib().vren_cs_assign_lights_lbvh(
+            _stream(stream), _ptr(cluster_keys), _ptr(key_count), cap, _ptr(frame_dev),
+            _ptr(nodes) if nodes is not None else None, _ptr(bvh) if bvh is not None else None, light_count,
+            _ptr(light_index) if light_index is not None else None,
+            _ptr(view_positions) if view_positions is not None else None,
+            _ptr(leaf_spheres) if leaf_spheres is not None else None,
+            _ptr(counts), _ptr(offsets), _ptr(indices) if indices is not None else None,
+            indices.numel() if indices is not None else 0, _ptr(total), _ptr(self._scratch)), "assign_lights_lbvh")
+
+
 class cluster_and_shade:
     """vren::cluster_and_shade (clustered_shading.hpp:147-182): owns an arena sized at creation."""
 
