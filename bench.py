@@ -244,6 +244,7 @@ def run_ours(args, rank: int, world: int):
     sweep = None if args.quick else primitive_sweep(args, dev, stream, flush, hbm_peak)
     shade = shade_bench(args, dev, stream, flush, ctx)
     batched = None if args.quick else batched_vs_plain(args, dev, stream, flush)
+    lbvh = None if args.quick else lbvh_bench(args, dev, stream, flush, depth, normals, pos, lights, view)
 
     clocks.__exit__(None, None, None)
     clk = clocks.summary()
@@ -299,6 +300,7 @@ def run_ours(args, rank: int, world: int):
             "batched_vs_plain": batched,
             "primitive_sweep": sweep,
             "shade": shade,
+            "karras_lbvh": lbvh,
             "cpu_baseline": cpu,
             "clocks": clk,
             "device_error": err,
@@ -323,6 +325,69 @@ def time_events(stream, fn, warmup, steps, flush=None):
                 evs.append((a, b))
         stream.synchronize()
     return sum(a.elapsed_time(b) for a, b in evs) / len(evs)
+
+
+def lbvh_bench(args, dev, stream, flush, depth, normals, pos, lights, view):
+    """Light assignment through the Karras tree (extension) against the 32-ary traversal, on the
+    cluster-assignment frame (1920x1080, 16384 lights uniform in the frustum box) and on the same
+    frame with 16384 lights packed near the camera (many lights per cluster)."""
+    import torch
+
+    import vren_gb300 as vg
+    import vren_gb300.clustered_shading as cs
+
+    def dense(seed, n):
+        rng = np.random.default_rng(seed)
+        p = np.zeros((n, 4), np.float32)
+        p[:, 0] = rng.uniform(-8, 8, n)
+        p[:, 1] = rng.uniform(-5, 5, n)
+        p[:, 2] = rng.uniform(0.5, 25, n)
+        p[:, 3] = 1
+        q = np.zeros((n, 4), np.float32)
+        q[:, 0:3] = rng.uniform(0, 1, (n, 3))
+        q[:, 3] = np.exp(np.log(2.0) + 0.5 * rng.standard_normal(n)).astype(np.float32) * 0.5
+        return p.reshape(-1), q.reshape(-1)
+
+    frame = cs.frame_to_device(cs.frame_build(view, W, H), dev)
+    T = ((W + 31) // 32) * ((H + 31) // 32)
+    keys = torch.zeros(T * 1024, dtype=torch.int32, device=dev)
+    kc = torch.zeros(1, dtype=torch.int32, device=dev)
+    refs = torch.zeros(W * H, dtype=torch.int32, device=dev)
+    cs.find_unique_cluster_list()(stream, W, H, frame, torch.from_numpy(depth).to(dev),
+                                  torch.from_numpy(normals).to(dev), keys, kc, refs)
+    out = {}
+    for name, (p, q) in (("uniform_frustum_lights", (pos, lights)), ("lights_near_camera", dense(SEED + 77, L))):
+        P = vg.calc_bvh_padded_leaf_count(L)
+        vp = torch.zeros(L * 4, dtype=torch.float32, device=dev)
+        bvh = torch.zeros(vg.calc_bvh_buffer_length(P) * 8, dtype=torch.int32, device=dev)
+        lidx = torch.zeros(L * 2, dtype=torch.int32, device=dev)
+        sph = torch.zeros(P * 4, dtype=torch.float32, device=dev)
+        cs.construct_point_light_bvh(15)(stream, torch.from_numpy(p).to(dev), torch.from_numpy(q).to(dev), L, frame,
+                                         vp, bvh, lidx, sph)
+        nodes = torch.zeros((L - 1) * 8, dtype=torch.int32, device=dev)
+        boxes, shift = cs.build_lbvh.group_boxes(bvh, L)
+        cap = keys.numel()
+        res = []
+        for kind in ("32ary", "lbvh"):
+            counts = torch.zeros(cap, dtype=torch.int32, device=dev)
+            offsets = torch.zeros(cap, dtype=torch.int32, device=dev)
+            indices = torch.zeros(1 << 24, dtype=torch.int32, device=dev)
+            total = torch.zeros(1, dtype=torch.int32, device=dev)
+            a32, al, bl = cs.assign_lights(), cs.assign_lights_lbvh(), cs.build_lbvh()
+            if kind == "32ary":
+                fn = lambda: a32(stream, keys, kc, frame, bvh, L, lidx, vp, counts, offsets, indices, total, sph)
+            else:
+                fn = lambda: al(stream, keys, kc, frame, nodes, bvh, L, lidx, vp, counts, offsets, indices, total, sph)
+                ms_build = time_events(stream, lambda: bl(stream, lidx, L, boxes, shift, nodes), 3, args.steps, flush)
+            ms = time_events(stream, fn, 3, args.steps, flush)
+            res.append((ms, counts, offsets, indices, total))
+        torch.cuda.synchronize()
+        tot = int(res[0][4].cpu()[0])
+        same = (int(res[1][4].cpu()[0]) == tot and torch.equal(res[0][1], res[1][1]) and
+                torch.equal(res[0][3][:tot], res[1][3][:tot]))
+        out[name] = {"assignments": tot, "assign_32ary_ms": round(res[0][0], 5), "assign_lbvh_ms": round(res[1][0], 5),
+                     "build_lbvh_ms": round(ms_build, 5), "lists_identical": bool(same)}
+    return out
 
 
 def radix_bench(args, dev, stream, flush, keys_np, hbm_peak):
@@ -693,7 +758,14 @@ def run_profile(args):
     dev = torch.device("cuda", 0)
     stream = torch.cuda.Stream(device=dev)
     reps = args.warmup + args.steps
-    if args.profile == "find_unique":
+    if args.profile == "frame":
+        # the benchmark's frame: 1920x1080, 16384 lights, one CUDA graph replay per frame
+        depth, normals, pos, lights, _ = make_inputs(0)
+        view = cs.view_from_camera(cs.scene_camera(W, H), "ref")
+        ctx = cs.cluster_and_shade(W, H, 65536, 1 << 24)
+        bufs = [torch.from_numpy(x).to(dev) for x in (depth, normals, pos, lights)]
+        fn = lambda: ctx.cluster(stream, view, W, H, *bufs, L)
+    elif args.profile == "find_unique":
         w, h = 3840, 2160  # 20 B/px -> 166 MB > L2
         depth, normals = scene.depth_planes(SEED, w, h)
         view = cs.view_from_camera(cs.scene_camera(w, h), "ref")
@@ -739,7 +811,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--quick", action="store_true", help="skip the primitive sweep and the large sorts")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--profile", choices=["find_unique", "radix", "scan", "shade", "shade_backward"], default=None,
+    ap.add_argument("--profile", choices=["frame", "find_unique", "radix", "scan", "shade", "shade_backward"],
+                    default=None,
                     help="run one kernel family on a case larger than L2 (for ncu) and exit")
     args = ap.parse_args()
     if args.profile:
