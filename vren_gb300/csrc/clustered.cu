@@ -800,13 +800,23 @@ int cs_enqueue(vren_cluster_and_shade* cs, cudaStream_t st, uint32_t W, uint32_t
 {
     const PdlScope pdl(1);  // consecutive kernels of the frame overlap their launches
     int rc = VREN_OK;
+    // The light BVH and the unique clusters are independent: the BVH is built on the context's second
+    // stream while the tiles run on st; the assignment waits for both.
     if (L > 0) {
-        rc = construct_light_bvh(st, positions, lights, L, cs->frame, cs->opt.morton_bits, cs->opt.sort_digit_bits,
-                                 cs->view_pos, cs->bvh, cs->light_index, cs->spheres, cs->lbvh_scratch);
-        if (rc != VREN_OK) return rc;
+        VREN_CUDA_TRY(cudaEventRecord(cs->ev_fork, st));
+        VREN_CUDA_TRY(cudaStreamWaitEvent(cs->aux, cs->ev_fork, 0));
+        rc = construct_light_bvh(cs->aux, positions, lights, L, cs->frame, cs->opt.morton_bits,
+                                 cs->opt.sort_digit_bits, cs->view_pos, cs->bvh, cs->light_index, cs->spheres,
+                                 cs->lbvh_scratch);
+        VREN_CUDA_TRY(cudaEventRecord(cs->ev_bvh, cs->aux));
+        if (rc != VREN_OK) {
+            cudaStreamWaitEvent(st, cs->ev_bvh, 0);  // rejoin before returning (a capture must end joined)
+            return rc;
+        }
     }
     rc = launch_find_unique(st, depth, normals, W, H, cs->frame, cs->keys, cs->key_cap, cs->key_count, cs->refs,
                             static_cast<uint32_t*>(cs->fuc_scratch));
+    if (L > 0) VREN_CUDA_TRY(cudaStreamWaitEvent(st, cs->ev_bvh, 0));
     if (rc != VREN_OK) return rc;
     return assign_lights(st, cs->keys, cs->key_count, cs->key_cap, cs->frame, cs->bvh, L, cs->light_index,
                          cs->view_pos, cs->spheres, cs->counts, cs->offsets, cs->indices, cs->max_assign, cs->total,
@@ -881,6 +891,16 @@ extern "C" int vren_cs_create(vren_cluster_and_shade** out, uint32_t max_width, 
     cs->lbvh_scratch = a + o_lbvh;
     cs->fuc_scratch = a + o_fuc;
     cs->assign_scratch = a + o_asg;
+    // the second and third streams (light BVH beside the tiles; banded uploads) and their events
+    bool ok = cudaStreamCreateWithFlags(&cs->aux, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&cs->up, cudaStreamNonBlocking) == cudaSuccess;
+    for (cudaEvent_t* e : {&cs->ev_fork, &cs->ev_bvh, &cs->ev_fuc, &cs->ev_join, &cs->ev_join_up, &cs->ev_band[0],
+                           &cs->ev_band[1], &cs->ev_band[2], &cs->ev_band[3]})
+        ok = ok && cudaEventCreateWithFlags(e, cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+        vren_cs_destroy(cs);
+        return VREN_ERR_CUDA;
+    }
     *out = cs;
     return VREN_OK;
 }
@@ -1060,7 +1080,7 @@ extern "C" int vren_cs_cluster_host(vren_cluster_and_shade* cs, vren_stream_t s,
     if (width > cs->max_w || height > cs->max_h || light_count > cs->max_lights) return VREN_ERR_CAPACITY;
     if (light_count > 0 && (!light_positions || !point_lights)) return VREN_ERR_ARG;
     cudaStream_t st = as_stream(s);
-    if (!cs->inputs) {  // first use: device copies of the inputs, the second stream and its events
+    if (!cs->inputs) {  // first use: device copies of the inputs
         cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
         VREN_CUDA_TRY(cudaStreamIsCapturing(st, &cap));
         if (cap != cudaStreamCaptureStatusNone) return VREN_ERR_STATE;
@@ -1075,11 +1095,6 @@ extern "C" int vren_cs_cluster_host(vren_cluster_and_shade* cs, vren_stream_t s,
         cs->in_normals = reinterpret_cast<float*>(cs->inputs + o_n);
         cs->in_pos = reinterpret_cast<float*>(cs->inputs + o_p);
         cs->in_lights = reinterpret_cast<float*>(cs->inputs + o_l);
-        VREN_CUDA_TRY(cudaStreamCreateWithFlags(&cs->aux, cudaStreamNonBlocking));
-        VREN_CUDA_TRY(cudaStreamCreateWithFlags(&cs->up, cudaStreamNonBlocking));
-        for (cudaEvent_t* e : {&cs->ev_fork, &cs->ev_bvh, &cs->ev_fuc, &cs->ev_join, &cs->ev_join_up, &cs->ev_band[0],
-                               &cs->ev_band[1], &cs->ev_band[2], &cs->ev_band[3]})
-            VREN_CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     }
     int rc = refresh_frame(cs, st, view, width, height, offscreen);
     if (rc != VREN_OK) return rc;
