@@ -76,9 +76,12 @@ uint32_t vren_set_wait_limit(uint32_t rounds);
  *                          tiles by bulk copies (2 and 3 whenever the alignment allows)
  *   VREN_TUNE_REDUCE_FORM  scalar reduce form: 0 = automatic (= 1), 1 = grid-stride loop of uint4
  *                          loads, 2..5 = streaming through shared-memory stages filled by bulk copies
- *                          (16 KB x 6 contiguous, 16 KB x 6 interleaved, 32 KB x 6, 8 KB x 12) */
+ *                          (16 KB x 6 contiguous, 16 KB x 6 interleaved, 32 KB x 6, 8 KB x 12)
+ *   VREN_TUNE_LIGHT_BVH_CLUSTER  light BVH of 2049..32768 lights (15-bit codes): 1 = one kernel on a
+ *                          16-CTA thread-block cluster when the device can hold one (default),
+ *                          0 = the multi-kernel path */
 enum { VREN_TUNE_SCAN_SLICES = 0, VREN_TUNE_SPIN_POLLS = 1, VREN_TUNE_RADIX_RANK = 2, VREN_TUNE_RADIX_ITEMS = 3,
-       VREN_TUNE_SCAN_STAGED = 4, VREN_TUNE_REDUCE_FORM = 5, VREN_TUNE_COUNT = 6 };
+       VREN_TUNE_SCAN_STAGED = 4, VREN_TUNE_REDUCE_FORM = 5, VREN_TUNE_LIGHT_BVH_CLUSTER = 6, VREN_TUNE_COUNT = 7 };
 int vren_tuning_set(int knob, int value);
 int vren_tuning_get(int knob);
 

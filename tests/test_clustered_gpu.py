@@ -81,6 +81,38 @@ def test_construct_light_bvh(cuda, L, morton_bits):
     assert np.all(s[L:, 3] == -1)
 
 
+@pytest.mark.parametrize("L", [2049, 5000, 16384, 32767, 32768])
+@pytest.mark.parametrize("cluster", [1, 0])
+@pytest.mark.parametrize("duplicates", [False, True])
+def test_light_bvh_cluster_and_multi_kernel_paths(cuda, L, cluster, duplicates):
+    """2049..32768 lights: the one-kernel 16-CTA cluster path and the multi-kernel path both give the
+    oracle's BVH, light index, view positions and leaf spheres (equal Morton codes included)."""
+    lib = vg.lib()
+    knob = vg._lib.TUNE["light_bvh_cluster"]
+    assert lib.vren_tuning_set(knob, cluster) == 0
+    try:
+        W, H = 1280, 720
+        view = make_view(W, H, moved=(L % 2 == 1))
+        if duplicates:
+            pos = np.tile(np.array([1.0, 2.0, 30.0, 1.0], np.float32), L)
+            pos[4 * 7: 4 * 7 + 3] = [5.0, -1.0, 60.0]
+            li = np.tile(np.array([0.5, 0.5, 0.5, 2.0], np.float32), L)
+        else:
+            pos, li = scene.lights(77 + L, L, W, H)
+        _, vp, bvh, lidx, sph = run_light_bvh(cuda, pos, li, L, view, W, H)
+        assert vg.device_error() == 0
+        evp, ebvh, elidx = oracle.cs_light_bvh(pos, li, L, view, 15)
+        assert np.array_equal(vp.cpu().numpy().view(np.uint32)[: 4 * L], evp.view(np.uint32))
+        assert np.array_equal(u32(lidx)[: 2 * L], elidx)
+        assert np.array_equal(u32(bvh).reshape(-1, 8), ebvh)
+        s = sph.cpu().numpy().reshape(-1, 4)
+        order = elidx.reshape(-1, 2)[:, 1]
+        assert np.array_equal(s[:L, 0:3], evp.reshape(-1, 4)[order, 0:3])
+        assert np.all(s[L:, 3] == -1)
+    finally:
+        lib.vren_tuning_set(knob, 1)
+
+
 @pytest.mark.parametrize("L", [2000, 3000])
 def test_construct_light_bvh_duplicate_positions(cuda, L):
     """Equal Morton codes (and a zero extent) exercise the stable tie order and the NaN path, in the

@@ -59,6 +59,7 @@ static int g_tuning[VREN_TUNE_COUNT] = {
     /* VREN_TUNE_RADIX_ITEMS */ 0,
     /* VREN_TUNE_SCAN_STAGED */ 0,
     /* VREN_TUNE_REDUCE_FORM */ 0,
+    /* VREN_TUNE_LIGHT_BVH_CLUSTER */ 1,
 };
 int tuning(int knob) { return (knob >= 0 && knob < VREN_TUNE_COUNT) ? g_tuning[knob] : 0; }
 }  // namespace vren_gb300
@@ -84,6 +85,9 @@ extern "C" int vren_tuning_set(int knob, int value)
         break;
     case VREN_TUNE_REDUCE_FORM:
         if (value < 0 || value > 5) return VREN_ERR_ARG;
+        break;
+    case VREN_TUNE_LIGHT_BVH_CLUSTER:
+        if (value != 0 && value != 1) return VREN_ERR_ARG;
         break;
     default: break;
     }

@@ -291,6 +291,314 @@ __global__ void __launch_bounds__(kSmallThreads) lbvh_small_kernel(const float4*
     }
 }
 
+// ------------------------------------------------------------------------------------------------
+// construct_point_light_bvh for 2049..32768 lights (15-bit codes), whose padded tree always has 32768
+// leaves: one kernel on a cluster of 16 CTAs (thread-block cluster, distributed shared memory).
+// CTA r owns leaf slots [2048 r, 2048 r + 2048).  Hardware cluster barriers replace the kernel
+// boundaries of the multi-kernel path:
+//   1. each CTA transforms its lights to view space and publishes its min/max; every CTA reads all
+//      sixteen (DSMEM) and computes the same bounds, then the Morton keys (code << 16 | light);
+//   2. two stable 8-bit passes over bits 16..31: each CTA ranks its keys (ballots, per-warp digit
+//      counters) and publishes its digit counts; each CTA reads the 16 x 256 counts and stores every
+//      key straight into the shared memory of the CTA that owns its destination slot;
+//   3. each CTA writes its slots' light index, leaves, spheres and their two parent levels
+//      (light_leaves_block), and CTA 0 the root once all level-2 nodes are written.
+// The output is the multi-kernel path's, bit for bit.
+// ------------------------------------------------------------------------------------------------
+constexpr int kClusterCtas = 16;
+constexpr uint32_t kClusterSlots = 2048;
+constexpr int kClusterThreads = 1024;
+constexpr uint32_t kClusterMaxLights = kClusterCtas * kClusterSlots;  // 32768 = the padded leaf count
+constexpr size_t kClusterSmem = (2 * kClusterSlots + 32 * 256) * sizeof(uint32_t);
+
+__device__ __forceinline__ void cluster_barrier()
+{
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// Address of `p` (this CTA's shared memory) in the shared memory of CTA `rank` of the cluster.
+__device__ __forceinline__ uint32_t dsmem_addr(const void* p, uint32_t rank)
+{
+    uint32_t out;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;"
+                 : "=r"(out)
+                 : "r"(static_cast<uint32_t>(__cvta_generic_to_shared(p))), "r"(rank));
+    return out;
+}
+__device__ __forceinline__ uint32_t dsmem_ld(uint32_t addr)
+{
+    uint32_t v;
+    asm volatile("ld.shared::cluster.u32 %0, [%1];" : "=r"(v) : "r"(addr) : "memory");
+    return v;
+}
+__device__ __forceinline__ void dsmem_st(uint32_t addr, uint32_t v)
+{
+    asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
+}
+
+__global__ void __launch_bounds__(kClusterThreads) lbvh_cluster_kernel(
+    const float4* __restrict__ positions, const float4* __restrict__ lights, uint32_t L,
+    const vren_cs_frame* __restrict__ F, float4* __restrict__ view_pos, uint2* __restrict__ light_index,
+    vren_bvh_node* __restrict__ bvh, float4* __restrict__ spheres)
+{
+    pdl_enter();
+    extern __shared__ uint32_t s_dyn[];
+    uint32_t* A = s_dyn;                 // this CTA's keys (code << 16 | light), by slot
+    uint32_t* B = A + kClusterSlots;     // destination of a pass (written by every CTA)
+    uint32_t* cnt = B + kClusterSlots;   // [32 warps][256 digits]
+    __shared__ uint32_t s_mm[32][6];
+    __shared__ uint32_t s_cta_mm[6];     // read by the other CTAs
+    __shared__ uint32_t s_bound[6];
+    __shared__ uint32_t s_hist[256];     // this CTA's digit counts, read by the other CTAs
+    __shared__ uint32_t s_base[256];     // global first slot of each digit for this CTA's keys
+    __shared__ uint32_t s_wsum[32];
+    __shared__ NodeF s_parent[32];
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const uint32_t rank = blockIdx.x;  // the grid is one cluster
+    const uint32_t base = rank * kClusterSlots;
+    const uint32_t own = L > base ? (L - base < kClusterSlots ? L - base : kClusterSlots) : 0u;
+
+    // 1. view positions, bounds, Morton keys
+    const float* V = F->view.view;
+    uint32_t kmin[3] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu}, kmax[3] = {0u, 0u, 0u};
+    for (uint32_t j = tid; j < own; j += kClusterThreads) {
+        const float4 v = light_to_view(V, positions[base + j]);
+        view_pos[base + j] = v;
+        const float c[3] = {v.x, v.y, v.z};
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const uint32_t key = fkey(c[a]);
+            kmin[a] = key < kmin[a] ? key : kmin[a];
+            kmax[a] = key > kmax[a] ? key : kmax[a];
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        kmin[a] = __reduce_min_sync(0xFFFFFFFFu, kmin[a]);
+        kmax[a] = __reduce_max_sync(0xFFFFFFFFu, kmax[a]);
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            s_mm[warp][a] = kmin[a];
+            s_mm[warp][3 + a] = kmax[a];
+        }
+    }
+    __syncthreads();
+    if (tid < 6) {
+        uint32_t v = tid < 3 ? 0xFFFFFFFFu : 0u;
+        for (int w = 0; w < 32; ++w) {
+            const uint32_t x = s_mm[w][tid];
+            v = tid < 3 ? (x < v ? x : v) : (x > v ? x : v);
+        }
+        s_cta_mm[tid] = v;
+    }
+    cluster_barrier();
+    if (tid < 6) {
+        uint32_t v = tid < 3 ? 0xFFFFFFFFu : 0u;
+        for (uint32_t c = 0; c < kClusterCtas; ++c) {
+            const uint32_t x = dsmem_ld(dsmem_addr(&s_cta_mm[tid], c));
+            v = tid < 3 ? (x < v ? x : v) : (x > v ? x : v);
+        }
+        s_bound[tid] = v;
+    }
+    __syncthreads();
+    float mn[3], mx[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        mn[a] = unkey(s_bound[a]);
+        mx[a] = unkey(s_bound[3 + a]);
+    }
+    for (uint32_t j = tid; j < own; j += kClusterThreads)
+        A[j] = (morton_code(view_pos[base + j], mn, mx, 5u) << 16) | (base + j);
+    __syncthreads();
+    // 2. two stable 8-bit passes over bits 16..31 across the cluster
+    for (uint32_t pass = 0; pass < 2; ++pass) {
+        const uint32_t* src = pass ? B : A;
+        uint32_t* dst = pass ? A : B;
+        const uint32_t shift = 16u + 8u * pass;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) cnt[tid * 8 + k] = 0u;
+        __syncthreads();
+        uint32_t rnk[2], dig[2];
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const uint32_t idx = warp * 64u + (uint32_t)j * 32u + lane;
+            const bool valid = idx < own;
+            const uint32_t d = valid ? (src[idx] >> shift) & 0xFFu : 0u;
+            uint32_t peers = __ballot_sync(0xFFFFFFFFu, valid);
+#pragma unroll
+            for (int b = 0; b < 8; ++b) {
+                const uint32_t m = __ballot_sync(0xFFFFFFFFu, (d >> b) & 1u);
+                const uint32_t mine = (uint32_t)((int32_t)(d << (31 - b)) >> 31);
+                peers &= ~(m ^ mine);
+            }
+            const uint32_t below = peers & lanemask_lt();
+            const uint32_t before = valid ? cnt[warp * 256u + d] : 0u;
+            __syncwarp();
+            if (valid && below == 0) cnt[warp * 256u + d] = before + __popc(peers);
+            __syncwarp();
+            rnk[j] = valid ? before + __popc(below) : 0xFFFFFFFFu;
+            dig[j] = d;
+        }
+        __syncthreads();
+        // thread d: this CTA's count of digit d, and the warp prefixes of d in place
+        if (tid < 256) {
+            uint32_t run = 0;
+            for (int w = 0; w < 32; ++w) {
+                const uint32_t c = cnt[w * 256 + tid];
+                cnt[w * 256 + tid] = run;
+                run += c;
+            }
+            s_hist[tid] = run;
+        }
+        cluster_barrier();  // every CTA's digit counts are published
+        if (warp < 8) {
+            // thread d: the cluster's count of digit d and that of the lower-ranked CTAs
+            uint32_t tot = 0, pre = 0;
+            for (uint32_t c = 0; c < kClusterCtas; ++c) {
+                const uint32_t h = dsmem_ld(dsmem_addr(&s_hist[tid], c));
+                tot += h;
+                pre += c < rank ? h : 0u;
+            }
+            uint32_t incl = tot;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                if (lane >= (uint32_t)o) incl += y;
+            }
+            if (lane == 31) s_wsum[warp] = incl;
+            __syncwarp();
+            s_base[tid] = incl - tot + pre;  // the other warps' sums are added below
+        }
+        __syncthreads();
+        if (tid < 256) {
+            uint32_t add = 0;
+            for (uint32_t w = 0; w < warp; ++w) add += s_wsum[w];
+            s_base[tid] += add;
+        }
+        __syncthreads();
+        // every key straight into the slot it sorts to, in the CTA that owns that slot
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            if (rnk[j] != 0xFFFFFFFFu) {
+                const uint32_t idx = warp * 64u + (uint32_t)j * 32u + lane;
+                const uint32_t slot = s_base[dig[j]] + cnt[warp * 256u + dig[j]] + rnk[j];
+                dsmem_st(dsmem_addr(&dst[slot & (kClusterSlots - 1u)], slot / kClusterSlots), src[idx]);
+            }
+        }
+        cluster_barrier();  // all keys have arrived; the counts may be reused
+    }
+
+    // 3. light index, leaves, spheres, levels 1 and 2 of this CTA's slots (as light_leaves_block),
+    //    then the root over the 32 level-2 nodes
+    constexpr uint32_t P = kClusterMaxLights;
+#pragma unroll 1
+    for (uint32_t h = 0; h < 2; ++h) {
+        const uint32_t j = h * 1024u + tid, i = base + j;
+        NodeF leaf;
+        float4 sph;
+        if (j < own) {
+            const uint32_t key = A[j], li = key & 0xFFFFu;
+            light_index[i] = make_uint2(key >> 16, li);
+            const float4 o = __ldcg(view_pos + li);  // written by another CTA of this cluster
+            const float r = __ldg(&lights[li].w);
+            leaf.mn[0] = fsub(o.x, r); leaf.mn[1] = fsub(o.y, r); leaf.mn[2] = fsub(o.z, r);
+            leaf.mx[0] = fadd(o.x, r); leaf.mx[1] = fadd(o.y, r); leaf.mx[2] = fadd(o.z, r);
+            leaf.next = VREN_BVH_LEAF_NODE;
+            sph = make_float4(o.x, o.y, o.z, fdiv(fsub(leaf.mx[0], leaf.mn[0]), 2.0f));
+        } else {
+            leaf.mn[0] = leaf.mn[1] = leaf.mn[2] = __int_as_float(0x7F800000);
+            leaf.mx[0] = leaf.mx[1] = leaf.mx[2] = __int_as_float(0xFF800000);
+            leaf.next = VREN_BVH_INVALID_NODE;
+            sph = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+        }
+        leaf.pad = 0u;
+        store_node(bvh, i, leaf);
+        if (spheres) spheres[i] = sph;
+        const NodeF p = warp_parent(leaf, true, i & ~31u);
+        if (lane == 0) {
+            store_node(bvh, P + (i >> 5), p);
+            s_parent[warp] = p;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            const uint32_t chunk = rank * 2u + h;
+            const NodeF g = warp_parent(s_parent[lane], true, P + chunk * 32u);
+            if (lane == 0) store_node(bvh, P + P / 32u + chunk, g);
+        }
+        __syncthreads();
+    }
+    cluster_barrier();  // every level-2 node is written
+    if (rank == 0 && warp == 0) {
+        const float4* q = reinterpret_cast<const float4*>(bvh + P + P / 32u + lane);
+        const float4 lo = __ldcg(q), hi = __ldcg(q + 1);
+        NodeF c;
+        c.mn[0] = lo.x; c.mn[1] = lo.y; c.mn[2] = lo.z; c.next = __float_as_uint(lo.w);
+        c.mx[0] = hi.x; c.mx[1] = hi.y; c.mx[2] = hi.z; c.pad = __float_as_uint(hi.w);
+        const NodeF root = warp_parent(c, true, P + P / 32u);
+        if (lane == 0) store_node(bvh, P + P / 32u + 32u, root);
+    }
+}
+
+// Whether a 16-CTA cluster of lbvh_cluster_kernel can be resident on the current device (checked once).
+static bool cluster_path_available()
+{
+    static int state = -1;
+    if (state < 0) {
+        bool ok = cudaFuncSetAttribute(lbvh_cluster_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+                      cudaSuccess &&
+                  cudaFuncSetAttribute(lbvh_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)kClusterSmem) == cudaSuccess;
+        int clusters = 0;
+        if (ok) {
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(kClusterCtas);
+            cfg.blockDim = dim3(kClusterThreads);
+            cfg.dynamicSmemBytes = kClusterSmem;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeClusterDimension;
+            attr[0].val.clusterDim.x = kClusterCtas;
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            ok = cudaOccupancyMaxActiveClusters(&clusters, lbvh_cluster_kernel, &cfg) == cudaSuccess;
+        }
+        if (!ok) cudaGetLastError();  // clear: the multi-kernel path is used instead
+        state = ok && clusters >= 1 ? 1 : 0;
+    }
+    return state == 1;
+}
+
+static int launch_lbvh_cluster(cudaStream_t st, const float* positions, const float* lights, uint32_t L,
+                               const vren_cs_frame* frame, float* view_pos, vren_bvh_node* bvh, uint32_t* light_index,
+                               float* spheres)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(kClusterCtas);
+    cfg.blockDim = dim3(kClusterThreads);
+    cfg.dynamicSmemBytes = kClusterSmem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[2];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kClusterCtas;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (g_pdl) {
+        attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[1].val.programmaticStreamSerializationAllowed = 1;
+        cfg.numAttrs = 2;
+    }
+    cudaLaunchKernelEx(&cfg, lbvh_cluster_kernel, reinterpret_cast<const float4*>(positions),
+                       reinterpret_cast<const float4*>(lights), L, frame, reinterpret_cast<float4*>(view_pos),
+                       reinterpret_cast<uint2*>(light_index), bvh, reinterpret_cast<float4*>(spheres));
+    VREN_LAUNCH_CHECK();
+    return VREN_OK;
+}
+
 static int construct_light_bvh(cudaStream_t st, const float* positions, const float* lights, uint32_t L,
                                const vren_cs_frame* frame, uint32_t morton_bits, uint32_t digit_bits, float* view_pos,
                                vren_bvh_node* bvh, uint32_t* light_index, float* spheres, void* scratch)
@@ -299,6 +607,9 @@ static int construct_light_bvh(cudaStream_t st, const float* positions, const fl
     const LbvhLayout lay = lbvh_layout(L, morton_bits, digit_bits);
     char* sc = static_cast<char*>(scratch);
     uint32_t* hdr = reinterpret_cast<uint32_t*>(sc);
+    if (morton_bits != 30 && L > kSmallPathLights && L <= kClusterMaxLights &&
+        tuning(VREN_TUNE_LIGHT_BVH_CLUSTER) != 0 && cluster_path_available())
+        return launch_lbvh_cluster(st, positions, lights, L, frame, view_pos, bvh, light_index, spheres);
     if (morton_bits != 30 && L <= kSmallPathLights) {
         static bool attr_set = false;  // the attribute is per function, set once
         if (!attr_set) {
