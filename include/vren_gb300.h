@@ -79,9 +79,12 @@ uint32_t vren_set_wait_limit(uint32_t rounds);
  *                          (16 KB x 6 contiguous, 16 KB x 6 interleaved, 32 KB x 6, 8 KB x 12)
  *   VREN_TUNE_LIGHT_BVH_CLUSTER  light BVH of 2049..32768 lights (15-bit codes): 1 = one kernel on a
  *                          16-CTA thread-block cluster when the device can hold one (default),
- *                          0 = the multi-kernel path */
+ *                          0 = the multi-kernel path
+ *   VREN_TUNE_ASSIGN_FUSED assign_lights: 0 = count kernel, exclusive scan, write kernel (default),
+ *                          1 = one kernel (count, look-back over the cluster counts, write) */
 enum { VREN_TUNE_SCAN_SLICES = 0, VREN_TUNE_SPIN_POLLS = 1, VREN_TUNE_RADIX_RANK = 2, VREN_TUNE_RADIX_ITEMS = 3,
-       VREN_TUNE_SCAN_STAGED = 4, VREN_TUNE_REDUCE_FORM = 5, VREN_TUNE_LIGHT_BVH_CLUSTER = 6, VREN_TUNE_COUNT = 7 };
+       VREN_TUNE_SCAN_STAGED = 4, VREN_TUNE_REDUCE_FORM = 5, VREN_TUNE_LIGHT_BVH_CLUSTER = 6,
+       VREN_TUNE_ASSIGN_FUSED = 7, VREN_TUNE_COUNT = 8 };
 int vren_tuning_set(int knob, int value);
 int vren_tuning_get(int knob);
 
@@ -332,7 +335,12 @@ int vren_cs_find_unique_clusters(vren_stream_t s, const float* depth, const floa
  * first *key_count of which are written; `total` (optional) receives the number of assignments;
  * indices beyond index_capacity are dropped and VREN_ERR_CAPACITY recorded.  `leaf_spheres` is
  * optional (from vren_cs_construct_light_bvh); without it the leaf data are read from the BVH,
- * the light index and the view positions as the reference does. */
+ * the light index and the view positions as the reference does.  Count kernel, exclusive scan and
+ * write kernel (clusters with no light skip the second traversal); VREN_TUNE_ASSIGN_FUSED selects
+ * one kernel in which a warp per cluster counts, resolves its first index by decoupled look-back over
+ * the preceding clusters' counts, then writes.  The scratch (vren_cs_assign_lights_scratch_bytes)
+ * must be zero-filled before its first use (and again after VREN_ERR_TIMEOUT); calls sharing it must
+ * not overlap. */
 size_t vren_cs_assign_lights_scratch_bytes(uint32_t key_capacity);
 int vren_cs_assign_lights(vren_stream_t s, const uint32_t* cluster_keys, const uint32_t* key_count,
                           uint32_t key_capacity, const vren_cs_frame* frame, const vren_bvh_node* bvh,

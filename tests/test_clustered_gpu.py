@@ -296,6 +296,42 @@ def test_assign_lights_dense(cuda, L, spheres):
     assert et > 0 or L == 1
 
 
+@pytest.mark.parametrize("fused", [1, 0])
+@pytest.mark.parametrize("L,seed", [(20, 20), (5000, 5000), (40000, 40000)])
+def test_assign_lights_fused_and_three_kernel_forms(cuda, fused, L, seed):
+    """One kernel (chunk totals resolved by look-back) and count/scan/write give the oracle's counts,
+    offsets and lists; three calls in a row reuse the scratch (epoch-tagged status words)."""
+    lib = vg.lib()
+    knob = vg._lib.TUNE["assign_fused"]
+    assert lib.vren_tuning_set(knob, fused) == 0
+    try:
+        W, H = 640, 360
+        view = make_view(W, H)
+        depth, normals = scene.depth_planes(77, W, H)
+        pos, li = dense_lights(seed, L)
+        evp, ebvh, elidx = oracle.cs_light_bvh(pos, li, L, view, 15)
+        frame, keys, kc, refs = run_unique(cuda, depth, normals, W, H, view)
+        _, vp, bvh, lidx, sph = run_light_bvh(cuda, pos, li, L, view, W, H)
+        U = int(u32(kc)[0])
+        ec, eo, ei, et = oracle.cs_assign_lights(u32(keys)[:U], W, H, view, ebvh, L, elidx, evp)
+        assert et > 0
+        stage = cs.assign_lights()  # one scratch for all calls
+        cap = keys.numel()
+        for spheres in (True, False, True):
+            counts = torch.zeros(cap, dtype=torch.int32, device=cuda)
+            offsets = torch.zeros(cap, dtype=torch.int32, device=cuda)
+            indices = torch.zeros(1 << 22, dtype=torch.int32, device=cuda)
+            total = torch.zeros(1, dtype=torch.int32, device=cuda)
+            stage(None, keys, kc, frame, bvh, L, lidx, vp, counts, offsets, indices, total,
+                  leaf_spheres=sph if spheres else None)
+            assert int(u32(total)[0]) == et
+            assert np.array_equal(u32(counts)[:U], ec) and np.array_equal(u32(offsets)[:U], eo)
+            assert np.array_equal(u32(indices)[:et], ei)
+        assert vg.device_error() == 0
+    finally:
+        lib.vren_tuning_set(knob, 0)
+
+
 @pytest.mark.parametrize("W,H,L", [(1920, 1080, 16384), (1280, 720, 65536), (640, 360, 1024)])
 def test_assign_lights_baseline_scene(cuda, W, H, L):
     view = make_view(W, H)

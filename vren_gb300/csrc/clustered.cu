@@ -17,6 +17,7 @@ VREN_DEFINE_ERROR_WORD(cs)
 }  // namespace vren_gb300
 
 #include "cs_device.cuh"
+#include "lookback.cuh"
 
 namespace vren_gb300 {
 
@@ -766,8 +767,78 @@ __global__ void __launch_bounds__(256) assign_kernel(AssignArgs a, LevelBase lb)
     uint32_t U = *a.key_count;
     if (U > a.key_cap) U = a.key_cap;
     for (uint32_t c = gw; c < U; c += nw) {
+        if (WRITE && a.counts[c] == 0u) continue;  // nothing to write: skip the second traversal
         const uint32_t acc = assign_cluster<LC, WRITE, SPHERES>(a, lb, a.keys[c], WRITE ? a.offsets[c] : 0u, lane);
         if (!WRITE && lane == 0) a.counts[c] = acc;
+    }
+}
+
+// assign_lights in one kernel: every warp takes one cluster at a time by ticket, counts its lights
+// (first traversal), publishes the count, resolves the cluster's first index by decoupled look-back
+// over the counts of the preceding clusters (the count -> exclusive scan -> offsets step of
+// assign_lights.comp and clustered_shading.cpp:612-640), then writes the list (second traversal).
+// A warp holds one ticket at a time and publishes its count before it waits on anything, so the
+// smallest unfinished cluster never waits on a later one.  One cluster per ticket keeps every warp
+// on a single pair of traversals (chunks of 16 clusters per warp measured 3x slower: the traversals
+// are chains of dependent loads).  Measured at 1920x1080 / 16384 lights: 31 us against 27 us for
+// count kernel + scan + write kernel, whose scan costs less than this kernel's look-back chain over
+// thousands of clusters, so the three-kernel form is the default (VREN_TUNE_ASSIGN_FUSED = 0).
+// Scratch: [0..1] 64-bit [epoch | ticket], [2] completion counter, [3] unused, then one 64-bit status
+// word per cluster; the last CTA to finish opens the next call's epoch.
+constexpr uint32_t kAssignHeaderWords = 4;
+
+size_t assign_fused_scratch_bytes(uint32_t key_cap)
+{
+    return (size_t)(kAssignHeaderWords * sizeof(uint32_t) + (uint64_t)(key_cap ? key_cap : 1) * sizeof(uint64_t));
+}
+
+template <int LC, bool SPHERES>
+__global__ void __launch_bounds__(256) assign_fused_kernel(AssignArgs a, LevelBase lb, uint32_t* __restrict__ offsets,
+                                                           uint32_t* __restrict__ scratch, uint32_t* __restrict__ total,
+                                                           uint32_t wait_limit, uint32_t spin)
+{
+    pdl_enter();
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t U = *a.key_count;
+    if (U > a.key_cap) U = a.key_cap;
+    uint64_t* status = reinterpret_cast<uint64_t*>(scratch + kAssignHeaderWords);
+    if (U == 0 && total && blockIdx.x == 0 && threadIdx.x == 0) *total = 0u;
+    uint32_t epoch = 0;
+    bool timed_out = false;
+    for (;;) {
+        unsigned long long w = 0;
+        if (lane == 0) w = atomicAdd(reinterpret_cast<unsigned long long*>(scratch), 1ull);
+        w = __shfl_sync(0xFFFFFFFFu, w, 0);
+        const uint32_t c = (uint32_t)w;
+        epoch = (uint32_t)(w >> 32) & 0x3FFFFFFFu;
+        if (c >= U) break;
+        const uint32_t key = a.keys[c];
+        const uint32_t cnt = assign_cluster<LC, false, SPHERES>(a, lb, key, 0u, lane);
+        uint32_t prefix = 0;
+        if (c == 0) {
+            if (lane == 0) st_relaxed_u64(status, make_status(epoch, 2u, cnt));
+        } else {
+            if (lane == 0) st_relaxed_u64(status + c, make_status(epoch, 1u, cnt));
+            bool lb_timeout = false;
+            prefix = warp_lookback(status, c, 0u, epoch, lane, wait_limit, spin, lb_timeout);
+            if (lb_timeout) timed_out = true;
+            if (lane == 0) st_relaxed_u64(status + c, make_status(epoch, 2u, prefix + cnt));
+        }
+        if (lane == 0) {
+            a.counts[c] = cnt;
+            offsets[c] = prefix;
+            if (c == U - 1 && total) *total = prefix + cnt;
+        }
+        if (cnt) assign_cluster<LC, true, SPHERES>(a, lb, key, prefix, lane);
+    }
+    if (__any_sync(0xFFFFFFFFu, timed_out) && lane == 0) VREN_RECORD_ERROR(VREN_ERR_TIMEOUT);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const uint32_t done = atomicAdd(scratch + 2, 1u);
+        if (done == gridDim.x - 1) {
+            st_relaxed_u64(reinterpret_cast<uint64_t*>(scratch), (uint64_t)(epoch + 1u) << 32);
+            scratch[2] = 0u;
+        }
     }
 }
 
@@ -816,6 +887,26 @@ static int assign_lights(cudaStream_t st, const uint32_t* keys, const uint32_t* 
     if (warps_per_cta < 1 || warps_per_cta > 8) warps_per_cta = 8;
     const dim3 block(32 * warps_per_cta);
     const dim3 grid(kNumSMsHint * (64 / warps_per_cta));
+    if (tuning(VREN_TUNE_ASSIGN_FUSED) != 0) {
+        uint32_t* sc = static_cast<uint32_t*>(scratch);
+        const uint32_t spin = (uint32_t)tuning(VREN_TUNE_SPIN_POLLS);
+#define VREN_FUSED(LCV)                                                                                        \
+    (spheres ? launch_kernel(assign_fused_kernel<LCV, true>, grid, block, 0, st, a, lb, offsets, sc, total,       \
+                             g_wait_limit, spin)                                                                  \
+             : launch_kernel(assign_fused_kernel<LCV, false>, grid, block, 0, st, a, lb, offsets, sc, total,      \
+                             g_wait_limit, spin))
+        switch (lc) {
+        case 1: VREN_FUSED(1); break;
+        case 2: VREN_FUSED(2); break;
+        case 3: VREN_FUSED(3); break;
+        case 4: VREN_FUSED(4); break;
+        case 5: VREN_FUSED(5); break;
+        default: VREN_FUSED(6); break;
+        }
+#undef VREN_FUSED
+        VREN_LAUNCH_CHECK();
+        return VREN_OK;
+    }
     if (spheres) launch_assign<false, true>(st, lc, grid, block, a, lb);
     else launch_assign<false, false>(st, lc, grid, block, a, lb);
     VREN_LAUNCH_CHECK();
@@ -1036,7 +1127,11 @@ extern "C" int vren_cs_find_unique_clusters(vren_stream_t s, const float* depth,
                               key_count, cluster_refs, static_cast<uint32_t*>(scratch));
 }
 
-extern "C" size_t vren_cs_assign_lights_scratch_bytes(uint32_t key_capacity) { return scan_scratch_bytes(key_capacity); }
+extern "C" size_t vren_cs_assign_lights_scratch_bytes(uint32_t key_capacity)
+{
+    const size_t a = scan_scratch_bytes(key_capacity), b = assign_fused_scratch_bytes(key_capacity);
+    return a > b ? a : b;
+}
 
 extern "C" int vren_cs_assign_lights(vren_stream_t s, const uint32_t* cluster_keys, const uint32_t* key_count,
                                      uint32_t key_capacity, const vren_cs_frame* frame, const vren_bvh_node* bvh,
@@ -1175,7 +1270,7 @@ extern "C" int vren_cs_create(vren_cluster_and_shade** out, uint32_t max_width, 
         }
     const size_t o_lbvh = carve(lbvh);
     const size_t o_fuc = carve(vren_cs_unique_clusters_scratch_bytes(max_width, max_height));
-    const size_t o_asg = carve(scan_scratch_bytes(cs->key_cap));
+    const size_t o_asg = carve(vren_cs_assign_lights_scratch_bytes(cs->key_cap));
     cs->arena_bytes = off;
     if (cudaMalloc(&cs->arena, off) != cudaSuccess) {
         delete cs;
