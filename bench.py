@@ -758,7 +758,21 @@ def run_profile(args):
     dev = torch.device("cuda", 0)
     stream = torch.cuda.Stream(device=dev)
     reps = args.warmup + args.steps
-    if args.profile == "frame":
+    if args.profile == "batch":
+        # the batched form on the 64 mixed frames (fixed options: 6-bit digits, 2 traversal warps)
+        specs = batch_specs()
+        frames = []
+        for k, (w, h, nl) in enumerate(specs):
+            v = cs.view_from_camera(cs.scene_camera(w, h), "ref")
+            depth, normals = scene.depth_planes(SEED + 5000 + k, w, h, planes=64)
+            pos, lights = scene.lights(SEED + 6000 + k, nl, w, h)
+            t = lambda a: torch.from_numpy(a).to(dev)
+            frames.append((v, w, h, t(depth), t(normals), t(pos), t(lights), nl))
+        batch = cs.cluster_batch()
+        batch.reserve(frames, 1 << 26)
+        batch.set_options(sort_digit_bits=6, radix_items=0, scan_slices=8, assign_warps=2)
+        fn = lambda: batch.run(stream, frames)
+    elif args.profile == "frame":
         # the benchmark's frame: 1920x1080, 16384 lights, one CUDA graph replay per frame
         depth, normals, pos, lights, _ = make_inputs(0)
         view = cs.view_from_camera(cs.scene_camera(W, H), "ref")
@@ -811,7 +825,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--quick", action="store_true", help="skip the primitive sweep and the large sorts")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--profile", choices=["frame", "find_unique", "radix", "scan", "shade", "shade_backward"],
+    ap.add_argument("--profile", choices=["frame", "batch", "find_unique", "radix", "scan", "shade",
+                                          "shade_backward"],
                     default=None,
                     help="run one kernel family on a case larger than L2 (for ncu) and exit")
     args = ap.parse_args()

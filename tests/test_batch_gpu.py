@@ -174,3 +174,19 @@ def test_batch_capacity_and_arguments(cuda, frames_and_plain):
     bad[1] = 9000  # width above 8192
     with pytest.raises(Exception):
         b.reserve([tuple(bad)], 1 << 20)
+
+
+def test_batch_frame_groups(cuda):
+    """A batch whose references exceed the unique-cluster group size (48 MB): eight 2560x1440 frames
+    (118 MB of references) run as several groups and still match the plain path frame by frame."""
+    specs = [(2560, 1440, 500 + 700 * k, "wrap", k % 2 == 1) for k in range(8)]
+    frames = make_frames(cuda, specs, seed=900)
+    plain = plain_outputs(cuda, frames)
+    stream = torch.cuda.Stream(device=cuda)
+    b = cs.cluster_batch()
+    b.reserve(frames, 1 << 24)
+    with torch.cuda.stream(stream):
+        b.run(stream, frames)
+    got = batch_outputs(b, stream, frames)
+    for f in range(len(frames)):
+        assert_same(got[f], plain[f], f)

@@ -209,6 +209,10 @@ __global__ void __launch_bounds__(1024) batch_levels_kernel(const BatchDesc* __r
 // ------------------------------------------------------------------------------------------------
 // Unique clusters over all frames' tiles
 // ------------------------------------------------------------------------------------------------
+// References of at most this many bytes per unique-cluster group (they must stay in the 129 MB L2
+// between the tile kernel and the fix-up).
+constexpr uint64_t kFucGroupBytes = 48ull << 20;
+
 struct BatchFuc {
     const BatchDesc* d;
     const uint32_t* tile_prefix;
@@ -231,8 +235,8 @@ __device__ __forceinline__ FucFrame batch_fuc_frame(const BatchFuc& b, uint32_t 
                     b.tile_count + t0, b.tile_offset + t0, fd.tiles, fd.vec};
 }
 
-// Every frame's tiles.
-__global__ void __launch_bounds__(kFucThreads, 6) batch_find_unique_kernel(BatchFuc b)
+// The tiles of a group of frames (global tile index = blockIdx.x + t0).
+__global__ void __launch_bounds__(kFucThreads, 6) batch_find_unique_kernel(BatchFuc b, uint32_t t0)
 {
     pdl_enter();
     __shared__ FucSmem sm;
@@ -241,23 +245,25 @@ __global__ void __launch_bounds__(kFucThreads, 6) batch_find_unique_kernel(Batch
     reinterpret_cast<uint4*>(sm.bits)[tid + kFucThreads] = make_uint4(0u, 0u, 0u, 0u);
     if (tid < 64) sm.used[tid] = 0u;
     __syncthreads();
-    const uint32_t f = frame_of(b.tile_prefix, b.n, blockIdx.x);
-    find_unique_tile(batch_fuc_frame(b, f), blockIdx.x - b.tile_prefix[f], sm);
+    const uint32_t t = blockIdx.x + t0;
+    const uint32_t f = frame_of(b.tile_prefix, b.n, t);
+    find_unique_tile(batch_fuc_frame(b, f), t - b.tile_prefix[f], sm);
 }
 
-// One CTA per frame: its tile counts into offsets.
-__global__ void __launch_bounds__(kFucScanThreads) batch_find_unique_scan_kernel(BatchFuc b)
+// One CTA per frame of the group (frame blockIdx.x + f0): its tile counts into offsets.
+__global__ void __launch_bounds__(kFucScanThreads) batch_find_unique_scan_kernel(BatchFuc b, uint32_t f0)
 {
     pdl_enter();
     __shared__ uint32_t s_warp[kFucScanThreads / 32];
-    find_unique_scan(batch_fuc_frame(b, blockIdx.x), s_warp);
+    find_unique_scan(batch_fuc_frame(b, blockIdx.x + f0), s_warp);
 }
 
-__global__ void __launch_bounds__(kFucThreads) batch_find_unique_fixup_kernel(BatchFuc b)
+__global__ void __launch_bounds__(kFucThreads) batch_find_unique_fixup_kernel(BatchFuc b, uint32_t t0)
 {
     pdl_enter();
-    const uint32_t f = frame_of(b.tile_prefix, b.n, blockIdx.x);
-    find_unique_fixup(batch_fuc_frame(b, f), blockIdx.x - b.tile_prefix[f]);
+    const uint32_t t = blockIdx.x + t0;
+    const uint32_t f = frame_of(b.tile_prefix, b.n, t);
+    find_unique_fixup(batch_fuc_frame(b, f), t - b.tile_prefix[f]);
 }
 
 // Dense cluster numbering: base[f] = sum of the unique-cluster counts of frames < f; base[n] = total.
@@ -349,7 +355,7 @@ __global__ void __launch_bounds__(256) batch_assign_kernel(BatchAssign b)
             if (lane == 0) b.counts[c] = acc;
         } else {
             const uint32_t out = b.goff[c];
-            if (fd.lc) batch_traverse<true>(a, fd.lb, fd.lc, key, out, lane);
+            if (fd.lc && b.counts[c] != 0u) batch_traverse<true>(a, fd.lb, fd.lc, key, out, lane);  // skip empty
             if (lane == 0) b.offsets[c] = out - b.goff[b.base[f]];
         }
     }
@@ -419,6 +425,10 @@ struct vren_cs_batch {
     char* host = nullptr;
     size_t host_bytes = 0;
     std::vector<char> uploaded;  // what the device copy currently holds
+    // frame groups of the unique-cluster stage (boundaries, first = 0, last = n) and the host copy of
+    // the tile prefix
+    std::vector<uint32_t> fuc_groups;
+    std::vector<uint32_t> fuc_tile_prefix;
     // layout of the current batch
     uint32_t n = 0, total_chunks = 0, total_leaf_blocks = 0, total_tiles = 0, total_lights = 0;
     uint64_t total_keys = 0;
@@ -544,6 +554,19 @@ int stage_batch(vren_cs_batch* b, cudaStream_t st, const vren_cs_batch_frame* fr
     // refs are written with 128-bit stores only when every frame's reference range is aligned
     for (uint32_t i = 0; i < count; ++i)
         if (desc[i].pixel_base % 4u != 0u) desc[i].vec = 0;
+    // unique-cluster groups: consecutive frames whose references total at most kFucGroupBytes
+    b->fuc_groups.assign(1, 0u);
+    b->fuc_tile_prefix.assign(pref + 2 * (count + 1), pref + 2 * (count + 1) + count + 1);
+    uint64_t group_bytes = 0;
+    for (uint32_t i = 0; i < count; ++i) {
+        const uint64_t bytes = (uint64_t)desc[i].W * desc[i].H * 4u;
+        if (group_bytes > 0 && group_bytes + bytes > kFucGroupBytes) {
+            b->fuc_groups.push_back(i);
+            group_bytes = 0;
+        }
+        group_bytes += bytes;
+    }
+    b->fuc_groups.push_back(count);
     b->n = count;
     b->total_chunks = chunk;
     b->total_leaf_blocks = leaf;
@@ -589,12 +612,18 @@ int enqueue_batch(vren_cs_batch* b, cudaStream_t st)
     }
     const BatchFuc bf{b->desc, tile_prefix, n, b->keys, b->key_counts, b->refs, b->tile_keys, b->tile_count,
                       b->tile_offset};
-    launch_kernel(batch_find_unique_kernel, b->total_tiles, kFucThreads, 0, st, bf);
-    VREN_LAUNCH_CHECK();
-    launch_kernel(batch_find_unique_scan_kernel, n, kFucScanThreads, 0, st, bf);
-    VREN_LAUNCH_CHECK();
-    launch_kernel(batch_find_unique_fixup_kernel, b->total_tiles, kFucThreads, 0, st, bf);
-    VREN_LAUNCH_CHECK();
+    // tiles -> tile-count scan -> reference fix-up per group of frames, so that the group's references
+    // are still in L2 when the fix-up adds the tile offsets
+    for (size_t g = 0; g + 1 < b->fuc_groups.size(); ++g) {
+        const uint32_t f0 = b->fuc_groups[g], f1 = b->fuc_groups[g + 1];
+        const uint32_t t0 = b->fuc_tile_prefix[f0], t1 = b->fuc_tile_prefix[f1];
+        launch_kernel(batch_find_unique_kernel, t1 - t0, kFucThreads, 0, st, bf, t0);
+        VREN_LAUNCH_CHECK();
+        launch_kernel(batch_find_unique_scan_kernel, f1 - f0, kFucScanThreads, 0, st, bf, f0);
+        VREN_LAUNCH_CHECK();
+        launch_kernel(batch_find_unique_fixup_kernel, t1 - t0, kFucThreads, 0, st, bf, t0);
+        VREN_LAUNCH_CHECK();
+    }
     launch_kernel(batch_bases_kernel, 1, 1024, 0, st, b->desc, n, b->key_counts, b->base);
     VREN_LAUNCH_CHECK();
     BatchAssign a{b->desc, n, b->base, b->keys, b->counts, b->goff, b->offsets, b->indices,
