@@ -429,6 +429,9 @@ struct vren_cs_batch {
     // the tile prefix
     std::vector<uint32_t> fuc_groups;
     std::vector<uint32_t> fuc_tile_prefix;
+    // second stream: the light BVHs are built beside the unique-cluster stage
+    cudaStream_t aux = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_bvh = nullptr;
     // layout of the current batch
     uint32_t n = 0, total_chunks = 0, total_leaf_blocks = 0, total_tiles = 0, total_lights = 0;
     uint64_t total_keys = 0;
@@ -594,36 +597,50 @@ int enqueue_batch(vren_cs_batch* b, cudaStream_t st)
     const uint32_t* chunk_prefix = b->prefixes;
     const uint32_t* leaf_prefix = b->prefixes + (n + 1);
     const uint32_t* tile_prefix = b->prefixes + 2 * (n + 1);
+    // The light BVHs (on the second stream) and the unique clusters (on st) are independent; the
+    // assignment waits for both.
     if (b->total_chunks > 0) {
-        launch_kernel(batch_transform_kernel, b->total_chunks, 256, 0, st, b->desc, chunk_prefix, n, b->view_pos, b->part, b->fmm,
-                                                                b->fticket);
-        VREN_LAUNCH_CHECK();
-        launch_kernel(batch_morton_kernel, b->total_chunks, 256, 0, st, b->desc, chunk_prefix, n, b->view_pos, b->fmm, b->pairs);
-        VREN_LAUNCH_CHECK();
-        int rc = sort_uvec2(st, reinterpret_cast<const uint32_t*>(b->pairs), reinterpret_cast<uint32_t*>(b->light_index),
+        cudaStream_t ls = b->aux;
+        VREN_CUDA_TRY(cudaEventRecord(b->ev_fork, st));
+        VREN_CUDA_TRY(cudaStreamWaitEvent(ls, b->ev_fork, 0));
+        int rc = VREN_OK;
+        do {
+            if (launch_kernel(batch_transform_kernel, b->total_chunks, 256, 0, ls, b->desc, chunk_prefix, n,
+                              b->view_pos, b->part, b->fmm, b->fticket) != cudaSuccess ||
+                launch_kernel(batch_morton_kernel, b->total_chunks, 256, 0, ls, b->desc, chunk_prefix, n, b->view_pos,
+                              b->fmm, b->pairs) != cudaSuccess) {
+                rc = VREN_ERR_CUDA;
+                break;
+            }
+            rc = sort_uvec2(ls, reinterpret_cast<const uint32_t*>(b->pairs), reinterpret_cast<uint32_t*>(b->light_index),
                             reinterpret_cast<uint32_t*>(b->sort_tmp), b->total_lights, 16u + b->frame_bits,
                             b->opt.sort_digit_bits, b->sort_scratch);
-        if (rc != VREN_OK) return rc;
-        launch_kernel(batch_leaves_kernel, b->total_leaf_blocks, 1024, 0, st, b->desc, leaf_prefix, n, b->light_index,
-                                                                   b->view_pos, b->bvh, b->spheres);
-        VREN_LAUNCH_CHECK();
-        launch_kernel(batch_levels_kernel, n, 1024, 0, st, b->desc, b->bvh);
-        VREN_LAUNCH_CHECK();
+            if (rc != VREN_OK) break;
+            if (launch_kernel(batch_leaves_kernel, b->total_leaf_blocks, 1024, 0, ls, b->desc, leaf_prefix, n,
+                              b->light_index, b->view_pos, b->bvh, b->spheres) != cudaSuccess ||
+                launch_kernel(batch_levels_kernel, n, 1024, 0, ls, b->desc, b->bvh) != cudaSuccess)
+                rc = VREN_ERR_CUDA;
+        } while (false);
+        const cudaError_t e1 = cudaEventRecord(b->ev_bvh, ls);
+        if (rc != VREN_OK || e1 != cudaSuccess) {
+            cudaStreamWaitEvent(st, b->ev_bvh, 0);  // rejoin before returning (a capture must end joined)
+            return rc != VREN_OK ? rc : VREN_ERR_CUDA;
+        }
     }
     const BatchFuc bf{b->desc, tile_prefix, n, b->keys, b->key_counts, b->refs, b->tile_keys, b->tile_count,
                       b->tile_offset};
     // tiles -> tile-count scan -> reference fix-up per group of frames, so that the group's references
     // are still in L2 when the fix-up adds the tile offsets
-    for (size_t g = 0; g + 1 < b->fuc_groups.size(); ++g) {
+    cudaError_t fe = cudaSuccess;
+    for (size_t g = 0; g + 1 < b->fuc_groups.size() && fe == cudaSuccess; ++g) {
         const uint32_t f0 = b->fuc_groups[g], f1 = b->fuc_groups[g + 1];
         const uint32_t t0 = b->fuc_tile_prefix[f0], t1 = b->fuc_tile_prefix[f1];
-        launch_kernel(batch_find_unique_kernel, t1 - t0, kFucThreads, 0, st, bf, t0);
-        VREN_LAUNCH_CHECK();
-        launch_kernel(batch_find_unique_scan_kernel, f1 - f0, kFucScanThreads, 0, st, bf, f0);
-        VREN_LAUNCH_CHECK();
-        launch_kernel(batch_find_unique_fixup_kernel, t1 - t0, kFucThreads, 0, st, bf, t0);
-        VREN_LAUNCH_CHECK();
+        fe = launch_kernel(batch_find_unique_kernel, t1 - t0, kFucThreads, 0, st, bf, t0);
+        if (fe == cudaSuccess) fe = launch_kernel(batch_find_unique_scan_kernel, f1 - f0, kFucScanThreads, 0, st, bf, f0);
+        if (fe == cudaSuccess) fe = launch_kernel(batch_find_unique_fixup_kernel, t1 - t0, kFucThreads, 0, st, bf, t0);
     }
+    if (b->total_chunks > 0) VREN_CUDA_TRY(cudaStreamWaitEvent(st, b->ev_bvh, 0));  // join the light BVHs
+    if (fe != cudaSuccess) return VREN_ERR_CUDA;
     launch_kernel(batch_bases_kernel, 1, 1024, 0, st, b->desc, n, b->key_counts, b->base);
     VREN_LAUNCH_CHECK();
     BatchAssign a{b->desc, n, b->base, b->keys, b->counts, b->goff, b->offsets, b->indices,
@@ -676,7 +693,14 @@ bool options_ok(const vren_cs_batch_options& o)
 extern "C" int vren_cs_batch_create(vren_cs_batch** out)
 {
     if (!out) return VREN_ERR_ARG;
-    *out = new vren_cs_batch();
+    auto* b = new vren_cs_batch();
+    if (cudaStreamCreateWithFlags(&b->aux, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_bvh, cudaEventDisableTiming) != cudaSuccess) {
+        vren_cs_batch_destroy(b);
+        return VREN_ERR_CUDA;
+    }
+    *out = b;
     return VREN_OK;
 }
 
@@ -684,6 +708,9 @@ extern "C" void vren_cs_batch_destroy(vren_cs_batch* b)
 {
     if (!b) return;
     drop_graph(b);
+    if (b->aux) cudaStreamDestroy(b->aux);
+    if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+    if (b->ev_bvh) cudaEventDestroy(b->ev_bvh);
     cudaFree(b->arena);
     cudaFreeHost(b->host);
     delete b;
