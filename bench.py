@@ -257,9 +257,9 @@ def run_ours(args, rank: int, world: int):
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(depth, normals, pos, lights, radix_keys, view)
 
-    # light BVH at 16384 lights: transform, Morton, sort histogram, 2 sort passes, leaves (6); unique
-    # clusters: tiles, tile-count scan, fix-up (3); assignment: count, scan, write (3)
-    launches_per_frame = 12
+    # light BVH at 16384 lights: one kernel on a 16-CTA cluster (1); unique clusters: tiles, tile-count
+    # scan, fix-up (3); assignment: count, scan, write (3)
+    launches_per_frame = 7
     if rank == 0:
         res = {
             "metric": METRIC,
