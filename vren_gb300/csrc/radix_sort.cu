@@ -147,8 +147,7 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_hist_kernel(
 template <int DIGIT_BITS, int ITEMS, int MODE, int RANK>
 struct PassSmem {
     static constexpr int RADIX = 1 << DIGIT_BITS;
-    uint32_t warp_hist[kSortWarps][RADIX];
-    uint32_t tile_excl[RADIX];
+    uint32_t warp_hist[kSortWarps][RADIX];  // per-warp digit counts, then each warp's first staging slot
     int32_t delta[RADIX];
     uint32_t wsum[kSortWarps];
 };
@@ -164,7 +163,7 @@ __device__ __forceinline__ void onesweep_pass_body(
     constexpr int TILE = kSortThreads * ITEMS;
     using Elem = typename std::conditional<MODE == kUvec2, uint2, uint32_t>::type;
     Elem* s_keys = reinterpret_cast<Elem*>(s_stage);
-    uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_keys + TILE);
+    uint2* s_pairs = reinterpret_cast<uint2*>(s_stage);  // MODE == kPairs: (key, value) as one 64-bit word
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
 
     uint32_t* status = scratch + kStatusOffset + (size_t)(pass & 1u) * num_tiles * RADIX;
@@ -237,7 +236,7 @@ __device__ __forceinline__ void onesweep_pass_body(
     if (tid < (uint32_t)RADIX) {
         const uint32_t d = tid;
 #pragma unroll
-        for (int w = 0; w < kSortWarps; ++w) {
+        for (int w = 0; w < kSortWarps; ++w) {  // digit d's count in the warps before w
             const uint32_t c = sm.warp_hist[w][d];
             sm.warp_hist[w][d] = count;
             count += c;
@@ -260,7 +259,8 @@ __device__ __forceinline__ void onesweep_pass_body(
         const uint32_t d = tid;
         excl = incl - count;
         for (uint32_t w = 0; w < warp; ++w) excl += sm.wsum[w];
-        sm.tile_excl[d] = excl;
+#pragma unroll
+        for (int w = 0; w < kSortWarps; ++w) sm.warp_hist[w][d] += excl;  // first staging slot of (w, d)
         if (tile != 0) lb_word = ld_relaxed_u32(status + (size_t)(tile - 1) * RADIX + d);
         goff = ld_relaxed_u32(scratch + kOffsOffset + pass * kMaxRadix + d);
     }
@@ -271,9 +271,9 @@ __device__ __forceinline__ void onesweep_pass_body(
     for (int j = 0; j < ITEMS; ++j) {
         if (FULL || pos[j] != 0xFFFFFFFFu) {
             const uint32_t d = pos[j] & 0xFFu;
-            const uint32_t p = sm.tile_excl[d] + sm.warp_hist[warp][d] + (pos[j] >> 8);
-            s_keys[p] = key[j];
-            if (MODE == kPairs) s_vals[p] = val[j];
+            const uint32_t p = sm.warp_hist[warp][d] + (pos[j] >> 8);
+            if (MODE == kPairs) s_pairs[p] = make_uint2(*reinterpret_cast<const uint32_t*>(&key[j]), val[j]);
+            else s_keys[p] = key[j];
         }
     }
 
@@ -282,16 +282,26 @@ __device__ __forceinline__ void onesweep_pass_body(
         const uint32_t d = tid;
         uint32_t prefix = 0;
         if (tile != 0) {
+            // four predecessors per step: tile t is examined while t-1..t-3 are already being read
             int64_t t = (int64_t)tile - 1;
-            uint32_t w = lb_word;
-            while (true) {
-                if (!(w & (3u << kFlagShift)))
-                    w = wait_for_flag(status + (size_t)t * RADIX + d, wait_limit, spin,
-                                      [] { VREN_RECORD_ERROR(VREN_ERR_TIMEOUT); });
-                prefix += w & kValueMask;
-                if ((w & kFlagPrefix) || t == 0) break;
-                --t;
-                w = ld_relaxed_u32(status + (size_t)t * RADIX + d);
+            uint32_t w[4];
+            w[0] = lb_word;
+            bool done = false;
+            while (!done) {
+#pragma unroll
+                for (int i = 1; i < 4; ++i) w[i] = t - i >= 0 ? ld_relaxed_u32(status + (size_t)(t - i) * RADIX + d) : 0u;
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    if (done || t - i < 0) continue;
+                    uint32_t x = w[i];
+                    if (!(x & (3u << kFlagShift)))
+                        x = wait_for_flag(status + (size_t)(t - i) * RADIX + d, wait_limit, spin,
+                                          [] { VREN_RECORD_ERROR(VREN_ERR_TIMEOUT); });
+                    prefix += x & kValueMask;
+                    if ((x & kFlagPrefix) || t - i == 0) done = true;
+                }
+                t -= 4;
+                if (!done) w[0] = ld_relaxed_u32(status + (size_t)t * RADIX + d);
             }
             st_relaxed_u32(status + (size_t)tile * RADIX + d, kFlagPrefix | (prefix + count));
         }
@@ -305,10 +315,17 @@ __device__ __forceinline__ void onesweep_pass_body(
     for (int j = 0; j < ITEMS; ++j) {
         const uint32_t p = j * kSortThreads + tid;
         if (FULL || p < tile_valid) {
-            const Elem e = s_keys[p];
-            uint32_t k;
-            if (MODE == kUvec2) k = (reinterpret_cast<const uint2*>(&e))->x;
-            else k = *(reinterpret_cast<const uint32_t*>(&e));
+            uint32_t k, v = 0;
+            Elem e{};
+            if (MODE == kPairs) {
+                const uint2 kv = s_pairs[p];
+                k = kv.x;
+                v = kv.y;
+            } else {
+                e = s_keys[p];
+                if (MODE == kUvec2) k = (reinterpret_cast<const uint2*>(&e))->x;
+                else k = *(reinterpret_cast<const uint32_t*>(&e));
+            }
             const uint32_t d = digit_of(k, shift, width);
             const uint32_t dst = (uint32_t)((int32_t)p + sm.delta[d]);
             if (dst < n) {  // false only after a timed-out look-back (error recorded)
@@ -316,7 +333,7 @@ __device__ __forceinline__ void onesweep_pass_body(
                     reinterpret_cast<uint2*>(out_keys)[dst] = *(reinterpret_cast<const uint2*>(&e));
                 } else {
                     out_keys[dst] = k;
-                    if (MODE == kPairs) out_vals[dst] = s_vals[p];
+                    if (MODE == kPairs) out_vals[dst] = v;
                 }
             }
         }
