@@ -81,10 +81,14 @@ uint32_t vren_set_wait_limit(uint32_t rounds);
  *                          16-CTA thread-block cluster when the device can hold one (default),
  *                          0 = the multi-kernel path
  *   VREN_TUNE_ASSIGN_FUSED assign_lights: 0 = count kernel, exclusive scan, write kernel (default),
- *                          1 = one kernel (count, look-back over the cluster counts, write) */
+ *                          1 = one kernel (count, look-back over the cluster counts, write)
+ *   VREN_TUNE_RADIX_PERSISTENT  sort passes over keys or pairs whose input starts 16-byte aligned:
+ *                          1 = persistent grid whose producer warp streams tiles into shared memory
+ *                          by bulk copies and publishes their digit counts on arrival, 0 = one CTA
+ *                          per tile (ballot ranking, 15/16 keys per thread only) */
 enum { VREN_TUNE_SCAN_SLICES = 0, VREN_TUNE_SPIN_POLLS = 1, VREN_TUNE_RADIX_RANK = 2, VREN_TUNE_RADIX_ITEMS = 3,
        VREN_TUNE_SCAN_STAGED = 4, VREN_TUNE_REDUCE_FORM = 5, VREN_TUNE_LIGHT_BVH_CLUSTER = 6,
-       VREN_TUNE_ASSIGN_FUSED = 7, VREN_TUNE_COUNT = 8 };
+       VREN_TUNE_ASSIGN_FUSED = 7, VREN_TUNE_RADIX_PERSISTENT = 8, VREN_TUNE_COUNT = 9 };
 int vren_tuning_set(int knob, int value);
 int vren_tuning_get(int knob);
 

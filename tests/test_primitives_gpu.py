@@ -248,6 +248,34 @@ def test_radix_sort_pairs_stable(cuda, bits, n):
         assert np.array_equal(host_u32(v), ev)
 
 
+@pytest.mark.parametrize("bits", [4, 6, 8])
+@pytest.mark.parametrize("n", [2, 1000, 3839, 3840, 3841, 100003, 1 << 20, 3_000_017])
+@pytest.mark.parametrize("values", [True, False])
+def test_radix_sort_persistent_pass(cuda, restore_tuning, bits, n, values):
+    """The persistent pass (bulk-copied tiles, digit counts published on arrival) sorts pairs and keys
+    exactly as the stable oracle: partial last tiles whose length is not a multiple of 4, one tile,
+    many tiles, equal keys; two sorts in a row on one scratch."""
+    assert restore_tuning.vren_tuning_set(vg._lib.TUNE["radix_persistent"], 1) == 0
+    rng = np.random.default_rng(7 * n + bits)
+    keys = rng.integers(0, 2**32, n, dtype=np.uint64).astype(np.uint32)
+    keys[: n // 3] = keys[n // 3: 2 * (n // 3)]
+    keys[0] = 0xFFFFFFFF
+    vals = np.arange(n, dtype=np.uint32)
+    rs = vg.radix_sort(bits)
+    s1 = rs.create_scratch_buffer_1(n, cuda)
+    ek, ev = oracle.stable_sort_u32(keys, vals)
+    for _ in range(2):
+        k = dev_u32(keys, cuda)
+        v = dev_u32(vals, cuda) if values else None
+        tk = torch.empty_like(k)
+        tv = torch.empty_like(v) if values else None
+        rs.sort(None, k, v, n, s1, tk, tv)
+        assert np.array_equal(host_u32(k), ek)
+        if values:
+            assert np.array_equal(host_u32(v), ev)
+    assert vg.device_error() == 0
+
+
 def test_radix_sort_pairs_2e20_config(cuda):
     """The benchmark configuration: 2^20 pairs, keys = PCG32 full range, values = index."""
     import ctypes

@@ -367,6 +367,12 @@ __global__ void __launch_bounds__(kSortThreads, 4) onesweep_pass_kernel(
                                                                  s_stage);
 }
 
+}  // namespace vren_gb300
+
+#include "radix_persistent.cuh"
+
+namespace vren_gb300 {
+
 // ------------------------------------------------------------------------------------------------
 // Bucket end offsets from the sorted output: end[b] = number of elements with bucket <= b.
 // Thread i (i in [-1, n)) writes end[b] = i + 1 for every b in [bucket(i), bucket(i+1)).
@@ -397,9 +403,10 @@ static uint32_t tile_of(uint32_t digit_bits, int variant)
 }
 
 // Scratch is sized for the smaller tile (more tiles), so every variant fits.
+// Status rows per buffer: enough for the smallest tile of either pass form.
 static uint32_t tiles_for(uint32_t n, uint32_t digit_bits)
 {
-    const uint32_t tile = tile_of(digit_bits, 0);
+    const uint32_t tile = tile_of(digit_bits, 0) < kPTile ? tile_of(digit_bits, 0) : kPTile;
     return (n + tile - 1) / tile;
 }
 
@@ -412,6 +419,30 @@ static size_t scratch1_bytes(uint32_t n, uint32_t digit_bits)
 }
 
 static bool supported_bits(uint32_t db) { return db == 4 || db == 5 || db == 6 || db == 8; }
+
+// Persistent pass grid: SMs x resident CTAs (shared memory opted in once per variant).
+template <int DB, int MODE>
+static int launch_persistent_pass(cudaStream_t st, const uint32_t* sk, const uint32_t* sv, uint32_t* ok, uint32_t* ov,
+                                  uint32_t n, uint32_t p, uint32_t shift, uint32_t width, uint32_t tiles,
+                                  uint32_t* scratch, uint32_t spin)
+{
+    constexpr size_t smem = persist_dyn_smem<DB, MODE>();
+    auto kern = onesweep_persistent_kernel<DB, MODE>;
+    static int grid = 0;  // per variant
+    if (grid == 0) {
+        VREN_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int dev = 0, sms = 0, per_sm = 0;
+        VREN_CUDA_TRY(cudaGetDevice(&dev));
+        VREN_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        VREN_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPThreads, smem));
+        grid = sms * (per_sm > 0 ? per_sm : 1);
+    }
+    const uint32_t g = tiles < (uint32_t)grid ? tiles : (uint32_t)grid;
+    VREN_CUDA_TRY(launch_kernel(kern, g, kPThreads, smem, st, sk, sv, ok, ov, n, p, shift, width, tiles, scratch,
+                                g_wait_limit, spin));
+    VREN_LAUNCH_CHECK();
+    return VREN_OK;
+}
 
 template <int DB, int MODE, int V, int RANK>
 static int launch_pass(cudaStream_t st, const uint32_t* sk, const uint32_t* sv, uint32_t* ok, uint32_t* ov, uint32_t n,
@@ -436,7 +467,15 @@ static int run_passes(cudaStream_t st, const uint32_t* src_k, const uint32_t* sr
     const int variant = tuning(VREN_TUNE_RADIX_ITEMS) == 1 ? 1 : 0;
     const int rank = tuning(VREN_TUNE_RADIX_RANK);
     const uint32_t spin = (uint32_t)tuning(VREN_TUNE_SPIN_POLLS);
-    const uint32_t tiles = (n + tile_of(DB, variant) - 1) / tile_of(DB, variant);
+    // One pass form for the whole sort (the two use different tile counts, hence status row strides):
+    // the persistent one when every buffer a pass may read starts 16-byte aligned.
+    const bool aligned = ((reinterpret_cast<uintptr_t>(src_k) | reinterpret_cast<uintptr_t>(src_v) |
+                           reinterpret_cast<uintptr_t>(dst_k) | reinterpret_cast<uintptr_t>(dst_v) |
+                           reinterpret_cast<uintptr_t>(tmp_k) | reinterpret_cast<uintptr_t>(tmp_v)) & 15u) == 0;
+    const bool persistent = MODE != kUvec2 && variant == 0 && rank == 0 &&
+                            tuning(VREN_TUNE_RADIX_PERSISTENT) != 0 && aligned;
+    const uint32_t tile_n = persistent ? kPTile : tile_of(DB, variant);
+    const uint32_t tiles = (n + tile_n - 1) / tile_n;
     const uint32_t status_tiles = tiles_for(n, DB);  // rows per status buffer (scratch layout)
 
     VREN_CUDA_TRY(cudaMemsetAsync(scratch, 0, kZeroWords * sizeof(uint32_t), st));
@@ -454,7 +493,11 @@ static int run_passes(cudaStream_t st, const uint32_t* src_k, const uint32_t* sr
         uint32_t* ov = to_final ? dst_v : tmp_v;
         int rc;
 #define VREN_PASS(V, R) launch_pass<DB, MODE, V, R>(st, src_k, src_v, ok, ov, n, p, passes.shift[p], passes.width[p], tiles, scratch, spin)
-        if (variant == 1) rc = rank == 1 ? VREN_PASS(1, 1) : rank == 2 ? VREN_PASS(1, 2) : VREN_PASS(1, 0);
+        if (persistent)
+            rc = launch_persistent_pass<DB, MODE == kUvec2 ? kKeys : MODE>(st, src_k, src_v, ok, ov, n, p,
+                                                                          passes.shift[p], passes.width[p], tiles,
+                                                                          scratch, spin);
+        else if (variant == 1) rc = rank == 1 ? VREN_PASS(1, 1) : rank == 2 ? VREN_PASS(1, 2) : VREN_PASS(1, 0);
         else rc = rank == 1 ? VREN_PASS(0, 1) : rank == 2 ? VREN_PASS(0, 2) : VREN_PASS(0, 0);
 #undef VREN_PASS
         if (rc != VREN_OK) return rc;
