@@ -215,10 +215,10 @@ __device__ __forceinline__ void onesweep_pass_body(
                 peers = FULL ? 0xFFFFFFFFu : __ballot_sync(0xFFFFFFFFu, valid);
 #pragma unroll
                 for (int b = 0; b < DIGIT_BITS; ++b) {
-                    const uint32_t m = __ballot_sync(0xFFFFFFFFu, (d >> b) & 1u);
                     // keep the lanes whose bit b equals mine: m where my bit is 1, ~m where it is 0
-                    const uint32_t mine = (uint32_t)((int32_t)(d << (31 - b)) >> 31);
-                    peers &= ~(m ^ mine);
+                    const bool bit = (d >> b) & 1u;
+                    const uint32_t m = __ballot_sync(0xFFFFFFFFu, bit);
+                    peers &= bit ? m : ~m;
                 }
             }
             const uint32_t below = peers & lanemask_lt();
