@@ -245,6 +245,7 @@ def run_ours(args, rank: int, world: int):
     shade = shade_bench(args, dev, stream, flush, ctx)
     batched = None if args.quick else batched_vs_plain(args, dev, stream, flush)
     lbvh = None if args.quick else lbvh_bench(args, dev, stream, flush, depth, normals, pos, lights, view)
+    bouncer = None if args.quick else bouncer_bench(args, dev, stream, flush, hbm_peak)
 
     clocks.__exit__(None, None, None)
     clk = clocks.summary()
@@ -301,6 +302,7 @@ def run_ours(args, rank: int, world: int):
             "primitive_sweep": sweep,
             "shade": shade,
             "karras_lbvh": lbvh,
+            "light_bouncer": bouncer,
             "cpu_baseline": cpu,
             "clocks": clk,
             "device_error": err,
@@ -387,6 +389,33 @@ def lbvh_bench(args, dev, stream, flush, depth, normals, pos, lights, view):
                 torch.equal(res[0][3][:tot], res[1][3][:tot]))
         out[name] = {"assignments": tot, "assign_32ary_ms": round(res[0][0], 5), "assign_lbvh_ms": round(res[1][0], 5),
                      "build_lbvh_ms": round(ms_build, 5), "lists_identical": bool(same)}
+    return out
+
+
+def bouncer_bench(args, dev, stream, flush, hbm_peak):
+    """vren_demo's point-light bouncer: 2^24 lights (64 B per light: position and direction read and
+    written) against the HBM roofline, and the frame's 16384 lights at 60 frames/s."""
+    import torch
+
+    import vren_gb300.clustered_shading as cs
+
+    out = {}
+    lo, hi = [-400.0, -250.0, 0.1], [400.0, 250.0, 1000.0]
+    for n, dt in ((1 << 24, 1.0 / 60.0), (L, 1.0 / 60.0)):
+        rng = np.random.default_rng(SEED + n)
+        pos = np.zeros((n, 4), np.float32)
+        pos[:, 0] = rng.uniform(lo[0], hi[0], n)
+        pos[:, 1] = rng.uniform(lo[1], hi[1], n)
+        pos[:, 2] = rng.uniform(lo[2], hi[2], n)
+        d = np.zeros((n, 4), np.float32)
+        d[:, :3] = rng.standard_normal((n, 3))
+        p_t = torch.from_numpy(pos.reshape(-1)).to(dev)
+        d_t = torch.from_numpy(d.reshape(-1)).to(dev)
+        ms = time_events(stream, lambda: cs.bounce_point_lights(stream, p_t, d_t, n, lo, hi, 20.0, dt), 3,
+                         args.steps, flush)
+        gbs = 64.0 * n / (ms * 1e-3) / 1e9
+        out[f"lights={n}"] = {"ms": round(ms, 5), "glights_s": round(n / (ms * 1e-3) / 1e9, 3),
+                              "gbs_at_64B_per_light": round(gbs, 1), "hbm_frac": round(gbs / hbm_peak, 4)}
     return out
 
 
@@ -669,10 +698,19 @@ def cpu_baseline(depth, normals, pos, lights, radix_keys, view, budget_s: float 
         if time.perf_counter() - t1 > budget_s / 4 or sorts >= 50:
             break
     ms_sort = (time.perf_counter() - t1) * 1e3 / sorts
+    rng = np.random.default_rng(SEED)
+    bp = np.zeros((1 << 20, 4), np.float32)
+    bp[:, :3] = rng.uniform(-100.0, 100.0, (1 << 20, 3))
+    bd = np.zeros((1 << 20, 4), np.float32)
+    bd[:, :3] = rng.standard_normal((1 << 20, 3))
+    t2 = time.perf_counter()
+    oracle.bounce_point_lights(bp, bd, 1 << 20, [-400.0, -250.0, 0.1], [400.0, 250.0, 1000.0], 20.0, 1.0 / 60.0)
+    ms_bounce = (time.perf_counter() - t2) * 1e3
     return {"value": round(ms_frame, 3), "unit": "ms", "cores": threads, "kind": "port",
             "sample": f"{frames} frames of the CPU oracle pipeline (a6+a7+a8) at 1920x1080/16384 lights",
             "radix_sort_2^20_pairs_ms": round(ms_sort, 3),
-            "radix_sort_gkeys_s": round(RADIX_N / (ms_sort * 1e-3) / 1e9, 4)}
+            "radix_sort_gkeys_s": round(RADIX_N / (ms_sort * 1e-3) / 1e9, 4),
+            "light_bouncer_2^20_lights_ms": round(ms_bounce, 3)}
 
 
 # ------------------------------------------------------------------------------------------------

@@ -322,6 +322,15 @@ int vren_cs_construct_light_bvh(vren_stream_t s, const float* light_positions, c
                                 float* view_positions, vren_bvh_node* bvh, uint32_t* light_index,
                                 float* leaf_spheres, void* scratch);
 
+/* Point-light bouncer (vren_demo: bounce_point_lights.comp:33-73, point_light_bouncer.cpp:17-57), the
+ * per-frame producer of the positions construct_point_light_bvh reads.  In place, per light: the
+ * position (vec4, w written 1) is clamped into [aabb_min, aabb_max], then moves speed * dt along the
+ * direction (vec4, w written 0), reflecting the direction components of the faces it reaches, at
+ * most 32 bounces.  Every operation rounded on its own, IEEE division, GLSL min/max.  Both arrays
+ * 16-byte aligned; aabb_min / aabb_max are 3 host floats. */
+int vren_bounce_point_lights(vren_stream_t s, float* light_positions, float* light_directions, uint32_t light_count,
+                             const float* aabb_min, const float* aabb_max, float speed, float dt);
+
 /* find_unique_cluster_list (clustered_shading.cpp:363-448, find_unique_clusters.comp:46-120).
  * key_count receives the number of keys written (the reference's dispatch_params.x); a list longer
  * than key_capacity is truncated and VREN_ERR_CAPACITY recorded.  tiles_x*tiles_y*1024 keys always fit.

@@ -385,3 +385,23 @@ private:
 };
 
 }  // namespace vren
+
+namespace vren_demo {
+
+// vren_demo/vren_demo/point_light_bouncer.cpp:17-57: moves each light speed * dt along its direction
+// inside [aabb_min, aabb_max], reflecting off the faces; both buffers (vec4 per light) updated in place.
+class point_light_bouncer {
+public:
+    void bounce(uint32_t /*frame_idx*/, cudaStream_t stream, vren::resource_container&,
+                vren::device_buffer const& point_light_position_buffer,
+                vren::device_buffer const& point_light_direction_buffer, uint32_t point_light_count,
+                const float (&aabb_min)[3], const float (&aabb_max)[3], float speed, float dt)
+    {
+        vren::check(vren_bounce_point_lights(stream, point_light_position_buffer.at<float>(),
+                                             point_light_direction_buffer.at<float>(), point_light_count, aabb_min,
+                                             aabb_max, speed, dt),
+                    "point_light_bouncer::bounce");
+    }
+};
+
+}  // namespace vren_demo

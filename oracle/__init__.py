@@ -37,6 +37,7 @@ _PROTOS = {
     "oracle_cs_find_unique_clusters": (u32, [vp, vp, u32, u32, vp, i32, vp, u32, vp, i32]),
     "oracle_cs_assign_lights": (u64, [vp, u32, u32, u32, vp, vp, u32, vp, vp, vp, vp, vp, u64, i32]),
     "oracle_lbvh_build": (None, [vp, vp, u32, vp]),
+    "oracle_bounce_point_lights": (None, [vp, vp, u32, vp, vp, C.c_float, C.c_float]),
     "oracle_cs_assign_lights_lbvh": (u64, [vp, u32, u32, u32, vp, vp, vp, vp, u32, vp, vp, vp, vp, vp, u64, i32]),
     "oracle_cs_shade_f64": (None, [vp, u32, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, u32, i32, i32, vp, vp, i32]),
     "oracle_cs_shade_grad_f64": (None, [vp, u32, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, u32, i32, vp, vp, i32]),
@@ -197,6 +198,16 @@ def cs_assign_lights(keys, W: int, H: int, view, bvh, L: int, light_index, view_
                                           _p(np.ascontiguousarray(view_pos, np.float32)), _p(counts), _p(offsets),
                                           _p(indices), cap, threads)
     return counts[:U], offsets[:U], indices[: min(total, cap)].copy(), int(total)
+
+
+def bounce_point_lights(positions, directions, L: int, aabb_min, aabb_max, speed: float, dt: float):
+    """vren_demo's point-light bouncer (vren_oracle.c); returns new (positions, directions) arrays."""
+    p = np.array(positions, np.float32).reshape(-1).copy()
+    d = np.array(directions, np.float32).reshape(-1).copy()
+    lo = np.array(aabb_min, np.float32)
+    hi = np.array(aabb_max, np.float32)
+    lib().oracle_bounce_point_lights(_p(p), _p(d), L, _p(lo), _p(hi), float(speed), float(dt))
+    return p, d
 
 
 def lbvh_group_boxes(bvh, L: int) -> np.ndarray:

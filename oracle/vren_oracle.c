@@ -880,3 +880,44 @@ uint64_t oracle_cs_assign_lights_lbvh(const uint32_t* keys, uint32_t U, uint32_t
     }
     return total;
 }
+
+/* ================================================================================================
+ * Point-light bouncer — vren_demo/resources/shaders/bounce_point_lights.comp:33-73 (host
+ * point_light_bouncer.cpp:17-57).  GLSL min(x, y) = y < x ? y : x, max(x, y) = x < y ? y : x; every
+ * operation rounded on its own (compiled with -ffp-contract=off), IEEE division.
+ * ================================================================================================ */
+void oracle_bounce_point_lights(float* positions, float* directions, uint32_t L, const float* aabb_min,
+                                const float* aabb_max, float speed, float dt)
+{
+    const float INF_ = 1e35f, EPS_ = 1e-5f;
+    for (uint32_t i = 0; i < L; ++i) {
+        float p[3], d[3];
+        for (int c = 0; c < 3; ++c) {
+            p[c] = glsl_min(glsl_max(positions[4 * i + c], aabb_min[c]), aabb_max[c]);
+            d[c] = directions[4 * i + c];
+        }
+        float rem = speed * dt;
+        for (int j = 0; j < 32 && rem > 0.0f; ++j) {
+            float t1[3], t2[3];
+            for (int c = 0; c < 3; ++c) {
+                t1[c] = (aabb_min[c] - p[c]) / d[c];
+                if (t1[c] <= 0.0f) t1[c] = INF_;
+                t2[c] = (aabb_max[c] - p[c]) / d[c];
+                if (t2[c] <= 0.0f) t2[c] = INF_;
+            }
+            const float min_t =
+                glsl_min(t1[0], glsl_min(t2[0], glsl_min(t1[1], glsl_min(t2[1], glsl_min(t1[2], t2[2])))));
+            const float step = glsl_min(min_t - EPS_, rem);
+            for (int c = 0; c < 3; ++c) p[c] = p[c] + step * d[c];
+            if (min_t < rem)
+                for (int c = 0; c < 3; ++c) d[c] = d[c] * ((t1[c] == min_t || t2[c] == min_t) ? -1.0f : 1.0f);
+            rem = rem - step;
+        }
+        for (int c = 0; c < 3; ++c) {
+            positions[4 * i + c] = p[c];
+            directions[4 * i + c] = d[c];
+        }
+        positions[4 * i + 3] = 1.0f;
+        directions[4 * i + 3] = 0.0f;
+    }
+}

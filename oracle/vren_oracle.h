@@ -127,6 +127,10 @@ uint64_t oracle_cs_assign_lights_lbvh(const uint32_t* keys, uint32_t U, uint32_t
                                       const uint32_t* light_index, const float* view_pos, uint32_t* counts,
                                       uint32_t* offsets, uint32_t* indices, uint64_t index_cap, int threads);
 
+/* Point-light bouncer (in place; vec4 positions and directions; aabb_min/max: 3 floats). */
+void oracle_bounce_point_lights(float* positions, float* directions, uint32_t L, const float* aabb_min,
+                                const float* aabb_max, float speed, float dt);
+
 /* ---- shading in FP64 (vren_oracle_shade.cpp): forward, forward-mode gradient, per-light loss ---- */
 void oracle_cs_shade_f64(const oracle_cs_view* v, uint32_t W, uint32_t H, const float* depth, const float* normals,
                          const float* albedo, const float* rough, const float* metal, const uint32_t* refs,

@@ -107,6 +107,21 @@ int main()
         // P = 1024: leaves [0, 1024), 32 parents at [1024, 1056), root 1056 whose first child is 1024
         EXPECT(root.min[0] == 0.0f && root.max[0] == (float)leaves && root.next == P);
     }
+    // point_light_bouncer.cpp:17-57: one light moving freely, one reflecting off the +x face
+    {
+        std::vector<float> pos = {0.0f, 0.0f, 0.0f, 1.0f, 0.75f, 0.0f, 0.0f, 1.0f};
+        std::vector<float> dir = {1.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 0.0f};
+        vren::owned_buffer pb(pos.size() * sizeof(float)), db(dir.size() * sizeof(float));
+        upload(pb, pos);
+        upload(db, dir);
+        const float lo[3] = {-1.0f, -1.0f, -1.0f}, hi[3] = {1.0f, 1.0f, 1.0f};
+        vren_demo::point_light_bouncer().bounce(0, stream, rc, pb, db, 2, lo, hi, 1.0f, 0.5f);
+        cudaStreamSynchronize(stream);
+        auto p = download<float>(pb, 8);
+        auto d = download<float>(db, 8);
+        EXPECT(p[0] == 0.5f && p[1] == 0.0f && d[0] == 1.0f);
+        EXPECT(p[4] > 0.7499f && p[4] < 0.7501f && d[4] == -1.0f);
+    }
     EXPECT(vren_device_error(1) == 0);
     cudaStreamDestroy(stream);
     std::printf("api ok\n");

@@ -56,6 +56,7 @@ PROTOTYPES: dict[str, tuple] = {
     "vren_build_bvh": (i32, [vp, vp, u32]),
     "vren_lbvh_scratch_bytes": (C.c_size_t, [u32]),
     "vren_build_lbvh": (i32, [vp, vp, u32, vp, u32, vp, vp]),
+    "vren_bounce_point_lights": (i32, [vp, vp, vp, u32, vp, vp, C.c_float, C.c_float]),
 }
 
 _LIB: C.CDLL | None = None

@@ -141,6 +141,16 @@ class assign_lights:
             indices.numel() if indices is not None else 0, _ptr(total), _ptr(self._scratch)), "assign_lights")
 
 
+def bounce_point_lights(stream, positions: torch.Tensor, directions: torch.Tensor, light_count: int, aabb_min,
+                        aabb_max, speed: float, dt: float) -> None:
+    """vren_demo's point-light bouncer (vren_bounce_point_lights): positions and directions (vec4 per
+    light, float32 device tensors) updated in place."""
+    lo = (C.c_float * 3)(*[float(x) for x in aabb_min])
+    hi = (C.c_float * 3)(*[float(x) for x in aabb_max])
+    check(lib().vren_bounce_point_lights(_stream(stream), _ptr(positions), _ptr(directions), light_count, lo, hi,
+                                         float(speed), float(dt)), "bounce_point_lights")
+
+
 class build_lbvh:
     """Karras binary radix tree over sorted leaves (extension; vren_build_lbvh).  `sorted_pairs` is a
     uvec2(key, payload) tensor in key order; leaf i's box is boxes[i >> box_shift] (None: infinite).
