@@ -246,6 +246,7 @@ def run_ours(args, rank: int, world: int):
     batched = None if args.quick else batched_vs_plain(args, dev, stream, flush)
     lbvh = None if args.quick else lbvh_bench(args, dev, stream, flush, depth, normals, pos, lights, view)
     bouncer = None if args.quick else bouncer_bench(args, dev, stream, flush, hbm_peak)
+    pyramid = None if args.quick else depth_pyramid_bench(args, dev, stream, flush, hbm_peak)
 
     clocks.__exit__(None, None, None)
     clk = clocks.summary()
@@ -303,6 +304,7 @@ def run_ours(args, rank: int, world: int):
             "shade": shade,
             "karras_lbvh": lbvh,
             "light_bouncer": bouncer,
+            "depth_pyramid": pyramid,
             "cpu_baseline": cpu,
             "clocks": clk,
             "device_error": err,
@@ -416,6 +418,29 @@ def bouncer_bench(args, dev, stream, flush, hbm_peak):
         gbs = 64.0 * n / (ms * 1e-3) / 1e9
         out[f"lights={n}"] = {"ms": round(ms, 5), "glights_s": round(n / (ms * 1e-3) / 1e9, 3),
                               "gbs_at_64B_per_light": round(gbs, 1), "hbm_frac": round(gbs / hbm_peak, 4)}
+    return out
+
+
+def depth_pyramid_bench(args, dev, stream, flush, hbm_peak):
+    """vren's depth-buffer pyramid (copy + all max levels, one launch) at the frame's 1920x1080, at
+    3840x2160 and at 8192x8192 (beyond L2); algorithmic bytes = 4 B read per level-0 texel + 4 B written
+    per texel of every level."""
+    import torch
+
+    from vren_gb300.depth_pyramid import depth_buffer_pyramid, depth_buffer_reductor
+
+    out = {}
+    red = depth_buffer_reductor()
+    for w, h in ((W, H), (3840, 2160), (8192, 8192)):
+        g = torch.Generator(device=dev).manual_seed(SEED + w)
+        depth = torch.rand(w * h, device=dev, generator=g)
+        pyr = depth_buffer_pyramid(w, h, dev)
+        texels = sum(max(w >> l, 1) * max(h >> l, 1) for l in range(pyr.get_level_count()))
+        ms = time_events(stream, lambda: red.copy_and_reduce(stream, depth, pyr), 3, args.steps, flush)
+        gbs = (4.0 * w * h + 4.0 * texels) / (ms * 1e-3) / 1e9
+        out[f"{w}x{h}"] = {"ms": round(ms, 5), "levels": pyr.get_level_count(), "gbs": round(gbs, 1),
+                           "hbm_frac": round(gbs / hbm_peak, 4)}
+        del depth, pyr
     return out
 
 
@@ -706,11 +731,15 @@ def cpu_baseline(depth, normals, pos, lights, radix_keys, view, budget_s: float 
     t2 = time.perf_counter()
     oracle.bounce_point_lights(bp, bd, 1 << 20, [-400.0, -250.0, 0.1], [400.0, 250.0, 1000.0], 20.0, 1.0 / 60.0)
     ms_bounce = (time.perf_counter() - t2) * 1e3
+    t3 = time.perf_counter()
+    oracle.depth_pyramid(depth, W, H)
+    ms_pyramid = (time.perf_counter() - t3) * 1e3
     return {"value": round(ms_frame, 3), "unit": "ms", "cores": threads, "kind": "port",
             "sample": f"{frames} frames of the CPU oracle pipeline (a6+a7+a8) at 1920x1080/16384 lights",
             "radix_sort_2^20_pairs_ms": round(ms_sort, 3),
             "radix_sort_gkeys_s": round(RADIX_N / (ms_sort * 1e-3) / 1e9, 4),
-            "light_bouncer_2^20_lights_ms": round(ms_bounce, 3)}
+            "light_bouncer_2^20_lights_ms": round(ms_bounce, 3),
+            "depth_pyramid_1920x1080_ms": round(ms_pyramid, 3)}
 
 
 # ------------------------------------------------------------------------------------------------
@@ -842,6 +871,16 @@ def run_profile(args):
         x = torch.from_numpy(scene.gen_u32(SEED, 2, n, mask=255).view(np.int32)).to(dev)
         scan = vg.blelloch_scan()
         fn = lambda: scan(stream, x, n)
+    elif args.profile in ("pyramid", "pyramid_4k"):
+        # the depth pyramid at 8192x8192 (268 MB read > L2) or at 3840x2160
+        from vren_gb300.depth_pyramid import depth_buffer_pyramid, depth_buffer_reductor
+
+        w, h = (8192, 8192) if args.profile == "pyramid" else (3840, 2160)
+        g = torch.Generator(device=dev).manual_seed(SEED)
+        depth = torch.rand(w * h, device=dev, generator=g)
+        pyr = depth_buffer_pyramid(w, h, dev)
+        red = depth_buffer_reductor()
+        fn = lambda: red.copy_and_reduce(stream, depth, pyr)
     elif args.profile in ("shade", "shade_backward"):
         ctx = cs.cluster_and_shade(SHADE_W, SHADE_H, 65536, 1 << 24)
         sb = shade_profile_setup(dev, stream, ctx)
@@ -864,7 +903,7 @@ def main():
     ap.add_argument("--quick", action="store_true", help="skip the primitive sweep and the large sorts")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--profile", choices=["frame", "batch", "find_unique", "radix", "scan", "shade",
-                                          "shade_backward"],
+                                          "shade_backward", "pyramid", "pyramid_4k"],
                     default=None,
                     help="run one kernel family on a case larger than L2 (for ncu) and exit")
     args = ap.parse_args()

@@ -331,6 +331,25 @@ int vren_cs_construct_light_bvh(vren_stream_t s, const float* light_positions, c
 int vren_bounce_point_lights(vren_stream_t s, float* light_positions, float* light_directions, uint32_t light_count,
                              const float* aabb_min, const float* aabb_max, float speed, float dt);
 
+/* ---- depth-buffer pyramid (vren/vren/pipeline/depth_buffer_pyramid.hpp) ---------------------------
+ * Level count floor(log2(max(width, height))) + 1 (depth_buffer_pyramid.cpp:18), level l is
+ * max(width >> l, 1) x max(height >> l, 1) texels (:48-54).  Levels are stored back to back in one
+ * float buffer, each row-major with a row pitch of its width, starting at
+ * vren_depth_pyramid_level_offset(width, height, l) floats (multiples of 64); level == level count
+ * gives the buffer length in floats.  Sides of 1..65535 texels (16 levels at most); 0 otherwise. */
+uint32_t vren_depth_pyramid_level_count(uint32_t width, uint32_t height);
+size_t vren_depth_pyramid_level_offset(uint32_t width, uint32_t height, uint32_t level);
+size_t vren_depth_pyramid_scratch_bytes(uint32_t width, uint32_t height);
+
+/* depth_buffer_reductor::copy_and_reduce (depth_buffer_pyramid.cpp:212-303; depth_buffer_copy.comp,
+ * depth_buffer_reduce.comp): level 0 = an exact copy of the row-major width x height depth buffer;
+ * each texel above = GLSL max folded from 0 over the 2x2 texels of the level below that lie inside it
+ * (NaN never enters, so texels above level 0 are +0 or positive).  One launch.  Both pointers 4-byte
+ * aligned (16-byte aligned with width % 4 == 0 takes 128-bit accesses); scratch sized by
+ * vren_depth_pyramid_scratch_bytes, zero-filled before first use, left reusable. */
+int vren_depth_pyramid_copy_and_reduce(vren_stream_t s, const float* depth_buffer, uint32_t width, uint32_t height,
+                                       float* pyramid, void* scratch);
+
 /* find_unique_cluster_list (clustered_shading.cpp:363-448, find_unique_clusters.comp:46-120).
  * key_count receives the number of keys written (the reference's dispatch_params.x); a list longer
  * than key_capacity is truncated and VREN_ERR_CAPACITY recorded.  tiles_x*tiles_y*1024 keys always fit.

@@ -345,6 +345,55 @@ private:
 }  // namespace clustered_shading
 
 // ------------------------------------------------------------------------------------------------
+// vren::depth_buffer_pyramid / vren::depth_buffer_reductor (pipeline/depth_buffer_pyramid.hpp):
+// all levels in one device buffer, level l at level_offset(l) floats, row pitch = its width.
+// ------------------------------------------------------------------------------------------------
+class depth_buffer_pyramid {
+public:
+    static const uint32_t k_max_depth_buffer_pyramid_level_count = 16;
+
+    depth_buffer_pyramid(uint32_t width, uint32_t height) :
+        m_base_width(width),
+        m_base_height(height),
+        m_level_count(vren_depth_pyramid_level_count(width, height))
+    {
+        if (m_level_count == 0) throw std::invalid_argument("depth_buffer_pyramid: unsupported size");
+        m_image = owned_buffer(vren_depth_pyramid_level_offset(width, height, m_level_count) * sizeof(float), false);
+    }
+
+    uint32_t get_image_width(uint32_t level) const { return (m_base_width >> level) ? (m_base_width >> level) : 1u; }
+    uint32_t get_image_height(uint32_t level) const { return (m_base_height >> level) ? (m_base_height >> level) : 1u; }
+    uint32_t get_level_count() const { return m_level_count; }
+    size_t level_offset(uint32_t level) const { return vren_depth_pyramid_level_offset(m_base_width, m_base_height, level); }
+    float* level(uint32_t level) const { return m_image.at<float>(level_offset(level) * sizeof(float)); }
+    device_buffer const& image() const { return m_image; }
+
+private:
+    friend class depth_buffer_reductor;
+    uint32_t m_base_width, m_base_height, m_level_count;
+    owned_buffer m_image;
+};
+
+class depth_buffer_reductor {
+public:
+    static const uint32_t k_workgroup_size_x = 32;
+    static const uint32_t k_workgroup_size_y = 32;
+
+    // depth_buffer: base_width x base_height floats, row-major (the depth attachment's texels).
+    void copy_and_reduce(cudaStream_t stream, resource_container&, device_buffer const& depth_buffer,
+                         depth_buffer_pyramid const& pyramid)
+    {
+        m_scratch.grow(vren_depth_pyramid_scratch_bytes(pyramid.m_base_width, pyramid.m_base_height));
+        check(vren_depth_pyramid_copy_and_reduce(stream, depth_buffer.at<float>(), pyramid.m_base_width,
+                                                 pyramid.m_base_height, pyramid.m_image.at<float>(), m_scratch.m_ptr),
+              "depth_buffer_reductor::copy_and_reduce");
+    }
+
+private:
+    owned_buffer m_scratch;
+};
+
+// ------------------------------------------------------------------------------------------------
 // vren::cluster_and_shade (clustered_shading.hpp:147-182): owns its buffers.
 // ------------------------------------------------------------------------------------------------
 class cluster_and_shade {

@@ -38,6 +38,8 @@ _PROTOS = {
     "oracle_cs_assign_lights": (u64, [vp, u32, u32, u32, vp, vp, u32, vp, vp, vp, vp, vp, u64, i32]),
     "oracle_lbvh_build": (None, [vp, vp, u32, vp]),
     "oracle_bounce_point_lights": (None, [vp, vp, u32, vp, vp, C.c_float, C.c_float]),
+    "oracle_depth_pyramid_level_count": (u32, [u32, u32]),
+    "oracle_depth_pyramid": (None, [vp, u32, u32, vp]),
     "oracle_cs_assign_lights_lbvh": (u64, [vp, u32, u32, u32, vp, vp, vp, vp, u32, vp, vp, vp, vp, vp, u64, i32]),
     "oracle_cs_shade_f64": (None, [vp, u32, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, u32, i32, i32, vp, vp, i32]),
     "oracle_cs_shade_grad_f64": (None, [vp, u32, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, u32, i32, vp, vp, i32]),
@@ -208,6 +210,25 @@ def bounce_point_lights(positions, directions, L: int, aabb_min, aabb_max, speed
     hi = np.array(aabb_max, np.float32)
     lib().oracle_bounce_point_lights(_p(p), _p(d), L, _p(lo), _p(hi), float(speed), float(dt))
     return p, d
+
+
+def depth_pyramid_level_count(width: int, height: int) -> int:
+    return int(lib().oracle_depth_pyramid_level_count(width, height))
+
+
+def depth_pyramid(depth, width: int, height: int) -> list:
+    """vren's depth-buffer pyramid (vren_oracle.c): one (h_l, w_l) float32 array per level."""
+    d = np.ascontiguousarray(depth, np.float32).reshape(-1)
+    assert d.size == width * height
+    levels = depth_pyramid_level_count(width, height)
+    sizes = [(max(height >> l, 1), max(width >> l, 1)) for l in range(levels)]
+    out = np.empty(sum(h * w for h, w in sizes), np.float32)
+    lib().oracle_depth_pyramid(_p(d), width, height, _p(out))
+    res, o = [], 0
+    for h, w in sizes:
+        res.append(out[o:o + h * w].reshape(h, w))
+        o += h * w
+    return res
 
 
 def lbvh_group_boxes(bvh, L: int) -> np.ndarray:

@@ -921,3 +921,44 @@ void oracle_bounce_point_lights(float* positions, float* directions, uint32_t L,
         directions[4 * i + 3] = 0.0f;
     }
 }
+
+/* ================================================================================================
+ * Depth-buffer pyramid — vren/vren/pipeline/depth_buffer_pyramid.cpp:18 (level count:
+ * glm::log2 of the integer max(width, height), from glm/gtc/integer.hpp = floor(log2) — plus 1),
+ * :48-54 (level size max(base >> level, 1)), :245-300 (one copy dispatch, then one reduce dispatch per
+ * level); vren/resources/shaders/depth_buffer_copy.comp:8-17 (nearest texel at an unnormalised
+ * integer coordinate: an exact copy) and depth_buffer_reduce.comp:10-34 (start from 0, GLSL max over
+ * the 2x2 sources that lie inside the source level, x outer, y inner).  Levels are stored back to back,
+ * row-major, with no padding.
+ * ================================================================================================ */
+uint32_t oracle_depth_pyramid_level_count(uint32_t width, uint32_t height)
+{
+    uint32_t m = width > height ? width : height, l = 0;
+    while (m >>= 1) ++l;
+    return l + 1;
+}
+
+void oracle_depth_pyramid(const float* depth, uint32_t width, uint32_t height, float* out)
+{
+    const uint32_t levels = oracle_depth_pyramid_level_count(width, height);
+    memcpy(out, depth, (size_t)width * height * sizeof(float));
+    float* from = out;
+    uint32_t fw = width, fh = height;
+    for (uint32_t l = 1; l < levels; ++l) {
+        const uint32_t tw = (width >> l) ? (width >> l) : 1u, th = (height >> l) ? (height >> l) : 1u;
+        float* to = from + (size_t)fw * fh;
+        for (uint32_t y = 0; y < th; ++y)
+            for (uint32_t x = 0; x < tw; ++x) {
+                float m = 0.0f;
+                for (uint32_t dx = 0; dx < 2; ++dx)
+                    for (uint32_t dy = 0; dy < 2; ++dy) {
+                        const uint32_t sx = 2 * x + dx, sy = 2 * y + dy;
+                        if (sx < fw && sy < fh) m = glsl_max(m, from[(size_t)sy * fw + sx]);
+                    }
+                to[(size_t)y * tw + x] = m;
+            }
+        from = to;
+        fw = tw;
+        fh = th;
+    }
+}

@@ -131,6 +131,10 @@ uint64_t oracle_cs_assign_lights_lbvh(const uint32_t* keys, uint32_t U, uint32_t
 void oracle_bounce_point_lights(float* positions, float* directions, uint32_t L, const float* aabb_min,
                                 const float* aabb_max, float speed, float dt);
 
+/* Depth-buffer pyramid: level count and all levels (level 0 = the depth copy), stored back to back. */
+uint32_t oracle_depth_pyramid_level_count(uint32_t width, uint32_t height);
+void oracle_depth_pyramid(const float* depth, uint32_t width, uint32_t height, float* out);
+
 /* ---- shading in FP64 (vren_oracle_shade.cpp): forward, forward-mode gradient, per-light loss ---- */
 void oracle_cs_shade_f64(const oracle_cs_view* v, uint32_t W, uint32_t H, const float* depth, const float* normals,
                          const float* albedo, const float* rough, const float* metal, const uint32_t* refs,

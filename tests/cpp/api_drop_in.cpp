@@ -122,6 +122,23 @@ int main()
         EXPECT(p[0] == 0.5f && p[1] == 0.0f && d[0] == 1.0f);
         EXPECT(p[4] > 0.7499f && p[4] < 0.7501f && d[4] == -1.0f);
     }
+    // depth_buffer_pyramid.cpp:212-303: a 5x3 depth buffer -> levels 5x3, 2x1, 1x1
+    {
+        std::vector<float> depth = {0.1f, 0.9f, 0.2f, 0.3f, 0.95f,  //
+                                    0.4f, -1.f, 0.5f, 0.8f, 0.99f,  //
+                                    0.7f, 0.6f, 0.2f, 0.1f, 0.98f};
+        vren::owned_buffer db(depth.size() * sizeof(float));
+        upload(db, depth);
+        vren::depth_buffer_pyramid pyramid(5, 3);
+        EXPECT(pyramid.get_level_count() == 3 && pyramid.get_image_width(1) == 2 && pyramid.get_image_height(1) == 1);
+        vren::depth_buffer_reductor().copy_and_reduce(stream, rc, db, pyramid);
+        cudaStreamSynchronize(stream);
+        std::vector<float> l1(2), l2(1);
+        cudaMemcpy(l1.data(), pyramid.level(1), 2 * sizeof(float), cudaMemcpyDeviceToHost);
+        cudaMemcpy(l2.data(), pyramid.level(2), sizeof(float), cudaMemcpyDeviceToHost);
+        // the last column and row of the odd level are never read
+        EXPECT(l1[0] == 0.9f && l1[1] == 0.8f && l2[0] == 0.9f);
+    }
     EXPECT(vren_device_error(1) == 0);
     cudaStreamDestroy(stream);
     std::printf("api ok\n");

@@ -131,3 +131,42 @@ def test_bvh_point_queries_match_linear_scan():
             lin = [i for i in range(leaf_count) if np.all(p >= f[i, 0:3]) and np.all(p <= f[i, 4:7])]
             got = sorted(oracle.bvh_point_query(built, root, p))
             assert got == lin
+
+
+def test_depth_pyramid_level_counts():
+    """depth_buffer_pyramid.cpp:18: glm::log2 of an unsigned integer (glm/gtc/integer.hpp) is the
+    floor of log2, so the level count is floor(log2(max(w, h))) + 1."""
+    for (w, h), n in {(1, 1): 1, (2, 1): 2, (1, 3): 2, (4, 4): 3, (5, 7): 3, (1920, 1080): 11,
+                      (2560, 1440): 12, (3840, 2160): 12, (4096, 1): 13, (65535, 3): 16}.items():
+        assert oracle.depth_pyramid_level_count(w, h) == n
+
+
+def _pyramid_closed_form(d0, w, h):
+    """Each level-l texel is max(+0, the non-NaN values of its level-0 block): the block is 2^l wide
+    on an axis until that axis reaches size 1 (at level floor(log2(size))), then stays at that width
+    (the odd last row or column of a level is never read)."""
+    pos = np.where(d0 > 0, d0, np.float32(0.0)).astype(np.float32)   # NaN, -0 and negatives -> +0
+    kx, ky = int(w).bit_length() - 1, int(h).bit_length() - 1
+    out = [d0]
+    for l in range(1, oracle.depth_pyramid_level_count(w, h)):
+        wl, hl = max(w >> l, 1), max(h >> l, 1)
+        bx, by = 1 << min(l, kx), 1 << min(l, ky)
+        out.append(pos[:hl * by, :wl * bx].reshape(hl, by, wl, bx).max(axis=(1, 3)))
+    return out
+
+
+@pytest.mark.parametrize("w,h", [(1, 1), (1, 9), (9, 1), (2, 2), (3, 5), (37, 64), (64, 64), (65, 127),
+                                 (128, 1), (200, 77), (333, 257), (1023, 17)])
+def test_depth_pyramid_restatement_against_closed_form(w, h):
+    rng = np.random.default_rng(w * 1000 + h)
+    d = rng.uniform(-0.2, 1.0, (h, w)).astype(np.float32)
+    flat = d.reshape(-1)
+    flat[rng.integers(0, flat.size, max(flat.size // 50, 1))] = np.nan
+    flat[rng.integers(0, flat.size, max(flat.size // 60, 1))] = -0.0
+    flat[rng.integers(0, flat.size, max(flat.size // 500, 1))] = np.inf
+    got = oracle.depth_pyramid(d, w, h)
+    want = _pyramid_closed_form(d, w, h)
+    assert len(got) == len(want)
+    assert np.array_equal(got[0].view(np.uint32), d.view(np.uint32))    # exact copy, NaN payloads kept
+    for g, e in zip(got[1:], want[1:]):
+        assert g.shape == e.shape and np.array_equal(g.view(np.uint32), e.view(np.uint32))

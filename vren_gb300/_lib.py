@@ -57,6 +57,10 @@ PROTOTYPES: dict[str, tuple] = {
     "vren_lbvh_scratch_bytes": (C.c_size_t, [u32]),
     "vren_build_lbvh": (i32, [vp, vp, u32, vp, u32, vp, vp]),
     "vren_bounce_point_lights": (i32, [vp, vp, vp, u32, vp, vp, C.c_float, C.c_float]),
+    "vren_depth_pyramid_level_count": (u32, [u32, u32]),
+    "vren_depth_pyramid_level_offset": (sz, [u32, u32, u32]),
+    "vren_depth_pyramid_scratch_bytes": (sz, [u32, u32]),
+    "vren_depth_pyramid_copy_and_reduce": (i32, [vp, vp, u32, u32, vp, vp]),
 }
 
 _LIB: C.CDLL | None = None
