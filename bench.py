@@ -245,6 +245,7 @@ def run_ours(args, rank: int, world: int):
     shade = shade_bench(args, dev, stream, flush, ctx)
     batched = None if args.quick else batched_vs_plain(args, dev, stream, flush)
     lbvh = None if args.quick else lbvh_bench(args, dev, stream, flush, depth, normals, pos, lights, view)
+    debug_views = None if args.quick else debug_views_bench(args, dev, stream, flush, ctx, hbm_peak)
     bouncer = None if args.quick else bouncer_bench(args, dev, stream, flush, hbm_peak)
     pyramid = None if args.quick else depth_pyramid_bench(args, dev, stream, flush, hbm_peak)
 
@@ -305,6 +306,7 @@ def run_ours(args, rank: int, world: int):
             "karras_lbvh": lbvh,
             "light_bouncer": bouncer,
             "depth_pyramid": pyramid,
+            "cluster_debug_views": debug_views,
             "cpu_baseline": cpu,
             "clocks": clk,
             "device_error": err,
@@ -339,18 +341,7 @@ def lbvh_bench(args, dev, stream, flush, depth, normals, pos, lights, view):
 
     import vren_gb300 as vg
     import vren_gb300.clustered_shading as cs
-
-    def dense(seed, n):
-        rng = np.random.default_rng(seed)
-        p = np.zeros((n, 4), np.float32)
-        p[:, 0] = rng.uniform(-8, 8, n)
-        p[:, 1] = rng.uniform(-5, 5, n)
-        p[:, 2] = rng.uniform(0.5, 25, n)
-        p[:, 3] = 1
-        q = np.zeros((n, 4), np.float32)
-        q[:, 0:3] = rng.uniform(0, 1, (n, 3))
-        q[:, 3] = np.exp(np.log(2.0) + 0.5 * rng.standard_normal(n)).astype(np.float32) * 0.5
-        return p.reshape(-1), q.reshape(-1)
+    import vren_gb300.scene as scene
 
     frame = cs.frame_to_device(cs.frame_build(view, W, H), dev)
     T = ((W + 31) // 32) * ((H + 31) // 32)
@@ -360,7 +351,7 @@ def lbvh_bench(args, dev, stream, flush, depth, normals, pos, lights, view):
     cs.find_unique_cluster_list()(stream, W, H, frame, torch.from_numpy(depth).to(dev),
                                   torch.from_numpy(normals).to(dev), keys, kc, refs)
     out = {}
-    for name, (p, q) in (("uniform_frustum_lights", (pos, lights)), ("lights_near_camera", dense(SEED + 77, L))):
+    for name, (p, q) in (("uniform_frustum_lights", (pos, lights)), ("lights_near_camera", scene.lights_near_camera(SEED + 77, L))):
         P = vg.calc_bvh_padded_leaf_count(L)
         vp = torch.zeros(L * 4, dtype=torch.float32, device=dev)
         bvh = torch.zeros(vg.calc_bvh_buffer_length(P) * 8, dtype=torch.int32, device=dev)
@@ -442,6 +433,31 @@ def depth_pyramid_bench(args, dev, stream, flush, hbm_peak):
                            "hbm_frac": round(gbs / hbm_peak, 4)}
         del depth, pyr
     return out
+
+
+def debug_views_bench(args, dev, stream, flush, ctx, hbm_peak):
+    """vren_demo's cluster debug views on the context's last frame (the 1920x1080 shading scene with
+    4096 lights near visible surfaces): show_clusters in every mode
+    (20 B per pixel: reference read, colour write; the per-cluster colour table is L2-resident) and
+    show_clusters_geometry (512 B written per cluster)."""
+    import vren_gb300.cluster_debug as cd
+    from vren_gb300.clustered_shading import read_device
+
+    out = ctx.outputs()
+    U = int(read_device(out.key_count, 1)[0])
+    view = cd.show_clusters()
+    rgba = None
+    res = {"clusters": U}
+    for name, mode in cd.MODES.items():
+        rgba = view(stream, mode, W, H, out, rgba)
+        ms = time_events(stream, lambda: view(stream, mode, W, H, out, rgba), 3, args.steps, flush)
+        gbs = 20.0 * W * H / (ms * 1e-3) / 1e9
+        res[f"show_clusters_{name}"] = {"ms": round(ms, 5), "gbs": round(gbs, 1), "hbm_frac": round(gbs / hbm_peak, 4)}
+    verts = cd.show_clusters_geometry(stream, out, max_clusters=max(U, 1))
+    ms = time_events(stream, lambda: cd.show_clusters_geometry(stream, out, verts, max_clusters=max(U, 1)), 3,
+                     args.steps, flush)
+    res["show_clusters_geometry"] = {"ms": round(ms, 5), "gbs": round(512.0 * U / (ms * 1e-3) / 1e9, 1)}
+    return res
 
 
 def radix_bench(args, dev, stream, flush, keys_np, hbm_peak):

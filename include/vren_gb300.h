@@ -448,6 +448,38 @@ int vren_cs_shade_backward(vren_stream_t s, const vren_cs_frame* frame, uint32_t
  * frame shape and replayed. */
 typedef struct vren_cluster_and_shade vren_cluster_and_shade;
 
+/* ---- headless cluster debug views (vren_demo/vren_demo/clustered_shading_debug.cpp:6-200) ---------- */
+#define VREN_SHOW_CLUSTERS_KEY 0
+#define VREN_SHOW_CLUSTERS_IJK 1
+#define VREN_SHOW_CLUSTERS_NORMAL 2
+#define VREN_SHOW_CLUSTERS_LIGHT_COUNTS 3
+#define VREN_SHOW_CLUSTERS_LIGHT_OFFSETS 4
+#define VREN_SHOW_CLUSTERS_LIGHT_INDICES 5
+
+/* vren::debug_renderer_vertex (vren/vren/pipeline/debug_renderer.hpp:25-31): 16 bytes. */
+typedef struct vren_debug_vertex {
+    float position[3];
+    uint32_t color; /* 0xRRGGBB */
+} vren_debug_vertex;
+
+/* show_clusters (show_clusters.comp:72-124): rgba (float4 per pixel, row-major width x height,
+ * 16-byte aligned) = the colour of each pixel's cluster for `mode` (VREN_SHOW_CLUSTERS_*; any other
+ * value draws red, as the shader does); tiles = ceil(size / 32) as in clustered_shading_debug.cpp:68-71.
+ * A reference >= min(*key_count, max_clusters) is drawn magenta (the shader reads out of bounds).
+ * counts/offsets are needed by the light modes, indices by LIGHT_INDICES.  scratch: 16-byte aligned,
+ * vren_cs_show_clusters_scratch_bytes(max_clusters). */
+size_t vren_cs_show_clusters_scratch_bytes(uint32_t max_clusters);
+int vren_cs_show_clusters(vren_stream_t s, int mode, uint32_t width, uint32_t height, const uint32_t* cluster_refs,
+                          const uint32_t* cluster_keys, const uint32_t* key_count, uint32_t max_clusters,
+                          const uint32_t* counts, const uint32_t* offsets, const uint32_t* indices, float* rgba,
+                          void* scratch);
+/* show_clusters_geometry (show_clusters_geometry.comp:55-110, debug.glsl): for each of the first
+ * min(*key_count, max_clusters) clusters, 32 vertices at vertices[32 c]: its view-space box as 12 lines
+ * (white; black for keys without a normal bin) and an arrow of length 0.01 along its normal bin (green
+ * shaft, red head; zero length without a bin).  The box is the one the light assignment tests. */
+int vren_cs_show_clusters_geometry(vren_stream_t s, const vren_cs_frame* frame, const uint32_t* cluster_keys,
+                                   const uint32_t* key_count, uint32_t max_clusters, vren_debug_vertex* vertices);
+
 typedef struct vren_cs_outputs {
     const float* view_positions;
     const vren_bvh_node* bvh;

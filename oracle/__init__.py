@@ -40,6 +40,8 @@ _PROTOS = {
     "oracle_bounce_point_lights": (None, [vp, vp, u32, vp, vp, C.c_float, C.c_float]),
     "oracle_depth_pyramid_level_count": (u32, [u32, u32]),
     "oracle_depth_pyramid": (None, [vp, u32, u32, vp]),
+    "oracle_cs_show_clusters": (None, [i32, u32, u32, vp, vp, u32, vp, vp, vp, vp]),
+    "oracle_cs_show_clusters_geometry": (None, [vp, u32, u32, vp, u32, vp]),
     "oracle_cs_assign_lights_lbvh": (u64, [vp, u32, u32, u32, vp, vp, vp, vp, u32, vp, vp, vp, vp, vp, u64, i32]),
     "oracle_cs_shade_f64": (None, [vp, u32, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, u32, i32, i32, vp, vp, i32]),
     "oracle_cs_shade_grad_f64": (None, [vp, u32, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, u32, i32, vp, vp, i32]),
@@ -200,6 +202,30 @@ def cs_assign_lights(keys, W: int, H: int, view, bvh, L: int, light_index, view_
                                           _p(np.ascontiguousarray(view_pos, np.float32)), _p(counts), _p(offsets),
                                           _p(indices), cap, threads)
     return counts[:U], offsets[:U], indices[: min(total, cap)].copy(), int(total)
+
+
+def cs_show_clusters(mode: int, W: int, H: int, refs, keys, counts=None, offsets=None, indices=None) -> np.ndarray:
+    """vren_demo's show_clusters view (vren_oracle.c): (H, W, 4) float32 RGBA."""
+    k = np.ascontiguousarray(keys, np.uint32)
+    U = k.size
+    z = np.zeros(1, np.uint32)
+    c = np.ascontiguousarray(counts if counts is not None else z, np.uint32)
+    o = np.ascontiguousarray(offsets if offsets is not None else z, np.uint32)
+    i = np.ascontiguousarray(indices if indices is not None and len(indices) else z, np.uint32)
+    out = np.empty((H, W, 4), np.float32)
+    lib().oracle_cs_show_clusters(mode, W, H, _p(np.ascontiguousarray(refs, np.uint32)), _p(k if U else z), U,
+                                  _p(c), _p(o), _p(i), _p(out))
+    return out
+
+
+def cs_show_clusters_geometry(view, W: int, H: int, keys) -> np.ndarray:
+    """vren_demo's show_clusters_geometry (vren_oracle.c): (U, 32, 4) uint32 debug vertices
+    (x, y, z float bits, colour)."""
+    k = np.ascontiguousarray(keys, np.uint32)
+    out = np.zeros((max(k.size, 1), 32, 4), np.uint32)
+    lib().oracle_cs_show_clusters_geometry(_view_ptr(view), W, H, _p(k if k.size else np.zeros(1, np.uint32)),
+                                           k.size, _p(out))
+    return out[:k.size]
 
 
 def bounce_point_lights(positions, directions, L: int, aabb_min, aabb_max, speed: float, dt: float):

@@ -962,3 +962,131 @@ void oracle_depth_pyramid(const float* depth, uint32_t width, uint32_t height, f
         fh = th;
     }
 }
+
+/* ================================================================================================
+ * Cluster debug views — vren_demo/resources/shaders/show_clusters.comp:50-124 (per pixel: the hash
+ * triple32 and hash(x) = float(triple32(x)) / float(0xffffffff), the six modes, red otherwise) and
+ * show_clusters_geometry.comp:55-110 with vren/resources/shaders/debug.glsl (VREN_DEBUG_WRITE_AABB /
+ * _ARROW vertex order); the box is cluster_aabb above (the one the assignment tests).  A pixel whose
+ * reference is >= U is drawn magenta (the shader would read out of bounds).
+ * ================================================================================================ */
+static uint32_t triple32(uint32_t x)
+{
+    x ^= x >> 17;
+    x *= 0xed5ad4bbu;
+    x ^= x >> 11;
+    x *= 0xac4c1b51u;
+    x ^= x >> 15;
+    x *= 0x31848babu;
+    x ^= x >> 14;
+    return x;
+}
+
+static float hash01(uint32_t x) { return (float)triple32(x) / (float)0xffffffffu; }
+
+void oracle_cs_show_clusters(int mode, uint32_t W, uint32_t H, const uint32_t* refs, const uint32_t* keys, uint32_t U,
+                             const uint32_t* counts, const uint32_t* offsets, const uint32_t* indices, float* out)
+{
+    const uint32_t TX = (W + 31) / 32, TY = (H + 31) / 32;
+    for (uint64_t p = 0; p < (uint64_t)W * H; ++p) {
+        float* o = out + 4 * p;
+        const uint32_t r = refs[p];
+        float c[3];
+        if (r >= U) {
+            c[0] = 1.0f; c[1] = 0.0f; c[2] = 1.0f;
+        } else {
+            const uint32_t key = keys[r];
+            const uint32_t ci = key & 0xFFu, cj = (key >> 8) & 0xFFu, ck = (key >> 16) & 0x3FFu, n = key >> 26;
+            if (mode == 0) {
+                c[0] = c[1] = c[2] = hash01(key);
+            } else if (mode == 1) {
+                c[0] = (float)ci / (float)TX;
+                c[1] = (float)cj / (float)TY;
+                c[2] = (float)ck / (float)1024;
+            } else if (mode == 2) {
+                c[0] = (float)(n / 9u) / 6.0f;
+                c[1] = (float)((n / 3u) % 3u) / 3.0f;
+                c[2] = (float)(n % 3u) / 3.0f;
+            } else if (mode == 3) {
+                c[0] = c[1] = c[2] = glsl_min((float)counts[r] / 64.0f, 1.0f);
+            } else if (mode == 4) {
+                c[0] = c[1] = c[2] = hash01(offsets[r]);
+            } else if (mode == 5) {
+                uint32_t h = 0;
+                for (uint32_t i = 0; i < counts[r]; ++i) h ^= indices[offsets[r] + i];
+                c[0] = c[1] = c[2] = hash01(h);
+            } else {
+                c[0] = 1.0f; c[1] = 0.0f; c[2] = 0.0f;
+            }
+        }
+        o[0] = c[0]; o[1] = c[1]; o[2] = c[2]; o[3] = 1.0f;
+    }
+}
+
+static void dbg_vertex(uint32_t* out, uint32_t* k, float x, float y, float z, uint32_t colour)
+{
+    memcpy(out + 4 * *k + 0, &x, 4);
+    memcpy(out + 4 * *k + 1, &y, 4);
+    memcpy(out + 4 * *k + 2, &z, 4);
+    out[4 * *k + 3] = colour;
+    ++*k;
+}
+
+static void dbg_line(uint32_t* out, uint32_t* k, const float a[3], const float b[3], uint32_t colour)
+{
+    dbg_vertex(out, k, a[0], a[1], a[2], colour);
+    dbg_vertex(out, k, b[0], b[1], b[2], colour);
+}
+
+void oracle_cs_show_clusters_geometry(const oracle_cs_view* v, uint32_t W, uint32_t H, const uint32_t* keys,
+                                      uint32_t U, uint32_t* out)
+{
+    const uint32_t TX = (W + 31) / 32, TY = (H + 31) / 32;
+    float bnear[ORACLE_SLICES], bfar[ORACLE_SLICES];
+    oracle_cs_slice_table(v, TY, bnear, bfar);
+    for (uint32_t c = 0; c < U; ++c) {
+        uint32_t* o = out + (size_t)c * 32 * 4;
+        uint32_t k = 0;
+        const caabb b = cluster_aabb(keys[c], TX, TY, v, bnear, bfar);
+        const float* m = b.mn;
+        const float* M = b.mx;
+        const uint32_t n = keys[c] >> 26;
+        const uint32_t col = n < 0x3Fu ? 0xFFFFFFu : 0u;
+        /* VREN_DEBUG_WRITE_AABB(_m, _M) */
+        const float e[24][3] = {
+            {m[0], m[1], m[2]}, {M[0], m[1], m[2]}, {M[0], m[1], m[2]}, {M[0], m[1], M[2]},
+            {M[0], m[1], M[2]}, {m[0], m[1], M[2]}, {m[0], m[1], M[2]}, {m[0], m[1], m[2]},
+            {m[0], M[1], m[2]}, {M[0], M[1], m[2]}, {M[0], M[1], m[2]}, {M[0], M[1], M[2]},
+            {M[0], M[1], M[2]}, {m[0], M[1], M[2]}, {m[0], M[1], M[2]}, {m[0], M[1], m[2]},
+            {m[0], m[1], m[2]}, {m[0], M[1], m[2]}, {M[0], m[1], m[2]}, {M[0], M[1], m[2]},
+            {M[0], m[1], M[2]}, {M[0], M[1], M[2]}, {m[0], m[1], M[2]}, {m[0], M[1], M[2]},
+        };
+        for (int i = 0; i < 24; i += 2) dbg_line(o, &k, e[i], e[i + 1], col);
+        float pos[3], to[3];
+        for (int a = 0; a < 3; ++a) pos[a] = (m[a] + M[a]) / 2.0f;
+        if (n < 0x3Fu) {
+            const uint32_t face = n / 9u, axis = face % 3u, uc = (axis + 1u) % 3u, vc = (axis + 2u) % 3u;
+            float d[3];
+            d[axis] = (face / 3u) == 1u ? 1.0f : -1.0f;
+            d[uc] = (((float)((n / 3u) % 3u) + 0.5f) / 3.0f) * 2.0f - 1.0f;
+            d[vc] = (((float)(n % 3u) + 0.5f) / 3.0f) * 2.0f - 1.0f;
+            const float len = sqrtf((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]);
+            for (int a = 0; a < 3; ++a) to[a] = pos[a] + (d[a] / len) * 0.01f;
+        } else {
+            for (int a = 0; a < 3; ++a) to[a] = pos[a];
+        }
+        /* VREN_DEBUG_WRITE_ARROW(pos, to, green, red) */
+        dbg_line(o, &k, pos, to, 0x00FF00u);
+        const float dx = pos[0] - to[0], dy = pos[1] - to[1], dz = pos[2] - to[2];
+        const float h = sqrtf((dx * dx + dy * dy) + dz * dz) * 0.1f;
+        const float sg[3][2][3] = {{{-1, -1, -1}, {1, 1, 1}}, {{1, 1, -1}, {-1, -1, 1}}, {{1, -1, -1}, {-1, 1, 1}}};
+        for (int l = 0; l < 3; ++l) {
+            float a0[3], a1[3];
+            for (int a = 0; a < 3; ++a) {
+                a0[a] = to[a] + sg[l][0][a] * h;
+                a1[a] = to[a] + sg[l][1][a] * h;
+            }
+            dbg_line(o, &k, a0, a1, 0xFF0000u);
+        }
+    }
+}

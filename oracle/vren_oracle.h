@@ -135,6 +135,13 @@ void oracle_bounce_point_lights(float* positions, float* directions, uint32_t L,
 uint32_t oracle_depth_pyramid_level_count(uint32_t width, uint32_t height);
 void oracle_depth_pyramid(const float* depth, uint32_t width, uint32_t height, float* out);
 
+/* Cluster debug views: RGBA float per pixel (mode 0..5, other values red); 32 debug vertices
+ * (x, y, z as float bits, colour) per cluster. */
+void oracle_cs_show_clusters(int mode, uint32_t W, uint32_t H, const uint32_t* refs, const uint32_t* keys, uint32_t U,
+                             const uint32_t* counts, const uint32_t* offsets, const uint32_t* indices, float* out);
+void oracle_cs_show_clusters_geometry(const oracle_cs_view* v, uint32_t W, uint32_t H, const uint32_t* keys,
+                                      uint32_t U, uint32_t* out);
+
 /* ---- shading in FP64 (vren_oracle_shade.cpp): forward, forward-mode gradient, per-light loss ---- */
 void oracle_cs_shade_f64(const oracle_cs_view* v, uint32_t W, uint32_t H, const float* depth, const float* normals,
                          const float* albedo, const float* rough, const float* metal, const uint32_t* refs,

@@ -61,6 +61,9 @@ PROTOTYPES: dict[str, tuple] = {
     "vren_depth_pyramid_level_offset": (sz, [u32, u32, u32]),
     "vren_depth_pyramid_scratch_bytes": (sz, [u32, u32]),
     "vren_depth_pyramid_copy_and_reduce": (i32, [vp, vp, u32, u32, vp, vp]),
+    "vren_cs_show_clusters_scratch_bytes": (sz, [u32]),
+    "vren_cs_show_clusters": (i32, [vp, i32, u32, u32, vp, vp, vp, u32, vp, vp, vp, vp, vp]),
+    "vren_cs_show_clusters_geometry": (i32, [vp, vp, vp, vp, u32, vp]),
 }
 
 _LIB: C.CDLL | None = None

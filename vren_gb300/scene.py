@@ -89,3 +89,18 @@ def lights_near_surfaces(seed: int, count: int, depth: np.ndarray, width: int, h
     d = np.ascontiguousarray(depth, np.float32)
     lib().vren_gen_lights_near_surfaces(seed, C.byref(cam), _p(d), count, _p(pos), _p(li))
     return pos, li
+
+
+def lights_near_camera(seed: int, count: int):
+    """Lights packed in front of the camera (x in [-8, 8], y in [-5, 5], z in [0.5, 25], radius
+    lognormal around 1): many lights per cluster.  Returns flat vec4 positions and point lights."""
+    rng = np.random.default_rng(seed)
+    p = np.zeros((count, 4), np.float32)
+    p[:, 0] = rng.uniform(-8, 8, count)
+    p[:, 1] = rng.uniform(-5, 5, count)
+    p[:, 2] = rng.uniform(0.5, 25, count)
+    p[:, 3] = 1
+    q = np.zeros((count, 4), np.float32)
+    q[:, 0:3] = rng.uniform(0, 1, (count, 3))
+    q[:, 3] = np.exp(np.log(2.0) + 0.5 * rng.standard_normal(count)).astype(np.float32) * 0.5
+    return p.reshape(-1), q.reshape(-1)
