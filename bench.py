@@ -248,6 +248,7 @@ def run_ours(args, rank: int, world: int):
     debug_views = None if args.quick else debug_views_bench(args, dev, stream, flush, ctx, hbm_peak)
     bouncer = None if args.quick else bouncer_bench(args, dev, stream, flush, hbm_peak)
     pyramid = None if args.quick else depth_pyramid_bench(args, dev, stream, flush, hbm_peak)
+    kdtree = None if args.quick else kd_tree_bench(args, dev, stream, flush)
 
     clocks.__exit__(None, None, None)
     clk = clocks.summary()
@@ -307,6 +308,7 @@ def run_ours(args, rank: int, world: int):
             "light_bouncer": bouncer,
             "depth_pyramid": pyramid,
             "cluster_debug_views": debug_views,
+            "kd_tree": kdtree,
             "cpu_baseline": cpu,
             "clocks": clk,
             "device_error": err,
@@ -458,6 +460,32 @@ def debug_views_bench(args, dev, stream, flush, ctx, hbm_peak):
                      args.steps, flush)
     res["show_clusters_geometry"] = {"ms": round(ms, 5), "gbs": round(512.0 * U / (ms * 1e-3) / 1e9, 1)}
     return res
+
+
+def kd_tree_bench(args, dev, stream, flush):
+    """vren's k-d tree: host build of 1M uniform points (max 8 per leaf, the reference test's tree),
+    then nearest-neighbour searches on the GPU: the reference test's 100 samples and 1M samples."""
+    import torch
+
+    from vren_gb300 import kd_tree as kd
+
+    rng = np.random.default_rng(SEED + 31)
+    pts = rng.uniform(0, 100, (1_000_000, 3)).astype(np.float32)
+    t0 = time.perf_counter()
+    nodes, _ = kd.kd_tree_build(pts)
+    build_ms = (time.perf_counter() - t0) * 1e3
+    depth = kd.kd_tree_depth(nodes)
+    d_pts = torch.from_numpy(pts.reshape(-1)).to(dev)
+    d_nodes = torch.from_numpy(nodes.view(np.int32).reshape(-1)).to(dev)
+    out = {"points": 1_000_000, "nodes": int(len(nodes)), "depth": depth, "host_build_ms": round(build_ms, 2)}
+    for q in (100, 1_000_000):
+        smp = torch.from_numpy(rng.uniform(0, 100, (q, 3)).astype(np.float32).reshape(-1)).to(dev)
+        bp = torch.empty(q, dtype=torch.int32, device=dev)
+        bd = torch.empty(q, dtype=torch.float32, device=dev)
+        ms = time_events(stream, lambda: kd.kd_tree_search_batch(stream, d_pts, d_nodes, smp, depth, best_points=bp,
+                                                                 best_distances=bd), 3, args.steps, flush)
+        out[f"gpu_search_{q}_samples"] = {"ms": round(ms, 4), "msearch_s": round(q / (ms * 1e-3) / 1e6, 2)}
+    return out
 
 
 def radix_bench(args, dev, stream, flush, keys_np, hbm_peak):
@@ -750,12 +778,19 @@ def cpu_baseline(depth, normals, pos, lights, radix_keys, view, budget_s: float 
     t3 = time.perf_counter()
     oracle.depth_pyramid(depth, W, H)
     ms_pyramid = (time.perf_counter() - t3) * 1e3
+    kp = np.random.default_rng(SEED + 31).uniform(0, 100, (1_000_000, 3)).astype(np.float32)
+    knodes, _ = oracle.kd_tree_build(kp)
+    ks = np.random.default_rng(SEED + 32).uniform(0, 100, (100_000, 3)).astype(np.float32)
+    t4 = time.perf_counter()
+    oracle.kd_tree_search(kp, knodes, ks)
+    ms_kd = (time.perf_counter() - t4) * 1e3
     return {"value": round(ms_frame, 3), "unit": "ms", "cores": threads, "kind": "port",
             "sample": f"{frames} frames of the CPU oracle pipeline (a6+a7+a8) at 1920x1080/16384 lights",
             "radix_sort_2^20_pairs_ms": round(ms_sort, 3),
             "radix_sort_gkeys_s": round(RADIX_N / (ms_sort * 1e-3) / 1e9, 4),
             "light_bouncer_2^20_lights_ms": round(ms_bounce, 3),
-            "depth_pyramid_1920x1080_ms": round(ms_pyramid, 3)}
+            "depth_pyramid_1920x1080_ms": round(ms_pyramid, 3),
+            "kd_tree_search_100k_samples_1m_points_ms": round(ms_kd, 3)}
 
 
 # ------------------------------------------------------------------------------------------------

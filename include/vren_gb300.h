@@ -448,6 +448,46 @@ int vren_cs_shade_backward(vren_stream_t s, const vren_cs_frame* frame, uint32_t
  * frame shape and replayed. */
 typedef struct vren_cluster_and_shade vren_cluster_and_shade;
 
+/* ---- k-d tree (vren/vren/base/kd_tree.hpp) --------------------------------------------------------
+ * vren::kd_tree_node: 12 bytes (the reference's 2-bit axis field and the union of 30-bit fields after
+ * it occupy separate words).  axis 0..2 = inner node splitting at `split`, right child `value` nodes
+ * after it, left child next; axis 3 = leaf holding point `index`, the first leaf of a run has
+ * value = run length, the others 0x3FFFFFFF. */
+typedef struct vren_kd_tree_node {
+    union {
+        float split;
+        uint32_t index;
+    };
+    uint32_t axis;
+    uint32_t value;
+} vren_kd_tree_node;
+
+/* Returns nonzero to accept `point` (the reference's kd_tree_search_filter_t). */
+typedef int (*vren_kd_tree_filter)(uint32_t point, void* user);
+
+/* kd_tree_build (kd_tree.cpp:5-77), on the host: same node array as the reference (pre-order, Welford
+ * mean split on the axis its variance test picks, in-place swap partition of `indices`).  Returns the
+ * offset after the last node written (the node count for node_offset = 0; at most 2 * count).  A node
+ * whose split separates nothing (where the reference asserts) becomes one leaf run of all its points. */
+size_t vren_kd_tree_build(const float* points, size_t point_stride, uint32_t* indices, size_t count,
+                          vren_kd_tree_node* kd_tree, size_t node_offset, size_t max_leaf_point_count);
+/* Inner nodes on the longest root-to-leaf path (host). */
+uint32_t vren_kd_tree_depth(const vren_kd_tree_node* kd_tree, size_t node_offset);
+/* kd_tree_search (kd_tree.cpp:79-131), on the host: best_point / best_distance_squared are in-out (start
+ * them at UINT32_MAX / +inf); filter NULL accepts every point. */
+void vren_kd_tree_search(const float* points, size_t point_stride, const uint32_t* indices, size_t count,
+                         const vren_kd_tree_node* kd_tree, size_t node_offset, const float* sample,
+                         vren_kd_tree_filter filter, void* filter_user, uint32_t* best_point,
+                         float* best_distance_squared);
+/* The same search for many samples on the GPU (device pointers; one thread per sample), same visit
+ * order and so the same results, ties included, as the host search started at UINT32_MAX / +inf.
+ * excluded (optional, one byte per point, nonzero = filtered out) stands for the filter.  max_depth
+ * (vren_kd_tree_depth) above 128 returns VREN_ERR_CAPACITY. */
+int vren_kd_tree_search_batch(vren_stream_t s, const float* points, uint32_t point_stride, uint32_t point_count,
+                              const vren_kd_tree_node* kd_tree, uint32_t node_count, uint32_t max_depth,
+                              const float* samples, uint32_t sample_stride, uint32_t sample_count,
+                              const uint8_t* excluded, uint32_t* best_points, float* best_distances_squared);
+
 /* ---- headless cluster debug views (vren_demo/vren_demo/clustered_shading_debug.cpp:6-200) ---------- */
 #define VREN_SHOW_CLUSTERS_KEY 0
 #define VREN_SHOW_CLUSTERS_IJK 1

@@ -42,6 +42,9 @@ _PROTOS = {
     "oracle_depth_pyramid": (None, [vp, u32, u32, vp]),
     "oracle_cs_show_clusters": (None, [i32, u32, u32, vp, vp, u32, vp, vp, vp, vp]),
     "oracle_cs_show_clusters_geometry": (None, [vp, u32, u32, vp, u32, vp]),
+    "oracle_kd_tree_build": (u64, [vp, u64, vp, u64, vp, u64]),
+    "oracle_kd_tree_search": (None, [vp, u64, vp, vp, u64, u32, vp, vp, vp]),
+    "oracle_linear_nn_search": (None, [vp, u64, vp, u64, vp, u64, u32, vp, vp]),
     "oracle_cs_assign_lights_lbvh": (u64, [vp, u32, u32, u32, vp, vp, vp, vp, u32, vp, vp, vp, vp, vp, u64, i32]),
     "oracle_cs_shade_f64": (None, [vp, u32, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, u32, i32, i32, vp, vp, i32]),
     "oracle_cs_shade_grad_f64": (None, [vp, u32, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, u32, i32, vp, vp, i32]),
@@ -226,6 +229,41 @@ def cs_show_clusters_geometry(view, W: int, H: int, keys) -> np.ndarray:
     lib().oracle_cs_show_clusters_geometry(_view_ptr(view), W, H, _p(k if k.size else np.zeros(1, np.uint32)),
                                            k.size, _p(out))
     return out[:k.size]
+
+
+def kd_tree_build(points, stride: int = 3, max_leaf: int = 8, indices=None):
+    """vren's kd_tree_build (vren_oracle.c): returns (nodes (n, 3) uint32, permuted indices)."""
+    pts = np.ascontiguousarray(points, np.float32).reshape(-1)
+    count = pts.size // stride
+    idx = np.arange(count, dtype=np.uint32) if indices is None else np.array(indices, np.uint32)
+    nodes = np.zeros((max(2 * len(idx), 1), 3), np.uint32)
+    n = lib().oracle_kd_tree_build(_p(pts), stride, _p(idx), len(idx), _p(nodes), max_leaf)
+    return nodes[:n].copy(), idx
+
+
+def kd_tree_search(points, nodes, samples, stride: int = 3, sample_stride: int = 3, excluded=None):
+    """Recursive kd_tree_search per sample from (UINT32_MAX, +inf): (best_points, best_dist)."""
+    pts = np.ascontiguousarray(points, np.float32).reshape(-1)
+    smp = np.ascontiguousarray(samples, np.float32).reshape(-1)
+    q = smp.size // sample_stride
+    bp = np.zeros(max(q, 1), np.uint32)
+    bd = np.zeros(max(q, 1), np.float32)
+    ex = None if excluded is None else np.ascontiguousarray(excluded, np.uint8)
+    lib().oracle_kd_tree_search(_p(pts), stride, _p(np.ascontiguousarray(nodes, np.uint32)), _p(smp), sample_stride,
+                                q, None if ex is None else _p(ex), _p(bp), _p(bd))
+    return bp[:q], bd[:q]
+
+
+def linear_nn_search(points, samples, stride: int = 3, sample_stride: int = 3, indices=None):
+    pts = np.ascontiguousarray(points, np.float32).reshape(-1)
+    smp = np.ascontiguousarray(samples, np.float32).reshape(-1)
+    count = pts.size // stride
+    idx = np.arange(count, dtype=np.uint32) if indices is None else np.ascontiguousarray(indices, np.uint32)
+    q = smp.size // sample_stride
+    bp = np.zeros(max(q, 1), np.uint32)
+    bd = np.zeros(max(q, 1), np.float32)
+    lib().oracle_linear_nn_search(_p(pts), stride, _p(idx), len(idx), _p(smp), sample_stride, q, _p(bp), _p(bd))
+    return bp[:q], bd[:q]
 
 
 def bounce_point_lights(positions, directions, L: int, aabb_min, aabb_max, speed: float, dt: float):

@@ -1090,3 +1090,122 @@ void oracle_cs_show_clusters_geometry(const oracle_cs_view* v, uint32_t W, uint3
         }
     }
 }
+
+/* ================================================================================================
+ * k-d tree — vren/vren/base/kd_tree.cpp:5-77 (build, recursive as written: Welford mean/variance in
+ * float, the axis test comparing variance[0] with variance[1] twice, swap partition by
+ * point[axis] < split) and :79-131 (search: near child first, far child when best > d * d), with the
+ * node as the reference lays it out (12 bytes: split/index, axis, 30-bit value).  Where a split
+ * separates nothing (the reference asserts), the node becomes one leaf run (canonical).
+ * vren_test/vren_test/kd_tree.cpp:9-27 (linear search) is the reference's own check.
+ * ================================================================================================ */
+static size_t kd_build_rec(const float* points, size_t stride, uint32_t* idx, size_t count, oracle_kd_node* t,
+                           size_t off, size_t max_leaf)
+{
+    int leaf = count <= max_leaf;
+    size_t middle = 0;
+    uint32_t axis = 0;
+    float split = 0.0f;
+    if (!leaf) {
+        float mean[3] = {0, 0, 0}, var[3] = {0, 0, 0}, n = 1.0f;
+        for (size_t i = 0; i < count; i++, n += 1.0f) {
+            const float* p = points + (size_t)idx[i] * stride;
+            for (int j = 0; j < 3; j++) {
+                float d = p[j] - mean[j];
+                mean[j] += d / n;
+                var[j] += (p[j] - mean[j]) * d;
+            }
+        }
+        axis = var[0] > var[1] && var[0] > var[1] ? 0 : (var[1] > var[2] ? 1 : 2);
+        split = mean[axis];
+        for (size_t i = 0; i < count; i++) {
+            const float* p = points + (size_t)idx[i] * stride;
+            if (p[axis] < split) {
+                uint32_t tmp = idx[i];
+                idx[i] = idx[middle];
+                idx[middle] = tmp;
+                middle++;
+            }
+        }
+        leaf = middle == 0 || middle == count;
+    }
+    if (leaf) {
+        for (size_t i = 0; i < count; i++) {
+            t[off + i].word0 = idx[i];
+            t[off + i].axis = 3;
+            t[off + i].value = i == 0 ? (uint32_t)count & 0x3FFFFFFFu : 0x3FFFFFFFu;
+        }
+        return off + count;
+    }
+    size_t next = kd_build_rec(points, stride, idx, middle, t, off + 1, max_leaf);
+    memcpy(&t[off].word0, &split, 4);
+    t[off].axis = axis;
+    t[off].value = (uint32_t)(next - off) & 0x3FFFFFFFu;
+    return kd_build_rec(points, stride, idx + middle, count - middle, t, next, max_leaf);
+}
+
+size_t oracle_kd_tree_build(const float* points, size_t stride, uint32_t* indices, size_t count, oracle_kd_node* tree,
+                            size_t max_leaf)
+{
+    return count ? kd_build_rec(points, stride, indices, count, tree, 0, max_leaf) : 0;
+}
+
+static void kd_search_rec(const float* points, size_t stride, const oracle_kd_node* t, size_t off, const float* s,
+                          const uint8_t* excluded, uint32_t* best_point, float* best)
+{
+    const oracle_kd_node* nd = &t[off];
+    if (nd->axis == 3) {
+        for (uint32_t i = 0; i < nd->value; i++) {
+            uint32_t id = t[off + i].word0;
+            if (excluded && excluded[id]) continue;
+            const float* p = points + (size_t)id * stride;
+            float dist = (s[0] - p[0]) * (s[0] - p[0]) + (s[1] - p[1]) * (s[1] - p[1]) + (s[2] - p[2]) * (s[2] - p[2]);
+            if (dist < *best) {
+                *best_point = id;
+                *best = dist;
+            }
+        }
+        return;
+    }
+    float split;
+    memcpy(&split, &nd->word0, 4);
+    float d = s[nd->axis] - split;
+    size_t first = d <= 0 ? off + 1 : off + nd->value;
+    size_t second = d <= 0 ? off + nd->value : off + 1;
+    kd_search_rec(points, stride, t, first, s, excluded, best_point, best);
+    if (*best > d * d) kd_search_rec(points, stride, t, second, s, excluded, best_point, best);
+}
+
+void oracle_kd_tree_search(const float* points, size_t stride, const oracle_kd_node* tree, const float* samples,
+                           size_t sample_stride, uint32_t sample_count, const uint8_t* excluded, uint32_t* best_points,
+                           float* best_dist)
+{
+    for (uint32_t q = 0; q < sample_count; q++) {
+        uint32_t bp = 0xFFFFFFFFu;
+        float bd = INFINITY;
+        kd_search_rec(points, stride, tree, 0, samples + (size_t)q * sample_stride, excluded, &bp, &bd);
+        best_points[q] = bp;
+        best_dist[q] = bd;
+    }
+}
+
+void oracle_linear_nn_search(const float* points, size_t stride, const uint32_t* indices, size_t count,
+                             const float* samples, size_t sample_stride, uint32_t sample_count, uint32_t* best_points,
+                             float* best_dist)
+{
+    for (uint32_t q = 0; q < sample_count; q++) {
+        const float* s = samples + (size_t)q * sample_stride;
+        float bd = INFINITY;
+        uint32_t bp = 0xFFFFFFFFu;
+        for (size_t i = 0; i < count; i++) {
+            const float* p = points + (size_t)indices[i] * stride;
+            float dist = (s[0] - p[0]) * (s[0] - p[0]) + (s[1] - p[1]) * (s[1] - p[1]) + (s[2] - p[2]) * (s[2] - p[2]);
+            if (dist < bd) {
+                bd = dist;
+                bp = indices[i];
+            }
+        }
+        best_points[q] = bp;
+        best_dist[q] = bd;
+    }
+}

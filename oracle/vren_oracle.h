@@ -142,6 +142,21 @@ void oracle_cs_show_clusters(int mode, uint32_t W, uint32_t H, const uint32_t* r
 void oracle_cs_show_clusters_geometry(const oracle_cs_view* v, uint32_t W, uint32_t H, const uint32_t* keys,
                                       uint32_t U, uint32_t* out);
 
+/* k-d tree: build (returns the node count), batched recursive search, linear search. */
+typedef struct oracle_kd_node {
+    uint32_t word0; /* split (float bits) or point index */
+    uint32_t axis;
+    uint32_t value;
+} oracle_kd_node;
+size_t oracle_kd_tree_build(const float* points, size_t stride, uint32_t* indices, size_t count, oracle_kd_node* tree,
+                            size_t max_leaf);
+void oracle_kd_tree_search(const float* points, size_t stride, const oracle_kd_node* tree, const float* samples,
+                           size_t sample_stride, uint32_t sample_count, const uint8_t* excluded, uint32_t* best_points,
+                           float* best_dist);
+void oracle_linear_nn_search(const float* points, size_t stride, const uint32_t* indices, size_t count,
+                             const float* samples, size_t sample_stride, uint32_t sample_count, uint32_t* best_points,
+                             float* best_dist);
+
 /* ---- shading in FP64 (vren_oracle_shade.cpp): forward, forward-mode gradient, per-light loss ---- */
 void oracle_cs_shade_f64(const oracle_cs_view* v, uint32_t W, uint32_t H, const float* depth, const float* normals,
                          const float* albedo, const float* rough, const float* metal, const uint32_t* refs,

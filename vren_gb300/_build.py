@@ -40,7 +40,7 @@ NVCC_FLAGS = [
 ]
 # Translation units whose float arithmetic must match the CPU oracle bit for bit are also
 # compiled without FMA contraction (the kernels use __f*_rn intrinsics on those paths too).
-NO_FMAD_UNITS = {"clustered.cu", "batch.cu", "lbvh.cu", "lights.cu", "cluster_debug.cu"}
+NO_FMAD_UNITS = {"clustered.cu", "batch.cu", "lbvh.cu", "lights.cu", "cluster_debug.cu", "kd_tree.cu"}
 
 
 def _nvcc() -> str:

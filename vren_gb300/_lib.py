@@ -64,6 +64,10 @@ PROTOTYPES: dict[str, tuple] = {
     "vren_cs_show_clusters_scratch_bytes": (sz, [u32]),
     "vren_cs_show_clusters": (i32, [vp, i32, u32, u32, vp, vp, vp, u32, vp, vp, vp, vp, vp]),
     "vren_cs_show_clusters_geometry": (i32, [vp, vp, vp, vp, u32, vp]),
+    "vren_kd_tree_build": (sz, [vp, sz, vp, sz, vp, sz, sz]),
+    "vren_kd_tree_depth": (u32, [vp, sz]),
+    "vren_kd_tree_search": (None, [vp, sz, vp, sz, vp, sz, vp, vp, vp, vp, vp]),
+    "vren_kd_tree_search_batch": (i32, [vp, vp, u32, u32, vp, u32, u32, vp, u32, u32, vp, vp, vp]),
 }
 
 _LIB: C.CDLL | None = None

@@ -21,6 +21,7 @@ extern "C" int vren_internal_error_batch(int clear);
 extern "C" int vren_internal_error_lbvh(int clear);
 extern "C" int vren_internal_error_lights(int clear);
 extern "C" int vren_internal_error_cluster_debug(int clear);
+extern "C" int vren_internal_error_kd_tree(int clear);
 
 extern "C" const char* vren_status_string(int status)
 {
@@ -41,7 +42,8 @@ extern "C" int vren_device_error(int clear)
     int (*const words[])(int) = {vren_internal_error_reduce, vren_internal_error_scan, vren_internal_error_radix,
                                  vren_internal_error_bvh, vren_internal_error_cs, vren_internal_error_shade,
                                  vren_internal_error_batch, vren_internal_error_lbvh,
-                                 vren_internal_error_lights, vren_internal_error_cluster_debug};
+                                 vren_internal_error_lights, vren_internal_error_cluster_debug,
+                                 vren_internal_error_kd_tree};
     int first = 0;
     for (auto w : words) {
         int e = w(clear);
