@@ -16,6 +16,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <functional>
 #include <stdexcept>
 #include <string>
 #include <type_traits>
@@ -343,6 +344,31 @@ private:
 };
 
 }  // namespace clustered_shading
+
+// ------------------------------------------------------------------------------------------------
+// vren::kd_tree_* (base/kd_tree.hpp): the reference's host build and search, same node array.
+// ------------------------------------------------------------------------------------------------
+using kd_tree_node = vren_kd_tree_node;
+using kd_tree_search_filter_t = std::function<bool(uint32_t point)>;
+inline const kd_tree_search_filter_t k_kd_tree_default_search_filter = [](uint32_t) -> bool { return true; };
+
+inline size_t kd_tree_build(float const* points, size_t point_stride, uint32_t* indices, size_t count,
+                            kd_tree_node* kd_tree, size_t node_offset, size_t max_leaf_point_count)
+{
+    return vren_kd_tree_build(points, point_stride, indices, count, kd_tree, node_offset, max_leaf_point_count);
+}
+
+inline void kd_tree_search(float const* points, size_t point_stride, uint32_t const* indices, size_t count,
+                           kd_tree_node* kd_tree, size_t node_offset, float const* sample,
+                           kd_tree_search_filter_t const& filter_predicate, uint32_t& best_point,
+                           float& best_distance_squared)
+{
+    auto trampoline = [](uint32_t point, void* user) -> int {
+        return (*static_cast<kd_tree_search_filter_t const*>(user))(point) ? 1 : 0;
+    };
+    vren_kd_tree_search(points, point_stride, indices, count, kd_tree, node_offset, sample, trampoline,
+                        const_cast<kd_tree_search_filter_t*>(&filter_predicate), &best_point, &best_distance_squared);
+}
 
 // ------------------------------------------------------------------------------------------------
 // vren::depth_buffer_pyramid / vren::depth_buffer_reductor (pipeline/depth_buffer_pyramid.hpp):

@@ -4,6 +4,7 @@
 #include "vren_gb300.hpp"
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <numeric>
 #include <vector>
@@ -138,6 +139,41 @@ int main()
         cudaMemcpy(l2.data(), pyramid.level(2), sizeof(float), cudaMemcpyDeviceToHost);
         // the last column and row of the odd level are never read
         EXPECT(l1[0] == 0.9f && l1[1] == 0.8f && l2[0] == 0.9f);
+    }
+    // vren_test/kd_tree.cpp:29-112 in small: k-d search equals the linear search, with a filter too
+    {
+        std::vector<float> points(3 * 5000);
+        uint32_t r = 12345u;
+        for (auto& p : points) {
+            r = r * 1664525u + 1013904223u;
+            p = (float)(r >> 8) / (float)(1u << 24) * 100.0f;
+        }
+        std::vector<uint32_t> indices(5000);
+        std::iota(indices.begin(), indices.end(), 0u);
+        std::vector<vren::kd_tree_node> tree(2 * 5000);
+        const size_t nodes = vren::kd_tree_build(points.data(), 3, indices.data(), indices.size(), tree.data(), 0, 8);
+        EXPECT(nodes > 0 && nodes <= tree.size());
+        for (int q = 0; q < 20; ++q) {
+            const float s[3] = {points[3 * q] + 0.5f, points[3 * q + 1] - 0.25f, points[3 * q + 2]};
+            for (int filtered = 0; filtered < 2; ++filtered) {
+                auto keep = [&](uint32_t p) { return filtered == 0 || p % 3 != 0; };
+                uint32_t best = UINT32_MAX, lin = UINT32_MAX;
+                float bd = INFINITY, ld = INFINITY;
+                vren::kd_tree_search(points.data(), 3, indices.data(), indices.size(), tree.data(), 0, s,
+                                     filtered ? vren::kd_tree_search_filter_t(keep) : vren::k_kd_tree_default_search_filter,
+                                     best, bd);
+                for (uint32_t i = 0; i < 5000; ++i) {
+                    if (!keep(i)) continue;
+                    const float* p = &points[3 * i];
+                    const float d = (s[0] - p[0]) * (s[0] - p[0]) + (s[1] - p[1]) * (s[1] - p[1]) + (s[2] - p[2]) * (s[2] - p[2]);
+                    if (d < ld) {
+                        ld = d;
+                        lin = i;
+                    }
+                }
+                EXPECT(best == lin && bd == ld);
+            }
+        }
     }
     EXPECT(vren_device_error(1) == 0);
     cudaStreamDestroy(stream);

@@ -12,7 +12,7 @@ SRC = ROOT / "tests/cpp/api_drop_in.cpp"
 
 def _cxx_cmd(out: Path, syntax_only: bool):
     cuda_inc = "/usr/local/cuda/include"
-    cmd = ["g++", "-std=c++20", "-O1", f"-I{ROOT / 'include'}", f"-I{cuda_inc}", str(SRC)]
+    cmd = ["g++", "-std=c++20", "-O1", "-ffp-contract=off", f"-I{ROOT / 'include'}", f"-I{cuda_inc}", str(SRC)]
     if syntax_only:
         return cmd + ["-fsyntax-only"]
     lib_dir = ROOT / "vren_gb300"
