@@ -945,6 +945,64 @@ def run_profile(args):
     print(json.dumps({"profile": args.profile, "runs": reps, "device_error": vg.device_error()}))
 
 
+VENDOR_RADIX_SRC = r"""
+// cub::DeviceRadixSort::SortPairs (u32 keys, u32 values, all 32 bits) timed with CUDA events on its
+// stream, a 256 MiB memset before each run (L2 flushed), 5 warm-up + 20 timed runs per size.
+#include <cub/device/device_radix_sort.cuh>
+#include <cstdint>
+#include <cstdio>
+#include <vector>
+int main() {
+  void* flush; cudaMalloc(&flush, 256u << 20);
+  cudaStream_t s; cudaStreamCreate(&s);
+  for (int lg : {20, 24, 26}) {
+    size_t n = size_t(1) << lg;
+    std::vector<uint32_t> hk(n); uint32_t r = 12345u;
+    for (auto& k : hk) { r ^= r << 13; r ^= r >> 17; r ^= r << 5; k = r; }
+    uint32_t *k0, *k1, *v0, *v1;
+    cudaMalloc(&k0, n * 4); cudaMalloc(&k1, n * 4); cudaMalloc(&v0, n * 4); cudaMalloc(&v1, n * 4);
+    cudaMemcpy(k0, hk.data(), n * 4, cudaMemcpyHostToDevice);
+    size_t tb = 0; cub::DeviceRadixSort::SortPairs(nullptr, tb, k0, k1, v0, v1, (int)n, 0, 32, s);
+    void* tmp; cudaMalloc(&tmp, tb);
+    cudaEvent_t a, b; cudaEventCreate(&a); cudaEventCreate(&b);
+    float tot = 0; int cnt = 0;
+    for (int i = 0; i < 25; ++i) {
+      cudaMemsetAsync(flush, i, 256u << 20, s);
+      cudaEventRecord(a, s);
+      cub::DeviceRadixSort::SortPairs(tmp, tb, k0, k1, v0, v1, (int)n, 0, 32, s);
+      cudaEventRecord(b, s); cudaEventSynchronize(b);
+      float ms; cudaEventElapsedTime(&ms, a, b); if (i >= 5) { tot += ms; ++cnt; }
+    }
+    printf("%d %.6f\n", lg, tot / cnt);
+    cudaFree(k0); cudaFree(k1); cudaFree(v0); cudaFree(v1); cudaFree(tmp);
+  }
+  return cudaDeviceSynchronize() == cudaSuccess ? 0 : 1;
+}
+"""
+
+
+def vendor_radix(args):
+    """The vendor's radix sort on the same GPU for comparison: CUB's onesweep SortPairs (the library
+    shipped with the CUDA toolkit), built from a short program at run time; one JSON line."""
+    import tempfile
+
+    with tempfile.TemporaryDirectory() as d:
+        src, exe = os.path.join(d, "cub_sort.cu"), os.path.join(d, "cub_sort")
+        with open(src, "w") as f:
+            f.write(VENDOR_RADIX_SRC)
+        subprocess.run(["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-o", exe, src],
+                       check=True)
+        out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout
+    res = {}
+    for line in out.split("\n"):
+        if line.strip():
+            lg, ms = line.split()
+            n = 1 << int(lg)
+            res[f"n=2^{lg}"] = {"ms": round(float(ms), 4), "gkeys_s": round(n / (float(ms) * 1e-3) / 1e9, 3),
+                                "gbs_at_64B_per_pair": round(64.0 * n / (float(ms) * 1e-3) / 1e9, 1)}
+    print(json.dumps({"vendor_radix": "cub::DeviceRadixSort::SortPairs u32/u32", "results": res}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -957,7 +1015,11 @@ def main():
                                           "shade_backward", "pyramid", "pyramid_4k"],
                     default=None,
                     help="run one kernel family on a case larger than L2 (for ncu) and exit")
+    ap.add_argument("--vendor-radix", action="store_true",
+                    help="time the CUDA toolkit's CUB radix sort (pairs) on this GPU for comparison and exit")
     args = ap.parse_args()
+    if args.vendor_radix:
+        return vendor_radix(args)
     if args.profile:
         return run_profile(args)
     args.warmup = max(args.warmup, 3)
