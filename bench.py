@@ -36,13 +36,13 @@ W, H, L = 1920, 1080, 16384
 SEED = 20240611
 RADIX_N = 1 << 20
 L2_FLUSH_BYTES = 256 << 20
-BYTES_PER_PX = 20  # depth 4 + normal 12 + cluster reference 4
-# DRAM bytes (read + write) of one find_unique_cluster_list call at 1920x1080 (its three kernels): one
-# ncu capture at 3840x2160 (profiles/find_unique_3840x2160.md: tile kernel 133.8 MB read + 17.6 MB
-# written, tile-count scan 0.04 MB, fix-up 34.3 MB read) scaled by the pixel count (1/4).  ncu flushed
-# the caches before each kernel, so the fix-up's read of the references (L2-resident in a timed run)
-# is counted here.
-FUC_TRAFFIC_BYTES = int((133.836032 + 17.552128 + 0.040192 + 34.295040 + 0.000512) * 1e6 / 4)
+BYTES_PER_PX = 16  # depth 4 + normal 8 (RGBA16F, the reference's G-buffer format) + cluster reference 4
+# DRAM bytes (read + write) of one find_unique_cluster_list call at 1920x1080 (its three kernels,
+# RGBA16F normals): one ncu capture at 3840x2160 (profiles/find_unique_3840x2160.md: tile kernel
+# 100.4 MB read + 13.2 MB written, tile-count scan 0.04 MB, fix-up 34.3 MB read) scaled by the pixel
+# count (1/4).  ncu flushed the caches before each kernel, so the fix-up's read of the references
+# (L2-resident in a timed run) is counted here.
+FUC_TRAFFIC_BYTES = int((100.403968 + 13.229056 + 0.040448 + 34.296832 + 0.001024) * 1e6 / 4)
 FUC_TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the three kernels at 3840x2160 (caches "
                       "flushed before each), scaled by pixels to 1920x1080")
 
@@ -115,12 +115,17 @@ class ClockSampler:
 # Inputs (identical for both arms)
 # ------------------------------------------------------------------------------------------------
 def make_inputs(rank: int = 0):
+    """Depth, normals (as f32x3 and in the reference's G-buffer format RGBA16F, holding the same values),
+    light positions, point lights, radix keys."""
     import vren_gb300.scene as scene
 
     depth, normals = scene.depth_planes(SEED + rank, W, H, planes=64)
+    normals_h = np.zeros((W * H, 4), np.float16)
+    normals_h[:, :3] = normals.reshape(-1, 3).astype(np.float16)
+    normals = np.ascontiguousarray(normals_h[:, :3].astype(np.float32)).reshape(-1)
     pos, lights = scene.lights(SEED + 1000 + rank, L, W, H)
     keys = scene.gen_u32(SEED + 7, 1, RADIX_N)
-    return depth, normals, pos, lights, keys
+    return depth, normals, normals_h, pos, lights, keys
 
 
 # ------------------------------------------------------------------------------------------------
@@ -137,7 +142,7 @@ def run_ours(args, rank: int, world: int):
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
     torch.cuda.set_device(dev)
     hbm_peak, peak_kind = peaks()
-    depth, normals, pos, lights, radix_keys = make_inputs(rank)
+    depth, normals, normals_h, pos, lights, radix_keys = make_inputs(rank)
     stream = torch.cuda.Stream(device=dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
 
@@ -145,7 +150,7 @@ def run_ours(args, rank: int, world: int):
     view = cs.view_from_camera(cam, "ref")
     ctx = cs.cluster_and_shade(W, H, 65536, 1 << 24)
     d_depth = torch.from_numpy(depth).to(dev)
-    d_norm = torch.from_numpy(normals).to(dev)
+    d_norm = torch.from_numpy(normals_h).to(dev)  # the reference's G-buffer normal format
     d_pos = torch.from_numpy(pos).to(dev)
     d_light = torch.from_numpy(lights).to(dev)
     torch.cuda.synchronize()
@@ -188,9 +193,9 @@ def run_ours(args, rank: int, world: int):
         job_ms = ms_frame
     err = vg.device_error()
 
-    # dominant HBM kernel of the frame: find_unique_cluster_list (20 B/px), timed alone
+    # dominant HBM kernel of the frame: find_unique_cluster_list (16 B/px with RGBA16F normals), timed alone
     frame_dev = torch.empty(0)
-    fr = cs.frame_build(view, W, H)
+    fr = cs.frame_build(view, W, H, "wrap", cs.NORMALS["rgba16f"])
     frame_dev = cs.frame_to_device(fr, dev)
     T = ((W + 31) // 32) * ((H + 31) // 32)
     keys = torch.zeros(T * 1024, dtype=torch.int32, device=dev)
@@ -217,14 +222,14 @@ def run_ours(args, rank: int, world: int):
     # G-buffer upload), downloads the cluster references during the light assignment, and has the
     # device write the light lists ([U, total, keys, counts, offsets, indices]) into host memory.
     h_depth = torch.from_numpy(depth).pin_memory()
-    h_norm = torch.from_numpy(normals).pin_memory()
+    h_norm = torch.from_numpy(normals_h).pin_memory()
     h_pos = torch.from_numpy(pos).pin_memory()
     h_light = torch.from_numpy(lights).pin_memory()
     h_refs = torch.empty(W * H, dtype=torch.int32).pin_memory()
     cap = T * 1024
     h_lists = torch.empty(2 + 3 * cap + (1 << 24), dtype=torch.int32).pin_memory()
 
-    h2d_bytes = (h_depth.numel() + h_norm.numel() + h_pos.numel() + h_light.numel()) * 4
+    h2d_bytes = sum(t.numel() * t.element_size() for t in (h_depth, h_norm, h_pos, h_light))
     e2e_ms, d2h_total = [], 0
     for i in range(args.warmup + args.steps):
         torch.cuda.synchronize()
@@ -238,6 +243,11 @@ def run_ours(args, rank: int, world: int):
             d2h_total = 8 + W * H * 4 + u * 12 + tot * 4
     e2e = sum(e2e_ms) / len(e2e_ms)
     e2e_refs_ok = bool(np.array_equal(h_refs.numpy(), cs.read_device(out.cluster_refs, W * H).view(np.int32)))
+
+    # the same frame with f32x3 normals (12 B/px instead of 8) for comparison
+    d_norm32 = torch.from_numpy(normals).to(dev)
+    f32_ms = time_events(stream, lambda: ctx.cluster(stream, view, W, H, d_depth, d_norm32, d_pos, d_light, L), 3,
+                         args.steps, flush)
 
     # radix sort: 2^20 key/value pairs (config 1), plus sizes beyond L2
     radix = radix_bench(args, dev, stream, flush, radix_keys, hbm_peak)
@@ -284,6 +294,8 @@ def run_ours(args, rank: int, world: int):
                 "unique_clusters": U, "assignments": total,
                 "l2": "flushed (256 MiB write) before every timed step",
                 "graph": "one CUDA graph replay per frame",
+                "normals": "RGBA16F per pixel (the reference's G-buffer format, vren/pipeline/gbuffer.cpp:7-12)",
+                "frame_ms_f32x3_normals": round(f32_ms, 5),
                 "parallelism": f"replicas x{world} (frames are independent)",
             },
             "e2e": {"value": round(e2e, 4), "unit": "ms", "h2d_bytes_per_step": h2d_bytes,
@@ -825,7 +837,7 @@ def run_reference(args, rank: int, world: int):
     from vren_gb300 import _build
 
     _build.build_scene()
-    depth, normals, pos, lights, radix_keys = make_inputs(0)
+    depth, normals, _, pos, lights, radix_keys = make_inputs(0)
     cores = os.cpu_count() or 1
     view = numpy_view(cs)
 
@@ -892,16 +904,18 @@ def run_profile(args):
         fn = lambda: batch.run(stream, frames)
     elif args.profile == "frame":
         # the benchmark's frame: 1920x1080, 16384 lights, one CUDA graph replay per frame
-        depth, normals, pos, lights, _ = make_inputs(0)
+        depth, _, normals, pos, lights, _ = make_inputs(0)
         view = cs.view_from_camera(cs.scene_camera(W, H), "ref")
         ctx = cs.cluster_and_shade(W, H, 65536, 1 << 24)
         bufs = [torch.from_numpy(x).to(dev) for x in (depth, normals, pos, lights)]
         fn = lambda: ctx.cluster(stream, view, W, H, *bufs, L)
     elif args.profile == "find_unique":
-        w, h = 3840, 2160  # 20 B/px -> 166 MB > L2
-        depth, normals = scene.depth_planes(SEED, w, h)
+        w, h = 3840, 2160  # 16 B/px (RGBA16F normals) -> 133 MB > L2
+        depth, normals32 = scene.depth_planes(SEED, w, h)
+        normals = np.zeros((w * h, 4), np.float16)
+        normals[:, :3] = normals32.reshape(-1, 3).astype(np.float16)
         view = cs.view_from_camera(cs.scene_camera(w, h), "ref")
-        frame = cs.frame_to_device(cs.frame_build(view, w, h), dev)
+        frame = cs.frame_to_device(cs.frame_build(view, w, h, "wrap", cs.NORMALS["rgba16f"]), dev)
         T = ((w + 31) // 32) * ((h + 31) // 32)
         keys = torch.zeros(T * 1024, dtype=torch.int32, device=dev)
         kc = torch.zeros(1, dtype=torch.int32, device=dev)

@@ -251,7 +251,8 @@ int vren_build_lbvh(vren_stream_t s, const uint32_t* sorted_pairs, uint32_t leaf
  *   light index      uvec2[L]: (morton code, light index), sorted by code, ties by light index
  *   BVH              vren_bvh_node[vren_calc_bvh_buffer_length(L)]
  *   depth            f32[W*H] NDC depth in [0, 1], row-major   (the reference's D32 depth buffer)
- *   normals          f32x3[W*H]                              (the reference's G-buffer normals)
+ *   normals          f32x3[W*H], or the reference's G-buffer format RGBA16F (half x4 per pixel,
+ *                    gbuffer.cpp:7-12; w ignored), chosen by the frame's normal_format
  *   cluster keys     u32[U]: i | j << 8 | k << 16 | normal << 26 (find_unique_clusters.comp:72-76)
  *   cluster refs     u32[W*H]: index of the pixel's key in the key list
  *   counts/offsets   u32[U]; indices u32[sum(counts)]        (assign_lights.comp:57-70)
@@ -266,6 +267,9 @@ int vren_build_lbvh(vren_stream_t s, const uint32_t* sorted_pairs, uint32_t leaf
 #define VREN_CS_SLICES 1024
 enum { VREN_CS_SLICING_REF = 0, VREN_CS_SLICING_FIXED32 = 1 };
 enum { VREN_CS_OFFSCREEN_WRAP = 0, VREN_CS_OFFSCREEN_SKIP = 1 };
+/* Normal buffer formats: f32x3 per pixel, or the reference's G-buffer RGBA16F (half x4 per pixel,
+ * converted exactly to float, so the keys equal those of the f32x3 normals holding the same values). */
+enum { VREN_CS_NORMALS_F32X3 = 0, VREN_CS_NORMALS_RGBA16F = 1 };
 
 /* vren::camera (vren/vren/camera.hpp:14-33) */
 typedef struct vren_camera {
@@ -295,8 +299,9 @@ typedef struct vren_cs_frame {
     vren_cs_view view;
     uint32_t width, height, tiles_x, tiles_y;
     uint32_t max_slice;
-    uint32_t offscreen;  /* VREN_CS_OFFSCREEN_* */
-    uint32_t reserved[2];
+    uint32_t offscreen;      /* VREN_CS_OFFSCREEN_* */
+    uint32_t normal_format;  /* VREN_CS_NORMALS_* (vren_cs_frame_build sets F32X3) */
+    uint32_t reserved;
     float slice_near[VREN_CS_SLICES];
     float slice_far[VREN_CS_SLICES];
 } vren_cs_frame;
@@ -542,6 +547,7 @@ typedef struct vren_cs_options {
     uint32_t use_graph;       /* capture/replay a CUDA graph on non-default streams */
     uint32_t sort_digit_bits; /* 4, 6 or 8: digit width of the light sort */
     uint32_t assign_warps;    /* warps per CTA of the traversal kernels (1..32) */
+    uint32_t normal_format;   /* VREN_CS_NORMALS_* of the normals passed to vren_cs_cluster(_host) */
 } vren_cs_options;
 
 int vren_cs_create(vren_cluster_and_shade** out, uint32_t max_width, uint32_t max_height, uint32_t max_lights,
@@ -583,8 +589,10 @@ typedef struct vren_cs_batch_frame {
     uint32_t width, height;       /* <= 8192 each */
     uint32_t light_count;         /* <= 2^20 */
     int32_t offscreen;            /* VREN_CS_OFFSCREEN_* */
+    uint32_t normal_format;       /* VREN_CS_NORMALS_* */
+    uint32_t reserved;
     const float* depth;           /* device: float[W*H] NDC depth */
-    const float* normals;         /* device: float[3*W*H] */
+    const float* normals;         /* device: float[3*W*H] or half[4*W*H] (normal_format) */
     const float* light_positions; /* device: vec4[L], 16-byte aligned (null when L == 0) */
     const float* point_lights;    /* device: {rgb, radius}[L], 16-byte aligned */
 } vren_cs_batch_frame;

@@ -34,12 +34,13 @@ class View(C.Structure):
 class Frame(C.Structure):
     _fields_ = [("view", View), ("width", C.c_uint32), ("height", C.c_uint32), ("tiles_x", C.c_uint32),
                 ("tiles_y", C.c_uint32), ("max_slice", C.c_uint32), ("offscreen", C.c_uint32),
-                ("reserved", C.c_uint32 * 2), ("slice_near", C.c_float * SLICES), ("slice_far", C.c_float * SLICES)]
+                ("normal_format", C.c_uint32), ("reserved", C.c_uint32), ("slice_near", C.c_float * SLICES),
+                ("slice_far", C.c_float * SLICES)]
 
 
 class Options(C.Structure):
     _fields_ = [("morton_bits", C.c_uint32), ("use_graph", C.c_uint32), ("sort_digit_bits", C.c_uint32),
-                ("assign_warps", C.c_uint32)]
+                ("assign_warps", C.c_uint32), ("normal_format", C.c_uint32)]
 
 
 class Outputs(C.Structure):
@@ -65,9 +66,18 @@ def view_from_camera(cam: Camera, slicing: str = "ref") -> View:
     return v
 
 
-def frame_build(view: View, width: int, height: int, offscreen: str = "wrap") -> Frame:
+NORMALS = {"f32x3": 0, "rgba16f": 1}
+
+
+def normal_format_of(normals) -> int:
+    """f32x3 normals for a float32 tensor, the reference's RGBA16F G-buffer layout for a float16 one."""
+    return NORMALS["rgba16f"] if getattr(normals, "dtype", None) in (torch.float16, np.float16) else NORMALS["f32x3"]
+
+
+def frame_build(view: View, width: int, height: int, offscreen: str = "wrap", normal_format: int = 0) -> Frame:
     f = Frame()
     check(lib().vren_cs_frame_build(C.byref(view), width, height, OFFSCREEN[offscreen], C.byref(f)), "frame_build")
+    f.normal_format = normal_format
     return f
 
 
@@ -213,9 +223,17 @@ class cluster_and_shade:
         self._h = h
         self.set_options(morton_bits, use_graph, sort_digit_bits, assign_warps)
 
-    def set_options(self, morton_bits=15, use_graph=True, sort_digit_bits=8, assign_warps=8):
-        o = Options(morton_bits, 1 if use_graph else 0, sort_digit_bits, assign_warps)
+    def set_options(self, morton_bits=15, use_graph=True, sort_digit_bits=8, assign_warps=8, normal_format=0):
+        o = Options(morton_bits, 1 if use_graph else 0, sort_digit_bits, assign_warps, normal_format)
         check(lib().vren_cs_set_options(self._h, C.byref(o)), "cs_set_options")
+        self._opts = o
+
+    def _follow_normals(self, normals):
+        """The normal format follows the normals' dtype (float16: the RGBA16F G-buffer layout)."""
+        fmt = normal_format_of(normals)
+        if fmt != self._opts.normal_format:
+            o = self._opts
+            self.set_options(o.morton_bits, bool(o.use_graph), o.sort_digit_bits, o.assign_warps, fmt)
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -226,6 +244,7 @@ class cluster_and_shade:
     def cluster(self, stream, view: View, width: int, height: int, depth: torch.Tensor, normals: torch.Tensor,
                 positions: torch.Tensor | None, lights: torch.Tensor | None, light_count: int,
                 offscreen: str = "wrap"):
+        self._follow_normals(normals)
         check(lib().vren_cs_cluster(self._h, _stream(stream), C.byref(view), width, height, OFFSCREEN[offscreen],
                                     _ptr(depth), _ptr(normals), _ptr(positions) if positions is not None else None,
                                     _ptr(lights) if lights is not None else None, light_count), "cs_cluster")
@@ -237,6 +256,7 @@ class cluster_and_shade:
         """The same frame from page-locked host tensors (uploads overlapped with the light BVH and the
         unique clusters; the references downloaded into refs_out while the light lists are assigned; the
         lists written by the device into lists_out as [U, total, keys, counts, offsets, indices])."""
+        self._follow_normals(normals)
         check(lib().vren_cs_cluster_host(self._h, _stream(stream), C.byref(view), width, height, OFFSCREEN[offscreen],
                                          depth.data_ptr(), normals.data_ptr(),
                                          positions.data_ptr() if positions is not None else None,
@@ -253,7 +273,8 @@ class cluster_and_shade:
 
 class BatchFrame(C.Structure):
     _fields_ = [("view", View), ("width", C.c_uint32), ("height", C.c_uint32), ("light_count", C.c_uint32),
-                ("offscreen", C.c_int32), ("depth", C.c_void_p), ("normals", C.c_void_p),
+                ("offscreen", C.c_int32), ("normal_format", C.c_uint32), ("reserved", C.c_uint32),
+                ("depth", C.c_void_p), ("normals", C.c_void_p),
                 ("light_positions", C.c_void_p), ("point_lights", C.c_void_p)]
 
 
@@ -292,6 +313,7 @@ class cluster_batch:
             arr[i].view = view
             arr[i].width, arr[i].height, arr[i].light_count = w, h, L
             arr[i].offscreen = OFFSCREEN[off]
+            arr[i].normal_format = normal_format_of(normals)
             arr[i].depth, arr[i].normals = _ptr(depth), _ptr(normals)
             arr[i].light_positions = _ptr(pos) if (pos is not None and L) else None
             arr[i].point_lights = _ptr(lights) if (lights is not None and L) else None

@@ -462,6 +462,7 @@ bool frame_ok(const vren_cs_batch_frame& f)
         if (!f.light_positions || !f.point_lights) return false;
         if (((uintptr_t)f.light_positions | (uintptr_t)f.point_lights) & 15u) return false;
     }
+    if (f.normal_format != VREN_CS_NORMALS_F32X3 && f.normal_format != VREN_CS_NORMALS_RGBA16F) return false;
     return f.offscreen == VREN_CS_OFFSCREEN_WRAP || f.offscreen == VREN_CS_OFFSCREEN_SKIP;
 }
 
@@ -518,6 +519,7 @@ int stage_batch(vren_cs_batch* b, cudaStream_t st, const vren_cs_batch_frame* fr
         const vren_cs_batch_frame& f = fr[i];
         int rc = vren_cs_frame_build(&f.view, f.width, f.height, f.offscreen, &frames[i]);
         if (rc != VREN_OK) return rc;
+        frames[i].normal_format = f.normal_format;
         BatchDesc& d = desc[i];
         std::memset(&d, 0, sizeof(d));
         d.depth = f.depth;
@@ -864,12 +866,14 @@ extern "C" int vren_cs_batch_run(vren_cs_batch* b, vren_stream_t s, const vren_c
     struct FrameKey {
         uint32_t w, h, L;
         int32_t off;
+        uint32_t normal_format, pad;
         const void *depth, *normals, *pos, *lights;
     };
     std::vector<char> key(sizeof(FrameKey) * count + sizeof(vren_cs_batch_options) + sizeof(st));
     for (uint32_t i = 0; i < count; ++i) {
-        const FrameKey k{fr[i].width, fr[i].height, fr[i].light_count, fr[i].offscreen,
-                         fr[i].depth, fr[i].normals, fr[i].light_positions, fr[i].point_lights};
+        const FrameKey k{fr[i].width,         fr[i].height, fr[i].light_count, fr[i].offscreen,
+                         fr[i].normal_format, 0u,           fr[i].depth,       fr[i].normals,
+                         fr[i].light_positions, fr[i].point_lights};
         std::memcpy(key.data() + i * sizeof(FrameKey), &k, sizeof(k));
     }
     std::memcpy(key.data() + sizeof(FrameKey) * count, &b->opt, sizeof(b->opt));

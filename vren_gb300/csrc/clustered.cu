@@ -1153,7 +1153,7 @@ extern "C" int vren_cs_assign_lights(vren_stream_t s, const uint32_t* cluster_ke
 struct vren_cluster_and_shade {
     uint32_t max_w = 0, max_h = 0, max_lights = 0, max_assign = 0;
     uint32_t key_cap = 0;
-    vren_cs_options opt{15, 1, 8, 8};
+    vren_cs_options opt{15, 1, 8, 8, VREN_CS_NORMALS_F32X3};
     char* arena = nullptr;
     size_t arena_bytes = 0;
     // carved buffers
@@ -1333,6 +1333,7 @@ extern "C" int vren_cs_set_options(vren_cluster_and_shade* cs, const vren_cs_opt
     if (o->morton_bits != 15 && o->morton_bits != 30) return VREN_ERR_ARG;
     if (o->sort_digit_bits != 4 && o->sort_digit_bits != 6 && o->sort_digit_bits != 8) return VREN_ERR_ARG;
     if (o->assign_warps < 1 || o->assign_warps > 8) return VREN_ERR_ARG;
+    if (o->normal_format != VREN_CS_NORMALS_F32X3 && o->normal_format != VREN_CS_NORMALS_RGBA16F) return VREN_ERR_ARG;
     cs->opt = *o;
     if (cs->graph) {
         cudaGraphExecDestroy(cs->graph);
@@ -1354,6 +1355,7 @@ int refresh_frame(vren_cluster_and_shade* cs, cudaStream_t st, const vren_cs_vie
     static thread_local vren_cs_frame fresh;
     int rc = vren_cs_frame_build(view, width, height, offscreen, &fresh);
     if (rc != VREN_OK) return rc;
+    fresh.normal_format = cs->opt.normal_format;
     if (!cs->frame_valid || std::memcmp(&fresh, cs->host_frame, sizeof(vren_cs_frame)) != 0) {
         VREN_CUDA_TRY(cudaStreamSynchronize(st));  // an earlier upload may still read host_frame
         std::memcpy(cs->host_frame, &fresh, sizeof(vren_cs_frame));
@@ -1392,13 +1394,15 @@ int cs_enqueue_host(vren_cluster_and_shade* cs, cudaStream_t st, uint32_t W, uin
                                   cs->key_count, cs->refs, static_cast<uint32_t*>(cs->fuc_scratch));
     const uint32_t TX = (W + 31) / 32, TY = (H + 31) / 32;
     const uint32_t bands = TY < 4u ? TY : 4u, per = (TY + bands - 1) / bands;
+    const size_t nbytes = cs->opt.normal_format == VREN_CS_NORMALS_RGBA16F ? 8 : 12;  // per pixel
     uint32_t band = 0;
     for (uint32_t ty0 = 0; ty0 < TY; ty0 += per, ++band) {  // uploads on `up`, one event per band
         const uint32_t ty1 = ty0 + per < TY ? ty0 + per : TY;
         const size_t y0 = (size_t)ty0 * 32, y1 = (size_t)ty1 * 32 < H ? (size_t)ty1 * 32 : H;
         VREN_CUDA_TRY(cudaMemcpyAsync(cs->in_depth + y0 * W, depth + y0 * W, (y1 - y0) * W * 4,
                                       cudaMemcpyHostToDevice, up));
-        VREN_CUDA_TRY(cudaMemcpyAsync(cs->in_normals + 3 * y0 * W, normals + 3 * y0 * W, (y1 - y0) * W * 12,
+        VREN_CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<char*>(cs->in_normals) + y0 * W * nbytes,
+                                      reinterpret_cast<const char*>(normals) + y0 * W * nbytes, (y1 - y0) * W * nbytes,
                                       cudaMemcpyHostToDevice, up));
         VREN_CUDA_TRY(cudaEventRecord(cs->ev_band[band], up));
     }

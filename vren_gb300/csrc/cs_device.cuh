@@ -10,6 +10,8 @@
 #include "common.cuh"
 #include "bvh_common.cuh"
 
+#include <cuda_fp16.h>
+
 namespace vren_gb300 {
 
 // ================================================================================================
@@ -316,18 +318,36 @@ __device__ __forceinline__ void find_unique_tile(const FucFrame& fr, uint32_t ti
     const uint32_t row = tid >> 3, strip = tid & 7u;
     const uint32_t gy = ty * 32u + row, gx0 = tx * 32u + strip * 4u;
     const bool full = vec && gy < H && gx0 + 3u < W;  // whole strip on screen, 16-byte aligned
-    float D[4], N[4][3];
+    // normals: f32x3, or RGBA16F (the reference's G-buffer format).  NR holds each pixel's raw normal
+    // words (f32x3: the three floats' bits; RGBA16F: x | y << 16 and z), compared along the strip; a
+    // normal is converted (half -> float is exact) and binned only where it differs from its left
+    // neighbour's.
+    const bool half_normals = F->normal_format == VREN_CS_NORMALS_RGBA16F;
+    const unsigned short* __restrict__ hnormals = reinterpret_cast<const unsigned short*>(normals);
+    float D[4];
+    uint32_t NR[4][3];
     bool on[4];
     if (full) {
         const size_t px0 = (size_t)gy * W + gx0;
         const float4 d4 = __ldg(reinterpret_cast<const float4*>(depth + px0));
-        const float4* np = reinterpret_cast<const float4*>(normals + 3 * px0);
-        const float4 a = __ldg(np), b = __ldg(np + 1), c = __ldg(np + 2);
         D[0] = d4.x; D[1] = d4.y; D[2] = d4.z; D[3] = d4.w;
-        N[0][0] = a.x; N[0][1] = a.y; N[0][2] = a.z;
-        N[1][0] = a.w; N[1][1] = b.x; N[1][2] = b.y;
-        N[2][0] = b.z; N[2][1] = b.w; N[2][2] = c.x;
-        N[3][0] = c.y; N[3][1] = c.z; N[3][2] = c.w;
+        if (half_normals) {
+            const uint4* hp = reinterpret_cast<const uint4*>(hnormals + 4 * px0);
+            const uint4 a = __ldg(hp), b = __ldg(hp + 1);
+            NR[0][0] = a.x; NR[0][1] = a.y & 0xFFFFu;
+            NR[1][0] = a.z; NR[1][1] = a.w & 0xFFFFu;
+            NR[2][0] = b.x; NR[2][1] = b.y & 0xFFFFu;
+            NR[3][0] = b.z; NR[3][1] = b.w & 0xFFFFu;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) NR[j][2] = 0u;
+        } else {
+            const uint4* np = reinterpret_cast<const uint4*>(normals + 3 * px0);
+            const uint4 a = __ldg(np), b = __ldg(np + 1), c = __ldg(np + 2);
+            NR[0][0] = a.x; NR[0][1] = a.y; NR[0][2] = a.z;
+            NR[1][0] = a.w; NR[1][1] = b.x; NR[1][2] = b.y;
+            NR[2][0] = b.z; NR[2][1] = b.w; NR[2][2] = c.x;
+            NR[3][0] = c.y; NR[3][1] = c.z; NR[3][2] = c.w;
+        }
 #pragma unroll
         for (int j = 0; j < 4; ++j) on[j] = true;
     } else {
@@ -339,8 +359,16 @@ __device__ __forceinline__ void find_unique_tile(const FucFrame& fr, uint32_t ti
             const uint32_t xw = gx < W ? gx : gx % W, yw = gy < H ? gy : gy % H;
             const size_t px = (size_t)yw * W + xw;
             D[j] = on[j] ? __ldg(depth + px) : 0.0f;
+            if (!on[j]) {
+                NR[j][0] = NR[j][1] = NR[j][2] = 0u;
+            } else if (half_normals) {
+                NR[j][0] = (uint32_t)__ldg(hnormals + 4 * px) | ((uint32_t)__ldg(hnormals + 4 * px + 1) << 16);
+                NR[j][1] = __ldg(hnormals + 4 * px + 2);
+                NR[j][2] = 0u;
+            } else {
 #pragma unroll
-            for (int c = 0; c < 3; ++c) N[j][c] = on[j] ? __ldg(normals + 3 * px + c) : 0.0f;
+                for (int c = 0; c < 3; ++c) NR[j][c] = __float_as_uint(__ldg(normals + 3 * px + c));
+            }
         }
     }
 
@@ -361,10 +389,21 @@ __device__ __forceinline__ void find_unique_tile(const FucFrame& fr, uint32_t ti
             }
             k = slice_of_geometric(fdiv(vz, vw), bound, kmax, b0, inv_log2_r);
         }
-        const bool same_n = j > 0 && __float_as_uint(N[j][0]) == __float_as_uint(N[j - 1][0]) &&
-                            __float_as_uint(N[j][1]) == __float_as_uint(N[j - 1][1]) &&
-                            __float_as_uint(N[j][2]) == __float_as_uint(N[j - 1][2]);
-        if (!same_n) nd = discretize_normal(N[j][0], N[j][1], N[j][2]);
+        const bool same_n =
+            j > 0 && NR[j][0] == NR[j - 1][0] && NR[j][1] == NR[j - 1][1] && NR[j][2] == NR[j - 1][2];
+        if (!same_n) {
+            float nx, ny, nz;
+            if (half_normals) {
+                nx = __half2float(__ushort_as_half((unsigned short)(NR[j][0] & 0xFFFFu)));
+                ny = __half2float(__ushort_as_half((unsigned short)(NR[j][0] >> 16)));
+                nz = __half2float(__ushort_as_half((unsigned short)NR[j][1]));
+            } else {
+                nx = __uint_as_float(NR[j][0]);
+                ny = __uint_as_float(NR[j][1]);
+                nz = __uint_as_float(NR[j][2]);
+            }
+            nd = discretize_normal(nx, ny, nz);
+        }
         sub[j] = on[j] ? (((k & 0x3FFu) | (nd << 10)) & 0xFFFFu) : 0xFFFFFFFFu;
     }
     // One set insert per run of equal sub-keys along the row (lane - 1 holds the strip to the left).
