@@ -230,6 +230,7 @@ def run_ours(args, rank: int, world: int):
     h_lists = torch.empty(2 + 3 * cap + (1 << 24), dtype=torch.int32).pin_memory()
 
     h2d_bytes = sum(t.numel() * t.element_size() for t in (h_depth, h_norm, h_pos, h_light))
+    lists_host = h_lists.numpy()  # the result is read from page-locked host memory
     e2e_ms, d2h_total = [], 0
     for i in range(args.warmup + args.steps):
         torch.cuda.synchronize()
@@ -237,7 +238,7 @@ def run_ours(args, rank: int, world: int):
         with torch.cuda.stream(stream):
             ctx.cluster_host(stream, view, W, H, h_depth, h_norm, h_pos, h_light, L, h_refs, h_lists)
             stream.synchronize()
-        u, tot = int(h_lists[0]), int(h_lists[1])
+        u, tot = int(lists_host[0]), int(lists_host[1])
         if i >= args.warmup:
             e2e_ms.append((time.perf_counter() - t0) * 1e3)
             d2h_total = 8 + W * H * 4 + u * 12 + tot * 4

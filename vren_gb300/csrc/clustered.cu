@@ -665,17 +665,18 @@ __global__ void __launch_bounds__(kFucThreads, 6) find_unique_kernel(FucFrame fr
     find_unique_tile(fr, tile_base + blockIdx.x, sm);
 }
 
-__global__ void __launch_bounds__(kFucScanThreads) find_unique_scan_kernel(FucFrame fr)
+__global__ void __launch_bounds__(kFucScanThreads) find_unique_scan_kernel(FucFrame fr, uint32_t t_begin,
+                                                                          uint32_t t_end)
 {
     pdl_enter();
     __shared__ uint32_t s_warp[kFucScanThreads / 32];
-    find_unique_scan(fr, s_warp);
+    find_unique_scan(fr, s_warp, t_begin, t_end);
 }
 
-__global__ void __launch_bounds__(kFucThreads) find_unique_fixup_kernel(FucFrame fr)
+__global__ void __launch_bounds__(kFucThreads) find_unique_fixup_kernel(FucFrame fr, uint32_t t_begin)
 {
     pdl_enter();
-    find_unique_fixup(fr, blockIdx.x);
+    find_unique_fixup(fr, t_begin + blockIdx.x);
 }
 
 // Scratch of find_unique_cluster_list for T tiles (uint32 words): tile counts [T], tile offsets [T],
@@ -701,12 +702,16 @@ static int launch_find_unique_tiles(cudaStream_t st, const FucFrame& fr, uint32_
     return VREN_OK;
 }
 
-// Stages 2 and 3 (after every tile).
-static int launch_find_unique_finish(cudaStream_t st, const FucFrame& fr)
+// Stages 2 and 3 for tiles [t_begin, t_end), after those tiles and after the stages of every tile
+// before t_begin (the offsets continue from there); by default the whole frame.
+static int launch_find_unique_finish(cudaStream_t st, const FucFrame& fr, uint32_t t_begin = 0,
+                                     uint32_t t_end = 0xFFFFFFFFu)
 {
-    launch_kernel(find_unique_scan_kernel, 1, kFucScanThreads, 0, st, fr);
+    t_end = t_end < fr.num_tiles ? t_end : fr.num_tiles;
+    if (t_end <= t_begin) return VREN_OK;
+    launch_kernel(find_unique_scan_kernel, 1, kFucScanThreads, 0, st, fr, t_begin, t_end);
     VREN_LAUNCH_CHECK();
-    launch_kernel(find_unique_fixup_kernel, fr.num_tiles, kFucThreads, 0, st, fr);
+    launch_kernel(find_unique_fixup_kernel, t_end - t_begin, kFucThreads, 0, st, fr, t_begin);
     VREN_LAUNCH_CHECK();
     return VREN_OK;
 }
@@ -1187,8 +1192,9 @@ struct vren_cluster_and_shade {
     char* inputs = nullptr;
     float *in_depth = nullptr, *in_normals = nullptr, *in_pos = nullptr, *in_lights = nullptr;
     cudaStream_t aux = nullptr, up = nullptr;  // light BVH and downloads; G-buffer uploads
-    cudaEvent_t ev_fork = nullptr, ev_bvh = nullptr, ev_fuc = nullptr, ev_join = nullptr, ev_join_up = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_bvh = nullptr, ev_join = nullptr, ev_join_up = nullptr;
     cudaEvent_t ev_band[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t ev_done[4] = {nullptr, nullptr, nullptr, nullptr};  // a band's references final
     cudaGraphExec_t host_graph = nullptr;
     struct HostKey {
         Key k;
@@ -1300,8 +1306,9 @@ extern "C" int vren_cs_create(vren_cluster_and_shade** out, uint32_t max_width, 
     // the second and third streams (light BVH beside the tiles; banded uploads) and their events
     bool ok = cudaStreamCreateWithFlags(&cs->aux, cudaStreamNonBlocking) == cudaSuccess &&
               cudaStreamCreateWithFlags(&cs->up, cudaStreamNonBlocking) == cudaSuccess;
-    for (cudaEvent_t* e : {&cs->ev_fork, &cs->ev_bvh, &cs->ev_fuc, &cs->ev_join, &cs->ev_join_up, &cs->ev_band[0],
-                           &cs->ev_band[1], &cs->ev_band[2], &cs->ev_band[3]})
+    for (cudaEvent_t* e : {&cs->ev_fork, &cs->ev_bvh, &cs->ev_join, &cs->ev_join_up, &cs->ev_band[0],
+                           &cs->ev_band[1], &cs->ev_band[2], &cs->ev_band[3], &cs->ev_done[0], &cs->ev_done[1],
+                           &cs->ev_done[2], &cs->ev_done[3]})
         ok = ok && cudaEventCreateWithFlags(e, cudaEventDisableTiming) == cudaSuccess;
     if (!ok) {
         vren_cs_destroy(cs);
@@ -1318,8 +1325,9 @@ extern "C" void vren_cs_destroy(vren_cluster_and_shade* cs)
     if (cs->host_graph) cudaGraphExecDestroy(cs->host_graph);
     if (cs->aux) cudaStreamDestroy(cs->aux);
     if (cs->up) cudaStreamDestroy(cs->up);
-    for (cudaEvent_t e : {cs->ev_fork, cs->ev_bvh, cs->ev_fuc, cs->ev_join, cs->ev_join_up, cs->ev_band[0],
-                          cs->ev_band[1], cs->ev_band[2], cs->ev_band[3]})
+    for (cudaEvent_t e : {cs->ev_fork, cs->ev_bvh, cs->ev_join, cs->ev_join_up, cs->ev_band[0],
+                          cs->ev_band[1], cs->ev_band[2], cs->ev_band[3], cs->ev_done[0], cs->ev_done[1],
+                          cs->ev_done[2], cs->ev_done[3]})
         if (e) cudaEventDestroy(e);
     cudaFree(cs->inputs);
     cudaFree(cs->arena);
@@ -1407,19 +1415,24 @@ int cs_enqueue_host(vren_cluster_and_shade* cs, cudaStream_t st, uint32_t W, uin
         VREN_CUDA_TRY(cudaEventRecord(cs->ev_band[band], up));
     }
     VREN_CUDA_TRY(cudaEventRecord(cs->ev_join_up, up));
+    // Each band once it has arrived: its tiles, then its tile offsets (continuing from the band above)
+    // and fix-up, after which its rows of references are final and go down on `aux` while the next
+    // bands are still coming up.
     band = 0;
-    for (uint32_t ty0 = 0; ty0 < TY; ty0 += per, ++band) {  // each band's tiles once it has arrived
+    for (uint32_t ty0 = 0; ty0 < TY; ty0 += per, ++band) {
         const uint32_t ty1 = ty0 + per < TY ? ty0 + per : TY;
         VREN_CUDA_TRY(cudaStreamWaitEvent(st, cs->ev_band[band], 0));
         rc = launch_find_unique_tiles(st, fr, ty0 * TX, (ty1 - ty0) * TX);
         if (rc != VREN_OK) return rc;
-    }
-    rc = launch_find_unique_finish(st, fr);
-    if (rc != VREN_OK) return rc;
-    if (refs_out) {
-        VREN_CUDA_TRY(cudaEventRecord(cs->ev_fuc, st));
-        VREN_CUDA_TRY(cudaStreamWaitEvent(aux, cs->ev_fuc, 0));
-        VREN_CUDA_TRY(cudaMemcpyAsync(refs_out, cs->refs, (size_t)W * H * 4, cudaMemcpyDeviceToHost, aux));
+        rc = launch_find_unique_finish(st, fr, ty0 * TX, ty1 * TX);
+        if (rc != VREN_OK) return rc;
+        if (refs_out) {
+            const size_t y0 = (size_t)ty0 * 32, y1 = (size_t)ty1 * 32 < H ? (size_t)ty1 * 32 : H;
+            VREN_CUDA_TRY(cudaEventRecord(cs->ev_done[band], st));
+            VREN_CUDA_TRY(cudaStreamWaitEvent(aux, cs->ev_done[band], 0));
+            VREN_CUDA_TRY(cudaMemcpyAsync(refs_out + y0 * W, cs->refs + y0 * W, (y1 - y0) * W * 4,
+                                          cudaMemcpyDeviceToHost, aux));
+        }
     }
     VREN_CUDA_TRY(cudaStreamWaitEvent(st, cs->ev_bvh, 0));
     rc = assign_lights(st, cs->keys, cs->key_count, cs->key_cap, cs->frame, cs->bvh, L, cs->light_index,

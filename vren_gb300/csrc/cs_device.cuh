@@ -489,12 +489,15 @@ __device__ __forceinline__ void find_unique_tile(const FucFrame& fr, uint32_t ti
 // loads, all in flight); chunks carry their running total.
 constexpr int kFucScanThreads = 1024;
 constexpr uint32_t kFucScanPer = 16;
-__device__ __forceinline__ void find_unique_scan(const FucFrame& fr, uint32_t* s_warp)
+// Tiles [t_begin, t_end) of the frame: offsets continue from the tile before t_begin (whose offset and
+// count an earlier scan wrote); the key count is written when t_end is the last tile.
+__device__ __forceinline__ void find_unique_scan(const FucFrame& fr, uint32_t* s_warp, uint32_t t_begin = 0,
+                                                 uint32_t t_end = 0xFFFFFFFFu)
 {
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-    const uint32_t T = fr.num_tiles;
-    uint32_t carry = 0;
-    for (uint32_t chunk = 0; chunk < T; chunk += kFucScanThreads * kFucScanPer) {
+    const uint32_t T = t_end < fr.num_tiles ? t_end : fr.num_tiles;
+    uint32_t carry = t_begin ? fr.tile_offset[t_begin - 1] + fr.tile_count[t_begin - 1] : 0u;
+    for (uint32_t chunk = t_begin; chunk < T; chunk += kFucScanThreads * kFucScanPer) {
         const uint32_t b0 = chunk + tid * kFucScanPer;
         uint32_t v[kFucScanPer], sum = 0;
 #pragma unroll
@@ -524,7 +527,7 @@ __device__ __forceinline__ void find_unique_scan(const FucFrame& fr, uint32_t* s
         }
         carry += total;
     }
-    if (tid == 0) {
+    if (tid == 0 && T == fr.num_tiles) {
         *fr.key_count = carry < fr.key_cap ? carry : fr.key_cap;
         if (carry > fr.key_cap) VREN_RECORD_ERROR(VREN_ERR_CAPACITY);
     }
