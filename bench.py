@@ -36,13 +36,13 @@ W, H, L = 1920, 1080, 16384
 SEED = 20240611
 RADIX_N = 1 << 20
 L2_FLUSH_BYTES = 256 << 20
-BYTES_PER_PX = 16  # depth 4 + normal 8 (RGBA16F, the reference's G-buffer format) + cluster reference 4
+BYTES_PER_PX = 20  # depth 4 + normal 12 (f32x3) + cluster reference 4
 # DRAM bytes (read + write) of one find_unique_cluster_list call at 1920x1080 (its three kernels,
-# RGBA16F normals): one ncu capture at 3840x2160 (profiles/find_unique_3840x2160.md: tile kernel
-# 100.4 MB read + 13.2 MB written, tile-count scan 0.04 MB, fix-up 34.3 MB read) scaled by the pixel
-# count (1/4).  ncu flushed the caches before each kernel, so the fix-up's read of the references
+# f32x3 normals): one ncu capture at 3840x2160 (profiles/find_unique_3840x2160.md: tile kernel 133.8 MB
+# read + 17.6 MB written, tile-count scan 0.04 MB, fix-up 34.3 MB read) scaled by the pixel count
+# (1/4).  ncu flushed the caches before each kernel, so the fix-up's read of the references
 # (L2-resident in a timed run) is counted here.
-FUC_TRAFFIC_BYTES = int((100.403968 + 13.229056 + 0.040448 + 34.296832 + 0.001024) * 1e6 / 4)
+FUC_TRAFFIC_BYTES = int((133.836032 + 17.552128 + 0.040192 + 34.295040 + 0.000512) * 1e6 / 4)
 FUC_TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the three kernels at 3840x2160 (caches "
                       "flushed before each), scaled by pixels to 1920x1080")
 
@@ -115,14 +115,13 @@ class ClockSampler:
 # Inputs (identical for both arms)
 # ------------------------------------------------------------------------------------------------
 def make_inputs(rank: int = 0):
-    """Depth, normals (as f32x3 and in the reference's G-buffer format RGBA16F, holding the same values),
-    light positions, point lights, radix keys."""
+    """Depth, normals f32x3 (the benchmark's G-buffer) and the same normals rounded into the reference's
+    own G-buffer format RGBA16F (a labelled extra measurement), light positions, point lights, radix keys."""
     import vren_gb300.scene as scene
 
     depth, normals = scene.depth_planes(SEED + rank, W, H, planes=64)
     normals_h = np.zeros((W * H, 4), np.float16)
     normals_h[:, :3] = normals.reshape(-1, 3).astype(np.float16)
-    normals = np.ascontiguousarray(normals_h[:, :3].astype(np.float32)).reshape(-1)
     pos, lights = scene.lights(SEED + 1000 + rank, L, W, H)
     keys = scene.gen_u32(SEED + 7, 1, RADIX_N)
     return depth, normals, normals_h, pos, lights, keys
@@ -150,7 +149,7 @@ def run_ours(args, rank: int, world: int):
     view = cs.view_from_camera(cam, "ref")
     ctx = cs.cluster_and_shade(W, H, 65536, 1 << 24)
     d_depth = torch.from_numpy(depth).to(dev)
-    d_norm = torch.from_numpy(normals_h).to(dev)  # the reference's G-buffer normal format
+    d_norm = torch.from_numpy(normals).to(dev)
     d_pos = torch.from_numpy(pos).to(dev)
     d_light = torch.from_numpy(lights).to(dev)
     torch.cuda.synchronize()
@@ -193,9 +192,9 @@ def run_ours(args, rank: int, world: int):
         job_ms = ms_frame
     err = vg.device_error()
 
-    # dominant HBM kernel of the frame: find_unique_cluster_list (16 B/px with RGBA16F normals), timed alone
+    # dominant HBM kernel of the frame: find_unique_cluster_list (20 B/px), timed alone
     frame_dev = torch.empty(0)
-    fr = cs.frame_build(view, W, H, "wrap", cs.NORMALS["rgba16f"])
+    fr = cs.frame_build(view, W, H)
     frame_dev = cs.frame_to_device(fr, dev)
     T = ((W + 31) // 32) * ((H + 31) // 32)
     keys = torch.zeros(T * 1024, dtype=torch.int32, device=dev)
@@ -222,7 +221,7 @@ def run_ours(args, rank: int, world: int):
     # G-buffer upload), downloads the cluster references during the light assignment, and has the
     # device write the light lists ([U, total, keys, counts, offsets, indices]) into host memory.
     h_depth = torch.from_numpy(depth).pin_memory()
-    h_norm = torch.from_numpy(normals_h).pin_memory()
+    h_norm = torch.from_numpy(normals).pin_memory()
     h_pos = torch.from_numpy(pos).pin_memory()
     h_light = torch.from_numpy(lights).pin_memory()
     h_refs = torch.empty(W * H, dtype=torch.int32).pin_memory()
@@ -245,10 +244,26 @@ def run_ours(args, rank: int, world: int):
     e2e = sum(e2e_ms) / len(e2e_ms)
     e2e_refs_ok = bool(np.array_equal(h_refs.numpy(), cs.read_device(out.cluster_refs, W * H).view(np.int32)))
 
-    # the same frame with f32x3 normals (12 B/px instead of 8) for comparison
-    d_norm32 = torch.from_numpy(normals).to(dev)
-    f32_ms = time_events(stream, lambda: ctx.cluster(stream, view, W, H, d_depth, d_norm32, d_pos, d_light, L), 3,
+    # extra, labelled: the frame with its normals in the reference's own G-buffer format (RGBA16F,
+    # 8 B/px instead of 12), on the device and end to end from host buffers
+    d_norm16 = torch.from_numpy(normals_h).to(dev)
+    f16_ms = time_events(stream, lambda: ctx.cluster(stream, view, W, H, d_depth, d_norm16, d_pos, d_light, L), 3,
                          args.steps, flush)
+    h_norm16 = torch.from_numpy(normals_h).pin_memory()
+    e2e16 = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        with torch.cuda.stream(stream):
+            ctx.cluster_host(stream, view, W, H, h_depth, h_norm16, h_pos, h_light, L, h_refs, h_lists)
+            stream.synchronize()
+        u16 = int(lists_host[0])
+        if i >= args.warmup:
+            e2e16.append((time.perf_counter() - t0) * 1e3)
+    rgba16f = {"frame_ms": round(f16_ms, 5), "e2e_ms": round(sum(e2e16) / len(e2e16), 4),
+               "h2d_bytes_per_step": h2d_bytes - h_norm.numel() * 4 + h_norm16.numel() * 2, "unique_clusters": u16,
+               "note": "normals rounded to half and passed as the reference's RGBA16F G-buffer "
+                       "(vren/pipeline/gbuffer.cpp:7-12); other inputs as the main line"}
 
     # radix sort: 2^20 key/value pairs (config 1), plus sizes beyond L2
     radix = radix_bench(args, dev, stream, flush, radix_keys, hbm_peak)
@@ -295,8 +310,7 @@ def run_ours(args, rank: int, world: int):
                 "unique_clusters": U, "assignments": total,
                 "l2": "flushed (256 MiB write) before every timed step",
                 "graph": "one CUDA graph replay per frame",
-                "normals": "RGBA16F per pixel (the reference's G-buffer format, vren/pipeline/gbuffer.cpp:7-12)",
-                "frame_ms_f32x3_normals": round(f32_ms, 5),
+                "normals": "f32x3 per pixel",
                 "parallelism": f"replicas x{world} (frames are independent)",
             },
             "e2e": {"value": round(e2e, 4), "unit": "ms", "h2d_bytes_per_step": h2d_bytes,
@@ -305,6 +319,7 @@ def run_ours(args, rank: int, world: int):
                             "BVH and the unique-cluster tiles, reference download overlapping the assignment, light "
                             "lists written to host memory by the device); host wall clock",
                     "refs_match_device": e2e_refs_ok},
+            "normals_rgba16f": rgba16f,
             "gpu_launches": launches_per_frame * args.steps,
             "roofline": {"bound": "hbm", "kernel": "find_unique_cluster_list (find_unique_kernel, "
                                                      "find_unique_scan_kernel, find_unique_fixup_kernel)",
@@ -905,18 +920,21 @@ def run_profile(args):
         fn = lambda: batch.run(stream, frames)
     elif args.profile == "frame":
         # the benchmark's frame: 1920x1080, 16384 lights, one CUDA graph replay per frame
-        depth, _, normals, pos, lights, _ = make_inputs(0)
+        depth, normals, _, pos, lights, _ = make_inputs(0)
         view = cs.view_from_camera(cs.scene_camera(W, H), "ref")
         ctx = cs.cluster_and_shade(W, H, 65536, 1 << 24)
         bufs = [torch.from_numpy(x).to(dev) for x in (depth, normals, pos, lights)]
         fn = lambda: ctx.cluster(stream, view, W, H, *bufs, L)
-    elif args.profile == "find_unique":
-        w, h = 3840, 2160  # 16 B/px (RGBA16F normals) -> 133 MB > L2
-        depth, normals32 = scene.depth_planes(SEED, w, h)
-        normals = np.zeros((w * h, 4), np.float16)
-        normals[:, :3] = normals32.reshape(-1, 3).astype(np.float16)
+    elif args.profile in ("find_unique", "find_unique_rgba16f"):
+        w, h = 3840, 2160  # 20 B/px (f32x3 normals; 16 with RGBA16F) -> 166 (133) MB > L2
+        depth, normals = scene.depth_planes(SEED, w, h)
+        fmt = cs.NORMALS["f32x3"]
+        if args.profile == "find_unique_rgba16f":
+            n16 = np.zeros((w * h, 4), np.float16)
+            n16[:, :3] = normals.reshape(-1, 3).astype(np.float16)
+            normals, fmt = n16, cs.NORMALS["rgba16f"]
         view = cs.view_from_camera(cs.scene_camera(w, h), "ref")
-        frame = cs.frame_to_device(cs.frame_build(view, w, h, "wrap", cs.NORMALS["rgba16f"]), dev)
+        frame = cs.frame_to_device(cs.frame_build(view, w, h, "wrap", fmt), dev)
         T = ((w + 31) // 32) * ((h + 31) // 32)
         keys = torch.zeros(T * 1024, dtype=torch.int32, device=dev)
         kc = torch.zeros(1, dtype=torch.int32, device=dev)
@@ -1026,8 +1044,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--quick", action="store_true", help="skip the primitive sweep and the large sorts")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--profile", choices=["frame", "batch", "find_unique", "radix", "scan", "shade",
-                                          "shade_backward", "pyramid", "pyramid_4k"],
+    ap.add_argument("--profile", choices=["frame", "batch", "find_unique", "find_unique_rgba16f", "radix", "scan",
+                                          "shade", "shade_backward", "pyramid", "pyramid_4k"],
                     default=None,
                     help="run one kernel family on a case larger than L2 (for ncu) and exit")
     ap.add_argument("--vendor-radix", action="store_true",
