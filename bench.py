@@ -955,6 +955,102 @@ def run_profile(args):
         x = torch.from_numpy(scene.gen_u32(SEED, 2, n, mask=255).view(np.int32)).to(dev)
         scan = vg.blelloch_scan()
         fn = lambda: scan(stream, x, n)
+    elif args.profile == "reduce":
+        # scalar u32 sum over 2^26 values (256 MB) and the reference's tree reduce over 2^24 (64 MB)
+        n = 1 << 26
+        x = torch.from_numpy(scene.gen_u32(SEED, 2, n, mask=255).view(np.int32)).to(dev)
+        from vren_gb300.primitives import alloc_scratch, reduce_scratch_bytes
+
+        o = torch.zeros(4, dtype=torch.int32, device=dev)
+        sc = alloc_scratch(reduce_scratch_bytes(n), dev)
+        t = torch.from_numpy(scene.gen_u32(SEED + 1, 2, 1 << 24, mask=255).view(np.int32)).to(dev)
+        tree = vg.reduce("uint", "add")
+        fn = lambda: (vg.reduce_scalar(stream, "add", x, o, sc), tree(stream, t, 1 << 24, 0))
+    elif args.profile == "bucket":
+        # 2^24 uvec2(key, index) into 1024 buckets on the low 10 bits
+        n = 1 << 24
+        kv = torch.empty(2 * n, dtype=torch.int32, device=dev)
+        kv[0::2] = torch.from_numpy(scene.gen_u32(SEED + 3, 1, n).view(np.int32)).to(dev)
+        kv[1::2] = torch.arange(n, dtype=torch.int32, device=dev)
+        bs = vg.bucket_sort(10)
+        out_b = torch.empty(bs.get_required_output_buffer_size(n) // 4, dtype=torch.int32, device=dev)
+        fn = lambda: bs(stream, kv, n, 0, out_b, 0)
+    elif args.profile == "build_bvh":
+        # BuildBVH over 2^20 leaves (32 MB of leaves, 33.8 MB of nodes)
+        n = 1 << 20
+        nodes = torch.zeros(vg.calc_bvh_buffer_length(n) * 8, dtype=torch.int32, device=dev)
+        leaves = np.zeros((n, 8), np.float32)
+        rng = np.random.default_rng(SEED)
+        p0 = rng.uniform(0, 100, (n, 3)).astype(np.float32)
+        leaves[:, 0:3], leaves[:, 4:7] = p0, p0 + 1.0
+        lv = leaves.view(np.uint32)
+        lv[:, 3] = 0xFFFFFFFF
+        nodes[: n * 8] = torch.from_numpy(lv.reshape(-1).view(np.int32)).to(dev)
+        bb = vg.build_bvh()
+        fn = lambda: bb(stream, nodes, n)
+    elif args.profile in ("assign", "karras"):
+        # the light assignment of the bench frame (1920x1080, 16384 lights), through the 32-ary BVH or
+        # through the Karras tree (build + assignment)
+        depth, normals, _, pos, lights, _ = make_inputs(0)
+        view = cs.view_from_camera(cs.scene_camera(W, H), "ref")
+        ctx = cs.cluster_and_shade(W, H, 65536, 1 << 24)
+        bufs = [torch.from_numpy(x).to(dev) for x in (depth, normals, pos, lights)]
+        ctx.cluster(stream, view, W, H, *bufs, L)
+        stream.synchronize()
+        o = ctx.outputs()
+        U = int(cs.read_device(o.key_count, 1)[0])
+        keys = torch.from_numpy(cs.read_device(o.cluster_keys, U).view(np.int32)).to(dev)
+        kc = torch.tensor([U], dtype=torch.int32, device=dev)
+        frame_dev = cs.frame_to_device(cs.frame_build(view, W, H), dev)
+        vp = torch.from_numpy(cs.read_device(o.view_positions, 4 * L, np.float32)).to(dev)
+        bvh = torch.from_numpy(cs.read_device(o.bvh, vg.calc_bvh_buffer_length(L) * 8).view(np.int32)).to(dev)
+        li = torch.from_numpy(cs.read_device(o.light_index, 2 * L).view(np.int32)).to(dev)
+        sph = torch.from_numpy(cs.read_device(o.leaf_spheres, 4 * vg.calc_bvh_padded_leaf_count(L), np.float32)).to(dev)
+        counts = torch.zeros(U, dtype=torch.int32, device=dev)
+        offs = torch.zeros(U, dtype=torch.int32, device=dev)
+        idx = torch.zeros(1 << 24, dtype=torch.int32, device=dev)
+        tot = torch.zeros(1, dtype=torch.int32, device=dev)
+        if args.profile == "assign":
+            al = cs.assign_lights()
+            fn = lambda: al(stream, keys, kc, frame_dev, bvh, L, li, vp, counts, offs, idx, tot, sph)
+        else:
+            nodes_k = torch.zeros(max(L - 1, 1) * 8, dtype=torch.int32, device=dev)
+            boxes, shift = cs.build_lbvh.group_boxes(bvh, L)
+            bl, al = cs.build_lbvh(), cs.assign_lights_lbvh()
+            fn = lambda: (bl(stream, li, L, boxes, shift, nodes_k),
+                          al(stream, keys, kc, frame_dev, nodes_k, bvh, L, li, vp, counts, offs, idx, tot, sph))
+    elif args.profile == "bouncer":
+        n = 1 << 24  # 1 GB of positions and directions
+        rng = np.random.default_rng(SEED)
+        p_t = torch.from_numpy(rng.uniform(-100, 100, (n, 4)).astype(np.float32).reshape(-1)).to(dev)
+        d_t = torch.from_numpy(rng.standard_normal((n, 4)).astype(np.float32).reshape(-1)).to(dev)
+        fn = lambda: cs.bounce_point_lights(stream, p_t, d_t, n, [-400, -250, 0.1], [400, 250, 1000], 20.0, 1 / 60)
+    elif args.profile == "debug_views":
+        # show_clusters (light-index mode) and the cluster geometry on the 1080p shading frame
+        import vren_gb300.cluster_debug as cd
+
+        ctx = cs.cluster_and_shade(SHADE_W, SHADE_H, 65536, 1 << 24)
+        shade_profile_setup(dev, stream, ctx)
+        o = ctx.outputs()
+        view_dbg = cd.show_clusters()
+        rgba = view_dbg(stream, "light_indices", SHADE_W, SHADE_H, o)
+        U = int(cs.read_device(o.key_count, 1)[0])
+        verts = cd.show_clusters_geometry(stream, o, max_clusters=U)
+        fn = lambda: (view_dbg(stream, "light_indices", SHADE_W, SHADE_H, o, rgba),
+                      cd.show_clusters_geometry(stream, o, verts, max_clusters=U))
+    elif args.profile == "kd_tree":
+        from vren_gb300 import kd_tree as kd
+
+        rng = np.random.default_rng(SEED + 31)
+        pts = rng.uniform(0, 100, (1_000_000, 3)).astype(np.float32)
+        nodes_np, _ = kd.kd_tree_build(pts)
+        depth_kd = kd.kd_tree_depth(nodes_np)
+        d_pts = torch.from_numpy(pts.reshape(-1)).to(dev)
+        d_nodes = torch.from_numpy(nodes_np.view(np.int32).reshape(-1)).to(dev)
+        smp = torch.from_numpy(rng.uniform(0, 100, (1 << 20, 3)).astype(np.float32).reshape(-1)).to(dev)
+        bp = torch.empty(1 << 20, dtype=torch.int32, device=dev)
+        bd = torch.empty(1 << 20, dtype=torch.float32, device=dev)
+        fn = lambda: kd.kd_tree_search_batch(stream, d_pts, d_nodes, smp, depth_kd, best_points=bp, best_distances=bd)
     elif args.profile in ("pyramid", "pyramid_4k"):
         # the depth pyramid at 8192x8192 (268 MB read > L2) or at 3840x2160
         from vren_gb300.depth_pyramid import depth_buffer_pyramid, depth_buffer_reductor
@@ -1045,7 +1141,8 @@ def main():
     ap.add_argument("--quick", action="store_true", help="skip the primitive sweep and the large sorts")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--profile", choices=["frame", "batch", "find_unique", "find_unique_rgba16f", "radix", "scan",
-                                          "shade", "shade_backward", "pyramid", "pyramid_4k"],
+                                          "shade", "shade_backward", "pyramid", "pyramid_4k", "reduce", "bucket",
+                                          "build_bvh", "assign", "karras", "bouncer", "debug_views", "kd_tree"],
                     default=None,
                     help="run one kernel family on a case larger than L2 (for ncu) and exit")
     ap.add_argument("--vendor-radix", action="store_true",
