@@ -273,6 +273,8 @@ def run_ours(args, rank: int, world: int):
     lbvh = None if args.quick else lbvh_bench(args, dev, stream, flush, depth, normals, pos, lights, view)
     debug_views = None if args.quick else debug_views_bench(args, dev, stream, flush, ctx, hbm_peak)
     bouncer = None if args.quick else bouncer_bench(args, dev, stream, flush, hbm_peak)
+    animated = None if args.quick else animated_bench(args, dev, stream, flush, ctx, depth, normals, pos, lights,
+                                                      view)
     pyramid = None if args.quick else depth_pyramid_bench(args, dev, stream, flush, hbm_peak)
     kdtree = None if args.quick else kd_tree_bench(args, dev, stream, flush)
 
@@ -334,6 +336,7 @@ def run_ours(args, rank: int, world: int):
             "shade": shade,
             "karras_lbvh": lbvh,
             "light_bouncer": bouncer,
+            "animated_frames": animated,
             "depth_pyramid": pyramid,
             "cluster_debug_views": debug_views,
             "kd_tree": kdtree,
@@ -514,6 +517,33 @@ def kd_tree_bench(args, dev, stream, flush):
                                                                  best_distances=bd), 3, args.steps, flush)
         out[f"gpu_search_{q}_samples"] = {"ms": round(ms, 4), "msearch_s": round(q / (ms * 1e-3) / 1e6, 2)}
     return out
+
+
+def animated_bench(args, dev, stream, flush, ctx, depth, normals, pos, lights, view):
+    """Animated frames as vren_demo runs them: the point-light bouncer moves the 16384 lights
+    (speed 20, 60 frames/s, inside the frustum's bounding box), then the clustered assignment runs on
+    the moved lights; one step = bounce + frame, L2 flushed before each."""
+    import torch
+
+    import vren_gb300.clustered_shading as cs
+
+    rng = np.random.default_rng(SEED + 44)
+    d_depth, d_norm = torch.from_numpy(depth).to(dev), torch.from_numpy(normals).to(dev)
+    d_pos = torch.from_numpy(pos.copy()).to(dev)
+    d_light = torch.from_numpy(lights).to(dev)
+    dirs = np.zeros((L, 4), np.float32)
+    dirs[:, :3] = rng.standard_normal((L, 3))
+    d_dir = torch.from_numpy(dirs.reshape(-1)).to(dev)
+    p = pos.reshape(-1, 4)
+    lo, hi = p[:, :3].min(0).tolist(), p[:, :3].max(0).tolist()
+
+    def step():
+        cs.bounce_point_lights(stream, d_pos, d_dir, L, lo, hi, 20.0, 1.0 / 60.0)
+        ctx.cluster(stream, view, W, H, d_depth, d_norm, d_pos, d_light, L)
+
+    ms = time_events(stream, step, 3, args.steps, flush)
+    return {"ms_per_animated_frame": round(ms, 5), "frames_per_s": round(1e3 / ms, 1),
+            "step": "bounce 16384 lights + cluster assignment (8 launches)"}
 
 
 def radix_bench(args, dev, stream, flush, keys_np, hbm_peak):

@@ -463,6 +463,32 @@ private:
 
 namespace vren_demo {
 
+// vren_demo/vren_demo/clustered_shading_debug.cpp:6-200, headless: the views are written to device
+// memory (RGBA float per pixel; 32 vren_debug_vertex per cluster) instead of a Vulkan image / draw buffer.
+class show_clusters {
+public:
+    void operator()(cudaStream_t stream, int32_t mode, uint32_t width, uint32_t height, vren_cs_outputs const& outputs,
+                    vren::device_buffer const& rgba_output)
+    {
+        m_scratch.grow(vren_cs_show_clusters_scratch_bytes(outputs.key_capacity));
+        vren::check(vren_cs_show_clusters(stream, mode, width, height, outputs.cluster_refs, outputs.cluster_keys,
+                                          outputs.key_count, outputs.key_capacity, outputs.counts, outputs.offsets,
+                                          outputs.indices, rgba_output.at<float>(), m_scratch.m_ptr),
+                    "show_clusters");
+    }
+
+private:
+    vren::owned_buffer m_scratch;
+};
+
+inline void show_clusters_geometry(cudaStream_t stream, vren_cs_outputs const& outputs,
+                                   vren::device_buffer const& vertices)
+{
+    vren::check(vren_cs_show_clusters_geometry(stream, outputs.frame, outputs.cluster_keys, outputs.key_count,
+                                               outputs.key_capacity, vertices.at<vren_debug_vertex>()),
+                "show_clusters_geometry");
+}
+
 // vren_demo/vren_demo/point_light_bouncer.cpp:17-57: moves each light speed * dt along its direction
 // inside [aabb_min, aabb_max], reflecting off the faces; both buffers (vec4 per light) updated in place.
 class point_light_bouncer {
