@@ -130,6 +130,18 @@ def make_inputs(rank: int = 0):
 # ------------------------------------------------------------------------------------------------
 # Our arm
 # ------------------------------------------------------------------------------------------------
+def job_ms_over_ranks(local_ms_sum: float, steps: int, world: int, device) -> float:
+    """Effective ms per frame of the whole job: frames are independent replicas, so the job's time is
+    the slowest rank's timed total over the frames all ranks processed (steps x world)."""
+    if world <= 1:
+        return local_ms_sum / steps
+    import torch
+
+    t = torch.tensor([local_ms_sum], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item()) / (steps * world)
+
+
 def run_ours(args, rank: int, world: int):
     import torch
 
@@ -184,12 +196,7 @@ def run_ours(args, rank: int, world: int):
     t_wall = time.perf_counter() - t_wall0
     step_ms = [a.elapsed_time(b) for a, b in ev]
     ms_frame = sum(step_ms) / len(step_ms)
-    if world > 1:
-        t = torch.tensor([sum(step_ms)], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        job_ms = float(t.item()) / (args.steps * world)
-    else:
-        job_ms = ms_frame
+    job_ms = job_ms_over_ranks(sum(step_ms), args.steps, world, dev)
     err = vg.device_error()
 
     # dominant HBM kernel of the frame: find_unique_cluster_list (20 B/px), timed alone
