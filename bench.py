@@ -941,9 +941,10 @@ def run_profile(args):
     dev = torch.device("cuda", 0)
     stream = torch.cuda.Stream(device=dev)
     reps = args.warmup + args.steps
-    if args.profile == "batch":
-        # the batched form on the 64 mixed frames (fixed options: 6-bit digits, 2 traversal warps)
-        specs = batch_specs()
+    if args.profile in ("batch", "batch_small"):
+        # the batched form on the 64 mixed frames, or on the first 8 of them (small enough for a full
+        # ncu capture); fixed options: 6-bit digits, 2 traversal warps
+        specs = batch_specs() if args.profile == "batch" else batch_specs()[:8]
         frames = []
         for k, (w, h, nl) in enumerate(specs):
             v = cs.view_from_camera(cs.scene_camera(w, h), "ref")
@@ -1056,6 +1057,20 @@ def run_profile(args):
             bl, al = cs.build_lbvh(), cs.assign_lights_lbvh()
             fn = lambda: (bl(stream, li, L, boxes, shift, nodes_k),
                           al(stream, keys, kc, frame_dev, nodes_k, bvh, L, li, vp, counts, offs, idx, tot, sph))
+    elif args.profile == "light_bvh_multi":
+        # construct_point_light_bvh for 65536 lights (above the single-cluster kernel's 32768): view
+        # transform, Morton codes, sort, leaves and BVH levels as separate kernels
+        nl = 65536
+        pos_l, li_l = scene.lights(SEED + 1000, nl, W, H)
+        view = cs.view_from_camera(cs.scene_camera(W, H), "ref")
+        frame_dev = cs.frame_to_device(cs.frame_build(view, W, H), dev)
+        d_p, d_l = torch.from_numpy(pos_l).to(dev), torch.from_numpy(li_l).to(dev)
+        vp = torch.zeros(4 * nl, dtype=torch.float32, device=dev)
+        bvh = torch.zeros(vg.calc_bvh_buffer_length(nl) * 8, dtype=torch.int32, device=dev)
+        lidx = torch.zeros(2 * nl, dtype=torch.int32, device=dev)
+        sph = torch.zeros(4 * vg.calc_bvh_padded_leaf_count(nl), dtype=torch.float32, device=dev)
+        cb = cs.construct_point_light_bvh()
+        fn = lambda: cb(stream, d_p, d_l, nl, frame_dev, vp, bvh, lidx, sph)
     elif args.profile == "bouncer":
         n = 1 << 24  # 1 GB of positions and directions
         rng = np.random.default_rng(SEED)
@@ -1179,7 +1194,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--profile", choices=["frame", "batch", "find_unique", "find_unique_rgba16f", "radix", "scan",
                                           "shade", "shade_backward", "pyramid", "pyramid_4k", "reduce", "bucket",
-                                          "build_bvh", "assign", "karras", "bouncer", "debug_views", "kd_tree"],
+                                          "build_bvh", "assign", "karras", "bouncer", "debug_views", "kd_tree",
+                                          "light_bvh_multi", "batch_small"],
                     default=None,
                     help="run one kernel family on a case larger than L2 (for ncu) and exit")
     ap.add_argument("--vendor-radix", action="store_true",
