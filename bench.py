@@ -251,6 +251,20 @@ def run_ours(args, rank: int, world: int):
     e2e = sum(e2e_ms) / len(e2e_ms)
     e2e_refs_ok = bool(np.array_equal(h_refs.numpy(), cs.read_device(out.cluster_refs, W * H).view(np.int32)))
 
+    # extra, labelled: the same frame with 16384 lights packed in front of the camera, so that the
+    # light lists are long (the workload's lights, uniform over a frustum box 1000 deep, reach few of
+    # the visible clusters)
+    import vren_gb300.scene as scene
+
+    dpos, dlights = scene.lights_near_camera(SEED + 77, L)
+    d_dpos, d_dlights = torch.from_numpy(dpos).to(dev), torch.from_numpy(dlights).to(dev)
+    dense_ms = time_events(stream, lambda: ctx.cluster(stream, view, W, H, d_depth, d_norm, d_dpos, d_dlights, L), 3,
+                           args.steps, flush)
+    od = ctx.outputs()
+    dense = {"frame_ms": round(dense_ms, 5), "assignments": int(cs.read_device(od.total, 1)[0]),
+             "unique_clusters": int(cs.read_device(od.key_count, 1)[0]),
+             "lights": "16384 lights uniform in x [-8, 8], y [-5, 5], z [0.5, 25], radius lognormal(ln 2, 0.5)"}
+
     # extra, labelled: the frame with its normals in the reference's own G-buffer format (RGBA16F,
     # 8 B/px instead of 12), on the device and end to end from host buffers
     d_norm16 = torch.from_numpy(normals_h).to(dev)
@@ -329,6 +343,7 @@ def run_ours(args, rank: int, world: int):
                             "lists written to host memory by the device); host wall clock",
                     "refs_match_device": e2e_refs_ok},
             "normals_rgba16f": rgba16f,
+            "dense_lights": dense,
             "gpu_launches": launches_per_frame * args.steps,
             "roofline": {"bound": "hbm", "kernel": "find_unique_cluster_list (find_unique_kernel, "
                                                      "find_unique_scan_kernel, find_unique_fixup_kernel)",
