@@ -9,6 +9,7 @@
 #include "common.cuh"
 #include "internal.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -772,9 +773,26 @@ __global__ void __launch_bounds__(256) assign_kernel(AssignArgs a, LevelBase lb)
     uint32_t U = *a.key_count;
     if (U > a.key_cap) U = a.key_cap;
     for (uint32_t c = gw; c < U; c += nw) {
-        if (WRITE && a.counts[c] == 0u) continue;  // nothing to write: skip the second traversal
-        const uint32_t acc = assign_cluster<LC, WRITE, SPHERES>(a, lb, a.keys[c], WRITE ? a.offsets[c] : 0u, lane);
-        if (!WRITE && lane == 0) a.counts[c] = acc;
+        const bool staged = a.stage != nullptr && c < a.stage_slots;
+        if (WRITE) {
+            const uint32_t n = a.counts[c];
+            if (n == 0u) continue;  // nothing to write: skip the second traversal
+            if (staged && n <= kStageLights) {
+                // the count pass kept the whole list, in list order: copy it instead of traversing again
+                const uint32_t o = a.offsets[c];
+                for (uint32_t i = lane; i < n; i += 32u) {
+                    const uint32_t pos = o + i;
+                    if (pos < a.index_cap) a.indices[pos] = a.stage[(size_t)c * kStageLights + i];
+                    else VREN_RECORD_ERROR(VREN_ERR_CAPACITY);
+                }
+                continue;
+            }
+            assign_cluster<LC, true, SPHERES>(a, lb, a.keys[c], a.offsets[c], lane);
+        } else {
+            const uint32_t acc = staged ? assign_cluster<LC, false, SPHERES, true>(a, lb, a.keys[c], c * kStageLights, lane)
+                                        : assign_cluster<LC, false, SPHERES>(a, lb, a.keys[c], 0u, lane);
+            if (lane == 0) a.counts[c] = acc;
+        }
     }
 }
 
@@ -876,7 +894,8 @@ static void launch_assign(cudaStream_t st, uint32_t lc, dim3 grid, dim3 block, c
 static int assign_lights(cudaStream_t st, const uint32_t* keys, const uint32_t* key_count, uint32_t key_cap,
                          const vren_cs_frame* frame, const vren_bvh_node* bvh, uint32_t L, const uint32_t* light_index,
                          const float* view_pos, const float* spheres, uint32_t* counts, uint32_t* offsets,
-                         uint32_t* indices, uint32_t index_cap, uint32_t* total, void* scratch, uint32_t warps_per_cta)
+                         uint32_t* indices, uint32_t index_cap, uint32_t* total, void* scratch, uint32_t warps_per_cta,
+                         uint32_t* stage = nullptr, uint32_t stage_slots = 0)
 {
     if (L == 0) {
         launch_kernel(zero_counts_kernel, 256, 256, 0, st, key_count, key_cap, counts, offsets, total);
@@ -888,7 +907,7 @@ static int assign_lights(cudaStream_t st, const uint32_t* keys, const uint32_t* 
     if (lc < 1 || lc > 6) return VREN_ERR_ARG;
     AssignArgs a{keys, key_count, key_cap, frame, bvh, reinterpret_cast<const uint2*>(light_index),
                  reinterpret_cast<const float4*>(view_pos), reinterpret_cast<const float4*>(spheres),
-                 counts, offsets, indices, index_cap};
+                 counts, offsets, indices, index_cap, stage, stage ? stage_slots : 0u};
     if (warps_per_cta < 1 || warps_per_cta > 8) warps_per_cta = 8;
     const dim3 block(32 * warps_per_cta);
     const dim3 grid(kNumSMsHint * (64 / warps_per_cta));
@@ -1174,6 +1193,8 @@ struct vren_cluster_and_shade {
     uint32_t* offsets = nullptr;
     uint32_t* indices = nullptr;
     uint32_t* total = nullptr;
+    uint32_t* stage = nullptr;  // the count pass's copy of each cluster's first kStageLights lights
+    uint32_t stage_slots = 0;
     void* lbvh_scratch = nullptr;
     void* fuc_scratch = nullptr;
     void* assign_scratch = nullptr;
@@ -1232,7 +1253,7 @@ int cs_enqueue(vren_cluster_and_shade* cs, cudaStream_t st, uint32_t W, uint32_t
     if (rc != VREN_OK) return rc;
     return assign_lights(st, cs->keys, cs->key_count, cs->key_cap, cs->frame, cs->bvh, L, cs->light_index,
                          cs->view_pos, cs->spheres, cs->counts, cs->offsets, cs->indices, cs->max_assign, cs->total,
-                         cs->assign_scratch, cs->opt.assign_warps);
+                         cs->assign_scratch, cs->opt.assign_warps, cs->stage, cs->stage_slots);
 }
 }  // namespace
 
@@ -1268,6 +1289,9 @@ extern "C" int vren_cs_create(vren_cluster_and_shade** out, uint32_t max_width, 
     const size_t o_offs = carve((size_t)cs->key_cap * 4);
     const size_t o_idx = carve((size_t)(max_assignments ? max_assignments : 1) * 4);
     const size_t o_total = carve(4);
+    // stage: one slot of kStageLights per cluster, up to the index capacity (the lists it can hold)
+    const uint64_t stage_words = std::min<uint64_t>((uint64_t)max_assignments, (uint64_t)cs->key_cap * kStageLights);
+    const size_t o_stage = carve((size_t)(stage_words ? stage_words : 1) * 4);
     size_t lbvh = 0;
     for (uint32_t db : {4u, 6u, 8u})
         for (uint32_t mb : {15u, 30u}) {
@@ -1300,6 +1324,8 @@ extern "C" int vren_cs_create(vren_cluster_and_shade** out, uint32_t max_width, 
     cs->offsets = reinterpret_cast<uint32_t*>(a + o_offs);
     cs->indices = reinterpret_cast<uint32_t*>(a + o_idx);
     cs->total = reinterpret_cast<uint32_t*>(a + o_total);
+    cs->stage = reinterpret_cast<uint32_t*>(a + o_stage);
+    cs->stage_slots = (uint32_t)(stage_words / kStageLights);
     cs->lbvh_scratch = a + o_lbvh;
     cs->fuc_scratch = a + o_fuc;
     cs->assign_scratch = a + o_asg;
@@ -1437,7 +1463,7 @@ int cs_enqueue_host(vren_cluster_and_shade* cs, cudaStream_t st, uint32_t W, uin
     VREN_CUDA_TRY(cudaStreamWaitEvent(st, cs->ev_bvh, 0));
     rc = assign_lights(st, cs->keys, cs->key_count, cs->key_cap, cs->frame, cs->bvh, L, cs->light_index,
                        cs->view_pos, cs->spheres, cs->counts, cs->offsets, cs->indices, cs->max_assign, cs->total,
-                       cs->assign_scratch, cs->opt.assign_warps);
+                       cs->assign_scratch, cs->opt.assign_warps, cs->stage, cs->stage_slots);
     if (rc != VREN_OK) return rc;
     if (lists_out) {
         launch_kernel(lists_to_host_kernel, kNumSMsHint, 256, 0, st, cs->key_count, cs->key_cap, cs->total, cs->keys,

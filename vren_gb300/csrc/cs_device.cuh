@@ -577,16 +577,21 @@ struct AssignArgs {
     const uint32_t* offsets;
     uint32_t* indices;
     uint32_t index_cap;
+    uint32_t* stage;       // optional: the count pass keeps each cluster's first kStageLights lights here
+    uint32_t stage_slots;  // clusters c < stage_slots own stage[c * kStageLights ..]
 };
+
+// Lights a cluster can keep from the count pass for the write pass to copy instead of traversing again.
+constexpr uint32_t kStageLights = 64;
 
 // The reference walks the 32-ary tree with an explicit state machine over per-level overlap
 // masks (assign_lights.comp:142-240): ENTERING tests the 32 nodes of a group with one ballot,
 // ADVANCE clears the lowest set bit and descends into the next overlapping child.  The same
 // depth-first order, written as a recursion over compile-time levels: the masks stay in
 // registers and the group address is built incrementally (assign_lights.comp:108-119).
-template <int LEVEL, int LC, bool WRITE, bool SPHERES>
+template <int LEVEL, int LC, bool WRITE, bool SPHERES, bool STAGE = false>
 __device__ __forceinline__ void visit(const AssignArgs& a, const LevelBase& lb, const Box& box, uint32_t rel,
-                                      uint32_t lane, uint32_t& acc, uint32_t out_base)
+                                      uint32_t lane, uint32_t& acc, uint32_t out_base)  // STAGE: out_base = c * kStageLights
 {
     const uint32_t addr = lb.base[LEVEL] + rel;
     if constexpr (LEVEL == LC - 1) {
@@ -595,7 +600,7 @@ __device__ __forceinline__ void visit(const AssignArgs& a, const LevelBase& lb, 
         if constexpr (SPHERES) {
             const float4 s = __ldg(a.spheres + addr + lane);
             hit = test_sphere_aabb(s.x, s.y, s.z, s.w, box);
-            if (WRITE && hit) li = __ldg(&a.light_index[addr + lane].y);
+            if ((WRITE || STAGE) && hit) li = __ldg(&a.light_index[addr + lane].y);
         } else {
             const NodeF n = load_node(a.bvh, addr + lane);
             if (n.next != VREN_BVH_INVALID_NODE) {
@@ -612,6 +617,10 @@ __device__ __forceinline__ void visit(const AssignArgs& a, const LevelBase& lb, 
             if (pos < a.index_cap) a.indices[pos] = li;
             else VREN_RECORD_ERROR(VREN_ERR_CAPACITY);
         }
+        if (STAGE && hit) {  // the same order, into the cluster's stage slots (the first kStageLights)
+            const uint32_t local = acc + __popc(mask & ~lanemask_lt()) - 1u;
+            if (local < kStageLights) a.stage[out_base + local] = li;
+        }
         acc += __popc(mask);
     } else {
         const NodeF n = load_node(a.bvh, addr + lane);
@@ -620,7 +629,7 @@ __device__ __forceinline__ void visit(const AssignArgs& a, const LevelBase& lb, 
         while (mask) {
             const uint32_t ch = __ffs(mask) - 1;
             mask &= mask - 1u;
-            visit<LEVEL + 1, LC, WRITE, SPHERES>(a, lb, box, 32u * (rel + ch), lane, acc, out_base);
+            visit<LEVEL + 1, LC, WRITE, SPHERES, STAGE>(a, lb, box, 32u * (rel + ch), lane, acc, out_base);
         }
     }
 }
@@ -628,13 +637,13 @@ __device__ __forceinline__ void visit(const AssignArgs& a, const LevelBase& lb, 
 
 // Traversal of one cluster (warp-wide): returns the number of lights assigned, and with WRITE writes
 // them from out_base on.
-template <int LC, bool WRITE, bool SPHERES>
+template <int LC, bool WRITE, bool SPHERES, bool STAGE = false>
 __device__ __forceinline__ uint32_t assign_cluster(const AssignArgs& a, const LevelBase& lb, uint32_t key,
                                                    uint32_t out_base, uint32_t lane)
 {
     const Box box = cluster_box(key, a.frame);
     uint32_t acc = 0;
-    visit<0, LC, WRITE, SPHERES>(a, lb, box, 0u, lane, acc, out_base);
+    visit<0, LC, WRITE, SPHERES, STAGE>(a, lb, box, 0u, lane, acc, out_base);
     return acc;
 }
 
