@@ -101,11 +101,31 @@ __global__ void __launch_bounds__(THREADS) reduce_tree_pass_kernel(
     const uint32_t limit = first_pass ? n_valid : count;           // elements that exist in memory
 
     T v[4];
+    if constexpr (sizeof(T) == 4) {
+        // first pass over 16-byte aligned u32 input: the thread's four consecutive elements in one load
+        if (base == 0 && j0 + 3u < limit && ((reinterpret_cast<uintptr_t>(src) & 15u) == 0)) {
+            const uint4 q = *reinterpret_cast<const uint4*>(src + j0);
+            v[0] = q.x;
+            v[1] = q.y;
+            v[2] = q.z;
+            v[3] = q.w;
+        } else {
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        uint32_t j = j0 + k;
-        v[k] = (j < limit) ? src[(size_t)((uint64_t)(j + 1) * stride - 1)] : Op::identity();
+            for (int k = 0; k < 4; ++k) {
+                uint32_t j = j0 + k;
+                v[k] = (j < limit) ? src[(size_t)((uint64_t)(j + 1) * stride - 1)] : Op::identity();
+            }
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            uint32_t j = j0 + k;
+            v[k] = (j < limit) ? src[(size_t)((uint64_t)(j + 1) * stride - 1)] : Op::identity();
+        }
     }
+    // Elements 0 and 2 of the thread keep their value (they are not the end of a level-1 or higher
+    // block); when this pass reads and writes the same positions, they need no store.
+    const bool in_place = src == dst;
 
     // Levels 0 and 1 inside the thread.
     v[1] = Op::apply(v[1], v[0]);
@@ -143,6 +163,7 @@ __global__ void __launch_bounds__(THREADS) reduce_tree_pass_kernel(
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         uint32_t j = j0 + k;
+        if ((k & 1) == 0 && in_place && j < limit) continue;  // loaded from this position, unchanged
         if (j < count) dst[(size_t)((uint64_t)(j + 1) * stride - 1)] = v[k];
     }
 }
