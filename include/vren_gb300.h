@@ -257,8 +257,8 @@ int vren_build_lbvh(vren_stream_t s, const uint32_t* sorted_pairs, uint32_t leaf
  *   cluster refs     u32[W*H]: index of the pixel's key in the key list
  *   counts/offsets   u32[U]; indices u32[sum(counts)]        (assign_lights.comp:57-70)
  *
- * Canonical semantics where the reference is nondeterministic or implementation-defined (the full
- * list is in the design doc): key lists are ordered by tile (row-major) then ascending key; texels are
+ * Canonical semantics where the reference is nondeterministic or implementation-defined (the main
+ * ones): key lists are ordered by tile (row-major) then ascending key; texels are
  * fetched at integer coordinates (x mod W, y mod H) like the reference's REPEAT sampler, or
  * skipped; depth slices come from a boundary table built on the host; light ties sort by index;
  * invalid BVH nodes are never traversed or assigned; float arithmetic follows a fixed order of

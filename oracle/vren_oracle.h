@@ -10,8 +10,9 @@
  * (vren_test/vren_test/primitives/*.cpp), restated as golden fixtures under tests/golden/.
  * The clustered-shading stages have no test, no CPU code and no golden vectors in the reference
  * (their shaders use GLSL built-ins compiled by a Vulkan driver that cannot run here), so
- * their parity is UNPINNED: this oracle restates the shaders under the canonical decisions
- * listed in DESIGN.md (§ "Canonical semantics") and the CUDA kernels are checked against it.
+ * their parity is UNPINNED: this oracle restates the shaders under canonical decisions (a fixed
+ * order where the reference's is unspecified, exactly rounded float steps, slice bounds from a
+ * host table) and the CUDA kernels are checked against it.
  *
  * Float rules shared with the CUDA kernels: IEEE single precision, round to nearest, no FMA
  * contraction (built with -ffp-contract=off), division and sqrt correctly rounded, float->uint
