@@ -1,7 +1,7 @@
 """CPU oracle (TEST INFRASTRUCTURE ONLY) — ctypes bindings over oracle/_build/libvren_oracle.so.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may use this package, and
-only as the checker / the timed CPU baseline.  See vren_oracle.h for what is pinned.
+only as the oracle results are compared with, or as the timed CPU baseline.  See vren_oracle.h for what is pinned.
 """
 from __future__ import annotations
 

@@ -1,6 +1,6 @@
 /*
  * vren_oracle.c — CPU oracle for the vren hot path.  TEST INFRASTRUCTURE ONLY: used by the
- * tests, the smoke check and the benchmark's CPU-baseline leg as the checker, never by the
+ * tests, the smoke check and the benchmark's CPU-baseline leg as the oracle, never by the
  * product path.  See vren_oracle.h for what is pinned (primitives) and what is unpinned
  * (clustered shading stages).
  *

@@ -2,7 +2,7 @@
  * vren_oracle.h — CPU oracle for the vren hot path.  TEST INFRASTRUCTURE ONLY.
  *
  * A plain-C restatement of the reference's algorithms (loryruta/vren), used by the tests, by
- * the smoke check and by the benchmark's CPU-baseline leg as the checker — never by the product
+ * the smoke check and by the benchmark's CPU-baseline leg as the oracle — never by the product
  * path.  Every function cites the reference file:line it restates.
  *
  * Pinning.  The primitives (reduce, scan, down-sweep, radix sort, bucket sort, BVH build and
