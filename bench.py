@@ -877,7 +877,7 @@ def cpu_baseline(depth, normals, pos, lights, radix_keys, view, budget_s: float 
 # Reference arm: the CPU implementation of the path (oracle port), all host threads
 # ------------------------------------------------------------------------------------------------
 def numpy_view(cs, near: float = 0.1, far: float = 1000.0, fov_deg: float = 45.0):
-    """The bench camera (origin, yaw = pitch = 0) with vren/vren/camera.cpp:66-84's formulas, so the
+    """The bench camera (origin, yaw = pitch = 0) with vren/vren/camera.cpp:32-50's formulas, so the
     CPU arm does not load the CUDA library."""
     fov = float(np.float32(np.deg2rad(fov_deg)))
     t = np.tan(fov / 2.0)

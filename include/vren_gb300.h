@@ -37,7 +37,7 @@ typedef void* vren_stream_t;
 
 /* ------------------------------------------------------------------------------------------------
  * Status codes.  The reference signals misuse with assert / std::invalid_argument
- * (radix_sort.cpp:212-215) and Vulkan failures with VREN_CHECK -> std::runtime_error
+ * (vren/primitives/radix_sort.cpp:158-161) and Vulkan failures with VREN_CHECK -> std::runtime_error
  * (vk_helpers/misc.cpp:8-37); capacity overflows are unchecked there (config.hpp:23-24).
  * ------------------------------------------------------------------------------------------------ */
 enum {
@@ -93,14 +93,14 @@ int vren_tuning_set(int knob, int value);
 int vren_tuning_get(int knob);
 
 /* ------------------------------------------------------------------------------------------------
- * Size helpers (vren/vren/base/base.hpp:281-328, integer restatements)
+ * Size helpers (vren/vren/base/base.hpp:32-79, integer restatements)
  * ------------------------------------------------------------------------------------------------ */
-uint32_t vren_round_to_next_power_of_2(uint32_t v);     /* base.hpp:286-296, 0 -> 0 */
-uint32_t vren_round_to_next_power_of(uint32_t n, uint32_t base); /* base.hpp:318-323 */
-uint32_t vren_divide_and_ceil(uint32_t value, uint32_t divider); /* base.hpp:325-328 */
+uint32_t vren_round_to_next_power_of_2(uint32_t v);     /* base.hpp:37-47; maps 0 to 0 */
+uint32_t vren_round_to_next_power_of(uint32_t n, uint32_t base); /* base.hpp:69-74 */
+uint32_t vren_divide_and_ceil(uint32_t value, uint32_t divider); /* base.hpp:76-79 */
 
 /* ------------------------------------------------------------------------------------------------
- * Reduce — vren::reduce<T,Op> (reduce.hpp:15-49, reduce.cpp:82-190, reduce.comp:50-86)
+ * Reduce — vren::reduce<T,Op> (reduce.hpp:15-49, vren/primitives/reduce.cpp:32-140, reduce.comp:50-86)
  *
  * The drop-in form writes the whole Blelloch up-sweep tree: with P = next power of two
  * of n, out[i] = Op over in[i-2^t+1 .. i] where t = min(trailing ones of i, log2 P),
@@ -112,7 +112,7 @@ uint32_t vren_divide_and_ceil(uint32_t value, uint32_t divider); /* base.hpp:325
  * ------------------------------------------------------------------------------------------------ */
 enum { VREN_REDUCE_ADD = 0, VREN_REDUCE_MIN = 1, VREN_REDUCE_MAX = 2 };
 
-uint32_t vren_calc_reduce_output_buffer_length(uint32_t count);          /* reduce.cpp:187-190 */
+uint32_t vren_calc_reduce_output_buffer_length(uint32_t count);          /* vren/primitives/reduce.cpp:137-140 */
 int vren_reduce_tree_u32(vren_stream_t s, int op, const uint32_t* in, uint32_t n,
                          uint32_t* out, uint32_t blocks);
 int vren_reduce_tree_vec4(vren_stream_t s, int op, const float* in /* vec4[n] */, uint32_t n,
@@ -128,10 +128,10 @@ int vren_reduce_f32(vren_stream_t s, int op, const float* in, uint32_t n, float*
                     void* scratch);
 
 /* ------------------------------------------------------------------------------------------------
- * Exclusive scan — vren::blelloch_scan (blelloch_scan.hpp:9-49, blelloch_scan.cpp:107-216)
+ * Exclusive scan — vren::blelloch_scan (blelloch_scan.hpp:9-49, vren/primitives/blelloch_scan.cpp:57-166)
  *
  * In-place exclusive prefix sum of uint32 (mod 2^32) over `blocks` independent segments
- * of length n.  The reference requires n to be a power of two (blelloch_scan.cpp:117);
+ * of length n.  The reference requires n to be a power of two (vren/primitives/blelloch_scan.cpp:67);
  * this implementation accepts any n (a power of two gives the reference's result).
  * Single pass with decoupled look-back.
  * ------------------------------------------------------------------------------------------------ */
@@ -148,7 +148,7 @@ int vren_exclusive_scan_u32(vren_stream_t s, uint32_t* data, uint32_t n, uint32_
  * array's address and should come before any stream capture. */
 int vren_exclusive_scan_u32_noalloc(vren_stream_t s, uint32_t* data, uint32_t n, uint32_t blocks);
 
-/* The reference's public down-sweep (blelloch_scan.cpp:107-189) applied to a buffer that
+/* The reference's public down-sweep (vren/primitives/blelloch_scan.cpp:57-139) applied to a buffer that
  * holds an up-sweep tree: n must be a power of two.  For n >= 1024 the root value is
  * kept unless `clear_last`; for n < 1024 the reference's single work-group pass always
  * propagates zero into the root, and so does this one. */
@@ -156,15 +156,15 @@ int vren_scan_downsweep_u32(vren_stream_t s, uint32_t* data, uint32_t n, uint32_
                             int clear_last);
 
 /* ------------------------------------------------------------------------------------------------
- * Radix sort — vren::radix_sort (radix_sort.hpp:9-53, radix_sort.cpp:178-392)
+ * Radix sort — vren::radix_sort (radix_sort.hpp:9-53, vren/primitives/radix_sort.cpp:149-338)
  *
  * Stable ascending LSD sort of uint32 keys, in place, onesweep (one histogram kernel
  * then one kernel per digit with decoupled look-back).  scratch1 is this
  * implementation's histogram/status region (size from vren_radix_sort_scratch1_bytes),
- * scratch2 holds n keys (the reference's create_scratch_buffer_2, radix_sort.cpp:192-201).
+ * scratch2 holds n keys (the reference's create_scratch_buffer_2, vren/primitives/radix_sort.cpp:138-147).
  *
  * vren_radix_sort_u32 is the drop-in: it keeps the reference's precondition (n >= 1024
- * and a power of two, else VREN_ERR_ARG — radix_sort.cpp:212-215).  The _ex form sorts
+ * and a power of two, else VREN_ERR_ARG — vren/primitives/radix_sort.cpp:158-161).  The _ex form sorts
  * any n, optionally carries a uint32 value per key (scratch_values holds n values), and
  * takes the digit width (4, 6 or 8 bits).
  * ------------------------------------------------------------------------------------------------ */
@@ -176,7 +176,7 @@ int vren_radix_sort_u32_ex(vren_stream_t s, uint32_t* keys, uint32_t* values, ui
                            uint32_t* scratch_values);
 
 /* ------------------------------------------------------------------------------------------------
- * Bucket sort — vren::bucket_sort (bucket_sort.hpp:9-45, bucket_sort.cpp:114-208)
+ * Bucket sort — vren::bucket_sort (bucket_sort.hpp:9-45, vren/primitives/bucket_sort.cpp:72-161)
  *
  * Groups uvec2(key, value) elements by (key & (2^key_bits - 1)).  The reference uses
  * key_bits = 16 and global atomics (so its order within a bucket is unspecified); this
@@ -184,7 +184,7 @@ int vren_radix_sort_u32_ex(vren_stream_t s, uint32_t* keys, uint32_t* values, ui
  * vren_bucket_sort_output_bytes(n, key_bits): the n sorted elements, then at byte offset
  * round_up(8n, 256) the 2^key_bits bucket END offsets (inclusive prefix of the counts),
  * which is what the reference leaves in its counter region after the call
- * (bucket_sort.cpp:114-117, 133, bucket_sort_write.comp:32).
+ * (vren/primitives/bucket_sort.cpp:116-121, 134-142, bucket_sort_write.comp:32).
  * ------------------------------------------------------------------------------------------------ */
 size_t vren_bucket_sort_output_bytes(uint32_t n, uint32_t key_bits);
 size_t vren_bucket_sort_scratch_bytes(uint32_t n, uint32_t key_bits);
@@ -192,7 +192,7 @@ int vren_bucket_sort_u32x2(vren_stream_t s, const uint32_t* in /* uvec2[n] */, u
                            void* out, uint32_t key_bits, void* scratch);
 
 /* ------------------------------------------------------------------------------------------------
- * BVH — vren::build_bvh (build_bvh.hpp:8-57, build_bvh.cpp:95-193, build_bvh.comp:32-55)
+ * BVH — vren::build_bvh (build_bvh.hpp:8-57, vren/primitives/build_bvh.cpp:38-136, build_bvh.comp:32-55)
  *
  * 32-ary bottom-up tree stored level after level: leaves [0, P), then P/32 parents, ...,
  * the root last.  A parent's next = index of its first child, or VREN_BVH_INVALID_NODE
@@ -209,11 +209,11 @@ typedef struct vren_bvh_node {
     uint32_t pad;
 } vren_bvh_node;
 
-uint32_t vren_calc_bvh_padded_leaf_count(uint32_t leaf_count);  /* build_bvh.cpp:158-161 */
-uint32_t vren_calc_bvh_buffer_length(uint32_t leaf_count);      /* build_bvh.cpp:163-175 */
-size_t vren_calc_bvh_buffer_size(uint32_t leaf_count);          /* build_bvh.cpp:177-181 */
-uint32_t vren_calc_bvh_root_index(uint32_t leaf_count);         /* build_bvh.cpp:183-187 */
-uint32_t vren_calc_bvh_level_count(uint32_t leaf_count);        /* build_bvh.cpp:189-193 */
+uint32_t vren_calc_bvh_padded_leaf_count(uint32_t leaf_count);  /* vren/primitives/build_bvh.cpp:101-104 */
+uint32_t vren_calc_bvh_buffer_length(uint32_t leaf_count);      /* vren/primitives/build_bvh.cpp:106-118 */
+size_t vren_calc_bvh_buffer_size(uint32_t leaf_count);          /* vren/primitives/build_bvh.cpp:120-124 */
+uint32_t vren_calc_bvh_root_index(uint32_t leaf_count);         /* vren/primitives/build_bvh.cpp:126-130 */
+uint32_t vren_calc_bvh_level_count(uint32_t leaf_count);        /* vren/primitives/build_bvh.cpp:132-136 */
 int vren_build_bvh(vren_stream_t s, vren_bvh_node* bvh, uint32_t padded_leaf_count);
 
 /* Karras binary radix tree (extension beside the reference's 32-ary BuildBVH; T. Karras, "Maximizing
@@ -244,8 +244,8 @@ int vren_build_lbvh(vren_stream_t s, const uint32_t* sorted_pairs, uint32_t leaf
  * vren::cluster_and_shade (clustered_shading.hpp:147-182, clustered_shading.cpp:817-1172).
  *
  * Data layouts (device memory, as in the reference):
- *   light positions  vec4[L], world space, w ignored        (light.hpp:190, light.cpp:260)
- *   point lights     {vec3 color; float intensity}[L]       (gpu_repr.hpp:146-149); intensity is
+ *   light positions  vec4[L], world space, w ignored        (light.hpp:27, light.cpp:11-21)
+ *   point lights     {vec3 color; float intensity}[L]       (gpu_repr.hpp:61-64); intensity is
  *                    the light radius
  *   view positions   vec4[L]: view * vec4(p.xyz, 1)          (point_light_position_to_view_space.comp:30)
  *   light index      uvec2[L]: (morton code, light index), sorted by code, ties by light index
@@ -280,8 +280,8 @@ typedef struct vren_camera {
 
 /* Camera-derived matrices, column-major m[c*4 + r] like glm. */
 typedef struct vren_cs_view {
-    float view[16];      /* world -> view (camera.cpp:66-72) */
-    float inv_proj[16];  /* inverse of the projection (camera.cpp:74-84) */
+    float view[16];      /* world -> view (camera.cpp:32-38) */
+    float inv_proj[16];  /* inverse of the projection (camera.cpp:40-50) */
     float inv_view[16];  /* view -> world */
     float eye[3];        /* camera position in world space */
     float near_plane, far_plane, half_fov_y;
@@ -292,7 +292,7 @@ typedef struct vren_cs_view {
 /* Per-frame parameter block that the kernels read from device memory (8448 bytes).
  * slice_near[k] / slice_far[k] are the view-space depth bounds of slice k:
  *   REF:     near * a^k and near * a^(k+1), a = 1 + 2 tan(fov_y/2) / tiles_y (find_unique_clusters.comp:65,
- *            clustered_shading.glsl:220-222), a^k by repeated double multiplication, rounded to float;
+ *            clustered_shading.glsl:99-101), a^k by repeated double multiplication, rounded to float;
  *   FIXED32: near * (far/near)^(k/32) for k <= 32, +inf beyond (max_slice = 31).
  * A pixel at view depth z falls in the largest slice k <= max_slice with slice_near[k] <= z (0 if none). */
 typedef struct vren_cs_frame {
@@ -316,8 +316,8 @@ int vren_cs_frame_build(const vren_cs_view* view, uint32_t width, uint32_t heigh
 int vren_cs_frame_upload(vren_stream_t s, const vren_cs_frame* host_frame, vren_cs_frame* device_frame);
 
 /* construct_point_light_bvh (clustered_shading.cpp:60-346): view transform, min/max, 15-bit Morton
- * codes (discretize_point_light_positions.comp:62-73; morton_bits = 30 selects 10 bits per axis),
- * stable sort by code, leaves = AABB(view position +- intensity) (init_light_array_bvh.comp:117-139),
+ * codes (discretize_point_light_positions.comp:30-39; morton_bits = 30 selects 10 bits per axis),
+ * stable sort by code, leaves = AABB(view position +- intensity) (init_light_array_bvh.comp:42-65),
  * BuildBVH.  `leaf_spheres` (optional, vec4[padded leaf count]) receives, per leaf, the light's view
  * position and the radius the traversal tests, (max.x - min.x) / 2 (assign_lights.comp:214); invalid
  * leaves get radius -1.  light_count = 0 writes nothing. */
@@ -405,7 +405,7 @@ int vren_cs_assign_lights_lbvh(vren_stream_t s, const uint32_t* cluster_keys, co
  * directional lights (the reference's constants: PI = 3.14, NDF with a = roughness, Smith with
  * k = roughness); VREN_CS_SHADE_COLOR adds 0.03 * albedo and applies pow(1/2.2) like the
  * reference, VREN_CS_SHADE_RADIANCE writes the point-light sum only (the quantity the adjoint
- * differentiates).  Falloff: VREN_CS_FALLOFF_REF = 1 - min(d/r, 1)^1.5 (pbr.glsl:231);
+ * differentiates).  Falloff: VREN_CS_FALLOFF_REF = 1 - min(d/r, 1)^1.5 (pbr.glsl:89);
  * VREN_CS_FALLOFF_WINDOWED_INV_SQ = saturate(1 - (d/r)^4)^2 / (d^2 + 1) (Karis 2013).
  * Pixels that are not shaded are left untouched (the reference does not store them). */
 enum { VREN_CS_FALLOFF_REF = 0, VREN_CS_FALLOFF_WINDOWED_INV_SQ = 1 };
@@ -426,7 +426,7 @@ typedef struct vren_cs_light_lists {
     const uint32_t* indices;      /* light indices */
 } vren_cs_light_lists;
 
-/* directional_lights: {float direction[3], pad, color[3], pad}[count] (gpu_repr.hpp:151-155) */
+/* directional_lights: {float direction[3], pad, color[3], pad}[count] (gpu_repr.hpp:66-70) */
 int vren_cs_shade(vren_stream_t s, const vren_cs_frame* frame, uint32_t width, uint32_t height,
                   const vren_cs_gbuffer* gbuffer, const vren_cs_light_lists* lists, const float* light_positions,
                   const float* point_lights, uint32_t light_count, const float* directional_lights,
@@ -470,7 +470,7 @@ typedef struct vren_kd_tree_node {
 /* Returns nonzero to accept `point` (the reference's kd_tree_search_filter_t). */
 typedef int (*vren_kd_tree_filter)(uint32_t point, void* user);
 
-/* kd_tree_build (kd_tree.cpp:5-77), on the host: same node array as the reference (pre-order, Welford
+/* kd_tree_build (vren/base/kd_tree.cpp:5-78), on the host: same node array as the reference (pre-order, Welford
  * mean split on the axis its variance test picks, in-place swap partition of `indices`).  Returns the
  * offset after the last node written (the node count for node_offset = 0; at most 2 * count).  A node
  * whose split separates nothing (where the reference asserts) becomes one leaf run of all its points. */
@@ -478,7 +478,7 @@ size_t vren_kd_tree_build(const float* points, size_t point_stride, uint32_t* in
                           vren_kd_tree_node* kd_tree, size_t node_offset, size_t max_leaf_point_count);
 /* Inner nodes on the longest root-to-leaf path (host). */
 uint32_t vren_kd_tree_depth(const vren_kd_tree_node* kd_tree, size_t node_offset);
-/* kd_tree_search (kd_tree.cpp:79-131), on the host: best_point / best_distance_squared are in-out (start
+/* kd_tree_search (vren/base/kd_tree.cpp:80-129), on the host: best_point / best_distance_squared are in-out (start
  * them at UINT32_MAX / +inf); filter NULL accepts every point. */
 void vren_kd_tree_search(const float* points, size_t point_stride, const uint32_t* indices, size_t count,
                          const vren_kd_tree_node* kd_tree, size_t node_offset, const float* sample,

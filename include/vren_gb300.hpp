@@ -6,7 +6,7 @@
 // vren::device_buffer (device pointer + size), and resource_container is kept as an empty type so
 // call sites keep their shape (nothing needs to be kept alive until a fence: the GPU work holds no
 // descriptor sets).  Errors follow the reference: precondition failures throw
-// std::invalid_argument (radix_sort.cpp:212-215), other failures std::runtime_error (VREN_CHECK,
+// std::invalid_argument (vren/primitives/radix_sort.cpp:158-161), other failures std::runtime_error (VREN_CHECK,
 // vk_helpers/misc.cpp:22-37).
 //
 // Header-only; link against libvren_gb300.so and the CUDA runtime.

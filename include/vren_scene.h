@@ -6,7 +6,7 @@
  * XSH-RR output.  (seed, stream) select the sequence; every function is deterministic and
  * single-valued for a given seed whatever the thread count.
  *
- * The scene follows the reference's camera conventions (vren/vren/camera.cpp:66-84): view space
+ * The scene follows the reference's camera conventions (vren/vren/camera.cpp:32-50): view space
  * is x right, y up, +z forward; the projection maps view z in [near, far] to depth [0, 1]
  * with m[2][2] = f/(f-n), m[3][2] = -f*n/(f-n), m[2][3] = 1.
  */

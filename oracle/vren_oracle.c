@@ -29,7 +29,7 @@ static int nthreads(int t)
 }
 
 /* ================================================================================================
- * Size helpers — vren/vren/base/base.hpp:286-328 and vren/vren/primitives/build_bvh.cpp:158-193,
+ * Size helpers — vren/vren/base/base.hpp:37-79 and vren/vren/primitives/build_bvh.cpp:101-136,
  * with the reference's double-precision log/pow where it uses them.
  * ================================================================================================ */
 uint32_t oracle_round_to_next_power_of_2(uint32_t v)
@@ -42,7 +42,7 @@ uint32_t oracle_round_to_next_power_of_2(uint32_t v)
 
 uint32_t oracle_round_to_next_power_of(uint32_t n, uint32_t base)
 {
-    /* base.hpp:318-323: exp = log(n)/log(base); return (uint32_t) pow(base, ceil(exp)); */
+    /* base.hpp:69-74: exp = log(n)/log(base); return (uint32_t) pow(base, ceil(exp)); */
     double e = log((double)n) / log((double)base);
     double r = pow((double)base, ceil(e));
     if (!(r >= 0.0) || r > 4294967295.0) return 0u;
@@ -51,19 +51,19 @@ uint32_t oracle_round_to_next_power_of(uint32_t n, uint32_t base)
 
 uint32_t oracle_divide_and_ceil(uint32_t value, uint32_t divider)
 {
-    /* base.hpp:325-328 */
+    /* base.hpp:76-79 */
     return (uint32_t)ceil((double)value / (double)divider);
 }
 
 uint32_t oracle_calc_bvh_padded_leaf_count(uint32_t leaf_count)
 {
-    /* build_bvh.cpp:158-161 */
+    /* vren/primitives/build_bvh.cpp:101-104 */
     return leaf_count <= 1 ? 32u : oracle_round_to_next_power_of(leaf_count, 32u);
 }
 
 uint32_t oracle_calc_bvh_buffer_length(uint32_t leaf_count)
 {
-    /* build_bvh.cpp:163-175 */
+    /* vren/primitives/build_bvh.cpp:106-118 */
     uint32_t p = oracle_calc_bvh_padded_leaf_count(leaf_count);
     uint64_t len = 0;
     while (p != 0) {
@@ -75,13 +75,13 @@ uint32_t oracle_calc_bvh_buffer_length(uint32_t leaf_count)
 
 uint32_t oracle_calc_bvh_root_index(uint32_t leaf_count)
 {
-    /* build_bvh.cpp:183-187 */
+    /* vren/primitives/build_bvh.cpp:126-130 */
     return oracle_calc_bvh_buffer_length(oracle_calc_bvh_padded_leaf_count(leaf_count)) - 1u;
 }
 
 uint32_t oracle_calc_bvh_level_count(uint32_t leaf_count)
 {
-    /* build_bvh.cpp:189-193: glm::log2 on an integer is the integer log2 */
+    /* vren/primitives/build_bvh.cpp:132-136: glm::log2 on an integer is the integer log2 */
     uint32_t p = oracle_calc_bvh_padded_leaf_count(leaf_count);
     uint32_t l = 0;
     while (p > 1) { p >>= 1; ++l; }
@@ -89,8 +89,8 @@ uint32_t oracle_calc_bvh_level_count(uint32_t leaf_count)
 }
 
 /* ================================================================================================
- * Reduce — tree order of run_cpu_reduce (vren_test/vren_test/primitives/reduce.cpp:326-341) with
- * the shader's combine b = OP(b, a) (vren/resources/shaders/reduce.comp:266) and the identities
+ * Reduce — tree order of run_cpu_reduce (vren_test/vren_test/primitives/reduce.cpp:72-87) with
+ * the shader's combine b = OP(b, a) (vren/resources/shaders/reduce.comp:76) and the identities
  * of VRen.cmake:70-75.  GLSL min(x,y) = y < x ? y : x, max(x,y) = x < y ? y : x.
  * ================================================================================================ */
 static uint32_t u32_apply(int op, uint32_t right, uint32_t left)
@@ -190,9 +190,9 @@ void oracle_exclusive_scan_u32(uint32_t* data, uint64_t n)
 void oracle_downsweep_u32(uint32_t* data, uint32_t n, int clear_last)
 {
     /* The reference's dispatch sequence, restated literally:
-     * global levels (blelloch_scan.cpp:139-172, blelloch_scan_downsweep.comp:250-269) for
+     * global levels (vren/primitives/blelloch_scan.cpp:89-122, blelloch_scan_downsweep.comp:33-53) for
      * level = log2(n)-1 down to 10, clearing the last element on the first one, then the
-     * 1024-wide work-group pass (blelloch_scan.cpp:174-188, blelloch_scan_downsweep.comp:275-341)
+     * 1024-wide work-group pass (vren/primitives/blelloch_scan.cpp:124-138, blelloch_scan_downsweep.comp:56-125)
      * which reads elements at index < n - clear_last and pads with zeros. */
     uint32_t log2n = 0;
     while ((1u << log2n) < n) ++log2n;
@@ -264,8 +264,8 @@ void oracle_stable_sort_u32(uint32_t* keys, uint32_t* values, uint64_t n)
 void oracle_bucket_sort_u32x2(const uint32_t* in, uint32_t n, uint32_t key_bits, uint32_t* out_pairs,
                               uint32_t* out_ends)
 {
-    /* Group uvec2(key, value) by key & mask (bucket_sort_count.comp:237-241,
-     * bucket_sort_write.comp:271-276), stably.  out_ends = the counters region after the call:
+    /* Group uvec2(key, value) by key & mask (bucket_sort_count.comp:29-33,
+     * bucket_sort_write.comp:29-34), stably.  out_ends = the counters region after the call:
      * exclusive scan of the counts, then +1 per written element = inclusive scan. */
     uint32_t nb = 1u << key_bits, mask = nb - 1u;
     uint32_t* cnt = (uint32_t*)calloc(nb + 1, sizeof(uint32_t));
@@ -281,7 +281,7 @@ void oracle_bucket_sort_u32x2(const uint32_t* in, uint32_t n, uint32_t key_bits,
 }
 
 /* ================================================================================================
- * BVH — vren/resources/shaders/build_bvh.comp:225-249 per level (build_bvh.cpp:126-151), with the
+ * BVH — vren/resources/shaders/build_bvh.comp:32-55 per level (vren/primitives/build_bvh.cpp:69-98), with the
  * canonical decisions: a parent's AABB is the min/max over its valid children in IEEE total
  * order; all-invalid parents get (+inf, -inf) and next = INVALID; pad = 0.
  * ================================================================================================ */
@@ -381,7 +381,7 @@ static float glsl_min(float x, float y) { return y < x ? y : x; }
 static float glsl_max(float x, float y) { return x < y ? y : x; }
 
 /* Slice boundaries: REF bound[k] = near * a^k, a = 1 + 2 tan(half_fov) / tiles_y
- * (find_unique_clusters.comp:65, clustered_shading.glsl:220-222), a^k by repeated double
+ * (find_unique_clusters.comp:65, clustered_shading.glsl:99-101), a^k by repeated double
  * multiplication; FIXED32 bound[k] = near * r^k, r = (far/near)^(1/32), k <= 32, +inf beyond. */
 void oracle_cs_slice_table(const oracle_cs_view* v, uint32_t tiles_y, float* near_out, float* far_out)
 {
@@ -418,7 +418,7 @@ static uint32_t slice_of(float z, const float* bnear, uint32_t kmax)
     return k;
 }
 
-/* clustered_shading.glsl:128-164 */
+/* clustered_shading.glsl:7-43 */
 static uint32_t discretize_normal(const float n[3])
 {
     if (n[0] == 0.0f && n[1] == 0.0f && n[2] == 0.0f) return 0xFFFFFFFFu;
@@ -443,8 +443,8 @@ static uint32_t discretize_normal(const float n[3])
 /* ================================================================================================
  * construct_point_light_bvh — vren/vren/pipeline/clustered_shading.cpp:60-346:
  * view transform (point_light_position_to_view_space.comp:30), vec4 min/max (reduce trees),
- * Morton codes (discretize_point_light_positions.comp:62-73), bucket sort on code & 0xFFFF
- * (stable), leaves (init_light_array_bvh.comp:117-139), build_bvh.
+ * Morton codes (discretize_point_light_positions.comp:30-39), bucket sort on code & 0xFFFF
+ * (stable), leaves (init_light_array_bvh.comp:42-65), build_bvh.
  * ================================================================================================ */
 void oracle_cs_light_bvh(const float* positions, const float* lights, uint32_t L, const oracle_cs_view* v,
                          uint32_t morton_bits, float* view_pos, oracle_bvh_node* bvh, uint32_t* light_index)
@@ -594,7 +594,7 @@ uint32_t oracle_cs_find_unique_clusters(const float* depth, const float* normals
 
 /* ================================================================================================
  * assign_lights — vren/resources/shaders/clustered_shading/assign_lights.comp:121-240 (count and
- * write variants), cluster AABB of clustered_shading.glsl:193-231, node addressing of
+ * write variants), cluster AABB of clustered_shading.glsl:72-110, node addressing of
  * assign_lights.comp:108-119, tests of :84-102.  INVALID nodes never overlap (canonical).
  * ================================================================================================ */
 typedef struct { float mn[3], mx[3]; } caabb;

@@ -30,7 +30,7 @@ extern "C" {
 
 enum { ORACLE_ADD = 0, ORACLE_MIN = 1, ORACLE_MAX = 2 };
 
-/* ---- size helpers (vren/vren/base/base.hpp:281-328, vren/vren/primitives/build_bvh.cpp:158-193),
+/* ---- size helpers (vren/vren/base/base.hpp:32-79, vren/vren/primitives/build_bvh.cpp:101-136),
  *      restated with the reference's own double-precision log/pow formulas ---- */
 uint32_t oracle_round_to_next_power_of_2(uint32_t v);
 uint32_t oracle_round_to_next_power_of(uint32_t n, uint32_t base);
@@ -40,15 +40,15 @@ uint32_t oracle_calc_bvh_buffer_length(uint32_t leaf_count);
 uint32_t oracle_calc_bvh_root_index(uint32_t leaf_count);
 uint32_t oracle_calc_bvh_level_count(uint32_t leaf_count);
 
-/* ---- reduce (vren_test/vren_test/primitives/reduce.cpp:326-352 tree order, :395-450 fill;
- *      operand order of vren/resources/shaders/reduce.comp:266) ---- */
+/* ---- reduce (vren_test/vren_test/primitives/reduce.cpp:72-98 tree order, :141-196 fill;
+ *      operand order of vren/resources/shaders/reduce.comp:76) ---- */
 void oracle_reduce_tree_u32(int op, const uint32_t* in, uint32_t n, uint32_t* out /* P */);
 void oracle_reduce_tree_vec4(int op, const float* in, uint32_t n, float* out /* 4P */);
 uint32_t oracle_reduce_u32(int op, const uint32_t* in, uint64_t n);
 float oracle_reduce_f32(int op, const float* in, uint64_t n); /* min/max in IEEE total order */
 
-/* ---- scan (blelloch_scan.cpp test:70-73 std::exclusive_scan) and the reference's down-sweep
- *      dispatch sequence (vren/vren/primitives/blelloch_scan.cpp:107-189,
+/* ---- scan (vren_test/vren_test/primitives/blelloch_scan.cpp:70-73 std::exclusive_scan) and the
+ *      reference's down-sweep dispatch sequence (vren/vren/primitives/blelloch_scan.cpp:57-139,
  *      vren/resources/shaders/blelloch_scan_downsweep.comp:33-125) ---- */
 void oracle_exclusive_scan_u32(uint32_t* data, uint64_t n);
 void oracle_downsweep_u32(uint32_t* data, uint32_t n, int clear_last);

@@ -1,7 +1,7 @@
 // vren_oracle_shade.cpp — CPU oracle for clustered shading in FP64.  TEST INFRASTRUCTURE ONLY.
 //
 // Restates shade.comp:69-141 and pbr.glsl:6-112 (PI = 3.14, a = k = roughness) with the two falloffs
-// (reference: 1 - min(d/r, 1)^1.5, pbr.glsl:231; windowed inverse square: saturate(1-(d/r)^4)^2/(d^2+1),
+// (reference: 1 - min(d/r, 1)^1.5, pbr.glsl:89; windowed inverse square: saturate(1-(d/r)^4)^2/(d^2+1),
 // Karis 2013), evaluated in double.  The reference gradient with respect to each light's position,
 // colour and radius is obtained by forward-mode differentiation (dual numbers carrying 7 tangents),
 // which is independent of the hand-written reverse-mode adjoint of the CUDA kernel.  Branch

@@ -37,7 +37,7 @@ int main()
     cudaStream_t stream;
     cudaStreamCreate(&stream);
 
-    // radix_sort.cpp:245-309: reversed iota, 1024 keys
+    // vren_test/primitives/radix_sort.cpp:68-132: reversed iota, 1024 keys
     {
         vren::radix_sort rs;
         const uint32_t n = 1024;
@@ -60,7 +60,7 @@ int main()
         }
         EXPECT(threw);
     }
-    // blelloch_scan.cpp:166-176: all ones
+    // vren_test/primitives/blelloch_scan.cpp:166-176: all ones
     {
         vren::blelloch_scan scan;
         const uint32_t n = 1 << 19;
@@ -71,7 +71,7 @@ int main()
         auto out = download<uint32_t>(buf, n);
         for (uint32_t i = 0; i < n; ++i) EXPECT(out[i] == i);
     }
-    // reduce.cpp:538-545: all-ones add, whole tree in place
+    // vren_test/primitives/reduce.cpp:284-291: all-ones add, whole tree in place
     {
         vren::reduce<vren::uint_tag, vren::ReduceOperationAdd> red;
         const uint32_t n = 10000, P = vren::calc_reduce_output_buffer_length(n);
@@ -85,7 +85,7 @@ int main()
         EXPECT(out[P - 1] == n);
         EXPECT(out[1] == 2 && out[3] == 4 && out[1023] == 1024);
     }
-    // build_bvh.cpp:223-254 helpers and a build of 1000 leaves
+    // vren_test/primitives/build_bvh.cpp:223-254 helpers and a build of 1000 leaves
     {
         EXPECT(vren::calc_bvh_padded_leaf_count(2193819) == 33554432u);
         EXPECT(vren::calc_bvh_root_index(129) == 32u * 32u + 32u);
@@ -123,7 +123,7 @@ int main()
         EXPECT(p[0] == 0.5f && p[1] == 0.0f && d[0] == 1.0f);
         EXPECT(p[4] > 0.7499f && p[4] < 0.7501f && d[4] == -1.0f);
     }
-    // depth_buffer_pyramid.cpp:212-303: a 5x3 depth buffer -> levels 5x3, 2x1, 1x1
+    // depth_buffer_pyramid.cpp:213-305: a 5x3 depth buffer -> levels 5x3, 2x1, 1x1
     {
         std::vector<float> depth = {0.1f, 0.9f, 0.2f, 0.3f, 0.95f,  //
                                     0.4f, -1.f, 0.5f, 0.8f, 0.99f,  //

@@ -31,7 +31,7 @@ def check_pyramid(pyr, want):
 
 
 def test_level_layout_matches_reference_sizes(native):
-    """Level count and sizes (depth_buffer_pyramid.cpp:18, :48-54); offsets 64-float aligned, disjoint."""
+    """Level count and sizes (depth_buffer_pyramid.cpp:18, :28-38, Vulkan mip sizes max(1, size >> level)); offsets 64-float aligned, disjoint."""
     for w, h in [(1, 1), (7, 3), (1920, 1080), (3840, 2160), (65535, 1), (1, 65535), (40000, 30000)]:
         n = lib().vren_depth_pyramid_level_count(w, h)
         assert n == oracle.depth_pyramid_level_count(w, h)

@@ -105,7 +105,7 @@ def test_bucket_sort(key_bits):
 
 
 def make_leaves(leaf_count: int, rng) -> np.ndarray:
-    """The reference test's leaves (build_bvh.cpp:114-130): pos, ext uniform [0, 100)."""
+    """The reference test's leaves (vren_test/primitives/build_bvh.cpp:114-130): pos, ext uniform [0, 100)."""
     P = oracle.size_helpers(leaf_count)["padded"]
     L = oracle.size_helpers(P)["length"]
     nodes = np.zeros((L, 8), np.uint32)

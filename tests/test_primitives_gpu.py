@@ -135,7 +135,7 @@ def test_reduce_scalar_f32_total_order(cuda, op):
 # Scan
 # ------------------------------------------------------------------------------------------------
 def test_scan_all_ones_reference_lengths(cuda):
-    # blelloch_scan.cpp:166-176: lengths 2^0 .. 2^19, all ones
+    # vren_test/primitives/blelloch_scan.cpp:166-176: lengths 2^0 .. 2^19, all ones
     scan = vg.blelloch_scan()
     for e in range(0, 20):
         n = 1 << e
@@ -202,7 +202,7 @@ def test_downsweep_segments(cuda):
 # Radix sort
 # ------------------------------------------------------------------------------------------------
 def test_radix_sort_reversed_iota_1024(cuda):
-    # radix_sort.cpp:245-309
+    # vren_test/primitives/radix_sort.cpp:68-132
     n = 1024
     rs = vg.radix_sort()
     buf = dev_u32(np.arange(n, dtype=np.uint32)[::-1].copy(), cuda)
@@ -345,7 +345,7 @@ def test_build_bvh(cuda, leaf_count, queries):
     expect = oracle.build_bvh(nodes, P)
     # invalid nodes: only next must agree (their AABB is +inf/-inf on both sides anyway)
     assert np.array_equal(got, expect)
-    # the reference's own check: point queries vs a linear scan (build_bvh.cpp:174-210)
+    # the reference's own check: point queries vs a linear scan (vren_test/primitives/build_bvh.cpp:174-210)
     root = vg.calc_bvh_root_index(P)
     f = got.view(np.float32)
     for _ in range(queries):

@@ -104,7 +104,7 @@ class VrenError(RuntimeError):
 
 def check(status: int, what: str = "") -> None:
     """Maps a C-ABI status to the reference's exception types: argument errors raise
-    ValueError (std::invalid_argument in radix_sort.cpp:212-215), the rest VrenError."""
+    ValueError (std::invalid_argument in vren/primitives/radix_sort.cpp:158-161), the rest VrenError."""
     if status == VREN_OK:
         return
     if status == VREN_ERR_ARG:

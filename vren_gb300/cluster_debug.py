@@ -1,4 +1,4 @@
-"""Headless cluster debug views (vren_demo/vren_demo/clustered_shading_debug.cpp:6-200).
+"""Headless cluster debug views (vren_demo/vren_demo/clustered_shading_debug.cpp:6-202).
 
 The reference draws these as Vulkan overlays.  Here the GPU writes the same data into device memory
 (``show_clusters``: an RGBA float image; ``show_clusters_geometry``: the debug renderer's line

@@ -1,4 +1,4 @@
-// BuildBVH — vren::build_bvh (vren/vren/primitives/build_bvh.cpp:95-156, build_bvh.comp:32-55).
+// BuildBVH — vren::build_bvh (vren/vren/primitives/build_bvh.cpp:38-99, build_bvh.comp:32-55).
 //
 // The reference dispatches once per level; a 32-lane subgroup turns 32 children into one parent
 // with subgroupMin/Max over the valid lanes.  Here one launch builds two levels: a 1024-thread CTA
@@ -74,7 +74,7 @@ extern "C" uint32_t vren_calc_bvh_level_count(uint32_t leaf_count)
 
 extern "C" int vren_build_bvh(vren_stream_t s, vren_bvh_node* bvh, uint32_t padded_leaf_count)
 {
-    // build_bvh.cpp:102: leaf_count >= 32 and a power of 32.
+    // vren/primitives/build_bvh.cpp:45: leaf_count >= 32 and a power of 32.
     if (!bvh || padded_leaf_count < 32 || vren_calc_bvh_padded_leaf_count(padded_leaf_count) != padded_leaf_count)
         return VREN_ERR_ARG;
     if ((uintptr_t)bvh & 15u) return VREN_ERR_ARG;

@@ -1,5 +1,5 @@
 // C ABI support: status strings, device error word, wait limit and the integer size helpers of
-// vren/vren/base/base.hpp:281-328.
+// vren/vren/base/base.hpp:32-79.
 #include "common.cuh"
 
 #include <cmath>

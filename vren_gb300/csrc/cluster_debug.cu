@@ -1,12 +1,12 @@
-// Headless cluster debug views (vren_demo/vren_demo/clustered_shading_debug.cpp:6-200):
+// Headless cluster debug views (vren_demo/vren_demo/clustered_shading_debug.cpp:6-202):
 //
-//  - show_clusters (vren_demo/resources/shaders/show_clusters.comp:72-124): one RGBA float colour per
+//  - show_clusters (vren_demo/resources/shaders/show_clusters.comp:68-125): one RGBA float colour per
 //    pixel of the cluster-reference image, by mode: a hash of the cluster key, the cluster's (i, j, k),
 //    its normal bin, its light count, a hash of its light-list offset, a hash of the XOR of its light
 //    indices.  Every mode's colour is a function of the pixel's cluster alone, so the kernel pair is:
 //    one colour per cluster (a warp per cluster, the XOR of its list reduced across lanes), then one
 //    gather per pixel (4 B reference read, 16 B colour from L2, 16 B written).
-//  - show_clusters_geometry (show_clusters_geometry.comp:55-110, debug.glsl): per cluster, the 12 edges
+//  - show_clusters_geometry (show_clusters_geometry.comp:54-112, debug.glsl): per cluster, the 12 edges
 //    of its view-space box and an arrow along its normal bin, 32 vertices of (vec3 position, u32 colour),
 //    the reference's debug-renderer vertex layout.  The box is the one the light assignment tests.
 //
@@ -26,7 +26,7 @@ namespace {
 constexpr uint32_t kNoNormal = 0x3Fu;
 constexpr int kGeomVerticesPerCluster = 32;  // 12 box edges (24) + arrow (2 + 6)
 
-// triple32 (show_clusters.comp:50-60): the integer hash with the three multiply-xorshift rounds
+// triple32 (show_clusters.comp:51-61): the integer hash with the three multiply-xorshift rounds
 // published by C. Wellons ("hash prospector"), constants as in the shader.
 __host__ __device__ __forceinline__ uint32_t triple32(uint32_t x)
 {
@@ -45,7 +45,7 @@ __device__ __forceinline__ float hash01(uint32_t x) { return fdiv(__uint2float_r
 
 __device__ __forceinline__ float4 grey(float c) { return make_float4(c, c, c, 1.0f); }
 
-// Colour of cluster c for `mode` (show_clusters.comp:81-120).
+// Colour of cluster c for `mode` (show_clusters.comp:81-119).
 __global__ void __launch_bounds__(256) show_clusters_colour_kernel(int mode, uint32_t tiles_x, uint32_t tiles_y,
                                                                    const uint32_t* __restrict__ keys,
                                                                    const uint32_t* __restrict__ key_count,
@@ -122,7 +122,7 @@ __device__ __forceinline__ void put_line(uint4* __restrict__ v, uint32_t& o, con
     put_vertex(v, o, b[0], b[1], b[2], colour);
 }
 
-// show_clusters_geometry.comp:55-110 with debug.glsl's VREN_DEBUG_WRITE_AABB / _ARROW vertex order.
+// show_clusters_geometry.comp:54-112 with debug.glsl's VREN_DEBUG_WRITE_AABB / _ARROW vertex order.
 __global__ void __launch_bounds__(128) show_clusters_geometry_kernel(const vren_cs_frame* __restrict__ F,
                                                                      const uint32_t* __restrict__ keys,
                                                                      const uint32_t* __restrict__ key_count,

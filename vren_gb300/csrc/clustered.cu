@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(kLbvhThreads) lbvh_transform_kernel(
     if (tid == 0) scratch[0] = 0u;
 }
 
-// discretize_point_light_positions.comp:58-75
+// discretize_point_light_positions.comp:30-39
 __global__ void lbvh_morton_kernel(const float4* __restrict__ view_pos, uint32_t L, const uint32_t* __restrict__ scratch,
                                    uint32_t bits, uint2* __restrict__ pairs)
 {
@@ -1027,19 +1027,19 @@ void m4_store(const M4 m, float* dst)
 extern "C" void vren_cs_view_from_camera(const vren_camera* cam, uint32_t slicing, vren_cs_view* out)
 {
     std::memset(out, 0, sizeof(*out));
-    // camera.cpp:43-49: orientation = rotate(yaw, Y) * rotate(-pitch, X)
+    // camera.cpp:9-15: orientation = rotate(yaw, Y) * rotate(-pitch, X)
     M4 ry, rx, orient, inv_orient, inv_t, view, proj, inv_proj, inv_view;
     m4_rotate(cam->yaw, 0, 1, 0, ry);
     m4_rotate(-(double)cam->pitch, 1, 0, 0, rx);
     m4_mul(ry, rx, orient);
     m4_inverse(orient, inv_orient);
-    // camera.cpp:66-72: view = inverse(orientation) * translate(-position)
+    // camera.cpp:32-38: view = inverse(orientation) * translate(-position)
     m4_identity(inv_t);
     inv_t[3][0] = -(double)cam->position[0];
     inv_t[3][1] = -(double)cam->position[1];
     inv_t[3][2] = -(double)cam->position[2];
     m4_mul(inv_orient, inv_t, view);
-    // camera.cpp:74-84
+    // camera.cpp:40-50
     const double th = std::tan((double)cam->fov_y / 2.0);
     const double n = cam->near_plane, f = cam->far_plane;
     for (int c = 0; c < 4; ++c)

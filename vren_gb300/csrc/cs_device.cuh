@@ -26,7 +26,7 @@ __device__ __forceinline__ float mv_row(const float* m, int r, float x, float y,
 __device__ __forceinline__ float glsl_min(float x, float y) { return y < x ? y : x; }
 __device__ __forceinline__ float glsl_max(float x, float y) { return x < y ? y : x; }
 
-// clustered_shading.glsl:128-164.  The reference walks the three axes with t_i = sign(n_i) / n_i
+// clustered_shading.glsl:7-43.  The reference walks the three axes with t_i = sign(n_i) / n_i
 // (= |rcp_rn(n_i)|, NaN for a zero or NaN component) and keeps the first strictly smaller t below
 // 1e35; the cube face and the 3x3 cell on it follow from that axis and t.  Here with one correctly
 // rounded reciprocal instead of three: rcp_rn is monotone non-increasing in |n|, so the smallest t
@@ -103,7 +103,7 @@ struct Box {
     float mn[3], mx[3];
 };
 
-// clustered_shading.glsl:193-231 (cluster_min / cluster_max in view space).
+// clustered_shading.glsl:72-110 (cluster_min / cluster_max in view space).
 __device__ __forceinline__ Box cluster_box(uint32_t key, const vren_cs_frame* __restrict__ F)
 {
     const uint32_t ci = key & 0xFFu, cj = (key >> 8) & 0xFFu, ck = (key >> 16) & 0x3FFu;
@@ -175,7 +175,7 @@ __device__ __forceinline__ float4 light_to_view(const float* V, float4 p)
     return v;
 }
 
-// discretize_point_light_positions.comp:58-75: `bits` bits per axis, interleaved x, y, z from bit 0.
+// discretize_point_light_positions.comp:30-39: `bits` bits per axis, interleaved x, y, z from bit 0.
 __device__ __forceinline__ uint32_t morton_code(float4 v, const float mn[3], const float mx[3], uint32_t bits)
 {
     const float scale = (float)(1u << bits);
@@ -192,7 +192,7 @@ __device__ __forceinline__ uint32_t morton_code(float4 v, const float mn[3], con
     return code;
 }
 
-// init_light_array_bvh.comp:117-139 fused with the first one or two BuildBVH levels, for one block of
+// init_light_array_bvh.comp:42-65 fused with the first one or two BuildBVH levels, for one block of
 // `threads` = min(P, 1024) leaves starting at leaf chunk * threads (all threads of the CTA call it;
 // threads >= `threads` only return).  The leaf sphere is the light centre and the radius tested by
 // the traversal ((max.x - min.x) / 2 of the leaf box, assign_lights.comp:214), -1 for padding.

@@ -8,7 +8,7 @@
 // point index; word 1 = axis (3 = leaf); word 2 = the distance to the right child (inner node) or the
 // leaf count (first leaf of a run; the other leaves of the run hold 0x3FFFFFFF, ~0 cut to 30 bits).
 //
-// Build (kd_tree.cpp:5-77): a run of at most max_leaf points becomes leaves; otherwise the Welford mean
+// Build (vren/base/kd_tree.cpp:5-78): a run of at most max_leaf points becomes leaves; otherwise the Welford mean
 // and (unnormalised) variance of the points in their current order, axis = (var0 > var1 ? 0 : var1 > var2
 // ? 1 : 2) (the reference compares var0 with var1 twice), split = mean[axis], an in-place swap
 // partition of the indices by point[axis] < split, the left subtree at offset + 1, the right one
@@ -39,7 +39,7 @@ inline void kd_write_leaves(vren_kd_tree_node* tree, size_t offset, const uint32
     }
 }
 
-// Welford mean / variance over the run (kd_tree.cpp:33-45), the axis choice (:50) and the partition
+// Welford mean / variance over the run (vren/base/kd_tree.cpp:34-47), the axis choice (:52) and the partition
 // (:53-66).  Returns the split point `middle`.
 size_t kd_split(const float* points, size_t stride, uint32_t* indices, size_t count, uint32_t& axis, float& split)
 {
@@ -73,7 +73,7 @@ struct KdPending {
     size_t parent;        // node whose right-child distance is set when the subtree starts
 };
 
-// kd_tree.cpp:88-131 on the host: near child first, the far one when best > d * d.
+// vren/base/kd_tree.cpp:88-129 on the host: near child first, the far one when best > d * d.
 void kd_search_host(const float* points, size_t stride, const vren_kd_tree_node* tree, size_t offset,
                     const float* s, vren_kd_tree_filter filter, void* user, uint32_t& best_point, float& best)
 {

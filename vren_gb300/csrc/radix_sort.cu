@@ -1,11 +1,11 @@
 // Onesweep LSD radix sort and stable bucket sort.
 //
-// Reference: vren::radix_sort (vren/vren/primitives/radix_sort.cpp:203-392) sorts uint32 keys with
+// Reference: vren::radix_sort (vren/vren/primitives/radix_sort.cpp:149-338) sorts uint32 keys with
 // eight 4-bit passes, each made of a buffer fill, a per-work-group 16-bin count
 // (radix_sort_local_count.comp), an up-sweep reduce of the counts, a 16-lane scan
 // (radix_sort_global_offset.comp), a down-sweep and a reorder that issues 16 ballots per key and
-// scatters uncoalesced (radix_sort_reorder.comp:183-241): ~48 commands per sort.
-// vren::bucket_sort (bucket_sort.cpp:119-208) counts with global atomics, scans 65536 counters and
+// scatters uncoalesced (radix_sort_reorder.comp:55-113): ~48 commands per sort.
+// vren::bucket_sort (vren/primitives/bucket_sort.cpp:102-160) counts with global atomics, scans 65536 counters and
 // scatters with atomics, so its order inside a bucket is unspecified.
 //
 // Here: one histogram kernel reads the keys once and builds the digit histograms of every pass;
@@ -576,7 +576,7 @@ extern "C" int vren_radix_sort_u32_ex(vren_stream_t s, uint32_t* keys, uint32_t*
 
 extern "C" int vren_radix_sort_u32(vren_stream_t s, uint32_t* keys, uint32_t n, void* scratch1, uint32_t* scratch2)
 {
-    // radix_sort.cpp:212-215: "Length must be higher than 1024 and a power of 2"
+    // vren/primitives/radix_sort.cpp:158-161: "Length must be higher than 1024 and a power of 2"
     if (!(n >= 1024 && (n & (n - 1)) == 0)) return VREN_ERR_ARG;
     return vren_radix_sort_u32_ex(s, keys, nullptr, n, 8, scratch1, scratch2, nullptr);
 }

@@ -1,6 +1,6 @@
 // Reduce — drop-in tree form and scalar form.
 //
-// Drop-in semantics (vren::reduce<T,Op>, vren/vren/primitives/reduce.cpp:82-178 and
+// Drop-in semantics (vren::reduce<T,Op>, vren/vren/primitives/reduce.cpp:32-128 and
 // vren/resources/shaders/reduce.comp:50-86): the output holds the Blelloch up-sweep tree
 // of the input padded with the operation's identity to P = next power of two.  The
 // reference walks the levels ten at a time with one dispatch each, reading strided
@@ -8,7 +8,7 @@
 // levels: two in registers (4 consecutive items per thread), five by warp shuffles and
 // the rest through shared memory, with vectorised loads/stores on the first pass.  The
 // combine order at every node is op(right, left), the reference's
-// VREN_OPERATION(s_data[b], s_data[a]) (reduce.comp:266), so float sums follow the same
+// VREN_OPERATION(s_data[b], s_data[a]) (reduce.comp:76), so float sums follow the same
 // pairwise tree and are bit-identical.
 //
 // Scalar form: a single pass, block partials in scratch and a last-block-done combine (no

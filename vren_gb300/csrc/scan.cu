@@ -1,5 +1,5 @@
-// Exclusive scan (vren::blelloch_scan, vren/vren/primitives/blelloch_scan.cpp:191-216) and the
-// reference's public down-sweep (blelloch_scan.cpp:107-189, blelloch_scan_downsweep.comp:33-125).
+// Exclusive scan (vren::blelloch_scan, vren/vren/primitives/blelloch_scan.cpp:141-166) and the
+// reference's public down-sweep (vren/primitives/blelloch_scan.cpp:57-139, blelloch_scan_downsweep.comp:33-125).
 //
 // The reference runs an up-sweep (reduce) and then log2(n)-10 global down-sweep dispatches plus
 // one shared-memory dispatch, all with strided access.  Here the scan is one kernel and one pass

@@ -243,7 +243,7 @@ __device__ __forceinline__ float ggx_den(const Px& q, const float* hv, float nhu
     return (q.a2 * nhu * nhu + fmaf(hl2, q.omn2, dot3(c, c))) * (rhl * rhl);
 }
 
-// pbr_apply_light (pbr.glsl:184-215) for light direction L (from the light towards the point) and
+// pbr_apply_light (pbr.glsl:42-73) for light direction L (from the light towards the point) and
 // radiance; accumulates into out.
 __device__ __forceinline__ void brdf_accumulate(const Px& q, const float L[3], const float rad[3], float out[3])
 {
@@ -268,7 +268,7 @@ __device__ __forceinline__ void brdf_accumulate(const Px& q, const float L[3], c
     }
 }
 
-// Attenuation: reference 1 - min(d/r, 1)^1.5 (pbr.glsl:231) or windowed inverse square.
+// Attenuation: reference 1 - min(d/r, 1)^1.5 (pbr.glsl:89) or windowed inverse square.
 __device__ __forceinline__ float falloff_value(int mode, float dist, float dd, float rr)
 {
     const float t = dist * rr;
@@ -281,7 +281,7 @@ __device__ __forceinline__ float falloff_value(int mode, float dist, float dd, f
     return w * w * rcp_a(dd + 1.0f);
 }
 
-// pbr_apply_point_light (pbr.glsl:218-232) for one light.
+// pbr_apply_point_light (pbr.glsl:75-93) for one light.
 __device__ __forceinline__ void point_light_fwd(const Px& q, float4 lp, float4 lc, int falloff, float out[3])
 {
     float d[3];

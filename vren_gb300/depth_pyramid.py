@@ -44,7 +44,7 @@ class depth_buffer_pyramid:
 
 
 class depth_buffer_reductor:
-    """vren::depth_buffer_reductor (depth_buffer_pyramid.cpp:172-303): copy_and_reduce writes level 0
+    """vren::depth_buffer_reductor (depth_buffer_pyramid.cpp:174-305): copy_and_reduce writes level 0
     (the depth buffer, copied exactly) and every level above it in one launch on `stream`."""
 
     k_workgroup_size_x = 32
