@@ -61,6 +61,14 @@ int vren_device_error(int clear);
  * previous value. */
 uint32_t vren_set_wait_limit(uint32_t rounds);
 
+/* Test hook (no counterpart in the reference): on the current device, the exclusive scans stop
+ * publishing the look-back status of tile `tile_plus_one - 1` (every tile of every scan call with
+ * that index), so the look-back waits of the tiles after it run out after the wait limit and record
+ * VREN_ERR_TIMEOUT; the call still returns and the kernels end.  0 restores normal operation.  Call
+ * it with no scan in flight (it copies to device memory synchronously).  After a timeout the scan's
+ * scratch must be zero-filled again before its next use. */
+int vren_test_withhold_scan_status(uint32_t tile_plus_one);
+
 /* Kernel variant knobs, read when work is enqueued (no counterpart in the reference; the autotuner
  * and benchmarks set them).  Every variant gives identical results.
  *   VREN_TUNE_SCAN_SLICES  128-element slices per warp in a scan tile: 4 (4096/tile) or 8 (8192/tile)

@@ -49,6 +49,8 @@ _PROTOS = {
     "oracle_cs_shade_f64": (None, [vp, u32, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, u32, i32, i32, vp, vp, i32]),
     "oracle_cs_shade_grad_f64": (None, [vp, u32, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, u32, i32, vp, vp, i32]),
     "oracle_cs_shade_light_loss_f64": (C.c_double, [vp, u32, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, u32, vp, i32, vp]),
+    "oracle_cs_shade_grad_lights_f64": (None, [vp, u32, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, u32, i32, vp,
+                                               vp, u32, C.c_double, vp, vp, vp, i32]),
 }
 
 OPS = {"add": 0, "min": 1, "max": 2}
@@ -374,3 +376,19 @@ def cs_shade_light_loss_f64(view, W, H, gb, lists, l, theta, grad, falloff=1):
     th = np.ascontiguousarray(theta, np.float64)
     return float(lib().oracle_cs_shade_light_loss_f64(_view_ptr(view), W, H, *(_p(x) for x in g),
                                                       *(_p(x) for x in ls), l, _p(th), falloff, _p(_f32(grad))))
+
+
+def cs_shade_grad_lights_f64(view, W, H, gb, lists, lpos, lights, L, grad, sel, h=1e-4, falloff=1, threads=0):
+    """FP64 gradient and central differences (step h) for the lights in `sel` only, over their own
+    (pixel, light) pairs: returns (g7, fd7, pairs) with g7 and fd7 of shape (len(sel), 7)."""
+    sel = _u32(sel)
+    n = len(sel)
+    g7 = np.zeros(n * 7, np.float64)
+    fd7 = np.zeros(n * 7, np.float64)
+    pairs = np.zeros(n, np.uint64)
+    g = [_f32(x) for x in gb]
+    ls = [_u32(x) for x in lists]
+    lib().oracle_cs_shade_grad_lights_f64(_view_ptr(view), W, H, *(_p(x) for x in g), *(_p(x) for x in ls),
+                                          _p(_f32(lpos)), _p(_f32(lights)), L, falloff, _p(_f32(grad)), _p(sel), n,
+                                          float(h), _p(g7), _p(fd7), _p(pairs), threads or 8)
+    return g7.reshape(n, 7), fd7.reshape(n, 7), pairs

@@ -174,6 +174,13 @@ double oracle_cs_shade_light_loss_f64(const oracle_cs_view* v, uint32_t W, uint3
                                       const uint32_t* refs, const uint32_t* counts, const uint32_t* offsets,
                                       const uint32_t* indices, uint32_t l, const double* theta, int falloff,
                                       const float* grad);
+void oracle_cs_shade_grad_lights_f64(const oracle_cs_view* v, uint32_t W, uint32_t H, const float* depth,
+                                     const float* normals, const float* albedo, const float* rough,
+                                     const float* metal, const uint32_t* refs, const uint32_t* counts,
+                                     const uint32_t* offsets, const uint32_t* indices, const float* lpos,
+                                     const float* lights, uint32_t L, int falloff, const float* grad,
+                                     const uint32_t* sel, uint32_t nsel, double h, double* g7, double* fd7,
+                                     uint64_t* pair_counts, int threads);
 
 #ifdef __cplusplus
 }

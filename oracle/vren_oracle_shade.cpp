@@ -84,62 +84,73 @@ inline Dual dsqrt(const Dual& a)
 inline Dual max0(const Dual& a) { return a.v > 0.0 ? a : cst(0.0); }
 inline Dual min1(const Dual& a) { return a.v < 1.0 ? a : cst(1.0); }
 inline Dual clamp01(const Dual& a) { return a.v <= 0.0 ? cst(0.0) : (a.v >= 1.0 ? cst(1.0) : a); }
+// the same operations on plain doubles (values only: the finite differences)
+inline double dsqrt(double a) { return std::sqrt(a); }
+inline double max0(double a) { return a > 0.0 ? a : 0.0; }
+inline double min1(double a) { return a < 1.0 ? a : 1.0; }
+inline double clamp01(double a) { return a <= 0.0 ? 0.0 : (a >= 1.0 ? 1.0 : a); }
+template <class T> inline T num(double v);
+template <> inline Dual num<Dual>(double v) { return cst(v); }
+template <> inline double num<double>(double v) { return v; }
 
-struct V3 {
-    Dual x, y, z;
+template <class T> struct V3T {
+    T x, y, z;
 };
+using V3 = V3T<Dual>;
 inline V3 v3(const Dual& x, const Dual& y, const Dual& z) { return {x, y, z}; }
-inline V3 v3c(double x, double y, double z) { return {cst(x), cst(y), cst(z)}; }
-inline Dual dot(const V3& a, const V3& b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-inline V3 sub(const V3& a, const V3& b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
-inline V3 scale(const V3& a, const Dual& s) { return {a.x * s, a.y * s, a.z * s}; }
-inline V3 divs(const V3& a, const Dual& s) { return {a.x / s, a.y / s, a.z / s}; }
+template <class T> inline V3T<T> v3n(double x, double y, double z) { return {num<T>(x), num<T>(y), num<T>(z)}; }
+inline V3 v3c(double x, double y, double z) { return v3n<Dual>(x, y, z); }
+template <class T> inline T dot(const V3T<T>& a, const V3T<T>& b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+template <class T> inline V3T<T> sub(const V3T<T>& a, const V3T<T>& b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+template <class T> inline V3T<T> divs(const V3T<T>& a, const T& s) { return {a.x / s, a.y / s, a.z / s}; }
 
 struct Pixel {
     double p[3], N[3], V[3], alb[3], rough, metal;
 };
 
-// pbr_apply_point_light for one (pixel, light) pair, returns the three channels.
-void point_light(const Pixel& q, const V3& lp, const V3& col, const Dual& r, int falloff, Dual out[3])
+// pbr_apply_point_light for one (pixel, light) pair, returns the three channels; T = Dual carries the
+// 7 tangents, T = double evaluates the value only.
+template <class T>
+void point_light(const Pixel& q, const V3T<T>& lp, const V3T<T>& col, const T& r, int falloff, T out[3])
 {
-    const V3 p = v3c(q.p[0], q.p[1], q.p[2]);
-    const V3 N = v3c(q.N[0], q.N[1], q.N[2]);
-    const V3 V = v3c(q.V[0], q.V[1], q.V[2]);
-    const V3 d = sub(p, lp);
-    const Dual dist = dsqrt(dot(d, d));
-    const V3 L = divs(d, dist);
-    Dual att;
+    const V3T<T> p = v3n<T>(q.p[0], q.p[1], q.p[2]);
+    const V3T<T> N = v3n<T>(q.N[0], q.N[1], q.N[2]);
+    const V3T<T> V = v3n<T>(q.V[0], q.V[1], q.V[2]);
+    const V3T<T> d = sub(p, lp);
+    const T dist = dsqrt(dot(d, d));
+    const V3T<T> L = divs(d, dist);
+    T att;
     if (falloff == 0) {
-        const Dual u = min1(dist / r);
+        const T u = min1(dist / r);
         att = 1.0 - u * dsqrt(u);
     } else {
-        const Dual t = dist / r;
-        const Dual t2 = t * t;
-        const Dual w = clamp01(1.0 - t2 * t2);
-        att = (w * w) / (dist * dist + cst(1.0));
+        const T t = dist / r;
+        const T t2 = t * t;
+        const T w = clamp01(1.0 - t2 * t2);
+        att = (w * w) / (dist * dist + num<T>(1.0));
     }
-    const V3 hv = sub(V, L);
-    const V3 H = divs(hv, dsqrt(dot(hv, hv)));
+    const V3T<T> hv = sub(V, L);
+    const V3T<T> H = divs(hv, dsqrt(dot(hv, hv)));
     const double a2 = q.rough * q.rough;
-    const Dual NdotH = max0(dot(N, H));
-    const Dual D = NdotH * NdotH * cst(a2 - 1.0) + cst(1.0);
-    const Dual NDF = cst(a2) / (kPi * D * D);
+    const T NdotH = max0(dot(N, H));
+    const T D = NdotH * NdotH * num<T>(a2 - 1.0) + num<T>(1.0);
+    const T NDF = num<T>(a2) / (kPi * D * D);
     const double k = q.rough;
     const double NdotV = std::max(q.N[0] * q.V[0] + q.N[1] * q.V[1] + q.N[2] * q.V[2], 0.0);
-    const Dual NdotL = max0(-dot(N, L));
+    const T NdotL = max0(-dot(N, L));
     const double ggxV = NdotV / (NdotV * (1.0 - k) + k);
-    const Dual ggxL = NdotL / (NdotL * cst(1.0 - k) + cst(k));
-    const Dual G = cst(ggxV) * ggxL;
-    const Dual HdotV = max0(dot(H, V));
-    const Dual x = 1.0 - HdotV;
-    const Dual f5 = x * x * x * x * x;
-    const Dual spec = NDF * G / (cst(4.0 * NdotV) * NdotL + cst(0.0001));
-    const Dual c3[3] = {col.x, col.y, col.z};
+    const T ggxL = NdotL / (NdotL * num<T>(1.0 - k) + num<T>(k));
+    const T G = num<T>(ggxV) * ggxL;
+    const T HdotV = max0(dot(H, V));
+    const T x = 1.0 - HdotV;
+    const T f5 = x * x * x * x * x;
+    const T spec = NDF * G / (num<T>(4.0 * NdotV) * NdotL + num<T>(0.0001));
+    const T c3[3] = {col.x, col.y, col.z};
     for (int c = 0; c < 3; ++c) {
         const double F0 = 0.04 * (1.0 - q.metal) + q.alb[c] * q.metal;
-        const Dual F = cst(F0) + cst(1.0 - F0) * f5;
-        const Dual kD = (1.0 - F) * cst(1.0 - q.metal);
-        out[c] = max0((kD * cst(q.alb[c] / kPi) + F * spec) * c3[c] * att * NdotL);
+        const T F = num<T>(F0) + num<T>(1.0 - F0) * f5;
+        const T kD = (1.0 - F) * num<T>(1.0 - q.metal);
+        out[c] = max0((kD * num<T>(q.alb[c] / kPi) + F * spec) * c3[c] * att * NdotL);
     }
 }
 
@@ -291,4 +302,81 @@ extern "C" double oracle_cs_shade_light_loss_f64(const oracle_cs_view* v, uint32
         }
     }
     return loss;
+}
+
+// The FP64 gradient (forward mode) and the central finite differences with step h of the loss with
+// respect to the 7 parameters of each light in `sel` only, evaluating only the (pixel, light) pairs of
+// those lights: g7[7 * i + t] and fd7[7 * i + t] for light sel[i].  The pairs are gathered once (one
+// pass over the pixels' lists); each light's 1 + 14 evaluations then run over its own pairs.
+extern "C" void oracle_cs_shade_grad_lights_f64(const oracle_cs_view* v, uint32_t W, uint32_t H, const float* depth,
+                                                const float* normals, const float* albedo, const float* rough,
+                                                const float* metal, const uint32_t* refs, const uint32_t* counts,
+                                                const uint32_t* offsets, const uint32_t* indices, const float* lpos,
+                                                const float* lights, uint32_t L, int falloff, const float* grad,
+                                                const uint32_t* sel, uint32_t nsel, double h, double* g7, double* fd7,
+                                                uint64_t* pair_counts, int threads)
+{
+    const int nt = threads > 0 ? threads : 1;
+    std::vector<int32_t> slot(L, -1);
+    for (uint32_t i = 0; i < nsel; ++i)
+        if (sel[i] < L) slot[sel[i]] = (int32_t)i;
+    // pairs per selected light, gathered per thread then merged in row order
+    std::vector<std::vector<std::vector<uint32_t>>> part(nt, std::vector<std::vector<uint32_t>>(nsel));
+#pragma omp parallel num_threads(nt)
+    {
+#ifdef _OPENMP
+        const int tid = omp_get_thread_num();
+#else
+        const int tid = 0;
+#endif
+#pragma omp for schedule(static)
+        for (int64_t y = 0; y < (int64_t)H; ++y)
+            for (uint32_t x = 0; x < W; ++x) {
+                const size_t px = (size_t)y * W + x;
+                const uint32_t c = refs[px];
+                for (uint32_t i = 0; i < counts[c]; ++i) {
+                    const uint32_t l = indices[offsets[c] + i];
+                    if (l < L && slot[l] >= 0) part[tid][slot[l]].push_back((uint32_t)px);
+                }
+            }
+    }
+    std::vector<std::vector<uint32_t>> pairs(nsel);
+    for (uint32_t i = 0; i < nsel; ++i)
+        for (int t = 0; t < nt; ++t) pairs[i].insert(pairs[i].end(), part[t][i].begin(), part[t][i].end());
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nt)
+    for (int64_t i = 0; i < (int64_t)nsel; ++i) {
+        const uint32_t l = sel[i];
+        double g[NT] = {0, 0, 0, 0, 0, 0, 0};
+        double fp[NT] = {0, 0, 0, 0, 0, 0, 0}, fm[NT] = {0, 0, 0, 0, 0, 0, 0};
+        const double base[NT] = {lpos[4 * l], lpos[4 * l + 1], lpos[4 * l + 2], lights[4 * l], lights[4 * l + 1],
+                                 lights[4 * l + 2], lights[4 * l + 3]};
+        pair_counts[i] = pairs[i].size();
+        for (uint32_t px : pairs[i]) {
+            Pixel q;
+            const uint32_t x = px % W, y = px / W;
+            if (!load_pixel(v, W, H, x, y, depth, normals, albedo, rough, metal, q)) continue;
+            LightParams P = seed_light(lpos, lights, l, true);
+            Dual o[3];
+            point_light(q, P.lp, P.col, P.r, falloff, o);
+            for (int k = 0; k < 3; ++k)
+                for (int t = 0; t < NT; ++t) g[t] += (double)grad[3 * px + k] * o[k].d[t];
+            for (int t = 0; t < NT; ++t) {
+                for (int sgn = 0; sgn < 2; ++sgn) {
+                    double th[NT];
+                    for (int u = 0; u < NT; ++u) th[u] = base[u];
+                    th[t] += sgn ? -h : h;
+                    double e[3];
+                    point_light<double>(q, v3n<double>(th[0], th[1], th[2]), v3n<double>(th[3], th[4], th[5]), th[6],
+                                        falloff, e);
+                    double s = 0.0;
+                    for (int k = 0; k < 3; ++k) s += (double)grad[3 * px + k] * e[k];
+                    (sgn ? fm : fp)[t] += s;
+                }
+            }
+        }
+        for (int t = 0; t < NT; ++t) {
+            g7[7 * i + t] = g[t];
+            fd7[7 * i + t] = (fp[t] - fm[t]) / (2.0 * h);
+        }
+    }
 }

@@ -332,9 +332,12 @@ def test_assign_lights_fused_and_three_kernel_forms(cuda, fused, L, seed):
         lib.vren_tuning_set(knob, 0)
 
 
-@pytest.mark.parametrize("W,H,L", [(1920, 1080, 16384), (1280, 720, 65536), (640, 360, 1024)])
-def test_assign_lights_baseline_scene(cuda, W, H, L):
-    view = make_view(W, H)
+@pytest.mark.parametrize("W,H,L,slicing", [(1920, 1080, 16384, "ref"), (1920, 1080, 16384, "fixed32"),
+                                           (1280, 720, 65536, "ref"), (640, 360, 1024, "ref")])
+def test_assign_lights_baseline_scene(cuda, W, H, L, slicing):
+    """The benchmark scenes (seeded planes, lights uniform in the frustum box), including the 1080p /
+    16,384-light frame with 32 exponential depth slices (FIXED32) as well as the reference's slicing."""
+    view = make_view(W, H, slicing)
     depth, normals = scene.depth_planes(W + L, W, H)
     pos, li = scene.lights(L, L, W, H)
     keys, kc, vp, bvh, lidx, counts, offsets, indices, total = run_assign(cuda, W, H, view, depth, normals, pos, li, L)
@@ -384,6 +387,24 @@ def check_context_outputs(ctx, W, H, view, depth, normals, pos, li, L):
     assert np.array_equal(cs.read_device(o.counts, U), ec)
     assert np.array_equal(cs.read_device(o.offsets, U), eo)
     assert np.array_equal(cs.read_device(o.indices, et), ei)
+
+
+@pytest.mark.parametrize("slicing", ["ref", "fixed32"])
+def test_cluster_and_shade_context_1080p(cuda, slicing):
+    """The benchmark frame through the context (graph replay): 1920x1080, 16,384 lights, both slicings."""
+    W, H, L = 1920, 1080, 16384
+    view = make_view(W, H, slicing)
+    depth, normals = scene.depth_planes(W + L, W, H)
+    pos, li = scene.lights(L, L, W, H)
+    ctx = cs.cluster_and_shade(W, H, L, 1 << 22)
+    stream = torch.cuda.Stream()
+    bufs = [to_dev(x, cuda) for x in (depth, normals, pos, li)]
+    torch.cuda.synchronize()
+    for _ in range(2):
+        with torch.cuda.stream(stream):
+            ctx.cluster(stream, view, W, H, *bufs, L)
+        stream.synchronize()
+        check_context_outputs(ctx, W, H, view, depth, normals, pos, li, L)
 
 
 @pytest.mark.parametrize("use_graph", [False, True])

@@ -37,6 +37,16 @@ constexpr int kScanItems = 16;
 constexpr uint32_t kScanTile = kScanThreads * kScanItems;  // 4096
 constexpr uint32_t kScanHeaderWords = 4;
 
+// Test hook (vren_test_withhold_scan_status): tile + 1 of the one tile whose look-back status the
+// scan never publishes, so that its successors' bounded waits run out and record VREN_ERR_TIMEOUT;
+// 0 (the default) publishes every tile.  Only lane 0 of the publishing warp reads it, once per tile.
+__device__ uint32_t g_scan_withheld_tile = 0;
+
+__device__ __forceinline__ void publish_status(uint64_t* status, uint32_t tile, uint64_t word)
+{
+    if (tile + 1u != *reinterpret_cast<volatile uint32_t*>(&g_scan_withheld_tile)) st_relaxed_u64(status + tile, word);
+}
+
 // Takes this CTA's tile and the call's epoch (thread 0 only); the taker of the last ticket opens the
 // next call's epoch.
 __device__ __forceinline__ uint32_t take_tile(uint32_t* scratch, uint32_t total_tiles, uint32_t& epoch)
@@ -148,16 +158,15 @@ __global__ void __launch_bounds__(kScanThreads, 4) exclusive_scan_kernel(
     }
 
     if (warp == 0) {
-        uint64_t* my_status = status + tile;
         uint32_t prefix = 0;
         if (tile_in_seg == 0) {
-            if (lane == 0) st_relaxed_u64(my_status, make_status(epoch, 2u, tile_sum));
+            if (lane == 0) publish_status(status, tile, make_status(epoch, 2u, tile_sum));
         } else {
-            if (lane == 0) st_relaxed_u64(my_status, make_status(epoch, 1u, tile_sum));
+            if (lane == 0) publish_status(status, tile, make_status(epoch, 1u, tile_sum));
             bool timed_out = false;
             prefix = warp_lookback(status, tile, tile - tile_in_seg, epoch, lane, wait_limit, spin, timed_out);
             if (__any_sync(0xFFFFFFFFu, timed_out) && lane == 0) VREN_RECORD_ERROR(VREN_ERR_TIMEOUT);
-            if (lane == 0) st_relaxed_u64(my_status, make_status(epoch, 2u, prefix + tile_sum));
+            if (lane == 0) publish_status(status, tile, make_status(epoch, 2u, prefix + tile_sum));
         }
         if (lane == 0) {
             s_prefix = prefix;
@@ -273,16 +282,15 @@ __global__ void __launch_bounds__(kScanThreads, 6) exclusive_scan_staged_kernel(
         tile_sum += x;
     }
     if (warp == 0) {
-        uint64_t* my_status = status + tile;
         uint32_t prefix = 0;
         if (tile_in_seg == 0) {
-            if (lane == 0) st_relaxed_u64(my_status, make_status(epoch, 2u, tile_sum));
+            if (lane == 0) publish_status(status, tile, make_status(epoch, 2u, tile_sum));
         } else {
-            if (lane == 0) st_relaxed_u64(my_status, make_status(epoch, 1u, tile_sum));
+            if (lane == 0) publish_status(status, tile, make_status(epoch, 1u, tile_sum));
             bool lb_timeout = false;
             prefix = warp_lookback(status, tile, tile - tile_in_seg, epoch, lane, wait_limit, spin, lb_timeout);
             if (lb_timeout) timed_out = true;
-            if (lane == 0) st_relaxed_u64(my_status, make_status(epoch, 2u, prefix + tile_sum));
+            if (lane == 0) publish_status(status, tile, make_status(epoch, 2u, prefix + tile_sum));
         }
         if (lane == 0) s_prefix = prefix;
     }
@@ -439,7 +447,7 @@ __global__ void __launch_bounds__(kPersistThreads) exclusive_scan_persistent_ker
                 for (int d = 16; d > 0; d >>= 1) sum += __shfl_xor_sync(0xFFFFFFFFu, sum, d);
                 if (lane == 0) {
                     s_agg[s] = sum;
-                    st_relaxed_u64(status + t, make_status(epoch, ts == 0 ? 2u : 1u, sum));
+                    publish_status(status, t, make_status(epoch, ts == 0 ? 2u : 1u, sum));
                 }
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&s_ready[s]);  // releases the stage's data, ticket and sum
@@ -517,7 +525,7 @@ __global__ void __launch_bounds__(kPersistThreads) exclusive_scan_persistent_ker
                     prefix = warp_lookback(status, tile, tile - tile_in_seg, epoch, lane, wait_limit, spin,
                                            lb_timeout);
                     if (lb_timeout) timed_out = true;
-                    if (lane == 0) st_relaxed_u64(status + tile, make_status(epoch, 2u, prefix + tile_sum));
+                    if (lane == 0) publish_status(status, tile, make_status(epoch, 2u, prefix + tile_sum));
                 }
                 if (lane == 0) s_prefix = prefix;
             }
@@ -702,6 +710,13 @@ extern "C" size_t vren_exclusive_scan_scratch_bytes(uint32_t n, uint32_t blocks)
     return (size_t)(kScanHeaderWords * sizeof(uint32_t) + tiles * sizeof(uint64_t));
 }
 
+extern "C" int vren_test_withhold_scan_status(uint32_t tile_plus_one)
+{
+    return cudaMemcpyToSymbol(g_scan_withheld_tile, &tile_plus_one, sizeof(tile_plus_one)) == cudaSuccess
+               ? VREN_OK
+               : VREN_ERR_CUDA;
+}
+
 extern "C" int vren_exclusive_scan_u32(vren_stream_t s, uint32_t* data, uint32_t n, uint32_t blocks, void* scratch)
 {
     if (blocks == 0 || !scratch || (n > 0 && !data)) return VREN_ERR_ARG;
@@ -745,10 +760,14 @@ extern "C" int vren_scan_downsweep_u32(vren_stream_t s, uint32_t* data, uint32_t
 // All calls share the array and it keeps the last call's contents, so each call first clears the
 // part it uses (tickets, epoch, one status word per tile) with cudaMemsetAsync on the caller's
 // stream.  Two calls that overlap on the GPU (other streams, other host threads) race on the array
-// and must be serialised by the caller.  The first call on a device looks the array's device
-// address up (cudaGetSymbolAddress, with that device current) and caches it; make that first call
-// before capturing a stream into a CUDA graph.
+// and must be serialised by the caller.  The first call on a device (and in each CUDA context on it)
+// looks the array's device address up (cudaGetSymbolAddress, with that device current) and caches
+// it under the (device, current context) pair: a context created after a cudaDeviceReset, or a
+// driver context other than the primary one, loads the library image again and gets its own copy
+// of the array, which is looked up afresh.  Make the first call in a context before capturing a
+// stream into a CUDA graph.
 // ================================================================================================
+#include <cuda.h>  // CUcontext and the cuCtxGetCurrent prototype (resolved at run time below)
 #include <mutex>
 
 namespace vren_gb300 {
@@ -758,22 +777,61 @@ constexpr uint32_t kNoAllocWords = kScanHeaderWords + 2u * kNoAllocMaxTiles;
 
 static __device__ __align__(256) uint32_t g_noalloc_scan_scratch[kNoAllocWords];
 
-constexpr int kNoAllocMaxDevices = 64;
+struct NoAllocEntry {
+    int dev;
+    CUcontext ctx;
+    void* ptr;
+};
+constexpr int kNoAllocMaxEntries = 64;
 static std::mutex g_noalloc_mutex;
-static void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+static NoAllocEntry g_noalloc_cache[kNoAllocMaxEntries];
+static int g_noalloc_entries = 0;
 
-// Device address of g_noalloc_scan_scratch on the current device (looked up once per device).
+// The calling thread's current driver context (the runtime's primary context after cudaGetDevice has
+// made one current); cuCtxGetCurrent is taken from the driver through the runtime, so the library
+// does not link libcuda itself.
+static int current_context(CUcontext* ctx)
+{
+    using GetCurrent = CUresult (*)(CUcontext*);
+    static GetCurrent fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<GetCurrent>(p);
+    }();
+    *ctx = nullptr;
+    if (!fn) return VREN_ERR_CUDA;
+    return fn(ctx) == CUDA_SUCCESS ? VREN_OK : VREN_ERR_CUDA;  // null when no context is current yet
+}
+
+// Device address of g_noalloc_scan_scratch in the current device's current context (looked up once
+// per device and context).
 static int noalloc_scratch(uint32_t** out)
 {
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) return VREN_ERR_CUDA;
+    if (cudaGetDevice(&dev) != cudaSuccess) return VREN_ERR_CUDA;
+    CUcontext ctx = nullptr;
+    if (current_context(&ctx) != VREN_OK) return VREN_ERR_CUDA;
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (g_noalloc_ptr[dev] == nullptr) {
-        void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_noalloc_scan_scratch) != cudaSuccess || p == nullptr) return VREN_ERR_CUDA;
-        g_noalloc_ptr[dev] = p;
-    }
-    *out = static_cast<uint32_t*>(g_noalloc_ptr[dev]);
+    for (int i = 0; ctx && i < g_noalloc_entries; ++i)
+        if (g_noalloc_cache[i].dev == dev && g_noalloc_cache[i].ctx == ctx) {
+            *out = static_cast<uint32_t*>(g_noalloc_cache[i].ptr);
+            return VREN_OK;
+        }
+    // the lookup makes the device's primary context current when no context is yet
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scan_scratch) != cudaSuccess || p == nullptr) return VREN_ERR_CUDA;
+    if (!ctx && (current_context(&ctx) != VREN_OK || !ctx)) return VREN_ERR_CUDA;
+    // a context handle can be reused after its context is destroyed: a stale entry for this device is
+    // replaced; otherwise the oldest entry makes room
+    int slot = -1;
+    for (int i = 0; i < g_noalloc_entries; ++i)
+        if (g_noalloc_cache[i].dev == dev) slot = i;
+    if (slot < 0) slot = g_noalloc_entries < kNoAllocMaxEntries ? g_noalloc_entries++ : 0;
+    g_noalloc_cache[slot] = {dev, ctx, p};
+    *out = static_cast<uint32_t*>(p);
     return VREN_OK;
 }
 }  // namespace vren_gb300
