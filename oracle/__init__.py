@@ -51,6 +51,12 @@ _PROTOS = {
     "oracle_cs_shade_light_loss_f64": (C.c_double, [vp, u32, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, u32, vp, i32, vp]),
     "oracle_cs_shade_grad_lights_f64": (None, [vp, u32, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, u32, i32, vp,
                                                vp, u32, C.c_double, vp, vp, vp, i32]),
+    "oracle_cs_light_codes": (None, [vp, u32, vp, u32, vp, vp, vp, vp]),
+    "oracle_cs_normal_bins": (None, [vp, u64, vp]),
+    "oracle_cs_pixel_keys": (None, [vp, vp, u32, u32, vp, vp]),
+    "oracle_cs_cluster_boxes": (None, [vp, u64, u32, u32, vp, vp, vp]),
+    "oracle_cs_test_aabb_aabb": (None, [vp, u64, vp]),
+    "oracle_cs_test_sphere_aabb": (None, [vp, u64, vp]),
 }
 
 OPS = {"add": 0, "min": 1, "max": 2}
@@ -392,3 +398,51 @@ def cs_shade_grad_lights_f64(view, W, H, gb, lists, lpos, lights, L, grad, sel, 
                                           _p(_f32(lpos)), _p(_f32(lights)), L, falloff, _p(_f32(grad)), _p(sel), n,
                                           float(h), _p(g7), _p(fd7), _p(pairs), threads or 8)
     return g7.reshape(n, 7), fd7.reshape(n, 7), pairs
+
+
+# ---- per-element steps (compared with the reference's shaders run on the CPU, oracle/ref.py) --------
+def cs_light_codes(positions, L: int, view, morton_bits: int = 15):
+    """(view positions vec4[L], min vec4, max vec4, unsorted (code, light) pairs uint32[L, 2])."""
+    vp = np.zeros(max(L, 1) * 4, np.float32)
+    mn = np.zeros(4, np.float32)
+    mx = np.zeros(4, np.float32)
+    codes = np.zeros(max(L, 1) * 2, np.uint32)
+    lib().oracle_cs_light_codes(_p(_f32(positions)), L, _view_ptr(view), morton_bits, _p(vp), _p(mn), _p(mx), _p(codes))
+    return vp[: 4 * L], mn, mx, codes[: 2 * L].reshape(L, 2)
+
+
+def cs_normal_bins(normals) -> np.ndarray:
+    n = _f32(normals).reshape(-1, 3)
+    out = np.zeros(len(n), np.uint32)
+    lib().oracle_cs_normal_bins(_p(np.ascontiguousarray(n)), len(n), _p(out))
+    return out
+
+
+def cs_pixel_keys(depth, normals, W: int, H: int, view) -> np.ndarray:
+    """Keys of every invocation of the unique-cluster dispatch: (TY*32, TX*32), overhang wrapped."""
+    TX, TY = (W + 31) // 32, (H + 31) // 32
+    out = np.zeros((TY * 32, TX * 32), np.uint32)
+    lib().oracle_cs_pixel_keys(_p(_f32(depth)), _p(_f32(normals)), W, H, _view_ptr(view), _p(out))
+    return out
+
+
+def cs_cluster_boxes(keys, W: int, H: int, view):
+    k = _u32(keys)
+    mn = np.zeros((len(k), 3), np.float32)
+    mx = np.zeros((len(k), 3), np.float32)
+    lib().oracle_cs_cluster_boxes(_p(k), len(k), W, H, _view_ptr(view), _p(mn), _p(mx))
+    return mn, mx
+
+
+def cs_test_aabb_aabb(t) -> np.ndarray:
+    t = _f32(t).reshape(-1, 12)
+    out = np.zeros(len(t), np.uint8)
+    lib().oracle_cs_test_aabb_aabb(_p(np.ascontiguousarray(t)), len(t), _p(out))
+    return out
+
+
+def cs_test_sphere_aabb(t) -> np.ndarray:
+    t = _f32(t).reshape(-1, 10)
+    out = np.zeros(len(t), np.uint8)
+    lib().oracle_cs_test_sphere_aabb(_p(np.ascontiguousarray(t)), len(t), _p(out))
+    return out

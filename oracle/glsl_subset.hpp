@@ -19,15 +19,15 @@
 //  - buffers: out-of-bounds reads return zero and out-of-bounds writes are dropped (Vulkan's robust
 //    buffer access); each such access is counted in glsl::g_oob.
 //  - sampler2D / usampler2D: NEAREST filtering with REPEAT addressing at normalised coordinates
-//    (texel i = floor(u * size) wrapped into [0, size)); image2D / uimage2D with imageLoad /
+//    (texel i = floor(u * size) wrapped into [0, size)), or at unnormalised coordinates with
+//    CLAMP_TO_BORDER (the depth-pyramid copy's sampler); image2D / uimage2D with imageLoad /
 //    imageStore / imageSize, out-of-bounds stores dropped.
-//  - one 32-wide subgroup: subgroupBallot and subgroupMin / subgroupMax over 32 host threads that
-//    run the same invocation in lockstep (a std::barrier per collective), subgroupElect picks lane 0
+//  - one 32-wide subgroup: subgroupBallot over 32 invocations that the driver runs in lockstep as
+//    coroutines (each ballot suspends a lane until all 32 have voted); subgroupElect picks lane 0
 //    (every call site here is in uniform control flow).
 #pragma once
 
 #include <atomic>
-#include <barrier>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -269,6 +269,7 @@ template <class T> struct buffer {
 struct sampler2D {
     const float* data = nullptr;  // row-major texels of `comps` floats
     int w = 0, h = 0, comps = 4;
+    bool unnormalized = false;  // unnormalised coordinates with CLAMP_TO_BORDER (border = 0)
 };
 struct usampler2D {
     const uint* data = nullptr;
@@ -288,6 +289,11 @@ inline vec4 texel(const sampler2D& s, int x, int y)
 }
 inline vec4 texture(const sampler2D& s, const vec2& uv)
 {
+    if (s.unnormalized) {
+        const int x = to_int(std::floor(uv.x)), y = to_int(std::floor(uv.y));
+        if (x < 0 || y < 0 || x >= s.w || y >= s.h) return vec4(0.0f);
+        return texel(s, x, y);
+    }
     const ivec2 i = nearest_repeat(uv, s.w, s.h);
     return texel(s, i.x, i.y);
 }
@@ -343,25 +349,12 @@ inline thread_local uvec3 gl_WorkGroupSize;
 inline thread_local uint gl_LocalInvocationIndex = 0, gl_SubgroupInvocationID = 0, gl_SubgroupID = 0;
 inline thread_local uint gl_SubgroupSize = 32, gl_NumSubgroups = 1;
 
-// ---- one subgroup of 32 host threads --------------------------------------------------------------
-struct Subgroup {
-    std::barrier<> bar{32};
-    uint votes[32] = {};
-    vec3 vals[32];
-    bool active[32] = {};
-};
-inline thread_local Subgroup* g_subgroup = nullptr;
+// ---- one 32-wide subgroup -------------------------------------------------------------------------
+// The driver runs the 32 invocations of a subgroup as coroutines on one host thread; a ballot stores
+// the lane's vote and suspends it until every lane has voted (g_ballot, set by the driver).
+inline thread_local uint (*g_ballot)(bool) = nullptr;
 
-inline uvec4 subgroupBallot(bool b)
-{
-    Subgroup& sg = *g_subgroup;
-    sg.votes[gl_SubgroupInvocationID] = b ? 1u : 0u;
-    sg.bar.arrive_and_wait();
-    uint m = 0;
-    for (uint i = 0; i < 32; ++i) m |= sg.votes[i] << i;
-    sg.bar.arrive_and_wait();
-    return uvec4(m, 0u, 0u, 0u);
-}
+inline uvec4 subgroupBallot(bool b) { return uvec4(g_ballot(b), 0u, 0u, 0u); }
 inline bool subgroupElect() { return gl_SubgroupInvocationID == 0; }
 inline void subgroupMemoryBarrierBuffer() {}
 

@@ -8,6 +8,9 @@
 // Built twice (VREN_REF_CANONICAL 0 / 1) from the two generated variants; the canonical variant's
 // replaced expressions call the canon_* functions below, which read the host-built tables that
 // ref_set_canonical installs.
+#include <ucontext.h>
+
+#include <algorithm>
 #include <thread>
 #include <vector>
 
@@ -99,6 +102,90 @@ template <class PC> void set_assign_constants(PC& pc, uint32_t tiles_x, uint32_t
     pc.bvh_root_idx = root;
     pc.bvh_level_count = levels;
 }
+
+// One work group of assign_lights.comp: 32 invocations run as coroutines on the calling thread.  Each
+// runs main() until its next subgroupBallot, where it stores its vote and yields; once all 32 have
+// voted the mask is formed and each lane resumes with it, in lane order.  The shader's per-invocation
+// globals (gl_SubgroupInvocationID, the thread_local g_level_overlaps) are swapped in and out at every
+// switch, since the 32 coroutines share the thread.
+struct Warp;
+thread_local Warp* t_warp = nullptr;
+
+struct Warp {
+    static constexpr size_t kStack = 1 << 16;
+    ucontext_t sched;
+    ucontext_t lane_ctx[32];
+    std::vector<char> stacks = std::vector<char>(32 * kStack);
+    uint32_t overlaps[32][sizeof(sh_assign_write::g_level_overlaps) / sizeof(uint)];
+    uint32_t votes[32] = {};
+    uint32_t mask = 0, cur = 0, cluster = 0, groups = 0;
+    bool done[32] = {};
+    int write = 0;
+
+    uint32_t* private_globals() const
+    {
+        return write ? sh_assign_write::g_level_overlaps : sh_assign_count::g_level_overlaps;
+    }
+    void enter_lane(uint32_t l)
+    {
+        cur = l;
+        gl_SubgroupInvocationID = l;
+        gl_LocalInvocationIndex = l;
+        gl_LocalInvocationID = uvec3(l, 0u, 0u);
+        gl_WorkGroupID = uvec3(cluster, 0u, 0u);
+        gl_GlobalInvocationID = uvec3(cluster * 32 + l, 0u, 0u);
+        gl_NumWorkGroups = uvec3(groups, 1u, 1u);
+        std::memcpy(private_globals(), overlaps[l], sizeof(overlaps[l]));
+    }
+    void leave_lane(uint32_t l) { std::memcpy(overlaps[l], private_globals(), sizeof(overlaps[l])); }
+
+    static uint ballot(bool b)
+    {
+        Warp& w = *t_warp;
+        const uint32_t l = w.cur;
+        w.votes[l] = b ? 1u : 0u;
+        w.leave_lane(l);
+        swapcontext(&w.lane_ctx[l], &w.sched);
+        w.enter_lane(l);
+        return w.mask;
+    }
+    static void entry()
+    {
+        Warp& w = *t_warp;
+        if (w.write) sh_assign_write::shader_main();
+        else sh_assign_count::shader_main();
+        w.leave_lane(w.cur);
+        w.done[w.cur] = true;  // returns to `sched` through uc_link
+    }
+    void run(uint32_t c, uint32_t U)
+    {
+        t_warp = this;
+        g_ballot = &Warp::ballot;
+        cluster = c;
+        groups = U;
+        for (uint32_t l = 0; l < 32; ++l) {
+            getcontext(&lane_ctx[l]);
+            lane_ctx[l].uc_stack.ss_sp = stacks.data() + l * kStack;
+            lane_ctx[l].uc_stack.ss_size = kStack;
+            lane_ctx[l].uc_link = &sched;
+            makecontext(&lane_ctx[l], &Warp::entry, 0);
+            std::memset(overlaps[l], 0, sizeof(overlaps[l]));
+            done[l] = false;
+        }
+        for (;;) {
+            for (uint32_t l = 0; l < 32; ++l) {
+                enter_lane(l);
+                swapcontext(&sched, &lane_ctx[l]);
+            }
+            uint32_t finished = 0;
+            for (uint32_t l = 0; l < 32; ++l) finished += done[l] ? 1u : 0u;
+            if (finished == 32) break;
+            if (finished != 0) std::abort();  // a ballot outside uniform control flow
+            mask = 0;
+            for (uint32_t l = 0; l < 32; ++l) mask |= votes[l] << l;
+        }
+    }
+};
 }  // namespace
 
 extern "C" {
@@ -252,25 +339,17 @@ void ref_assign_lights(int write, const uint32_t* keys, uint32_t U, uint32_t til
         view_space_point_light_positions = buf<vec4>(view_pos, L);
         for (uint32_t c = 0; c < U; ++c) counts[c] = 0;  // the reference clears the counts first
     }
-    Subgroup sg;
-    std::vector<std::thread> lanes;
-    for (uint lane = 0; lane < 32; ++lane)
-        lanes.emplace_back([&, lane] {
-            g_subgroup = &sg;
-            gl_SubgroupInvocationID = lane;
-            gl_SubgroupID = 0;
-            gl_LocalInvocationIndex = lane;
-            gl_NumWorkGroups = uvec3(U, 1u, 1u);
-            for (uint32_t c = 0; c < U; ++c) {
-                gl_WorkGroupID = uvec3(c, 0u, 0u);
-                gl_LocalInvocationID = uvec3(lane, 0u, 0u);
-                gl_GlobalInvocationID = uvec3(c * 32 + lane, 0u, 0u);
-                if (write) sh_assign_write::shader_main();
-                else sh_assign_count::shader_main();
-                sg.bar.arrive_and_wait();  // the next work group starts when every lane has finished
-            }
+    // Work groups are independent (each writes its own count or its own list range), so they are
+    // spread over host threads; inside one, the 32 invocations run as a Warp of coroutines.
+    const unsigned nthreads = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    std::vector<std::thread> pool;
+    for (unsigned t = 0; t < nthreads; ++t)
+        pool.emplace_back([=] {
+            Warp w;
+            w.write = write;
+            for (uint32_t c = t; c < U; c += nthreads) w.run(c, U);
         });
-    for (auto& t : lanes) t.join();
+    for (auto& t : pool) t.join();
 }
 
 // ---- shade.comp ------------------------------------------------------------------------------------
@@ -336,7 +415,9 @@ void ref_bounce(float* positions, float* directions, uint32_t L, const float* mn
 void ref_depth_copy(const float* depth, uint32_t W, uint32_t H, float* level0)
 {
     using namespace sh_depth_copy;
-    depth_buffer = sampler2D{depth, (int)W, (int)H, 1};
+    // the reference's depth sampler: NEAREST, unnormalised coordinates, CLAMP_TO_BORDER
+    // (depth_buffer_pyramid.cpp:197-211)
+    depth_buffer = sampler2D{depth, (int)W, (int)H, 1, true};
     depth_buffer_pyramid_base = image2D{level0, (int)W, (int)H, 1};
     dispatch_2d((W + 31) / 32, (H + 31) / 32, [] { sh_depth_copy::shader_main(); });
 }

@@ -16,6 +16,7 @@ The rewrite, applied to each shader with its #include files inlined:
   - `out T x` / `inout T x` parameters become `T& x`;
   - float literals get the `f` suffix (GLSL literals are single precision);
   - uint(...), int(...), float(...), bool(...) casts call glsl_uint etc.;
+  - scalar locals declared without a value start at zero (GLSL leaves them undefined);
   - `v.xy = e;` becomes `v.set_swz<0, 1>(e);`, swizzles `.xyz` become `.swz<0, 1, 2>()`, single
     components .r .g .b .a become .x .y .z .w;
   - main() becomes shader_main();
@@ -222,6 +223,9 @@ def _rewrite_expressions(text: str) -> str:
     # casts
     for ty in ("uint", "int", "float", "bool"):
         text = re.sub(r"(?<![\w.])" + ty + r"\s*\(", f"glsl_{ty}(", text)
+    # scalar locals declared without a value (undefined until written in GLSL) start at zero, so that
+    # an input that never writes them (a NaN normal in clustered_shading_discretize_normal) is defined
+    text = re.sub(r"(?m)^(\s*)(uint|int|float|bool)\s+(\w+)\s*;", r"\1\2 \3 = 0;", text)
     # assignments to swizzles
     def set_swz(m):
         idx = ", ".join(str(SWZ[c]) for c in m.group(2))

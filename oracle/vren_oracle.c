@@ -446,10 +446,11 @@ static uint32_t discretize_normal(const float n[3])
  * Morton codes (discretize_point_light_positions.comp:30-39), bucket sort on code & 0xFFFF
  * (stable), leaves (init_light_array_bvh.comp:42-65), build_bvh.
  * ================================================================================================ */
-void oracle_cs_light_bvh(const float* positions, const float* lights, uint32_t L, const oracle_cs_view* v,
-                         uint32_t morton_bits, float* view_pos, oracle_bvh_node* bvh, uint32_t* light_index)
+/* view positions, their min / max (vec4) and the unsorted (Morton code, light) pairs */
+void oracle_cs_light_codes(const float* positions, uint32_t L, const oracle_cs_view* v, uint32_t morton_bits,
+                           float* view_pos, float* mn, float* mx, uint32_t* codes)
 {
-    float mn[4] = {INFINITY, INFINITY, INFINITY, INFINITY}, mx[4] = {-INFINITY, -INFINITY, -INFINITY, -INFINITY};
+    for (int c = 0; c < 4; ++c) { mn[c] = INFINITY; mx[c] = -INFINITY; }
     for (uint32_t i = 0; i < L; ++i) {
         float p[4] = {positions[4 * i], positions[4 * i + 1], positions[4 * i + 2], 1.0f};
         matvec(v->view, p, &view_pos[4 * i]);
@@ -460,7 +461,6 @@ void oracle_cs_light_bvh(const float* positions, const float* lights, uint32_t L
     }
     const uint32_t bits = morton_bits == 30 ? 10u : 5u;
     const float scale = (float)(1u << bits);
-    uint32_t* codes = (uint32_t*)malloc((size_t)L * 8 + 8);
     for (uint32_t i = 0; i < L; ++i) {
         uint32_t q[3];
         for (int c = 0; c < 3; ++c) q[c] = floor_to_u32(((view_pos[4 * i + c] - mn[c]) / (mx[c] - mn[c])) * scale);
@@ -473,6 +473,14 @@ void oracle_cs_light_bvh(const float* positions, const float* lights, uint32_t L
         codes[2 * i] = code;
         codes[2 * i + 1] = i;
     }
+}
+
+void oracle_cs_light_bvh(const float* positions, const float* lights, uint32_t L, const oracle_cs_view* v,
+                         uint32_t morton_bits, float* view_pos, oracle_bvh_node* bvh, uint32_t* light_index)
+{
+    float mn[4], mx[4];
+    uint32_t* codes = (uint32_t*)malloc((size_t)L * 8 + 8);
+    oracle_cs_light_codes(positions, L, v, morton_bits, view_pos, mn, mx, codes);
     /* bucket sort on the low 16 bits (bucket_sort.hpp:15-16) for 15-bit codes; the 30-bit
      * extension sorts on the whole code (stable either way) */
     {
@@ -728,6 +736,63 @@ uint64_t oracle_cs_assign_lights(const uint32_t* keys, uint32_t U, uint32_t W, u
         traverse_cluster(&box, bvh, root, levels, light_index, view_pos, indices + offsets[c]);
     }
     return total;
+}
+
+/* ---- the restatement's per-element steps, for the comparison with the reference's own shaders ---- */
+void oracle_cs_normal_bins(const float* normals, uint64_t count, uint32_t* out)
+{
+    for (uint64_t i = 0; i < count; ++i) out[i] = discretize_normal(normals + 3 * i);
+}
+
+void oracle_cs_pixel_keys(const float* depth, const float* normals, uint32_t W, uint32_t H, const oracle_cs_view* v,
+                          uint32_t* keys)
+{
+    const uint32_t TX = (W + 31) / 32, TY = (H + 31) / 32;
+    float bnear[ORACLE_SLICES], bfar[ORACLE_SLICES];
+    oracle_cs_slice_table(v, TY, bnear, bfar);
+    const uint32_t kmax = v->slicing == ORACLE_SLICING_FIXED32 ? 31u : (ORACLE_SLICES - 1u);
+#pragma omp parallel for schedule(static)
+    for (int64_t gy = 0; gy < (int64_t)TY * 32; ++gy)
+        for (uint32_t gx = 0; gx < TX * 32; ++gx)
+            keys[(size_t)gy * TX * 32 + gx] = pixel_key(depth, normals, W, H, gx, (uint32_t)gy, v, bnear, kmax);
+}
+
+void oracle_cs_cluster_boxes(const uint32_t* keys, uint64_t count, uint32_t W, uint32_t H, const oracle_cs_view* v,
+                             float* mn, float* mx)
+{
+    const uint32_t TX = (W + 31) / 32, TY = (H + 31) / 32;
+    float bnear[ORACLE_SLICES], bfar[ORACLE_SLICES];
+    oracle_cs_slice_table(v, TY, bnear, bfar);
+    for (uint64_t i = 0; i < count; ++i) {
+        caabb b = cluster_aabb(keys[i], TX, TY, v, bnear, bfar);
+        for (int c = 0; c < 3; ++c) { mn[3 * i + c] = b.mn[c]; mx[3 * i + c] = b.mx[c]; }
+    }
+}
+
+void oracle_cs_test_aabb_aabb(const float* t, uint64_t count, uint8_t* out)
+{
+    for (uint64_t i = 0; i < count; ++i) {
+        const float* q = t + 12 * i;
+        caabb c;
+        oracle_bvh_node n;
+        for (int k = 0; k < 3; ++k) {
+            c.mn[k] = q[k];
+            c.mx[k] = q[3 + k];
+            n.min[k] = q[6 + k];
+            n.max[k] = q[9 + k];
+        }
+        out[i] = (uint8_t)test_aabb_aabb(&c, &n);
+    }
+}
+
+void oracle_cs_test_sphere_aabb(const float* t, uint64_t count, uint8_t* out)
+{
+    for (uint64_t i = 0; i < count; ++i) {
+        const float* q = t + 10 * i;
+        caabb c;
+        for (int k = 0; k < 3; ++k) { c.mn[k] = q[4 + k]; c.mx[k] = q[7 + k]; }
+        out[i] = (uint8_t)test_sphere_aabb(q, q[3], &c);
+    }
 }
 
 /* ================================================================================================

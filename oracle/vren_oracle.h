@@ -94,6 +94,22 @@ void oracle_cs_light_bvh(const float* positions, const float* lights, uint32_t L
                          uint32_t morton_bits, float* view_pos /* vec4[L] */, oracle_bvh_node* bvh,
                          uint32_t* light_index /* uvec2[L] */);
 
+/* The restatement's per-element steps, compared one by one with the reference's shaders run on the
+ * CPU (oracle/_ref): view positions, their vec4 min / max and the unsorted (code, light) pairs; the
+ * normal bin of each normal; the key of every invocation of the unique-cluster dispatch
+ * ((TY*32) rows of TX*32, overhang included, WRAP texels); the view-space box of each key (3 floats
+ * per corner); the two overlap tests (12 floats per AABB test: min1, max1, min2, max2; 10 per sphere
+ * test: centre, radius, min, max). */
+void oracle_cs_light_codes(const float* positions, uint32_t L, const oracle_cs_view* v, uint32_t morton_bits,
+                           float* view_pos, float* mn, float* mx, uint32_t* codes);
+void oracle_cs_normal_bins(const float* normals, uint64_t count, uint32_t* out);
+void oracle_cs_pixel_keys(const float* depth, const float* normals, uint32_t W, uint32_t H, const oracle_cs_view* v,
+                          uint32_t* keys);
+void oracle_cs_cluster_boxes(const uint32_t* keys, uint64_t count, uint32_t W, uint32_t H, const oracle_cs_view* v,
+                             float* mn, float* mx);
+void oracle_cs_test_aabb_aabb(const float* t, uint64_t count, uint8_t* out);
+void oracle_cs_test_sphere_aabb(const float* t, uint64_t count, uint8_t* out);
+
 /* Returns the number of unique cluster keys U (keys[0..U) written), refs[W*H]. */
 uint32_t oracle_cs_find_unique_clusters(const float* depth, const float* normals, uint32_t W, uint32_t H,
                                         const oracle_cs_view* v, int policy, uint32_t* keys, uint32_t key_cap,
