@@ -250,6 +250,7 @@ def run_ours(args, rank: int, world: int):
             d2h_total = 8 + W * H * 4 + u * 12 + tot * 4
     e2e = sum(e2e_ms) / len(e2e_ms)
     e2e_refs_ok = bool(np.array_equal(h_refs.numpy(), cs.read_device(out.cluster_refs, W * H).view(np.int32)))
+    link = link_bench(dev, stream, h2d_bytes, d2h_total, max(5, args.steps), e2e)
 
     # extra, labelled: the same frame with 16384 lights packed in front of the camera, so that the
     # light lists are long (the workload's lights, uniform over a frustum box 1000 deep, reach few of
@@ -264,6 +265,29 @@ def run_ours(args, rank: int, world: int):
     dense = {"frame_ms": round(dense_ms, 5), "assignments": int(cs.read_device(od.total, 1)[0]),
              "unique_clusters": int(cs.read_device(od.key_count, 1)[0]),
              "lights": "16384 lights uniform in x [-8, 8], y [-5, 5], z [0.5, 25], radius lognormal(ln 2, 0.5)"}
+
+    # extra, labelled: the same frame with 32 exponential depth slices (FIXED32) instead of the
+    # reference's slicing
+    view32 = cs.view_from_camera(cam, "fixed32")
+    f32s_ms = time_events(stream, lambda: ctx.cluster(stream, view32, W, H, d_depth, d_norm, d_pos, d_light, L), 3,
+                          args.steps, flush)
+    o32 = ctx.outputs()
+    fixed32 = {"frame_ms": round(f32s_ms, 5), "unique_clusters": int(cs.read_device(o32.key_count, 1)[0]),
+               "assignments": int(cs.read_device(o32.total, 1)[0]),
+               "slicing": "32 exponential slices: near * (far/near)^(k/32)"}
+
+    # extra, labelled: cluster_and_shade::operator() in one call (clustering, then shading over the
+    # context's own light lists, one graph): the workload's frame with a seeded G-buffer (its normals are
+    # the depth planes' normals), reference falloff, colour output with ambient and gamma
+    gn_, galb, grough, gmetal = scene.gbuffer(SEED + 11, W, H)
+    d_alb, d_rough, d_metal = (torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in (galb, grough, gmetal))
+    gbuf = cs.gbuffer(d_depth, d_norm, d_alb, d_rough, d_metal)
+    img = torch.empty(W * H * 3, dtype=torch.float32, device=dev)
+    cas_ms = time_events(stream, lambda: ctx(stream, view, W, H, gbuf, d_pos, d_light, L, img), 3, args.steps, flush)
+    ocs = ctx.outputs()
+    cluster_and_shade = {"frame_ms": round(cas_ms, 5), "assignments": int(cs.read_device(ocs.total, 1)[0]),
+                         "path": "vren_cs_cluster_and_shade: light BVH, unique clusters, light lists, then shade "
+                                 "(f32x3 colour out), one graph replay"}
 
     # extra, labelled: the frame with its normals in the reference's own G-buffer format (RGBA16F,
     # 8 B/px instead of 12), on the device and end to end from host buffers
@@ -289,7 +313,7 @@ def run_ours(args, rank: int, world: int):
     # radix sort: 2^20 key/value pairs (config 1), plus sizes beyond L2
     radix = radix_bench(args, dev, stream, flush, radix_keys, hbm_peak)
     sweep = None if args.quick else primitive_sweep(args, dev, stream, flush, hbm_peak)
-    shade = shade_bench(args, dev, stream, flush, ctx)
+    shade_host, shade = shade_bench(args, dev, stream, flush, ctx)
     batched = None if args.quick else batched_vs_plain(args, dev, stream, flush)
     lbvh = None if args.quick else lbvh_bench(args, dev, stream, flush, depth, normals, pos, lights, view)
     debug_views = None if args.quick else debug_views_bench(args, dev, stream, flush, ctx, hbm_peak)
@@ -308,7 +332,7 @@ def run_ours(args, rank: int, world: int):
                          "backward_frac": round(shade["backward_tflops"] / peak32, 4)}
     cpu = None
     if rank == 0 and not args.no_cpu:
-        cpu = cpu_baseline(depth, normals, pos, lights, radix_keys, view)
+        cpu = cpu_baseline(depth, normals, pos, lights, radix_keys, view, shade_host)
 
     # light BVH at 16384 lights: one kernel on a 16-CTA cluster (1); unique clusters: tiles, tile-count
     # scan, fix-up (3); assignment: count, scan, write (3)
@@ -342,8 +366,11 @@ def run_ours(args, rank: int, world: int):
                             "BVH and the unique-cluster tiles, reference download overlapping the assignment, light "
                             "lists written to host memory by the device); host wall clock",
                     "refs_match_device": e2e_refs_ok},
+            "link": link,
             "normals_rgba16f": rgba16f,
             "dense_lights": dense,
+            "fixed32_slicing": fixed32,
+            "cluster_and_shade": cluster_and_shade,
             "gpu_launches": launches_per_frame * args.steps,
             "roofline": {"bound": "hbm", "kernel": "find_unique_cluster_list (find_unique_kernel, "
                                                      "find_unique_scan_kernel, find_unique_fixup_kernel)",
@@ -367,7 +394,59 @@ def run_ours(args, rank: int, world: int):
             "device_error": err,
             "wall_s_timed": round(t_wall, 4),
         }
+        # the three targets of the workload definition, last on the line (the record keeps its tail)
+        r26 = (radix or {}).get("n=2^26", {})
+        adj = (cpu or {}).get("adjoint_check") or {}
+        res["targets"] = {
+            "radix_hbm_frac_2^26_pairs": r26.get("hbm_frac"), "radix_target": 0.60,
+            "radix_bit_exact_2^20": (radix or {}).get("n=2^20", {}).get("bit_exact_vs_stable_sort"),
+            "batched_speedup": (batched or {}).get("speedup"),
+            "batched_bit_exact_all_frames": (batched or {}).get("bit_exact_all_frames"),
+            "adjoint_rel_err_vs_fp64": adj.get("rel_err_max_group"), "adjoint_target": 1e-4,
+            "adjoint_lights_checked": adj.get("lights_checked"),
+            "e2e_ms": round(e2e, 4), "e2e_link_floor_ms": link["e2e_floor_ms"],
+        }
         print(json.dumps(res), flush=True)
+
+
+def link_bench(dev, stream, up_bytes: int, down_bytes: int, steps: int, e2e_ms: float):
+    """The host <-> device link at the end-to-end frame's byte counts (page-locked buffers, CUDA events):
+    the upload alone, the download alone, and both at once on two streams.  Moving a frame's bytes both
+    ways at once is the floor of the end-to-end frame; `frac` = that floor / the measured e2e time."""
+    import torch
+
+    up_h = torch.empty(up_bytes // 4, dtype=torch.int32).pin_memory()
+    up_d = torch.empty(up_h.numel(), dtype=torch.int32, device=dev)
+    dn_d = torch.zeros(down_bytes // 4, dtype=torch.int32, device=dev)
+    dn_h = torch.empty(dn_d.numel(), dtype=torch.int32).pin_memory()
+    side = torch.cuda.Stream(device=dev)
+
+    def up():
+        up_d.copy_(up_h, non_blocking=True)
+
+    def down():
+        dn_h.copy_(dn_d, non_blocking=True)
+
+    def both():
+        fork = torch.cuda.Event()
+        fork.record(stream)
+        side.wait_event(fork)
+        with torch.cuda.stream(side):
+            down()
+        up()
+        join = torch.cuda.Event()
+        join.record(side)
+        stream.wait_event(join)
+
+    ms_up = time_events(stream, up, 3, steps)
+    ms_down = time_events(stream, down, 3, steps)
+    ms_both = time_events(stream, both, 3, steps)
+    return {"h2d_bytes": up_bytes, "d2h_bytes": down_bytes, "h2d_ms": round(ms_up, 4), "d2h_ms": round(ms_down, 4),
+            "h2d_gbs": round(up_bytes / (ms_up * 1e6), 1), "d2h_gbs": round(down_bytes / (ms_down * 1e6), 1),
+            "both_ms": round(ms_both, 4), "both_gbs": round((up_bytes + down_bytes) / (ms_both * 1e6), 1),
+            "e2e_floor_ms": round(ms_both, 4), "e2e_frac_of_floor": round(ms_both / e2e_ms, 4),
+            "note": "page-locked copies, upload and download at once on two streams: the link carries "
+                    "the frame's bytes no faster; e2e_frac_of_floor = floor / e2e"}
 
 
 def time_events(stream, fn, warmup, steps, flush=None):
@@ -670,16 +749,22 @@ def shade_profile_setup(dev, stream, ctx):
     gcol = torch.zeros(L_ * 3, dtype=torch.float32, device=dev)
     grr = torch.zeros(L_, dtype=torch.float32, device=dev)
     keep = (d_depth, d_np, d_pos, d_light, d_n, d_alb, d_r, d_m, d_grad, img, gpos, gcol, grr)
+    # host copies for the FP64 check of the adjoint (the CPU leg)
+    host = {"view": view, "W": W_, "H": H_, "L": L_, "gb": (depth, gn, galb, grough, gmetal), "pos": pos,
+            "lights": lights, "grad": grad,
+            "lists": (refs, counts, cs.read_device(out.offsets, U), cs.read_device(out.indices, total))}
     return {
         "forward": lambda: fwd(stream, out.frame, W_, H_, gb, ll, d_pos, d_light, L_, img),
         "backward": lambda: bwd(stream, out.frame, W_, H_, gb, ll, total, d_pos, d_light, L_, d_grad, gpos, gcol, grr),
-        "pairs": pairs, "unique_clusters": U, "assignments": total, "img": img, "gpos": gpos, "keep": keep,
+        "pairs": pairs, "unique_clusters": U, "assignments": total, "img": img, "gpos": gpos, "gcol": gcol,
+        "grr": grr, "keep": keep, "host": host,
     }
 
 
 def shade_bench(args, dev, stream, flush, ctx):
     """Differentiable shading at 1920x1080 with 4096 lights: forward radiance and the adjoint w.r.t.
-    light position/colour/radius, each timed alone with CUDA events (L2 flushed between runs)."""
+    light position/colour/radius, each timed alone with CUDA events (L2 flushed between runs).  Returns
+    (host copies of the inputs, lists and GPU gradient for the CPU leg's FP64 check, results)."""
     import torch
 
     sb = shade_profile_setup(dev, stream, ctx)
@@ -688,7 +773,12 @@ def shade_bench(args, dev, stream, flush, ctx):
     ms_b = time_events(stream, sb["backward"], 3, steps, flush)
     pairs = sb["pairs"]
     ok = bool(torch.isfinite(sb["img"]).all().item() and torch.isfinite(sb["gpos"]).all().item())
-    return {
+    L_ = sb["host"]["L"]
+    torch.cuda.synchronize()
+    sb["host"]["gpu_gradient"] = np.concatenate([sb["gpos"].cpu().numpy().reshape(L_, 3),
+                                                 sb["gcol"].cpu().numpy().reshape(L_, 3),
+                                                 sb["grr"].cpu().numpy().reshape(L_, 1)], 1).astype(np.float64)
+    return sb["host"], {
         "workload": "1920x1080 G-buffer, 4096 lights near visible surfaces, windowed inverse-square falloff, "
                     "radiance output; adjoint for an N(0,1) upstream gradient",
         "pairs": pairs, "unique_clusters": sb["unique_clusters"], "assignments": sb["assignments"],
@@ -824,9 +914,40 @@ def primitive_sweep(args, dev, stream, flush, hbm_peak):
     return res
 
 
-def cpu_baseline(depth, normals, pos, lights, radix_keys, view, budget_s: float = 12.0, threads: int = 1):
-    """The CPU oracle (port of the reference's algorithms) on a bounded sample, single-threaded."""
+def adjoint_check(oracle, host, lights_checked: int = 64):
+    """The GPU adjoint of the differentiable-shading workload (1920x1080, 4096 lights) against the FP64
+    forward-mode gradient of the oracle on `lights_checked` seeded lights, evaluated over those lights'
+    own (pixel, light) pairs with all host threads: relative error per parameter group (normwise over
+    the lights) and per light."""
+    refs, counts, offsets, indices = host["lists"]
+    total = int(counts.sum(dtype=np.uint64))
+    pix = np.bincount(refs, minlength=len(counts)).astype(np.int64)
+    pairs = np.bincount(indices[:total], weights=np.repeat(pix, counts.astype(np.int64)), minlength=host["L"])
+    rng = np.random.default_rng(SEED + 505)
+    sel = np.sort(rng.choice(np.flatnonzero(pairs > 0), lights_checked, replace=False)).astype(np.uint32)
+    t0 = time.perf_counter()
+    ref, _, _ = oracle.cs_shade_grad_lights_f64(host["view"], host["W"], host["H"], host["gb"], host["lists"],
+                                                host["pos"], host["lights"], host["L"], host["grad"], sel, h=0.0,
+                                                falloff=1, threads=os.cpu_count())
+    got = host["gpu_gradient"][sel]
+    groups = {name: float(np.linalg.norm(got[:, sl] - ref[:, sl]) / np.linalg.norm(ref[:, sl]))
+              for name, sl in (("position", slice(0, 3)), ("colour", slice(3, 6)), ("radius", slice(6, 7)))}
+    nz = np.linalg.norm(ref, axis=1) > 0
+    per_light = np.linalg.norm(got[nz] - ref[nz], axis=1) / np.linalg.norm(ref[nz], axis=1)
+    return {"lights_checked": lights_checked, "pairs_checked": int(pairs[sel].sum()),
+            "rel_err_by_group": {k: float(f"{v:.3g}") for k, v in groups.items()},
+            "rel_err_max_group": float(f"{max(groups.values()):.3g}"),
+            "rel_err_per_light_max": float(f"{per_light.max():.3g}"),
+            "check_s": round(time.perf_counter() - t0, 2), "reference": "FP64 forward-mode gradient (dual numbers)"}
+
+
+def cpu_baseline(depth, normals, pos, lights, radix_keys, view, shade_host=None, budget_s: float = 12.0,
+                 threads: int = 1):
+    """The CPU oracle (port of the reference's algorithms) on a bounded sample, single-threaded; the
+    primitive sweep's CPU counterparts (the reference test's tree reduce, std::exclusive_scan, the
+    stable sort by masked key); and, as the checker, the FP64 gradient the GPU adjoint is held to."""
     import oracle
+    import vren_gb300.scene as scene
 
     t0 = time.perf_counter()
     frames = 0
@@ -864,7 +985,28 @@ def cpu_baseline(depth, normals, pos, lights, radix_keys, view, budget_s: float 
     t4 = time.perf_counter()
     oracle.kd_tree_search(kp, knodes, ks)
     ms_kd = (time.perf_counter() - t4) * 1e3
+    # the primitive sweep's CPU counterparts at n = 2^24 (u32 uniform in [0, 255]), one core
+    n2 = 1 << 24
+    xs = scene.gen_u32(SEED + 24, 2, n2, mask=255)
+    sweep = {}
+    for name, fn, nbytes in (("tree_reduce_u32_add", lambda: oracle.reduce_tree_u32("add", xs), 8 * n2),
+                             ("reduce_f32_max", lambda: oracle.reduce_f32("max", xs.astype(np.float32)), 4 * n2),
+                             ("exclusive_scan", lambda: oracle.exclusive_scan_u32(xs), 8 * n2)):
+        t5 = time.perf_counter()
+        fn()
+        ms = (time.perf_counter() - t5) * 1e3
+        sweep[name] = {"ms": round(ms, 3), "gbs": round(nbytes / (ms * 1e6), 2)}
+    nb = 1 << 22
+    bkeys = scene.gen_u32(SEED + 99, 3, nb)
+    bpairs = np.stack([bkeys, np.arange(nb, dtype=np.uint32)], 1).reshape(-1)
+    t6 = time.perf_counter()
+    oracle.bucket_sort_u32x2(bpairs, 10)
+    ms_b = (time.perf_counter() - t6) * 1e3
+    sweep["bucket_sort_2^22_10bit"] = {"ms": round(ms_b, 3), "gbs_at_24B": round(24 * nb / (ms_b * 1e6), 2)}
+    sweep["n"] = "2^24 (bucket sort 2^22), 1 core; bytes counted as for the GPU lines"
+    adjoint = adjoint_check(oracle, shade_host) if shade_host is not None else None
     return {"value": round(ms_frame, 3), "unit": "ms", "cores": threads, "kind": "port",
+            "primitive_sweep": sweep, "adjoint_check": adjoint,
             "sample": f"{frames} frames of the CPU oracle pipeline (a6+a7+a8) at 1920x1080/16384 lights",
             "radix_sort_2^20_pairs_ms": round(ms_sort, 3),
             "radix_sort_gkeys_s": round(RADIX_N / (ms_sort * 1e-3) / 1e9, 4),

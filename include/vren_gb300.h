@@ -567,6 +567,18 @@ int vren_cs_cluster(vren_cluster_and_shade* cs, vren_stream_t s, const vren_cs_v
                     uint32_t height, int offscreen, const float* depth, const float* normals,
                     const float* light_positions, const float* point_lights, uint32_t light_count);
 int vren_cs_get_outputs(const vren_cluster_and_shade* cs, vren_cs_outputs* out);
+/* cluster_and_shade::operator() (clustered_shading.cpp:924-1172): the three clustering stages of
+ * vren_cs_cluster, then shade over the context's own light lists (the reference's m_shade call,
+ * clustered_shading.cpp:1153-1168), in one CUDA graph of the context per frame shape (replayed on a
+ * non-default stream when use_graph is set).  gbuffer->depth and gbuffer->normals are also the
+ * clustering inputs, so the context's normal format must be VREN_CS_NORMALS_F32X3 (else
+ * VREN_ERR_ARG).  Shading as vren_cs_shade: out_rgb is f32x3[W*H], pixels that are not shaded are
+ * left untouched.  The clustering outputs are those of vren_cs_cluster on the same inputs. */
+int vren_cs_cluster_and_shade(vren_cluster_and_shade* cs, vren_stream_t s, const vren_cs_view* view,
+                              uint32_t width, uint32_t height, int offscreen, const vren_cs_gbuffer* gbuffer,
+                              const float* light_positions, const float* point_lights, uint32_t light_count,
+                              const float* directional_lights, uint32_t directional_count, int falloff,
+                              int output_mode, float* out_rgb);
 /* vren_cs_cluster for a frame held in page-locked host memory (no counterpart in the reference, whose
  * G-buffer is rendered on the GPU).  The lights are uploaded and their BVH built on a second stream
  * of the context while the depth and normals upload; when cluster_refs_out (page-locked, W*H) is

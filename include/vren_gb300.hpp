@@ -446,6 +446,25 @@ public:
               "cluster_and_shade");
     }
 
+    // cluster_and_shade::operator() (clustered_shading.cpp:924-1172): the light assignment of cluster(),
+    // then shade over this context's light lists into `output` (f32x3 per pixel).  The G-buffer's
+    // depth and normals (f32x3) are the clustering inputs too.
+    void operator()(cudaStream_t stream, camera const& cam, uint32_t width, uint32_t height,
+                    vren_cs_gbuffer const& gbuffer, device_buffer const& light_positions,
+                    device_buffer const& point_lights, uint32_t light_count, device_buffer const& output,
+                    float const* directional_lights = nullptr, uint32_t directional_count = 0,
+                    int falloff = VREN_CS_FALLOFF_REF, int output_mode = VREN_CS_SHADE_COLOR,
+                    uint32_t slicing = VREN_CS_SLICING_REF, int offscreen = VREN_CS_OFFSCREEN_WRAP)
+    {
+        vren_cs_view v;
+        vren_cs_view_from_camera(&cam, slicing, &v);
+        check(vren_cs_cluster_and_shade(m_handle, stream, &v, width, height, offscreen, &gbuffer,
+                                        light_positions.at<float>(), point_lights.at<float>(), light_count,
+                                        directional_lights, directional_count, falloff, output_mode,
+                                        output.at<float>()),
+              "cluster_and_shade");
+    }
+
     vren_cs_outputs outputs() const
     {
         vren_cs_outputs o;

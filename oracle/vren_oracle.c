@@ -410,12 +410,16 @@ void oracle_cs_slice_table(const oracle_cs_view* v, uint32_t tiles_y, float* nea
 
 static uint32_t slice_of(float z, const float* bnear, uint32_t kmax)
 {
-    /* largest k in [0, kmax] with bnear[k] <= z; 0 if none */
-    uint32_t k = 0;
-    for (uint32_t i = 0; i <= kmax; ++i)
-        if (bnear[i] <= z) k = i;
-        else break;
-    return k;
+    /* largest k in [0, kmax] with bnear[k] <= z; 0 if none (the table ascends, so a binary search over
+     * it finds the first bound above z; a NaN z is above no bound and below none: k = 0) */
+    if (!(bnear[0] <= z)) return 0;
+    uint32_t lo = 0, hi = kmax;  /* invariant: bnear[lo] <= z */
+    while (lo < hi) {
+        const uint32_t mid = lo + (hi - lo + 1) / 2;
+        if (bnear[mid] <= z) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
 }
 
 /* clustered_shading.glsl:7-43 */
@@ -553,17 +557,19 @@ uint32_t oracle_cs_find_unique_clusters(const float* depth, const float* normals
     oracle_cs_slice_table(v, TY, bnear, bfar);
     const uint32_t kmax = v->slicing == ORACLE_SLICING_FIXED32 ? 31u : (ORACLE_SLICES - 1u);
     uint32_t* tile_keys = (uint32_t*)malloc((size_t)T * 1024 * sizeof(uint32_t));
+    uint32_t* pix_keys = (uint32_t*)malloc((size_t)T * 1024 * sizeof(uint32_t)); /* each pixel's key, tile order */
     uint32_t* tile_count = (uint32_t*)malloc((size_t)T * sizeof(uint32_t));
 #pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads(threads))
     for (int64_t t = 0; t < (int64_t)T; ++t) {
         uint32_t ti = (uint32_t)t % TX, tj = (uint32_t)t / TX;
         uint32_t* tk = tile_keys + (size_t)t * 1024;
+        uint32_t* pk = pix_keys + (size_t)t * 1024;
         uint32_t m = 0;
         for (uint32_t ly = 0; ly < 32; ++ly)
             for (uint32_t lx = 0; lx < 32; ++lx) {
                 uint32_t gx = ti * 32 + lx, gy = tj * 32 + ly;
                 if (policy == ORACLE_SKIP && (gx >= W || gy >= H)) continue;
-                tk[m++] = pixel_key(depth, normals, W, H, gx, gy, v, bnear, kmax);
+                pk[ly * 32 + lx] = tk[m++] = pixel_key(depth, normals, W, H, gx, gy, v, bnear, kmax);
             }
         qsort(tk, m, sizeof(uint32_t), cmp_u32);
         uint32_t u = 0;
@@ -584,7 +590,7 @@ uint32_t oracle_cs_find_unique_clusters(const float* depth, const float* normals
             for (uint32_t lx = 0; lx < 32; ++lx) {
                 uint32_t gx = ti * 32 + lx, gy = tj * 32 + ly;
                 if (gx >= W || gy >= H) continue;  /* stores outside the screen are dropped */
-                uint32_t key = pixel_key(depth, normals, W, H, gx, gy, v, bnear, kmax);
+                uint32_t key = pix_keys[(size_t)t * 1024 + ly * 32 + lx];
                 /* rank of key among the tile's unique keys */
                 uint32_t lo = 0, hi = tile_count[t];
                 while (lo < hi) {
@@ -595,6 +601,7 @@ uint32_t oracle_cs_find_unique_clusters(const float* depth, const float* normals
             }
     }
     free(tile_keys);
+    free(pix_keys);
     free(tile_count);
     free(tile_off);
     return U;

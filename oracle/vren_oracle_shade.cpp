@@ -306,7 +306,7 @@ extern "C" double oracle_cs_shade_light_loss_f64(const oracle_cs_view* v, uint32
 
 // The FP64 gradient (forward mode) and the central finite differences with step h of the loss with
 // respect to the 7 parameters of each light in `sel` only, evaluating only the (pixel, light) pairs of
-// those lights: g7[7 * i + t] and fd7[7 * i + t] for light sel[i].  The pairs are gathered once (one
+// those lights: g7[7 * i + t] and fd7[7 * i + t] for light sel[i] (h <= 0: no differences, fd7 = 0).  The pairs are gathered once (one
 // pass over the pixels' lists); each light's 1 + 14 evaluations then run over its own pairs.
 extern "C" void oracle_cs_shade_grad_lights_f64(const oracle_cs_view* v, uint32_t W, uint32_t H, const float* depth,
                                                 const float* normals, const float* albedo, const float* rough,
@@ -360,7 +360,7 @@ extern "C" void oracle_cs_shade_grad_lights_f64(const oracle_cs_view* v, uint32_
             point_light(q, P.lp, P.col, P.r, falloff, o);
             for (int k = 0; k < 3; ++k)
                 for (int t = 0; t < NT; ++t) g[t] += (double)grad[3 * px + k] * o[k].d[t];
-            for (int t = 0; t < NT; ++t) {
+            for (int t = 0; t < NT && h > 0.0; ++t) {
                 for (int sgn = 0; sgn < 2; ++sgn) {
                     double th[NT];
                     for (int u = 0; u < NT; ++u) th[u] = base[u];

@@ -145,3 +145,43 @@ def test_shade_backward_full_size_config(cuda):
     fd4_err = np.linalg.norm(fd4[nz] - ref[nz], axis=1) / norm
     assert np.median(fd6_err) < 1e-6 and fd6_err.max() < 1e-3, (np.median(fd6_err), fd6_err.max())
     assert np.median(fd4_err) < 1e-3 and fd4_err.max() < 2e-2, (np.median(fd4_err), fd4_err.max())
+
+
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_cluster_and_shade_one_call(cuda, use_graph):
+    """cluster_and_shade::operator(): clustering and shading in one call of the context (one graph per
+    frame shape, replayed on the second call): the light lists equal the oracle's, the image equals the
+    FP64 oracle shading of those lists within the bounds of test_shade_forward."""
+    W, H, L = 1280, 720, 2048
+    s = shade_scene.make(W, H, L, seed=51)
+    frame, d, gb, ll = device_inputs(s, cuda)
+    ctx = cs.cluster_and_shade(W, H, L, 1 << 23, use_graph=use_graph)
+    stream = torch.cuda.Stream(device=cuda)
+    # the context clusters with the G-buffer's own normals
+    gb = cs.gbuffer(d["depth"], d["normals"], d["albedo"], d["rough"], d["metal"])
+    for _ in range(2):
+        out = torch.full((W * H * 3,), -7.0, dtype=torch.float32, device=cuda)
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            ctx(stream, s["view"], W, H, gb, d["pos"], d["lights"], L, out, falloff="ref", mode="color")
+        stream.synchronize()
+        o = ctx.outputs()
+        U = int(cs.read_device(o.key_count, 1)[0])
+        keys, refs = oracle.cs_find_unique_clusters(s["depth"], s["normals"], W, H, s["view"], 0)
+        assert np.array_equal(cs.read_device(o.cluster_keys, U), keys)
+        assert np.array_equal(cs.read_device(o.cluster_refs, W * H), refs)
+        vp, bvh, lidx = oracle.cs_light_bvh(s["pos"], s["lights"], L, s["view"], 15)
+        counts, offsets, indices, total = oracle.cs_assign_lights(keys, W, H, s["view"], bvh, L, lidx, vp)
+        assert int(cs.read_device(o.total, 1)[0]) == total > 0
+        assert np.array_equal(cs.read_device(o.counts, U), counts)
+        assert np.array_equal(cs.read_device(o.indices, total), indices)
+        got = out.cpu().numpy().astype(np.float64)
+        exp, shaded = oracle.cs_shade_f64(s["view"], W, H, shade_scene.gb(s), (refs, counts, offsets, indices),
+                                          s["pos"], s["lights"], L, cs.FALLOFF["ref"], cs.SHADE_MODE["color"])
+        sh = np.repeat(shaded, 3)
+        assert np.all(got[~sh] == -7.0) and shaded.mean() > 0.5
+        assert np.linalg.norm(got[sh] - exp[sh]) / np.linalg.norm(exp[sh]) < 1e-5
+        rel = (np.abs(got - exp) / np.maximum(np.abs(exp), 1e-3)).reshape(-1, 3).max(1)
+        s2 = dict(s, normals=s["normals"])
+        nv = shade_scene.ndotv(s2)
+        assert rel[shaded & (nv >= 1e-3)].max() < 5e-4 and rel[shaded].max() < 1e-2

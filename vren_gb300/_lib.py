@@ -133,6 +133,7 @@ PROTOTYPES_CS: dict[str, tuple] = {
     "vren_cs_set_options": (i32, [vp, vp]),
     "vren_cs_cluster": (i32, [vp, vp, vp, u32, u32, i32, vp, vp, vp, vp, u32]),
     "vren_cs_get_outputs": (i32, [vp, vp]),
+    "vren_cs_cluster_and_shade": (i32, [vp, vp, vp, u32, u32, i32, vp, vp, vp, u32, vp, u32, i32, i32, vp]),
     "vren_cs_cluster_host": (i32, [vp, vp, vp, u32, u32, i32, vp, vp, vp, vp, u32, vp, vp, C.c_uint64]),
     "vren_cs_shade": (i32, [vp, vp, u32, u32, vp, vp, vp, vp, u32, vp, u32, i32, i32, vp]),
     "vren_cs_shade_backward_scratch_bytes": (sz, [u32, u32]),

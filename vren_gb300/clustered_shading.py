@@ -265,6 +265,19 @@ class cluster_and_shade:
                                          lists_out.data_ptr() if lists_out is not None else None,
                                          lists_out.numel() if lists_out is not None else 0), "cs_cluster_host")
 
+    def __call__(self, stream, view: View, width: int, height: int, gbuf: "GBuffer", positions, lights,
+                 light_count: int, out: torch.Tensor, directional=None, directional_count: int = 0,
+                 falloff: str = "ref", mode: str = "color", offscreen: str = "wrap"):
+        """cluster_and_shade::operator() (clustered_shading.cpp:924-1172): the clustering stages, then
+        shade over this context's light lists into `out` (f32x3 per pixel), one graph per frame shape."""
+        if self._opts.normal_format != 0:
+            o = self._opts
+            self.set_options(o.morton_bits, bool(o.use_graph), o.sort_digit_bits, o.assign_warps, 0)
+        check(lib().vren_cs_cluster_and_shade(self._h, _stream(stream), C.byref(view), width, height,
+                                              OFFSCREEN[offscreen], C.byref(gbuf), _addr(positions), _addr(lights),
+                                              light_count, _addr(directional), directional_count, FALLOFF[falloff],
+                                              SHADE_MODE[mode], _addr(out)), "cs_cluster_and_shade")
+
     def outputs(self) -> Outputs:
         o = Outputs()
         check(lib().vren_cs_get_outputs(self._h, C.byref(o)), "cs_get_outputs")

@@ -1223,10 +1223,39 @@ struct vren_cluster_and_shade {
         void* lists_out;
         uint64_t lists_cap;
     } host_key{};
+    // vren_cs_cluster_and_shade: the graph of the last clustered-and-shaded frame shape
+    cudaGraphExec_t shade_graph = nullptr;
+    struct ShadeKey {
+        Key k;
+        vren_cs_gbuffer gb;
+        const void* dir;
+        uint32_t ndir;
+        int falloff, mode;
+        void* out;
+    } shade_key{};
 };
 
 namespace {
 size_t align256(size_t x) { return (x + 255) / 256 * 256; }
+
+// The key a captured frame graph is replayed under, compared byte for byte: zero-filled first so that
+// padding bytes compare equal too.
+void fill_key(vren_cluster_and_shade::Key& k, const vren_cluster_and_shade* cs, uint32_t W, uint32_t H, uint32_t L,
+              int offscreen, const void* depth, const void* normals, const void* pos, const void* lights,
+              cudaStream_t st)
+{
+    std::memset(&k, 0, sizeof(k));
+    k.w = W;
+    k.h = H;
+    k.L = L;
+    k.off = (uint32_t)offscreen;
+    k.depth = depth;
+    k.normals = normals;
+    k.pos = pos;
+    k.lights = lights;
+    k.stream = st;
+    k.opt = cs->opt;
+}
 
 int cs_enqueue(vren_cluster_and_shade* cs, cudaStream_t st, uint32_t W, uint32_t H, const float* depth,
                const float* normals, const float* positions, const float* lights, uint32_t L)
@@ -1349,6 +1378,7 @@ extern "C" void vren_cs_destroy(vren_cluster_and_shade* cs)
     if (!cs) return;
     if (cs->graph) cudaGraphExecDestroy(cs->graph);
     if (cs->host_graph) cudaGraphExecDestroy(cs->host_graph);
+    if (cs->shade_graph) cudaGraphExecDestroy(cs->shade_graph);
     if (cs->aux) cudaStreamDestroy(cs->aux);
     if (cs->up) cudaStreamDestroy(cs->up);
     for (cudaEvent_t e : {cs->ev_fork, cs->ev_bvh, cs->ev_join, cs->ev_join_up, cs->ev_band[0],
@@ -1376,6 +1406,10 @@ extern "C" int vren_cs_set_options(vren_cluster_and_shade* cs, const vren_cs_opt
     if (cs->host_graph) {
         cudaGraphExecDestroy(cs->host_graph);
         cs->host_graph = nullptr;
+    }
+    if (cs->shade_graph) {
+        cudaGraphExecDestroy(cs->shade_graph);
+        cs->shade_graph = nullptr;
     }
     return VREN_OK;
 }
@@ -1487,8 +1521,8 @@ extern "C" int vren_cs_cluster(vren_cluster_and_shade* cs, vren_stream_t s, cons
     cudaStream_t st = as_stream(s);
     int rc = refresh_frame(cs, st, view, width, height, offscreen);
     if (rc != VREN_OK) return rc;
-    const vren_cluster_and_shade::Key key{width, height, light_count, (uint32_t)offscreen, depth, normals,
-                                          light_positions, point_lights, st, cs->opt};
+    vren_cluster_and_shade::Key key;
+    fill_key(key, cs, width, height, light_count, offscreen, depth, normals, light_positions, point_lights, st);
     const bool use_graph = cs->opt.use_graph && st != nullptr;
     if (!use_graph) return cs_enqueue(cs, st, width, height, depth, normals, light_positions, point_lights, light_count);
     if (cs->graph && std::memcmp(&key, &cs->graph_key, sizeof(key)) == 0) {
@@ -1514,7 +1548,7 @@ extern "C" int vren_cs_cluster(vren_cluster_and_shade* cs, vren_stream_t s, cons
         cs->graph = nullptr;
         return VREN_ERR_CUDA;
     }
-    cs->graph_key = key;
+    std::memcpy(&cs->graph_key, &key, sizeof(key));
     VREN_CUDA_TRY(cudaGraphLaunch(cs->graph, st));
     return VREN_OK;
 }
@@ -1547,9 +1581,12 @@ extern "C" int vren_cs_cluster_host(vren_cluster_and_shade* cs, vren_stream_t s,
     }
     int rc = refresh_frame(cs, st, view, width, height, offscreen);
     if (rc != VREN_OK) return rc;
-    const vren_cluster_and_shade::HostKey key{{width, height, light_count, (uint32_t)offscreen, depth, normals,
-                                               light_positions, point_lights, st, cs->opt},
-                                              cluster_refs_out, lists_out, lists_capacity};
+    vren_cluster_and_shade::HostKey key;
+    std::memset(&key, 0, sizeof(key));
+    fill_key(key.k, cs, width, height, light_count, offscreen, depth, normals, light_positions, point_lights, st);
+    key.refs_out = cluster_refs_out;
+    key.lists_out = lists_out;
+    key.lists_cap = lists_capacity;
     const bool use_graph = cs->opt.use_graph && st != nullptr;
     if (!use_graph)
         return cs_enqueue_host(cs, st, width, height, depth, normals, light_positions, point_lights, light_count,
@@ -1578,8 +1615,70 @@ extern "C" int vren_cs_cluster_host(vren_cluster_and_shade* cs, vren_stream_t s,
         cs->host_graph = nullptr;
         return VREN_ERR_CUDA;
     }
-    cs->host_key = key;
+    std::memcpy(&cs->host_key, &key, sizeof(key));
     VREN_CUDA_TRY(cudaGraphLaunch(cs->host_graph, st));
+    return VREN_OK;
+}
+
+extern "C" int vren_cs_cluster_and_shade(vren_cluster_and_shade* cs, vren_stream_t s, const vren_cs_view* view,
+                                         uint32_t width, uint32_t height, int offscreen, const vren_cs_gbuffer* gbuffer,
+                                         const float* light_positions, const float* point_lights, uint32_t light_count,
+                                         const float* directional_lights, uint32_t directional_count, int falloff,
+                                         int output_mode, float* out_rgb)
+{
+    if (!cs || !view || !gbuffer || !gbuffer->depth || !gbuffer->normals || !out_rgb) return VREN_ERR_ARG;
+    if (cs->opt.normal_format != VREN_CS_NORMALS_F32X3) return VREN_ERR_ARG;  // the shading kernels read f32x3
+    if (width > cs->max_w || height > cs->max_h || light_count > cs->max_lights) return VREN_ERR_CAPACITY;
+    if (light_count > 0 && (!light_positions || !point_lights)) return VREN_ERR_ARG;
+    if (falloff != VREN_CS_FALLOFF_REF && falloff != VREN_CS_FALLOFF_WINDOWED_INV_SQ) return VREN_ERR_ARG;
+    if (output_mode != VREN_CS_SHADE_COLOR && output_mode != VREN_CS_SHADE_RADIANCE) return VREN_ERR_ARG;
+    cudaStream_t st = as_stream(s);
+    int rc = refresh_frame(cs, st, view, width, height, offscreen);
+    if (rc != VREN_OK) return rc;
+    const vren_cs_light_lists lists{cs->refs, cs->counts, cs->offsets, cs->indices};
+    auto enqueue = [&]() -> int {
+        int r = cs_enqueue(cs, st, width, height, gbuffer->depth, gbuffer->normals, light_positions, point_lights,
+                           light_count);
+        if (r != VREN_OK) return r;
+        return vren_cs_shade(st, cs->frame, width, height, gbuffer, &lists, light_positions, point_lights, light_count,
+                             directional_lights, directional_count, falloff, output_mode, out_rgb);
+    };
+    if (!(cs->opt.use_graph && st != nullptr)) return enqueue();
+    vren_cluster_and_shade::ShadeKey key;
+    std::memset(&key, 0, sizeof(key));
+    fill_key(key.k, cs, width, height, light_count, offscreen, gbuffer->depth, gbuffer->normals, light_positions,
+             point_lights, st);
+    key.gb = *gbuffer;
+    key.dir = directional_lights;
+    key.ndir = directional_count;
+    key.falloff = falloff;
+    key.mode = output_mode;
+    key.out = out_rgb;
+    if (cs->shade_graph && std::memcmp(&key, &cs->shade_key, sizeof(key)) == 0) {
+        VREN_CUDA_TRY(cudaGraphLaunch(cs->shade_graph, st));
+        return VREN_OK;
+    }
+    if (cs->shade_graph) {
+        cudaGraphExecDestroy(cs->shade_graph);
+        cs->shade_graph = nullptr;
+    }
+    cudaGraph_t g;
+    VREN_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    rc = enqueue();
+    cudaError_t e = cudaStreamEndCapture(st, &g);
+    if (rc != VREN_OK) {
+        if (e == cudaSuccess) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return VREN_ERR_CUDA;
+    e = cudaGraphInstantiate(&cs->shade_graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        cs->shade_graph = nullptr;
+        return VREN_ERR_CUDA;
+    }
+    std::memcpy(&cs->shade_key, &key, sizeof(key));
+    VREN_CUDA_TRY(cudaGraphLaunch(cs->shade_graph, st));
     return VREN_OK;
 }
 
