@@ -741,7 +741,7 @@ def shade_profile_setup(dev, stream, ctx):
     counts = cs.read_device(out.counts, U)
     pairs = int(counts[refs].astype(np.int64).sum()) if U else 0
     gb = cs.gbuffer(d_depth, d_n, d_alb, d_r, d_m)
-    ll = cs.light_lists(out.cluster_refs, out.counts, out.offsets, out.indices)
+    ll = cs.light_lists(out.cluster_refs, out.counts, out.offsets, out.indices, out.index_capacity)
     img = torch.empty(W_ * H_ * 3, dtype=torch.float32, device=dev)
     fwd = cs.shade("windowed_inv_sq", "radiance")
     bwd = cs.shade_backward("windowed_inv_sq")

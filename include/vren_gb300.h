@@ -93,10 +93,13 @@ int vren_test_withhold_scan_status(uint32_t tile_plus_one);
  *   VREN_TUNE_RADIX_PERSISTENT  sort passes over keys or pairs whose input starts 16-byte aligned:
  *                          1 = persistent grid whose producer warp streams tiles into shared memory
  *                          by bulk copies and publishes their digit counts on arrival, 0 = one CTA
- *                          per tile (ballot ranking, 15/16 keys per thread only) */
+ *                          per tile (ballot ranking, 15/16 keys per thread only)
+ *   VREN_TUNE_FUC_FUSED    find_unique_cluster_list in the context's device frames: 0 = one kernel
+ *                          (tiles taken by ticket, offsets by look-back over the tile counts; the
+ *                          default), 1 = tiles, tile-count scan and fix-up as three kernels */
 enum { VREN_TUNE_SCAN_SLICES = 0, VREN_TUNE_SPIN_POLLS = 1, VREN_TUNE_RADIX_RANK = 2, VREN_TUNE_RADIX_ITEMS = 3,
        VREN_TUNE_SCAN_STAGED = 4, VREN_TUNE_REDUCE_FORM = 5, VREN_TUNE_LIGHT_BVH_CLUSTER = 6,
-       VREN_TUNE_ASSIGN_FUSED = 7, VREN_TUNE_RADIX_PERSISTENT = 8, VREN_TUNE_COUNT = 9 };
+       VREN_TUNE_ASSIGN_FUSED = 7, VREN_TUNE_RADIX_PERSISTENT = 8, VREN_TUNE_FUC_FUSED = 9, VREN_TUNE_COUNT = 10 };
 int vren_tuning_set(int knob, int value);
 int vren_tuning_get(int knob);
 
@@ -427,11 +430,17 @@ typedef struct vren_cs_gbuffer {
     const float* metallic;  /* f32[W*H] */
 } vren_cs_gbuffer;
 
+/* index_capacity: the entries `indices` holds (the assignment's index capacity).  After an assignment
+ * that ran out of index capacity (VREN_ERR_CAPACITY), counts and offsets describe lists that reach
+ * past it: the shading kernels cut every list there instead of reading beyond the buffer (and record
+ * VREN_ERR_CAPACITY again).  Must be non-zero when lights are shaded. */
 typedef struct vren_cs_light_lists {
     const uint32_t* cluster_refs; /* u32[W*H] */
     const uint32_t* counts;       /* per cluster */
     const uint32_t* offsets;      /* per cluster */
     const uint32_t* indices;      /* light indices */
+    uint32_t index_capacity;      /* entries of indices */
+    uint32_t reserved;
 } vren_cs_light_lists;
 
 /* directional_lights: {float direction[3], pad, color[3], pad}[count] (gpu_repr.hpp:66-70) */
@@ -515,17 +524,19 @@ typedef struct vren_debug_vertex {
     uint32_t color; /* 0xRRGGBB */
 } vren_debug_vertex;
 
-/* show_clusters (show_clusters.comp:72-124): rgba (float4 per pixel, row-major width x height,
+/* show_clusters (show_clusters.comp:68-125): rgba (float4 per pixel, row-major width x height,
  * 16-byte aligned) = the colour of each pixel's cluster for `mode` (VREN_SHOW_CLUSTERS_*; any other
  * value draws red, as the shader does); tiles = ceil(size / 32) as in clustered_shading_debug.cpp:68-71.
  * A reference >= min(*key_count, max_clusters) is drawn magenta (the shader reads out of bounds).
- * counts/offsets are needed by the light modes, indices by LIGHT_INDICES.  scratch: 16-byte aligned,
+ * counts/offsets are needed by the light modes, indices by LIGHT_INDICES; index_capacity = the
+ * entries `indices` holds (lists reaching past it, after an assignment that ran out of capacity, are
+ * cut there and VREN_ERR_CAPACITY recorded).  scratch: 16-byte aligned,
  * vren_cs_show_clusters_scratch_bytes(max_clusters). */
 size_t vren_cs_show_clusters_scratch_bytes(uint32_t max_clusters);
 int vren_cs_show_clusters(vren_stream_t s, int mode, uint32_t width, uint32_t height, const uint32_t* cluster_refs,
                           const uint32_t* cluster_keys, const uint32_t* key_count, uint32_t max_clusters,
-                          const uint32_t* counts, const uint32_t* offsets, const uint32_t* indices, float* rgba,
-                          void* scratch);
+                          const uint32_t* counts, const uint32_t* offsets, const uint32_t* indices,
+                          uint32_t index_capacity, float* rgba, void* scratch);
 /* show_clusters_geometry (show_clusters_geometry.comp:55-110, debug.glsl): for each of the first
  * min(*key_count, max_clusters) clusters, 32 vertices at vertices[32 c]: its view-space box as 12 lines
  * (white; black for keys without a normal bin) and an arrow of length 0.01 along its normal bin (green
@@ -634,7 +645,10 @@ int vren_cs_batch_reserve(vren_cs_batch* b, const vren_cs_batch_frame* frames, u
 int vren_cs_batch_set_options(vren_cs_batch* b, const vren_cs_batch_options* options);
 int vren_cs_batch_get_options(const vren_cs_batch* b, vren_cs_batch_options* options);
 /* Enqueues the batch on stream s (VREN_ERR_CAPACITY when it exceeds the reserved arena).  The
- * radix and scan tile variants of the options are applied to this batch's launches only. */
+ * radix and scan tile variants of the options are applied to this batch's launches only.  Runs of
+ * one batch object may be enqueued on different streams: when the frames' parameters change, the new
+ * ones are uploaded after the previous upload has been read and the previous run (on whatever
+ * stream) has ended.  The outputs of a run are overwritten by the next run of the same object. */
 int vren_cs_batch_run(vren_cs_batch* b, vren_stream_t s, const vren_cs_batch_frame* frames, uint32_t count);
 /* Times candidate option sets on these frames (digit bits x radix tile x scan tile x traversal
  * warps), keeps the fastest, and caches it per shape bucket (frame count, log2 of the total pixels

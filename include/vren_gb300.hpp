@@ -492,7 +492,8 @@ public:
         m_scratch.grow(vren_cs_show_clusters_scratch_bytes(outputs.key_capacity));
         vren::check(vren_cs_show_clusters(stream, mode, width, height, outputs.cluster_refs, outputs.cluster_keys,
                                           outputs.key_count, outputs.key_capacity, outputs.counts, outputs.offsets,
-                                          outputs.indices, rgba_output.at<float>(), m_scratch.m_ptr),
+                                          outputs.indices, outputs.index_capacity, rgba_output.at<float>(),
+                                          m_scratch.m_ptr),
                     "show_clusters");
     }
 

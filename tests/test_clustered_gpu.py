@@ -389,22 +389,37 @@ def check_context_outputs(ctx, W, H, view, depth, normals, pos, li, L):
     assert np.array_equal(cs.read_device(o.indices, et), ei)
 
 
+@pytest.mark.parametrize("fuc_form", [0, 1])  # unique clusters: one kernel (look-back) / three kernels
 @pytest.mark.parametrize("slicing", ["ref", "fixed32"])
-def test_cluster_and_shade_context_1080p(cuda, slicing):
-    """The benchmark frame through the context (graph replay): 1920x1080, 16,384 lights, both slicings."""
-    W, H, L = 1920, 1080, 16384
-    view = make_view(W, H, slicing)
-    depth, normals = scene.depth_planes(W + L, W, H)
-    pos, li = scene.lights(L, L, W, H)
-    ctx = cs.cluster_and_shade(W, H, L, 1 << 22)
-    stream = torch.cuda.Stream()
-    bufs = [to_dev(x, cuda) for x in (depth, normals, pos, li)]
-    torch.cuda.synchronize()
-    for _ in range(2):
+def test_cluster_and_shade_context_1080p(cuda, slicing, fuc_form):
+    """The benchmark frame through the context (graph replay): 1920x1080, 16,384 lights, both slicings,
+    both forms of the unique-cluster stage; a dense frame follows on the same context."""
+    lib = vg.lib()
+    knob = vg._lib.TUNE["fuc_fused"]
+    assert lib.vren_tuning_set(knob, fuc_form) == 0
+    try:
+        W, H, L = 1920, 1080, 16384
+        view = make_view(W, H, slicing)
+        depth, normals = scene.depth_planes(W + L, W, H)
+        pos, li = scene.lights(L, L, W, H)
+        ctx = cs.cluster_and_shade(W, H, L, 1 << 22)
+        stream = torch.cuda.Stream()
+        bufs = [to_dev(x, cuda) for x in (depth, normals, pos, li)]
+        torch.cuda.synchronize()
+        for _ in range(2):
+            with torch.cuda.stream(stream):
+                ctx.cluster(stream, view, W, H, *bufs, L)
+            stream.synchronize()
+            check_context_outputs(ctx, W, H, view, depth, normals, pos, li, L)
+        dpos, dli = dense_lights(5, L)
+        dbufs = bufs[:2] + [to_dev(x, cuda) for x in (dpos, dli)]
+        torch.cuda.synchronize()
         with torch.cuda.stream(stream):
-            ctx.cluster(stream, view, W, H, *bufs, L)
+            ctx.cluster(stream, view, W, H, *dbufs, L)
         stream.synchronize()
-        check_context_outputs(ctx, W, H, view, depth, normals, pos, li, L)
+        check_context_outputs(ctx, W, H, view, depth, normals, dpos, dli, L)
+    finally:
+        lib.vren_tuning_set(knob, 0)
 
 
 @pytest.mark.parametrize("use_graph", [False, True])

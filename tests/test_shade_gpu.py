@@ -155,7 +155,7 @@ def test_cluster_and_shade_one_call(cuda, use_graph):
     W, H, L = 1280, 720, 2048
     s = shade_scene.make(W, H, L, seed=51)
     frame, d, gb, ll = device_inputs(s, cuda)
-    ctx = cs.cluster_and_shade(W, H, L, 1 << 23, use_graph=use_graph)
+    ctx = cs.cluster_and_shade(W, H, L, 1 << 25, use_graph=use_graph)  # the frame assigns 23.3M pairs
     stream = torch.cuda.Stream(device=cuda)
     # the context clusters with the G-buffer's own normals
     gb = cs.gbuffer(d["depth"], d["normals"], d["albedo"], d["rough"], d["metal"])
@@ -185,3 +185,34 @@ def test_cluster_and_shade_one_call(cuda, use_graph):
         s2 = dict(s, normals=s["normals"])
         nv = shade_scene.ndotv(s2)
         assert rel[shaded & (nv >= 1e-3)].max() < 5e-4 and rel[shaded].max() < 1e-2
+
+
+def test_cluster_and_shade_index_capacity_overflow(cuda):
+    """The same frame with an index capacity of 2^20 (it assigns 23.3M pairs): the assignment records
+    VREN_ERR_CAPACITY and drops what does not fit; shading and the light-index debug view then read the
+    lists only up to the capacity (each list cut there, the error recorded again) instead of reading
+    past the index buffer."""
+    import vren_gb300 as vg
+    import vren_gb300.cluster_debug as cd
+    from vren_gb300 import _lib
+
+    W, H, L = 1280, 720, 2048
+    s = shade_scene.make(W, H, L, seed=51)
+    frame, d, gb, ll = device_inputs(s, cuda)
+    ctx = cs.cluster_and_shade(W, H, L, 1 << 20)
+    stream = torch.cuda.Stream(device=cuda)
+    gb = cs.gbuffer(d["depth"], d["normals"], d["albedo"], d["rough"], d["metal"])
+    out = torch.full((W * H * 3,), -7.0, dtype=torch.float32, device=cuda)
+    torch.cuda.synchronize()
+    vg.device_error(clear=True)
+    with torch.cuda.stream(stream):
+        ctx(stream, s["view"], W, H, gb, d["pos"], d["lights"], L, out, falloff="ref", mode="color")
+    stream.synchronize()
+    assert vg.device_error(clear=True) == _lib.VREN_ERR_CAPACITY
+    o = ctx.outputs()
+    assert int(cs.read_device(o.total, 1)[0]) > o.index_capacity == 1 << 20
+    assert torch.isfinite(out).all()
+    img = cd.show_clusters()(stream, "light_indices", W, H, o, device=cuda)
+    stream.synchronize()
+    assert vg.device_error(clear=True) == _lib.VREN_ERR_CAPACITY
+    assert torch.isfinite(img).all()

@@ -14,7 +14,7 @@ from vren_gb300 import _lib
 pytestmark = pytest.mark.gpu
 
 SHORT_WAIT = 4096  # polling rounds (a few milliseconds at most with the nanosleep back-off)
-SCAN_FORM_KNOB = 4  # VREN_TUNE_SCAN_STAGED: 0 automatic, 1 one tile per CTA in registers
+SCAN_FORM_KNOB = _lib.TUNE["scan_staged"]  # 0 automatic, 1 one tile per CTA in registers
 
 
 def run_scan(lib, buf, n, scratch):

@@ -18,7 +18,8 @@ VREN_ERR_CUDA = 4
 VREN_ERR_STATE = 5
 
 REDUCE_OPS = {"add": 0, "min": 1, "max": 2}
-TUNE = {"scan_slices": 0, "spin_polls": 1, "radix_rank": 2, "radix_items": 3, "scan_staged": 4, "reduce_form": 5, "light_bvh_cluster": 6, "assign_fused": 7, "radix_persistent": 8}
+TUNE = {"scan_slices": 0, "spin_polls": 1, "radix_rank": 2, "radix_items": 3, "scan_staged": 4, "reduce_form": 5,
+        "light_bvh_cluster": 6, "assign_fused": 7, "radix_persistent": 8, "fuc_fused": 9}
 
 u32, u64, i32, sz, vp, fp = C.c_uint32, C.c_uint64, C.c_int, C.c_size_t, C.c_void_p, C.c_float
 
@@ -63,7 +64,7 @@ PROTOTYPES: dict[str, tuple] = {
     "vren_depth_pyramid_scratch_bytes": (sz, [u32, u32]),
     "vren_depth_pyramid_copy_and_reduce": (i32, [vp, vp, u32, u32, vp, vp]),
     "vren_cs_show_clusters_scratch_bytes": (sz, [u32]),
-    "vren_cs_show_clusters": (i32, [vp, i32, u32, u32, vp, vp, vp, u32, vp, vp, vp, vp, vp]),
+    "vren_cs_show_clusters": (i32, [vp, i32, u32, u32, vp, vp, vp, u32, vp, vp, vp, u32, vp, vp]),
     "vren_cs_show_clusters_geometry": (i32, [vp, vp, vp, vp, u32, vp]),
     "vren_kd_tree_build": (sz, [vp, sz, vp, sz, vp, sz, sz]),
     "vren_kd_tree_depth": (u32, [vp, sz]),

@@ -42,8 +42,8 @@ class show_clusters:
             self._scratch = alloc_scratch(need, rgba.device)
         check(lib().vren_cs_show_clusters(_stream(stream), _mode(mode), width, height, outputs.cluster_refs,
                                           outputs.cluster_keys, outputs.key_count, outputs.key_capacity,
-                                          outputs.counts, outputs.offsets, outputs.indices, rgba.data_ptr(),
-                                          self._scratch.data_ptr()), "show_clusters")
+                                          outputs.counts, outputs.offsets, outputs.indices, outputs.index_capacity,
+                                          rgba.data_ptr(), self._scratch.data_ptr()), "show_clusters")
         return rgba
 
 

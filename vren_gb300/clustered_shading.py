@@ -402,7 +402,8 @@ class GBuffer(C.Structure):
 
 
 class LightLists(C.Structure):
-    _fields_ = [(n, C.c_void_p) for n in ("cluster_refs", "counts", "offsets", "indices")]
+    _fields_ = [(n, C.c_void_p) for n in ("cluster_refs", "counts", "offsets", "indices")] + \
+               [("index_capacity", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 def _addr(x):
@@ -415,8 +416,13 @@ def gbuffer(depth, normals, albedo, roughness, metallic) -> GBuffer:
     return GBuffer(*(_addr(t) for t in (depth, normals, albedo, roughness, metallic)))
 
 
-def light_lists(cluster_refs, counts, offsets, indices) -> LightLists:
-    return LightLists(*(_addr(t) for t in (cluster_refs, counts, offsets, indices)))
+def light_lists(cluster_refs, counts, offsets, indices, index_capacity: int | None = None) -> LightLists:
+    """index_capacity: the entries `indices` holds (a tensor's size by default; required for an address)."""
+    if index_capacity is None:
+        if not isinstance(indices, torch.Tensor):
+            raise ValueError("light_lists: index_capacity is required when indices is an address")
+        index_capacity = indices.numel()
+    return LightLists(*(_addr(t) for t in (cluster_refs, counts, offsets, indices)), int(index_capacity), 0)
 
 
 class shade:

@@ -432,6 +432,9 @@ struct vren_cs_batch {
     // second stream: the light BVHs are built beside the unique-cluster stage
     cudaStream_t aux = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_bvh = nullptr;
+    // the last upload of the staged block and the end of the last run, on whatever stream they were
+    // enqueued: a new staging waits for both before it overwrites the pinned and the device copies
+    cudaEvent_t ev_uploaded = nullptr, ev_done = nullptr;
     // layout of the current batch
     uint32_t n = 0, total_chunks = 0, total_leaf_blocks = 0, total_tiles = 0, total_lights = 0;
     uint64_t total_keys = 0;
@@ -580,12 +583,14 @@ int stage_batch(vren_cs_batch* b, cudaStream_t st, const vren_cs_batch_frame* fr
     b->total_keys = key;
     b->frame_bits = count > 1 ? ceil_log2(count) : 0u;
     if (b->uploaded.size() != staged.size() || std::memcmp(b->uploaded.data(), staged.data(), staged.size()) != 0) {
-        VREN_CUDA_TRY(cudaStreamSynchronize(st));  // an earlier upload may still read the pinned copy
+        VREN_CUDA_TRY(cudaEventSynchronize(b->ev_uploaded));  // an earlier upload may still read the pinned copy
+        VREN_CUDA_TRY(cudaStreamWaitEvent(st, b->ev_done, 0));  // an earlier run may still read the device copy
         std::memcpy(b->host, staged.data(), staged.size());
         VREN_CUDA_TRY(cudaMemcpyAsync(b->desc, b->host, desc_bytes, cudaMemcpyHostToDevice, st));
         VREN_CUDA_TRY(cudaMemcpyAsync(b->prefixes, b->host + desc_bytes, pref_bytes, cudaMemcpyHostToDevice, st));
         VREN_CUDA_TRY(cudaMemcpyAsync(b->frames, b->host + desc_bytes + pref_bytes, frame_bytes,
                                       cudaMemcpyHostToDevice, st));
+        VREN_CUDA_TRY(cudaEventRecord(b->ev_uploaded, st));
         b->uploaded.swap(staged);
     }
     return VREN_OK;
@@ -698,7 +703,9 @@ extern "C" int vren_cs_batch_create(vren_cs_batch** out)
     auto* b = new vren_cs_batch();
     if (cudaStreamCreateWithFlags(&b->aux, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&b->ev_bvh, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&b->ev_bvh, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_uploaded, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_done, cudaEventDisableTiming) != cudaSuccess) {
         vren_cs_batch_destroy(b);
         return VREN_ERR_CUDA;
     }
@@ -713,6 +720,8 @@ extern "C" void vren_cs_batch_destroy(vren_cs_batch* b)
     if (b->aux) cudaStreamDestroy(b->aux);
     if (b->ev_fork) cudaEventDestroy(b->ev_fork);
     if (b->ev_bvh) cudaEventDestroy(b->ev_bvh);
+    if (b->ev_uploaded) cudaEventDestroy(b->ev_uploaded);
+    if (b->ev_done) cudaEventDestroy(b->ev_done);
     cudaFree(b->arena);
     cudaFreeHost(b->host);
     delete b;
@@ -842,6 +851,13 @@ extern "C" int vren_cs_batch_get_options(const vren_cs_batch* b, vren_cs_batch_o
     return VREN_OK;
 }
 
+// Marks the end of a run on its stream (the next staging waits for it).
+static int mark_done(vren_cs_batch* b, cudaStream_t st, int rc)
+{
+    if (rc == VREN_OK && cudaEventRecord(b->ev_done, st) != cudaSuccess) return VREN_ERR_CUDA;
+    return rc;
+}
+
 extern "C" int vren_cs_batch_run(vren_cs_batch* b, vren_stream_t s, const vren_cs_batch_frame* fr, uint32_t count)
 {
     if (!b || (count > 0 && !fr)) return VREN_ERR_ARG;
@@ -860,7 +876,7 @@ extern "C" int vren_cs_batch_run(vren_cs_batch* b, vren_stream_t s, const vren_c
     int rc = stage_batch(b, st, fr, count);
     if (rc != VREN_OK) return rc;
     const bool use_graph = b->opt.use_graph && st != nullptr;
-    if (!use_graph) return enqueue_with_options(b, st);
+    if (!use_graph) return mark_done(b, st, enqueue_with_options(b, st));
     // Graph key: every frame's shape and buffers, the options and the stream.  Cameras are not part
     // of it: the frame blocks the kernels read are uploaded above, outside the graph.
     struct FrameKey {
@@ -878,10 +894,8 @@ extern "C" int vren_cs_batch_run(vren_cs_batch* b, vren_stream_t s, const vren_c
     }
     std::memcpy(key.data() + sizeof(FrameKey) * count, &b->opt, sizeof(b->opt));
     std::memcpy(key.data() + key.size() - sizeof(st), &st, sizeof(st));
-    if (b->graph && key == b->graph_key) {
-        VREN_CUDA_TRY(cudaGraphLaunch(b->graph, st));
-        return VREN_OK;
-    }
+    if (b->graph && key == b->graph_key)
+        return mark_done(b, st, cudaGraphLaunch(b->graph, st) == cudaSuccess ? VREN_OK : VREN_ERR_CUDA);
     drop_graph(b);
     cudaGraph_t g;
     VREN_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -899,8 +913,7 @@ extern "C" int vren_cs_batch_run(vren_cs_batch* b, vren_stream_t s, const vren_c
         return VREN_ERR_CUDA;
     }
     b->graph_key.swap(key);
-    VREN_CUDA_TRY(cudaGraphLaunch(b->graph, st));
-    return VREN_OK;
+    return mark_done(b, st, cudaGraphLaunch(b->graph, st) == cudaSuccess ? VREN_OK : VREN_ERR_CUDA);
 }
 
 extern "C" int vren_cs_batch_autotune(vren_cs_batch* b, vren_stream_t s, const vren_cs_batch_frame* fr, uint32_t count,

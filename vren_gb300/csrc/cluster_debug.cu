@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(256) show_clusters_colour_kernel(int mode, uin
                                                                    const uint32_t* __restrict__ counts,
                                                                    const uint32_t* __restrict__ offsets,
                                                                    const uint32_t* __restrict__ indices,
-                                                                   float4* __restrict__ colours)
+                                                                   uint32_t index_cap, float4* __restrict__ colours)
 {
     const uint32_t U = min(*key_count, max_clusters);
     const uint32_t lane = threadIdx.x & 31;
@@ -81,7 +81,12 @@ __global__ void __launch_bounds__(256) show_clusters_colour_kernel(int mode, uin
         }
         case VREN_SHOW_CLUSTERS_LIGHT_OFFSETS: col = grey(hash01(offsets[c])); break;
         case VREN_SHOW_CLUSTERS_LIGHT_INDICES: {
-            const uint32_t n = counts[c], o = offsets[c];
+            uint32_t n = counts[c];
+            const uint32_t o = offsets[c];
+            if (o >= index_cap || n > index_cap - o) {  // a list cut by the assignment's index capacity
+                n = o >= index_cap ? 0u : index_cap - o;
+                if (lane == 0) VREN_RECORD_ERROR(VREN_ERR_CAPACITY);
+            }
             uint32_t h = 0;
             for (uint32_t i = lane; i < n; i += 32) h ^= indices[o + i];
 #pragma unroll
@@ -204,7 +209,8 @@ extern "C" size_t vren_cs_show_clusters_scratch_bytes(uint32_t max_clusters)
 extern "C" int vren_cs_show_clusters(vren_stream_t s, int mode, uint32_t width, uint32_t height,
                                      const uint32_t* cluster_refs, const uint32_t* cluster_keys,
                                      const uint32_t* key_count, uint32_t max_clusters, const uint32_t* counts,
-                                     const uint32_t* offsets, const uint32_t* indices, float* rgba, void* scratch)
+                                     const uint32_t* offsets, const uint32_t* indices, uint32_t index_capacity,
+                                     float* rgba, void* scratch)
 {
     if (width == 0 || height == 0) return VREN_OK;
     if (!cluster_refs || !cluster_keys || !key_count || !rgba || !scratch || max_clusters == 0) return VREN_ERR_ARG;
@@ -212,7 +218,7 @@ extern "C" int vren_cs_show_clusters(vren_stream_t s, int mode, uint32_t width, 
          mode == VREN_SHOW_CLUSTERS_LIGHT_INDICES) &&
         (!counts || !offsets))
         return VREN_ERR_ARG;
-    if (mode == VREN_SHOW_CLUSTERS_LIGHT_INDICES && !indices) return VREN_ERR_ARG;
+    if (mode == VREN_SHOW_CLUSTERS_LIGHT_INDICES && (!indices || index_capacity == 0)) return VREN_ERR_ARG;
     if (((uintptr_t)rgba | (uintptr_t)scratch) & 15u) return VREN_ERR_ARG;
     const uint64_t npix = (uint64_t)width * height;
     if (npix > 0xFFFFFFFFull) return VREN_ERR_ARG;
@@ -221,7 +227,7 @@ extern "C" int vren_cs_show_clusters(vren_stream_t s, int mode, uint32_t width, 
     float4* colours = static_cast<float4*>(scratch);
     const uint32_t cgrid = min((max_clusters + 7) / 8, (uint32_t)kNumSMsHint * 16);
     launch_kernel(show_clusters_colour_kernel, cgrid, 256, 0, st, mode, tiles_x, tiles_y, cluster_keys, key_count,
-                  max_clusters, counts, offsets, indices, colours);
+                  max_clusters, counts, offsets, indices, index_capacity, colours);
     VREN_LAUNCH_CHECK();
     const uint64_t pblocks = (npix + 255) / 256;
     const uint32_t pgrid = pblocks < (uint64_t)kNumSMsHint * 16 ? (uint32_t)pblocks : (uint32_t)kNumSMsHint * 16;

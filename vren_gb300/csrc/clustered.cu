@@ -666,6 +666,27 @@ __global__ void __launch_bounds__(kFucThreads, 6) find_unique_kernel(FucFrame fr
     find_unique_tile(fr, tile_base + blockIdx.x, sm);
 }
 
+// The one-kernel form: tiles taken by ticket from the 64-bit word at `header` (zero-filled before
+// the first use; the last ticket of every call re-opens it for the next).
+__global__ void __launch_bounds__(kFucThreads, 6) find_unique_fused_kernel(FucFrame fr, uint32_t* header)
+{
+    pdl_enter();
+    __shared__ FucSmem sm;
+    __shared__ uint32_t s_tile, s_epoch;
+    const uint32_t tid = threadIdx.x;
+    reinterpret_cast<uint4*>(sm.bits)[tid] = make_uint4(0u, 0u, 0u, 0u);
+    reinterpret_cast<uint4*>(sm.bits)[tid + kFucThreads] = make_uint4(0u, 0u, 0u, 0u);
+    if (tid < 64) sm.used[tid] = 0u;
+    if (tid == 0) {
+        uint32_t e;
+        s_tile = take_ticket(header, fr.num_tiles, e);
+        s_epoch = e;
+    }
+    __syncthreads();
+    if (s_tile >= fr.num_tiles) return;  // a header left inconsistent by a failed launch
+    find_unique_tile<true>(fr, s_tile, sm, s_epoch);
+}
+
 __global__ void __launch_bounds__(kFucScanThreads) find_unique_scan_kernel(FucFrame fr, uint32_t t_begin,
                                                                           uint32_t t_end)
 {
@@ -691,7 +712,8 @@ static FucFrame fuc_frame(const float* depth, const float* normals, uint32_t W, 
     const int vec = (W % 4u == 0u) && ((uintptr_t)depth % 16u == 0u) && ((uintptr_t)normals % 16u == 0u) &&
                     ((uintptr_t)refs % 16u == 0u);
     return FucFrame{depth, normals, W, H, frame, keys, key_cap, key_count, refs,
-                    scratch + fuc_keys_offset_words(tiles), scratch, scratch + tiles, tiles, vec};
+                    scratch ? scratch + fuc_keys_offset_words(tiles) : nullptr, scratch,
+                    scratch ? scratch + tiles : nullptr, tiles, vec, nullptr, 0u, 0u};
 }
 
 // Stage 1 over tiles [tile_begin, tile_begin + count).
@@ -726,18 +748,39 @@ static int launch_find_unique(cudaStream_t st, const float* depth, const float* 
     return rc != VREN_OK ? rc : launch_find_unique_finish(st, fr);
 }
 
+// Look-back state of the one-kernel form for up to `tiles` tiles: a 16-byte header (ticket word),
+// then one 64-bit status word per tile.
+static size_t fuc_lookback_bytes(uint32_t tiles) { return 16u + 8ull * tiles; }
+
+// find_unique_cluster_list in one launch (the one-kernel form); `lookback` as above, zero-filled
+// before its first use.
+static int launch_find_unique_fused(cudaStream_t st, const float* depth, const float* normals, uint32_t W, uint32_t H,
+                                    const vren_cs_frame* frame, uint32_t* keys, uint32_t key_cap,
+                                    uint32_t* key_count, uint32_t* refs, uint32_t* lookback)
+{
+    FucFrame fr = fuc_frame(depth, normals, W, H, frame, keys, key_cap, key_count, refs, nullptr);
+    fr.status = reinterpret_cast<uint64_t*>(lookback + 4);
+    fr.wait_limit = g_wait_limit;
+    fr.spin = (uint32_t)tuning(VREN_TUNE_SPIN_POLLS);
+    launch_kernel(find_unique_fused_kernel, fr.num_tiles, kFucThreads, 0, st, fr, lookback);
+    VREN_LAUNCH_CHECK();
+    return VREN_OK;
+}
+
 // The light lists of a frame copied into page-locked host memory by the device (no host round trip
 // for their lengths): out = [U, total, keys[U], counts[U], offsets[U], indices[total]], cut at cap
-// words (VREN_ERR_CAPACITY recorded when it does not fit).
+// words (VREN_ERR_CAPACITY recorded when it does not fit).  `total` is the number of index entries
+// the device holds: the assignment's total, cut at its index capacity.
 __global__ void lists_to_host_kernel(const uint32_t* __restrict__ key_count, uint32_t key_cap,
                                      const uint32_t* __restrict__ total_p, const uint32_t* __restrict__ keys,
                                      const uint32_t* __restrict__ counts, const uint32_t* __restrict__ offsets,
-                                     const uint32_t* __restrict__ indices, uint32_t* __restrict__ out, uint64_t cap)
+                                     const uint32_t* __restrict__ indices, uint32_t index_cap,
+                                     uint32_t* __restrict__ out, uint64_t cap)
 {
     pdl_enter();
     uint32_t U = *key_count;
     U = U < key_cap ? U : key_cap;
-    const uint32_t total = *total_p;
+    const uint32_t total = *total_p < index_cap ? *total_p : index_cap;
     const uint64_t need = 2ull + 3ull * U + total;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         if (cap >= 2) {
@@ -1197,6 +1240,7 @@ struct vren_cluster_and_shade {
     uint32_t stage_slots = 0;
     void* lbvh_scratch = nullptr;
     void* fuc_scratch = nullptr;
+    uint32_t* fuc_lookback = nullptr;  // ticket word and tile statuses of the one-kernel unique clusters
     void* assign_scratch = nullptr;
     // host frame block (pinned) and the CUDA graph of the last frame shape
     vren_cs_frame* host_frame = nullptr;
@@ -1276,8 +1320,11 @@ int cs_enqueue(vren_cluster_and_shade* cs, cudaStream_t st, uint32_t W, uint32_t
             return rc;
         }
     }
-    rc = launch_find_unique(st, depth, normals, W, H, cs->frame, cs->keys, cs->key_cap, cs->key_count, cs->refs,
-                            static_cast<uint32_t*>(cs->fuc_scratch));
+    rc = tuning(VREN_TUNE_FUC_FUSED) == 0
+             ? launch_find_unique_fused(st, depth, normals, W, H, cs->frame, cs->keys, cs->key_cap, cs->key_count,
+                                        cs->refs, cs->fuc_lookback)
+             : launch_find_unique(st, depth, normals, W, H, cs->frame, cs->keys, cs->key_cap, cs->key_count, cs->refs,
+                                  static_cast<uint32_t*>(cs->fuc_scratch));
     if (L > 0) VREN_CUDA_TRY(cudaStreamWaitEvent(st, cs->ev_bvh, 0));
     if (rc != VREN_OK) return rc;
     return assign_lights(st, cs->keys, cs->key_count, cs->key_cap, cs->frame, cs->bvh, L, cs->light_index,
@@ -1329,6 +1376,7 @@ extern "C" int vren_cs_create(vren_cluster_and_shade** out, uint32_t max_width, 
         }
     const size_t o_lbvh = carve(lbvh);
     const size_t o_fuc = carve(vren_cs_unique_clusters_scratch_bytes(max_width, max_height));
+    const size_t o_fuc_lb = carve(fuc_lookback_bytes(tiles));
     const size_t o_asg = carve(vren_cs_assign_lights_scratch_bytes(cs->key_cap));
     cs->arena_bytes = off;
     if (cudaMalloc(&cs->arena, off) != cudaSuccess) {
@@ -1357,6 +1405,7 @@ extern "C" int vren_cs_create(vren_cluster_and_shade** out, uint32_t max_width, 
     cs->stage_slots = (uint32_t)(stage_words / kStageLights);
     cs->lbvh_scratch = a + o_lbvh;
     cs->fuc_scratch = a + o_fuc;
+    cs->fuc_lookback = reinterpret_cast<uint32_t*>(a + o_fuc_lb);
     cs->assign_scratch = a + o_asg;
     // the second and third streams (light BVH beside the tiles; banded uploads) and their events
     bool ok = cudaStreamCreateWithFlags(&cs->aux, cudaStreamNonBlocking) == cudaSuccess &&
@@ -1501,7 +1550,7 @@ int cs_enqueue_host(vren_cluster_and_shade* cs, cudaStream_t st, uint32_t W, uin
     if (rc != VREN_OK) return rc;
     if (lists_out) {
         launch_kernel(lists_to_host_kernel, kNumSMsHint, 256, 0, st, cs->key_count, cs->key_cap, cs->total, cs->keys,
-                      cs->counts, cs->offsets, cs->indices, lists_out, lists_cap);
+                      cs->counts, cs->offsets, cs->indices, cs->max_assign, lists_out, lists_cap);
         VREN_LAUNCH_CHECK();
     }
     VREN_CUDA_TRY(cudaEventRecord(cs->ev_join, aux));
@@ -1635,7 +1684,7 @@ extern "C" int vren_cs_cluster_and_shade(vren_cluster_and_shade* cs, vren_stream
     cudaStream_t st = as_stream(s);
     int rc = refresh_frame(cs, st, view, width, height, offscreen);
     if (rc != VREN_OK) return rc;
-    const vren_cs_light_lists lists{cs->refs, cs->counts, cs->offsets, cs->indices};
+    const vren_cs_light_lists lists{cs->refs, cs->counts, cs->offsets, cs->indices, cs->max_assign, 0u};
     auto enqueue = [&]() -> int {
         int r = cs_enqueue(cs, st, width, height, gbuffer->depth, gbuffer->normals, light_positions, point_lights,
                            light_count);

@@ -9,6 +9,7 @@
 
 #include "common.cuh"
 #include "bvh_common.cuh"
+#include "lookback.cuh"
 
 #include <cuda_fp16.h>
 
@@ -260,10 +261,17 @@ constexpr int kFucThreads = 256;
 // 2. One CTA scans the tile counts into tile offsets (row-major tile order) and the key count.
 // 3. One CTA per tile adds the tile's offset to its references (still in L2) and copies its keys to
 //    their place in the dense key list.
+//
+// One-kernel form (the context's device frames): the CTAs take their tiles by ticket, so every tile's
+// predecessors have started; each tile publishes its key count as soon as its set is complete,
+// resolves its offset among the tiles before it by decoupled look-back (warp 0), and writes its
+// references and keys in their final places; the last tile writes the key count.  Stages 2 and 3 and
+// their launches disappear, and the references are written once.
 struct FucSmem {
     __align__(16) uint32_t bits[2048];
     uint32_t prefix[2048];
     uint32_t used[64];  // bit w: word w of bits is non-zero
+    uint32_t offset;    // one-kernel form: the tile's offset in the dense key list
 };
 
 // Where one frame's find_unique_cluster_list reads and writes.
@@ -281,11 +289,16 @@ struct FucFrame {
     uint32_t* tile_offset;  // [num_tiles]: exclusive prefix of tile_count
     uint32_t num_tiles;
     int vec;  // 128-bit accesses allowed (W % 4 == 0, 16-byte aligned depth, normals, refs)
+    // one-kernel form only: look-back status per tile ([epoch:30 | flag:2 | value:32]), the polling
+    // limit and the polls before back-off
+    uint64_t* status;
+    uint32_t wait_limit, spin;
 };
 
 // Stage 1 for tile `tile` of frame `fr`, all threads of the CTA; sm.bits and sm.used must be zero
-// (and synchronised) on entry.
-__device__ __forceinline__ void find_unique_tile(const FucFrame& fr, uint32_t tile, FucSmem& sm)
+// (and synchronised) on entry.  FUSED: the one-kernel form (`epoch` from the tile's ticket).
+template <bool FUSED = false>
+__device__ __forceinline__ void find_unique_tile(const FucFrame& fr, uint32_t tile, FucSmem& sm, uint32_t epoch = 0)
 {
     const float* __restrict__ depth = fr.depth;
     const float* __restrict__ normals = fr.normals;
@@ -445,7 +458,43 @@ __device__ __forceinline__ void find_unique_tile(const FucFrame& fr, uint32_t ti
         }
     }
     __syncwarp();
-    if (warp == 0) {
+    uint32_t off = 0;  // one-kernel form: the tile's offset, added to its references
+    if constexpr (FUSED) {
+        if (warp == 0) {
+            // publish the tile's count, find the keys before it, publish the inclusive prefix
+            const uint32_t count = __shfl_sync(0xFFFFFFFFu, incl, 31);
+            uint32_t prefix = 0;
+            if (tile == 0) {
+                if (lane == 0) st_relaxed_u64(fr.status, make_status(epoch, 2u, count));
+            } else {
+                if (lane == 0) st_relaxed_u64(fr.status + tile, make_status(epoch, 1u, count));
+                bool timed_out = false;
+                prefix = warp_lookback(fr.status, tile, 0u, epoch, lane, fr.wait_limit, fr.spin, timed_out);
+                if (__any_sync(0xFFFFFFFFu, timed_out) && lane == 0) VREN_RECORD_ERROR(VREN_ERR_TIMEOUT);
+                if (lane == 0) st_relaxed_u64(fr.status + tile, make_status(epoch, 2u, prefix + count));
+            }
+            // the tile's keys, ascending, at their place in the dense list
+            const uint32_t low = ((ty & 0xFFu) << 8) | (tx & 0xFFu);
+            uint32_t pos = prefix + excl;
+            for (int h = 0; h < 2; ++h) {
+                for (uint32_t m = h ? u1 : u0; m; m &= m - 1u) {
+                    const uint32_t w = 64u * lane + 32u * h + __ffs(m) - 1u;
+                    for (uint32_t bits = s_bits[w]; bits; bits &= bits - 1u, ++pos)
+                        if (pos < fr.key_cap) fr.keys[pos] = ((w * 32u + __ffs(bits) - 1u) << 16) | low;
+                }
+            }
+            if (lane == 0) {
+                sm.offset = prefix;
+                if (tile == fr.num_tiles - 1) {
+                    const uint32_t total = prefix + count;
+                    *fr.key_count = total < fr.key_cap ? total : fr.key_cap;
+                    if (total > fr.key_cap) VREN_RECORD_ERROR(VREN_ERR_CAPACITY);
+                }
+            }
+        }
+        __syncthreads();
+        off = sm.offset;
+    } else if (warp == 0) {
         // the tile's keys, ascending (word w bit b is the sub-key 32 w + b), and their count
         const uint32_t low = ((ty & 0xFFu) << 8) | (tx & 0xFFu);
         uint32_t* out = fr.tile_keys + (size_t)tile * 1024u;
@@ -469,7 +518,7 @@ __device__ __forceinline__ void find_unique_tile(const FucFrame& fr, uint32_t ti
             r[j] = r[j - 1];
         } else if (sj != 0xFFFFFFFFu) {
             const uint32_t w = sj >> 5;
-            r[j] = s_prefix[w] + __popc(s_bits[w] & ((1u << (sj & 31u)) - 1u));
+            r[j] = off + s_prefix[w] + __popc(s_bits[w] & ((1u << (sj & 31u)) - 1u));
         } else {
             r[j] = 0u;
         }

@@ -12,6 +12,21 @@ __device__ __forceinline__ uint64_t make_status(uint32_t epoch, uint32_t flag, u
     return ((uint64_t)((epoch << 2) | flag) << 32) | value;
 }
 
+// Takes the calling CTA's unit (a ticket) and the call's epoch from the 64-bit word
+// [epoch:32 | ticket:32] at `header`, one thread per CTA: units are taken in the order the CTAs start,
+// so a unit's predecessors have all started when it looks back.  The taker of the last ticket opens
+// the next call's epoch with ticket 0 (every other CTA of the launch has its ticket by then).
+__device__ __forceinline__ uint32_t take_ticket(uint32_t* header, uint32_t total_units, uint32_t& epoch)
+{
+    unsigned long long* word = reinterpret_cast<unsigned long long*>(header);
+    const unsigned long long w = atomicAdd(word, 1ull);
+    const uint32_t unit = (uint32_t)w;
+    epoch = (uint32_t)(w >> 32);
+    if (unit == total_units - 1) st_relaxed_u64(reinterpret_cast<uint64_t*>(header), (uint64_t)(epoch + 1u) << 32);
+    epoch &= 0x3FFFFFFFu;
+    return unit;
+}
+
 // Warp-wide decoupled look-back over status[seg_first .. tile-1]: lane i examines tile - 1 - i
 // (then 32 further back, ...) and the warp sums aggregates up to the nearest inclusive prefix.
 // Returns the exclusive prefix of `tile` in every lane.

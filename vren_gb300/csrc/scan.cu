@@ -51,13 +51,7 @@ __device__ __forceinline__ void publish_status(uint64_t* status, uint32_t tile, 
 // next call's epoch.
 __device__ __forceinline__ uint32_t take_tile(uint32_t* scratch, uint32_t total_tiles, uint32_t& epoch)
 {
-    unsigned long long* word = reinterpret_cast<unsigned long long*>(scratch);
-    const unsigned long long w = atomicAdd(word, 1ull);
-    const uint32_t tile = (uint32_t)w;
-    epoch = (uint32_t)(w >> 32);
-    if (tile == total_tiles - 1) st_relaxed_u64(reinterpret_cast<uint64_t*>(scratch), (uint64_t)(epoch + 1u) << 32);
-    epoch &= 0x3FFFFFFFu;
-    return tile;
+    return take_ticket(scratch, total_tiles, epoch);
 }
 
 // One CTA = one 4096-element tile; warp w owns 512 contiguous elements as four 128-element slices,

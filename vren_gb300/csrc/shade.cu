@@ -638,8 +638,13 @@ __global__ void __launch_bounds__(kTileThreads) shade_forward_kernel(ShadeArgs a
         float Lo[3] = {0.0f, 0.0f, 0.0f};
         if (a.L) {
             const uint32_t cref = S.cmin + c;
-            const uint32_t cnt = a.lists.counts[cref];
-            const uint32_t* idx = a.lists.indices + a.lists.offsets[cref];
+            const uint32_t off = a.lists.offsets[cref], cap = a.lists.index_capacity;
+            uint32_t cnt = a.lists.counts[cref];
+            if (off >= cap || cnt > cap - off) {  // a list cut by the assignment's index capacity
+                cnt = off >= cap ? 0u : cap - off;
+                if (lane == 0) VREN_RECORD_ERROR(VREN_ERR_CAPACITY);
+            }
+            const uint32_t* idx = a.lists.indices + off;
             for (uint32_t i = 0; i < cnt; ++i) {
                 const uint32_t l = idx[i];
                 point_light_fwd(q, a.lpos[l], a.lights[l], a.falloff, Lo);
@@ -781,7 +786,8 @@ static bool shade_args(const vren_cs_frame* frame, uint32_t W, uint32_t H, const
 {
     if (!frame || !g || !lists || W == 0 || H == 0) return false;
     if (!g->depth || !g->normals || !g->albedo || !g->roughness || !g->metallic || !lists->cluster_refs) return false;
-    if (L > 0 && (!lpos || !lights || !lists->counts || !lists->offsets || !lists->indices)) return false;
+    if (L > 0 && (!lpos || !lights || !lists->counts || !lists->offsets || !lists->indices || !lists->index_capacity))
+        return false;
     if (((uintptr_t)lpos | (uintptr_t)lights) & 15u) return false;
     std::memset(&a, 0, sizeof(a));
     a.frame = frame;
@@ -836,6 +842,9 @@ extern "C" int vren_cs_shade_backward(vren_stream_t s, const vren_cs_frame* fram
     if (light_count > 65536 || !grad_radiance || !scratch || ((uintptr_t)scratch & 255u)) return VREN_ERR_ARG;
     if (light_count > 0 && (!grad_positions || !grad_colors || !grad_radii)) return VREN_ERR_ARG;
     if (light_count == 0) return VREN_OK;
+    // the slots are the index entries [0, assignments): lists cut by the assignment's capacity cannot
+    // be differentiated
+    if (assignments > lists->index_capacity) return VREN_ERR_CAPACITY;
     a.falloff = falloff;
     cudaStream_t st = as_stream(s);
     const BwdLayout lay = bwd_layout(light_count, assignments);
