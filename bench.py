@@ -276,6 +276,19 @@ def run_ours(args, rank: int, world: int):
                "assignments": int(cs.read_device(o32.total, 1)[0]),
                "slicing": "32 exponential slices: near * (far/near)^(k/32)"}
 
+    # extra, labelled: the frame with each form of the unique-cluster stage (a fresh context each, the
+    # form being read when the frame's graph is captured)
+    lib = vg.lib()
+    knob = vg._lib.TUNE["fuc_fused"]
+    fuc_forms = {}
+    for form, name in ((0, "tiles+self_offset_fixup"), (1, "tiles+scan+fixup"), (2, "one_kernel_lookback")):
+        lib.vren_tuning_set(knob, form)
+        ctx_f = cs.cluster_and_shade(W, H, 65536, 1 << 24)
+        fuc_forms[name] = round(time_events(stream, lambda: ctx_f.cluster(stream, view, W, H, d_depth, d_norm, d_pos,
+                                                                           d_light, L), 3, args.steps, flush), 5)
+        del ctx_f
+    lib.vren_tuning_set(knob, 0)
+
     # extra, labelled: cluster_and_shade::operator() in one call (clustering, then shading over the
     # context's own light lists, one graph): the workload's frame with a seeded G-buffer (its normals are
     # the depth planes' normals), reference falloff, colour output with ambient and gamma
@@ -334,9 +347,9 @@ def run_ours(args, rank: int, world: int):
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(depth, normals, pos, lights, radix_keys, view, shade_host)
 
-    # light BVH at 16384 lights: one kernel on a 16-CTA cluster (1); unique clusters: tiles, tile-count
-    # scan, fix-up (3); assignment: count, scan, write (3)
-    launches_per_frame = 7
+    # light BVH at 16384 lights: one kernel on a 16-CTA cluster (1); unique clusters: tiles, then a
+    # fix-up that sums the preceding tile counts itself (2); assignment: count, scan, write (3)
+    launches_per_frame = 6
     if rank == 0:
         res = {
             "metric": METRIC,
@@ -370,10 +383,11 @@ def run_ours(args, rank: int, world: int):
             "normals_rgba16f": rgba16f,
             "dense_lights": dense,
             "fixed32_slicing": fixed32,
+            "unique_cluster_forms_frame_ms": fuc_forms,
             "cluster_and_shade": cluster_and_shade,
             "gpu_launches": launches_per_frame * args.steps,
             "roofline": {"bound": "hbm", "kernel": "find_unique_cluster_list (find_unique_kernel, "
-                                                     "find_unique_scan_kernel, find_unique_fixup_kernel)",
+                                                     "find_unique_fixup_self_kernel)",
                          "achieved": round(fuc_gbs, 1),
                          "peak": hbm_peak, "unit": "GB/s", "frac": round(fuc_gbs / hbm_peak, 4),
                          "peak_kind": peak_kind, "traffic": FUC_TRAFFIC_BYTES,

@@ -94,9 +94,11 @@ int vren_test_withhold_scan_status(uint32_t tile_plus_one);
  *                          1 = persistent grid whose producer warp streams tiles into shared memory
  *                          by bulk copies and publishes their digit counts on arrival, 0 = one CTA
  *                          per tile (ballot ranking, 15/16 keys per thread only)
- *   VREN_TUNE_FUC_FUSED    find_unique_cluster_list in the context's device frames: 0 = one kernel
- *                          (tiles taken by ticket, offsets by look-back over the tile counts; the
- *                          default), 1 = tiles, tile-count scan and fix-up as three kernels */
+ *   VREN_TUNE_FUC_FUSED    find_unique_cluster_list: 0 = tiles, then a fix-up whose CTAs sum their
+ *                          own tile offsets (two kernels, up to 16384 tiles; the default), 1 = tiles,
+ *                          tile-count scan and fix-up (three kernels), 2 = in the context's device
+ *                          frames one kernel (tiles taken by ticket, offsets by look-back over the
+ *                          tile counts) */
 enum { VREN_TUNE_SCAN_SLICES = 0, VREN_TUNE_SPIN_POLLS = 1, VREN_TUNE_RADIX_RANK = 2, VREN_TUNE_RADIX_ITEMS = 3,
        VREN_TUNE_SCAN_STAGED = 4, VREN_TUNE_REDUCE_FORM = 5, VREN_TUNE_LIGHT_BVH_CLUSTER = 6,
        VREN_TUNE_ASSIGN_FUSED = 7, VREN_TUNE_RADIX_PERSISTENT = 8, VREN_TUNE_FUC_FUSED = 9, VREN_TUNE_COUNT = 10 };

@@ -389,7 +389,7 @@ def check_context_outputs(ctx, W, H, view, depth, normals, pos, li, L):
     assert np.array_equal(cs.read_device(o.indices, et), ei)
 
 
-@pytest.mark.parametrize("fuc_form", [0, 1])  # unique clusters: one kernel (look-back) / three kernels
+@pytest.mark.parametrize("fuc_form", [0, 1, 2])  # unique clusters: self-offset fix-up / scan + fix-up / one kernel
 @pytest.mark.parametrize("slicing", ["ref", "fixed32"])
 def test_cluster_and_shade_context_1080p(cuda, slicing, fuc_form):
     """The benchmark frame through the context (graph replay): 1920x1080, 16,384 lights, both slicings,

@@ -95,9 +95,11 @@ extern "C" int vren_tuning_set(int knob, int value)
         if (value < 0 || value > 5) return VREN_ERR_ARG;
         break;
     case VREN_TUNE_LIGHT_BVH_CLUSTER:
+    case VREN_TUNE_FUC_FUSED:
+        if (value < 0 || value > 2) return VREN_ERR_ARG;
+        break;
     case VREN_TUNE_ASSIGN_FUSED:
     case VREN_TUNE_RADIX_PERSISTENT:
-    case VREN_TUNE_FUC_FUSED:
         if (value != 0 && value != 1) return VREN_ERR_ARG;
         break;
     default: break;

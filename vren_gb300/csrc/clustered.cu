@@ -701,6 +701,13 @@ __global__ void __launch_bounds__(kFucThreads) find_unique_fixup_kernel(FucFrame
     find_unique_fixup(fr, t_begin + blockIdx.x);
 }
 
+// The fix-up that sums its own tile offset (no scan kernel before it).
+__global__ void __launch_bounds__(kFucThreads) find_unique_fixup_self_kernel(FucFrame fr, uint32_t t_begin)
+{
+    pdl_enter();
+    find_unique_fixup<true>(fr, t_begin + blockIdx.x);
+}
+
 // Scratch of find_unique_cluster_list for T tiles (uint32 words): tile counts [T], tile offsets [T],
 // then (16-byte aligned) the tiles' key slots [T][1024].
 static size_t fuc_keys_offset_words(uint32_t T) { return (2ull * T + 3) / 4 * 4; }
@@ -732,6 +739,11 @@ static int launch_find_unique_finish(cudaStream_t st, const FucFrame& fr, uint32
 {
     t_end = t_end < fr.num_tiles ? t_end : fr.num_tiles;
     if (t_end <= t_begin) return VREN_OK;
+    if (fr.num_tiles <= kFucSelfScanTiles && tuning(VREN_TUNE_FUC_FUSED) == 0) {
+        launch_kernel(find_unique_fixup_self_kernel, t_end - t_begin, kFucThreads, 0, st, fr, t_begin);
+        VREN_LAUNCH_CHECK();
+        return VREN_OK;
+    }
     launch_kernel(find_unique_scan_kernel, 1, kFucScanThreads, 0, st, fr, t_begin, t_end);
     VREN_LAUNCH_CHECK();
     launch_kernel(find_unique_fixup_kernel, t_end - t_begin, kFucThreads, 0, st, fr, t_begin);
@@ -1320,7 +1332,7 @@ int cs_enqueue(vren_cluster_and_shade* cs, cudaStream_t st, uint32_t W, uint32_t
             return rc;
         }
     }
-    rc = tuning(VREN_TUNE_FUC_FUSED) == 0
+    rc = tuning(VREN_TUNE_FUC_FUSED) == 2
              ? launch_find_unique_fused(st, depth, normals, W, H, cs->frame, cs->keys, cs->key_cap, cs->key_count,
                                         cs->refs, cs->fuc_lookback)
              : launch_find_unique(st, depth, normals, W, H, cs->frame, cs->keys, cs->key_cap, cs->key_count, cs->refs,

@@ -582,11 +582,39 @@ __device__ __forceinline__ void find_unique_scan(const FucFrame& fr, uint32_t* s
     }
 }
 
-// Stage 2 for tile `tile`: references += tile offset, keys to their place in the dense list.
+// Stages 2 and 3 together, for frames of at most kFucSelfScanTiles tiles: the CTA of tile `tile` sums
+// the counts of the tiles before it (from L2) into its own offset, so no scan kernel runs between the
+// tiles and the fix-up; the CTA of the last tile writes the key count.
+constexpr uint32_t kFucSelfScanTiles = 16384;
+__device__ __forceinline__ uint32_t find_unique_self_offset(const FucFrame& fr, uint32_t tile)
+{
+    __shared__ uint32_t s_part[kFucThreads / 32];
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    uint32_t sum = 0;
+#pragma unroll 8
+    for (uint32_t i = tid; i < tile; i += kFucThreads) sum += fr.tile_count[i];
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) sum += __shfl_xor_sync(0xFFFFFFFFu, sum, d);
+    if (lane == 0) s_part[warp] = sum;
+    __syncthreads();
+    uint32_t off = 0;
+#pragma unroll
+    for (int w = 0; w < kFucThreads / 32; ++w) off += s_part[w];
+    if (tid == 0 && tile == fr.num_tiles - 1) {
+        const uint32_t total = off + fr.tile_count[tile];
+        *fr.key_count = total < fr.key_cap ? total : fr.key_cap;
+        if (total > fr.key_cap) VREN_RECORD_ERROR(VREN_ERR_CAPACITY);
+    }
+    return off;
+}
+
+// Stage 2 for tile `tile`: references += tile offset, keys to their place in the dense list (the
+// offset from the scan, or summed here when SELF).
+template <bool SELF = false>
 __device__ __forceinline__ void find_unique_fixup(const FucFrame& fr, uint32_t tile)
 {
     const uint32_t tid = threadIdx.x;
-    const uint32_t off = fr.tile_offset[tile], n = fr.tile_count[tile];
+    const uint32_t off = SELF ? find_unique_self_offset(fr, tile) : fr.tile_offset[tile], n = fr.tile_count[tile];
     const uint32_t* src = fr.tile_keys + (size_t)tile * 1024u;
     for (uint32_t j = tid; j < n; j += kFucThreads)
         if (off + j < fr.key_cap) fr.keys[off + j] = src[j];
