@@ -919,12 +919,21 @@ def primitive_sweep(args, dev, stream, flush, hbm_peak):
     keys = scene.gen_u32(SEED + 99, 3, n)
     pairs = np.stack([keys, np.arange(n, dtype=np.uint32)], 1).reshape(-1)
     src = torch.from_numpy(pairs.view(np.int32)).to(dev)
-    for kb in (10, 16):
+    lib = vg.lib()
+    knobs = (vg._lib.TUNE["bucket_form"], vg._lib.TUNE["radix_rank"])
+    saved = [lib.vren_tuning_get(k) for k in knobs]
+    # 10 bits: the one-scatter form (tile histograms, column scan, scatter) and the radix-pass form;
+    # 16 bits: radix passes
+    for kb, form, rank, label in ((10, 0, 0, ""), (10, 1, 0, "_radix_passes"), (16, 0, 0, "")):
+        lib.vren_tuning_set(knobs[0], form)
+        lib.vren_tuning_set(knobs[1], rank)
         bs = vg.bucket_sort(kb)
         outb = torch.empty(bs.get_required_output_buffer_size(n) // 4, dtype=torch.int32, device=dev)
         ms_b = time_events(stream, lambda: bs(stream, src, n, 0, outb, 0), 3, steps, flush)
-        res[f"bucket_sort_2^24_{kb}bit"] = {"ms": round(ms_b, 5), "gbs_at_24B": round(24 * n / ms_b / 1e6, 1),
-                                            "hbm_frac": round(24 * n / ms_b / 1e6 / hbm_peak, 4)}
+        res[f"bucket_sort_2^24_{kb}bit{label}"] = {"ms": round(ms_b, 5), "gbs_at_24B": round(24 * n / ms_b / 1e6, 1),
+                                                   "hbm_frac": round(24 * n / ms_b / 1e6 / hbm_peak, 4)}
+    for k, v in zip(knobs, saved):
+        lib.vren_tuning_set(k, v)
     return res
 
 

@@ -98,10 +98,15 @@ int vren_test_withhold_scan_status(uint32_t tile_plus_one);
  *                          own tile offsets (two kernels, up to 16384 tiles; the default), 1 = tiles,
  *                          tile-count scan and fix-up (three kernels), 2 = in the context's device
  *                          frames one kernel (tiles taken by ticket, offsets by look-back over the
- *                          tile counts) */
+ *                          tile counts)
+ *   VREN_TUNE_BUCKET_FORM  bucket sort of up to 10 key bits: 0 = one pass over the elements (a
+ *                          histogram kernel, then one scatter kernel with a look-back over 1024
+ *                          buckets; the default), 1 = stable radix passes of at most 8 bits, then
+ *                          the end offsets read back from the sorted elements */
 enum { VREN_TUNE_SCAN_SLICES = 0, VREN_TUNE_SPIN_POLLS = 1, VREN_TUNE_RADIX_RANK = 2, VREN_TUNE_RADIX_ITEMS = 3,
        VREN_TUNE_SCAN_STAGED = 4, VREN_TUNE_REDUCE_FORM = 5, VREN_TUNE_LIGHT_BVH_CLUSTER = 6,
-       VREN_TUNE_ASSIGN_FUSED = 7, VREN_TUNE_RADIX_PERSISTENT = 8, VREN_TUNE_FUC_FUSED = 9, VREN_TUNE_COUNT = 10 };
+       VREN_TUNE_ASSIGN_FUSED = 7, VREN_TUNE_RADIX_PERSISTENT = 8, VREN_TUNE_FUC_FUSED = 9, VREN_TUNE_BUCKET_FORM = 10,
+       VREN_TUNE_COUNT = 11 };
 int vren_tuning_set(int knob, int value);
 int vren_tuning_get(int knob);
 

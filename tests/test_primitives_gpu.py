@@ -317,6 +317,53 @@ def test_bucket_sort(cuda, key_bits, n):
     assert np.array_equal(got[off: off + (1 << key_bits)], exp_ends)
 
 
+@pytest.fixture
+def bucket_form():
+    lib = vg.lib()
+    knobs = (vg._lib.TUNE["bucket_form"], vg._lib.TUNE["radix_rank"])
+    saved = [lib.vren_tuning_get(k) for k in knobs]
+    yield lambda form, rank: [lib.vren_tuning_set(k, v) for k, v in zip(knobs, (form, rank))]
+    for k, v in zip(knobs, saved):
+        lib.vren_tuning_set(k, v)
+
+
+@pytest.mark.parametrize("form,rank", [(0, 0), (0, 1), (0, 2), (1, 0), (1, 2)])
+@pytest.mark.parametrize("keys", ["uniform", "one_bucket", "two_buckets", "runs", "descending"])
+@pytest.mark.parametrize("key_bits,n", [(10, 4096), (10, 4097), (10, 8192), (10, 8193), (10, 3 * 4096 - 5),
+                                        (10, 3 * 4096), (10, 16384), (10, 16385), (10, 2 * 16384 + 3 * 4096 + 7),
+                                        (10, 300001), (7, 123457), (1, 65537), (10, 1 << 22)])
+def test_bucket_sort_forms(cuda, bucket_form, form, rank, keys, key_bits, n):
+    """Both forms of the bucket sort of up to 10 key bits (one scatter pass over rows of two
+    4096-element tiles, and radix passes) against the stable oracle: rows and tiles full, ragged and
+    empty, and key sets that put every element in one bucket, in two, in long runs or in descending
+    order."""
+    bucket_form(form, rank)
+    rng = np.random.default_rng(n * 7 + key_bits)
+    if keys == "uniform":
+        k = rng.integers(0, 2**32, n, dtype=np.uint64).astype(np.uint32)
+    elif keys == "one_bucket":
+        k = (rng.integers(0, 2**20, n, dtype=np.uint64).astype(np.uint32) << 10) | 5
+    elif keys == "two_buckets":
+        k = rng.integers(0, 2, n).astype(np.uint32) * 0x3FF
+    elif keys == "runs":
+        k = (np.arange(n, dtype=np.uint64) // 5000).astype(np.uint32) * 0x9E3779B1
+    else:
+        k = (n - np.arange(n, dtype=np.uint64)).astype(np.uint32)
+    pairs = np.stack([k, np.arange(n, dtype=np.uint32)], 1).reshape(-1)
+    bs = vg.bucket_sort(key_bits)
+    out = torch.zeros(bs.get_required_output_buffer_size(n) // 4, dtype=torch.int32, device=cuda)
+    inp = dev_u32(pairs, cuda)
+    exp_pairs, exp_ends = oracle.bucket_sort_u32x2(pairs.reshape(-1, 2), key_bits)
+    off = ((8 * n + 255) // 256 * 256) // 4
+    for _ in range(2):  # a second call on the same scratch
+        out.zero_()
+        bs(None, inp, n, 0, out, 0)
+        got = host_u32(out)
+        assert np.array_equal(got[: 2 * n].reshape(-1, 2), exp_pairs)
+        assert np.array_equal(got[off: off + (1 << key_bits)], exp_ends)
+    assert vg.lib().vren_device_error(1) == 0
+
+
 # ------------------------------------------------------------------------------------------------
 # BVH
 # ------------------------------------------------------------------------------------------------

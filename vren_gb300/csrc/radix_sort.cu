@@ -391,6 +391,358 @@ __global__ void bucket_end_offsets_kernel(const uint2* __restrict__ sorted, uint
 }
 
 // ------------------------------------------------------------------------------------------------
+// Bucket sort in one scatter pass, for up to 10 key bits (1024 buckets).
+//
+// The reference counts with global atomics, scans its 65536 counters and scatters with atomics
+// (vren/primitives/bucket_sort.cpp:116-160, bucket_sort_count.comp:27-33, bucket_sort_write.comp:27-34).
+// Here, over tiles of 4096 elements (one matrix row each):
+//   1. bucket_tile_hist_kernel: one CTA per row reads it once and writes its 1024 bucket counts as one
+//      row of a [rows][1024] matrix (4 KB per 32 KB of elements);
+//   2. bucket_column_scan_kernel: each CTA turns 8 columns of the matrix into exclusive prefixes over
+//      the rows (in place) and the bucket totals; the last CTA scans the totals into the bucket
+//      start offsets (scratch) and the end offsets (the output's counters region);
+//   3. bucket_scatter_kernel: one CTA per row reads it again (keys first; values when staging, from
+//      L2), ranks it stably in shared memory (1024 16-bit counters per warp), stages it in bucket
+//      order and writes each element to start[bucket] + (the bucket's count in the elements before
+//      its tile) + (its rank in the tile).
+// Every row's place is known before the scatter starts, so no CTA waits on another (an earlier
+// form resolved the tile prefixes by decoupled look-back over 1024 buckets; measured per CTA, that
+// look-back was its longest phase).  The scatter takes the rows from the last one down: the
+// histogram read the end of the input last, so that part is still in L2.  One tile per row keeps
+// the CTAs that write the two halves of a bucket boundary's 32-byte sector running at the same
+// time: with two or four tiles per row, written one after the other by one CTA, the DRAM traffic of
+// the scatter grew by a third (sectors evicted half written).
+// Traffic: the elements read twice and written once (24 B each), plus the matrix written, read and
+// written by the scan and read by the scatter (16 KB per 4096 elements, 1/6 of the 96 KB; most of
+// it stays in L2 between the three kernels).
+// ------------------------------------------------------------------------------------------------
+constexpr int kBucketBits = 10;
+constexpr uint32_t kBucketRadix = 1u << kBucketBits;
+constexpr int kBucketItems = 16;
+constexpr uint32_t kBucketTile = kSortThreads * kBucketItems;   // 4096 elements
+constexpr uint32_t kBucketRow = kBucketTile;                      // elements per matrix row (one tile)
+constexpr int kBucketScanThreads = 512;
+constexpr uint32_t kBucketScanCols = 8;                          // columns per scan CTA (32 B of a row)
+constexpr uint32_t kBucketScanRows = 8;                          // rows per scan thread and chunk
+// Scratch, in uint32 words: [0] scan CTA ticket, [16, 1040) bucket totals, [1040, 2064) bucket
+// start offsets, then the count matrix [rows][1024] (16-byte aligned).
+constexpr uint32_t kBkTotals = 16, kBkStarts = kBkTotals + kBucketRadix, kBkRows = kBkStarts + kBucketRadix;
+
+__global__ void __launch_bounds__(kSortThreads) bucket_tile_hist_kernel(const uint2* __restrict__ in, uint32_t n,
+                                                                       uint32_t key_bits,
+                                                                       uint32_t* __restrict__ scratch)
+{
+    pdl_enter();
+    __shared__ alignas(16) uint32_t s_hist[kBucketRadix];
+    const uint32_t tid = threadIdx.x, row = blockIdx.x;
+    reinterpret_cast<uint4*>(s_hist)[tid] = make_uint4(0u, 0u, 0u, 0u);
+    if (row == 0 && tid == 0) scratch[0] = 0u;  // the scan's CTA ticket
+    __syncthreads();
+    const uint32_t mask = (1u << key_bits) - 1u;
+    const uint32_t base = row * kBucketRow;
+    if (base + kBucketRow <= n) {
+        // chunks of 4096 uint4 (two elements each), sixteen per thread, each chunk's loads in flight
+        constexpr int Q = kBucketRow >= 2u * 16u * kSortThreads ? 16 : (int)(kBucketRow / 2u / kSortThreads);
+        constexpr uint32_t kChunk = 2u * Q * kSortThreads;
+        static_assert(kBucketRow % kChunk == 0, "rows are whole chunks");
+#pragma unroll 1
+        for (uint32_t c = 0; c < kBucketRow; c += kChunk) {
+            const uint4* p4 = reinterpret_cast<const uint4*>(in + base + c);
+            uint4 q[Q];
+#pragma unroll
+            for (int k = 0; k < Q; ++k) q[k] = __ldg(p4 + tid + k * kSortThreads);
+#pragma unroll
+            for (int k = 0; k < Q; ++k) {
+                atomicAdd(&s_hist[q[k].x & mask], 1u);
+                atomicAdd(&s_hist[q[k].z & mask], 1u);
+            }
+        }
+    } else {
+        for (uint32_t i = base + tid; i < n; i += kSortThreads) atomicAdd(&s_hist[__ldg(&in[i].x) & mask], 1u);
+    }
+    __syncthreads();
+    reinterpret_cast<uint4*>(scratch + kBkRows + (size_t)row * kBucketRadix)[tid] =
+        reinterpret_cast<const uint4*>(s_hist)[tid];
+}
+
+__global__ void __launch_bounds__(kBucketScanThreads) bucket_column_scan_kernel(uint32_t* __restrict__ scratch,
+                                                                              uint32_t rows_n, uint32_t key_bits,
+                                                                              uint32_t* __restrict__ ends)
+{
+    pdl_enter();
+    constexpr uint32_t C = kBucketScanCols, R = kBucketScanRows;
+    constexpr uint32_t kWarps = kBucketScanThreads / 32;
+    __shared__ uint32_t s_warp[kWarps][C];
+    __shared__ uint32_t s_carry[C];
+    __shared__ uint32_t s_wsum[kWarps];
+    __shared__ bool s_last;
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const uint32_t c0 = blockIdx.x * C;
+    uint32_t* rows = scratch + kBkRows + c0;
+    if (tid < C) s_carry[tid] = 0u;
+    __syncthreads();
+    for (uint32_t r0 = 0; r0 < rows_n; r0 += kBucketScanThreads * R) {
+        const uint32_t rb = r0 + tid * R;
+        uint32_t v[R][C], sum[C];
+#pragma unroll
+        for (uint32_t c = 0; c < C; ++c) sum[c] = 0u;
+#pragma unroll
+        for (uint32_t r = 0; r < R; ++r) {
+            uint4 lo = make_uint4(0u, 0u, 0u, 0u), hi = lo;
+            if (rb + r < rows_n) {
+                const uint4* p = reinterpret_cast<const uint4*>(rows + (size_t)(rb + r) * kBucketRadix);
+                lo = p[0];
+                hi = p[1];
+            }
+            v[r][0] = lo.x; v[r][1] = lo.y; v[r][2] = lo.z; v[r][3] = lo.w;
+            v[r][4] = hi.x; v[r][5] = hi.y; v[r][6] = hi.z; v[r][7] = hi.w;
+#pragma unroll
+            for (uint32_t c = 0; c < C; ++c) sum[c] += v[r][c];
+        }
+        // exclusive prefix of each column over the threads (rows before mine), plus the carry
+        uint32_t incl[C];
+#pragma unroll
+        for (uint32_t c = 0; c < C; ++c) {
+            incl[c] = sum[c];
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl[c], d);
+                if (lane >= (uint32_t)d) incl[c] += y;
+            }
+        }
+        if (lane == 31) {
+#pragma unroll
+            for (uint32_t c = 0; c < C; ++c) s_warp[warp][c] = incl[c];
+        }
+        __syncthreads();
+        uint32_t run[C];
+#pragma unroll
+        for (uint32_t c = 0; c < C; ++c) {
+            run[c] = s_carry[c] + incl[c] - sum[c];
+            for (uint32_t w = 0; w < warp; ++w) run[c] += s_warp[w][c];
+        }
+#pragma unroll
+        for (uint32_t r = 0; r < R; ++r) {
+            if (rb + r < rows_n) {
+                uint4* p = reinterpret_cast<uint4*>(rows + (size_t)(rb + r) * kBucketRadix);
+                p[0] = make_uint4(run[0], run[1], run[2], run[3]);
+                p[1] = make_uint4(run[4], run[5], run[6], run[7]);
+            }
+#pragma unroll
+            for (uint32_t c = 0; c < C; ++c) run[c] += v[r][c];
+        }
+        __syncthreads();  // every thread has read s_carry and s_warp
+        if (tid == kBucketScanThreads - 1) {
+#pragma unroll
+            for (uint32_t c = 0; c < C; ++c) s_carry[c] = run[c];
+        }
+        __syncthreads();
+    }
+    if (tid < C) {
+        scratch[kBkTotals + c0 + tid] = s_carry[tid];
+        __threadfence();
+    }
+    __syncthreads();
+    if (tid == 0) {
+        __threadfence();
+        s_last = (atomicAdd(scratch, 1u) == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    // Bucket starts (exclusive) and ends (inclusive) from the totals, two buckets per thread.
+    const uint32_t b = 2u * tid;
+    const uint32_t t0 = ld_relaxed_u32(scratch + kBkTotals + b), t1 = ld_relaxed_u32(scratch + kBkTotals + b + 1u);
+    uint32_t incl2 = t0 + t1;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl2, d);
+        if (lane >= (uint32_t)d) incl2 += y;
+    }
+    if (lane == 31) s_wsum[warp] = incl2;
+    __syncthreads();
+    for (uint32_t w = 0; w < warp; ++w) incl2 += s_wsum[w];
+    const uint32_t start0 = incl2 - t0 - t1;
+    scratch[kBkStarts + b] = start0;
+    scratch[kBkStarts + b + 1u] = start0 + t0;
+    const uint32_t mask = (1u << key_bits) - 1u;
+    if (b <= mask) ends[b] = start0 + t0;
+    if (b + 1u <= mask) ends[b + 1u] = incl2;
+}
+
+__device__ __forceinline__ uint4 ld_v4_after_wait(const uint32_t* p)
+{
+    uint4 v;
+    asm volatile("ld.relaxed.gpu.global.v4.u32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p) : "memory");
+    return v;
+}
+
+struct alignas(16) BucketSmem {
+    uint16_t warp_hist[kSortWarps][kBucketRadix];  // per-warp bucket counts, then each warp's first staging slot
+    int32_t delta[kBucketRadix];  // the tile's place in each bucket - the bucket's staging start
+    uint32_t wsum[kSortWarps];
+};
+
+// Tile `tile` (4096 elements, one matrix row); sm.warp_hist is zero on entry.  In the RAGGED last
+// tile the slots past n take the key `mask`, the last bucket: ranked after every element of the
+// tile (their indices are the highest), they land at or past the end of that bucket, which is n,
+// and are not written.
+template <int RANK, bool RAGGED>
+__device__ __forceinline__ void bucket_scatter_body(const uint2* __restrict__ in, uint2* __restrict__ out, uint32_t n,
+                                                    uint32_t key_bits, uint32_t tile,
+                                                    const uint32_t* __restrict__ scratch, BucketSmem& sm,
+                                                    uint2* s_stage)
+{
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const uint32_t mask = (1u << key_bits) - 1u;
+
+    // Striped load of the keys: item j of lane l is element warp_base + 32*j + l.  The values are
+    // read again when the tile is staged (the line is still in L2), so only keys stay in registers.
+    const uint32_t warp_base = tile * kBucketTile + warp * (32u * kBucketItems);
+    const uint32_t* keys = reinterpret_cast<const uint32_t*>(in);
+    uint32_t k[kBucketItems];
+    uint32_t pos[kBucketItems];
+#pragma unroll
+    for (int j = 0; j < kBucketItems; ++j) {
+        const uint32_t idx = warp_base + 32u * j + lane;
+        k[j] = (!RAGGED || idx < n) ? __ldg(keys + 2u * idx) : mask;
+    }
+    // RANK 1's per-warp bucket-name table (1 KB per warp), inside the staging area, which is free
+    // until the tile is ranked.
+    uint8_t* rep_tab = reinterpret_cast<uint8_t*>(s_stage) + warp * kBucketRadix;
+
+    // Stable in-warp ranks, items in order: peers (lanes with my bucket) from one ballot per key bit
+    // (RANK 0; bits at and above key_bits are zero in every lane, so all ten ballots serve any
+    // key_bits), from a bucket name and five ballots (RANK 1) or from match.any (RANK 2).
+#pragma unroll
+    for (int j = 0; j < kBucketItems; ++j) {
+        const uint32_t d = k[j] & mask;
+        uint32_t peers;
+        if (RANK == 2) {
+            peers = __match_any_sync(0xFFFFFFFFu, d);
+        } else if (RANK == 1) {
+            // Every lane writes its id into its bucket's slot of a per-warp table; the lanes of one
+            // bucket then read back the same id (whichever write landed), a 5-bit name for the bucket
+            // within the warp, and five ballots on that name find the peers.
+            rep_tab[d] = (uint8_t)lane;
+            __syncwarp();
+            const uint32_t r = rep_tab[d];
+            peers = 0xFFFFFFFFu;
+#pragma unroll
+            for (int b = 0; b < 5; ++b) {
+                const bool bit = (r >> b) & 1u;
+                const uint32_t m = __ballot_sync(0xFFFFFFFFu, bit);
+                peers &= bit ? m : ~m;
+            }
+        } else {
+            peers = 0xFFFFFFFFu;
+#pragma unroll
+            for (int b = 0; b < kBucketBits; ++b) {
+                const bool bit = (d >> b) & 1u;
+                const uint32_t m = __ballot_sync(0xFFFFFFFFu, bit);
+                peers &= bit ? m : ~m;
+            }
+        }
+        const uint32_t below = peers & lanemask_lt();
+        const uint32_t before = sm.warp_hist[warp][d];
+        __syncwarp();
+        if (below == 0) sm.warp_hist[warp][d] = (uint16_t)(before + __popc(peers));
+        __syncwarp();
+        pos[j] = d | ((before + __popc(below)) << kBucketBits);
+    }
+    __syncthreads();
+
+    // Thread t owns buckets 4t..4t+3: warp prefixes, the tile's counts and tile-local offsets.
+    uint32_t cnt[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+    for (int w = 0; w < kSortWarps; ++w) {
+        uint2* row = reinterpret_cast<uint2*>(sm.warp_hist[w]) + tid;  // four uint16 counters
+        const uint2 x = *row;
+        *row = make_uint2(cnt[0] | (cnt[1] << 16), cnt[2] | (cnt[3] << 16));
+        cnt[0] += x.x & 0xFFFFu; cnt[1] += x.x >> 16; cnt[2] += x.y & 0xFFFFu; cnt[3] += x.y >> 16;
+    }
+    const uint32_t sum4 = cnt[0] + cnt[1] + cnt[2] + cnt[3];
+    uint32_t incl = sum4;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= (uint32_t)o) incl += y;
+    }
+    if (lane == 31) sm.wsum[warp] = incl;
+    __syncthreads();
+    uint32_t excl0 = incl - sum4;
+    for (uint32_t w = 0; w < warp; ++w) excl0 += sm.wsum[w];
+    const uint32_t excl1 = excl0 + cnt[0], excl2 = excl1 + cnt[1], excl3 = excl2 + cnt[2];
+    const uint32_t e01 = excl0 | (excl1 << 16), e23 = excl2 | (excl3 << 16);
+#pragma unroll
+    for (int w = 0; w < kSortWarps; ++w) {
+        uint2* row = reinterpret_cast<uint2*>(sm.warp_hist[w]) + tid;
+        const uint2 x = *row;  // per-lane sums stay below 2^16 (at most 4096)
+        *row = make_uint2(x.x + e01, x.y + e23);
+    }
+    __syncthreads();
+
+    // Stage in bucket order (the value read again, from L2).
+#pragma unroll
+    for (int j = 0; j < kBucketItems; ++j) {
+        const uint32_t d = pos[j] & (kBucketRadix - 1u);
+        const uint32_t idx = warp_base + 32u * j + lane;
+        const uint32_t v = (!RAGGED || idx < n) ? __ldg(keys + 2u * idx + 1u) : 0u;
+        s_stage[sm.warp_hist[warp][d] + (pos[j] >> kBucketBits)] = make_uint2(k[j], v);
+    }
+    {
+        // The tile's place in each bucket: start + the bucket's count in the tiles before (the column
+        // scan's output, which this grid may only read once that kernel has completed), less the
+        // bucket's staging start (warp 0's first slot, which is the tile-local exclusive offset).
+        // (inline-assembly loads, so the compiler cannot move them above the wait, as it may move
+        // loads through a const __restrict__ pointer)
+        asm volatile("griddepcontrol.wait;" ::: "memory");
+        const uint4 col = ld_v4_after_wait(scratch + kBkRows + (size_t)tile * kBucketRadix + 4u * tid);
+        const uint4 start = ld_v4_after_wait(scratch + kBkStarts + 4u * tid);
+        const uint2 w0 = reinterpret_cast<const uint2*>(sm.warp_hist[0])[tid];
+        reinterpret_cast<int4*>(sm.delta)[tid] = make_int4((int32_t)(start.x + col.x) - (int32_t)(w0.x & 0xFFFFu),
+                                                           (int32_t)(start.y + col.y) - (int32_t)(w0.x >> 16),
+                                                           (int32_t)(start.z + col.z) - (int32_t)(w0.y & 0xFFFFu),
+                                                           (int32_t)(start.w + col.w) - (int32_t)(w0.y >> 16));
+    }
+    __syncthreads();
+
+    // Write out: consecutive threads take consecutive staged elements.
+#pragma unroll
+    for (int j = 0; j < kBucketItems; ++j) {
+        const uint32_t p = j * kSortThreads + tid;
+        const uint2 v = s_stage[p];
+        const uint32_t dst = (uint32_t)((int32_t)p + sm.delta[v.x & mask]);
+        if (dst < n) out[dst] = v;
+    }
+}
+
+// Launched as a programmatic dependent of the column scan: each CTA loads and ranks its tile while
+// the scan may still be running, and waits for it (griddepcontrol.wait) only before reading the
+// scan's output.
+template <int RANK>
+__global__ void __launch_bounds__(kSortThreads, 4) bucket_scatter_kernel(const uint2* __restrict__ in,
+                                                                        uint2* __restrict__ out, uint32_t n,
+                                                                        uint32_t key_bits, uint32_t num_rows,
+                                                                        const uint32_t* __restrict__ scratch)
+{
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    extern __shared__ uint4 s_dyn[];
+    __shared__ BucketSmem sm;
+    const uint32_t tid = threadIdx.x;
+    uint4* h4 = reinterpret_cast<uint4*>(&sm.warp_hist[0][0]);
+    for (uint32_t i = tid; i < sizeof(sm.warp_hist) / 16u; i += kSortThreads) h4[i] = make_uint4(0u, 0u, 0u, 0u);
+    __syncthreads();
+    const uint32_t tile = num_rows - 1u - blockIdx.x;
+    uint2* s_stage = reinterpret_cast<uint2*>(s_dyn);
+    if ((uint64_t)(tile + 1) * kBucketTile <= n)
+        bucket_scatter_body<RANK, false>(in, out, n, key_bits, tile, scratch, sm, s_stage);
+    else
+        bucket_scatter_body<RANK, true>(in, out, n, key_bits, tile, scratch, sm, s_stage);
+}
+
+// ------------------------------------------------------------------------------------------------
 // Host side
 // ------------------------------------------------------------------------------------------------
 // Keys per thread: variant 0 = 15 (8-bit digits) / 16, variant 1 = 23 / 24 (bigger tiles).
@@ -595,12 +947,58 @@ extern "C" size_t vren_bucket_sort_output_bytes(uint32_t n, uint32_t key_bits)
     return pairs + ((size_t)1 << key_bits) * sizeof(uint32_t);
 }
 
+// The one-scatter form (up to 10 key bits): header, bucket totals and starts, and one 1024-word row
+// of the count matrix per 4096-element tile.
+static size_t bucket_onepass_scratch_bytes(uint32_t n)
+{
+    const uint64_t rows = ((uint64_t)n + kBucketRow - 1) / kBucketRow;
+    return (size_t)(kBkRows + (rows ? rows : 1) * kBucketRadix) * sizeof(uint32_t);
+}
+
+// The radix-pass form: digit-pass scratch, then a ping-pong element buffer.
+static size_t bucket_passes_scratch_bytes(uint32_t n, uint32_t key_bits)
+{
+    const size_t status = scratch1_bytes(n, bucket_digit_bits(key_bits));
+    const size_t tmp = ((size_t)n * 8 + 255) / 256 * 256;
+    return ((status + 255) / 256 * 256) + tmp;
+}
+
 extern "C" size_t vren_bucket_sort_scratch_bytes(uint32_t n, uint32_t key_bits)
 {
     if (key_bits == 0 || key_bits > 16) return 0;
-    const size_t status = scratch1_bytes(n, bucket_digit_bits(key_bits));
-    const size_t tmp = ((size_t)n * 8 + 255) / 256 * 256;  // ping-pong elements for a two-pass sort
-    return ((status + 255) / 256 * 256) + tmp;
+    const size_t passes = bucket_passes_scratch_bytes(n, key_bits);
+    if (key_bits > (uint32_t)kBucketBits) return passes;
+    // Either form may run (VREN_TUNE_BUCKET_FORM), so the scratch fits both.
+    const size_t one = bucket_onepass_scratch_bytes(n);
+    return one > passes ? one : passes;
+}
+
+static int bucket_sort_onepass(cudaStream_t st, const uint2* in, uint32_t n, uint2* out, uint32_t* ends,
+                               uint32_t key_bits, uint32_t* scratch)
+{
+    if (n == 0) {
+        VREN_CUDA_TRY(cudaMemsetAsync(ends, 0, sizeof(uint32_t) << key_bits, st));
+        return VREN_OK;
+    }
+    const uint32_t rows = (n + kBucketRow - 1) / kBucketRow;
+    VREN_CUDA_TRY(launch_kernel(bucket_tile_hist_kernel, rows, kSortThreads, 0, st, in, n, key_bits, scratch));
+    VREN_LAUNCH_CHECK();
+    PdlScope pdl(1);  // the scan and the scatter start early and wait for their predecessor in-kernel
+    VREN_CUDA_TRY(launch_kernel(bucket_column_scan_kernel, kBucketRadix / kBucketScanCols, kBucketScanThreads, 0, st,
+                                scratch, rows, key_bits, ends));
+    VREN_LAUNCH_CHECK();
+    constexpr size_t smem = (size_t)kBucketTile * sizeof(uint2);
+    const int rank = tuning(VREN_TUNE_RADIX_RANK);
+    auto kern = rank == 0 ? bucket_scatter_kernel<0> : rank == 1 ? bucket_scatter_kernel<1> : bucket_scatter_kernel<2>;
+    static bool opted[3] = {false, false, false};
+    if (!opted[rank]) {
+        VREN_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        opted[rank] = true;
+    }
+    VREN_CUDA_TRY(launch_kernel(kern, rows, kSortThreads, smem, st, in, out, n, key_bits, rows,
+                                static_cast<const uint32_t*>(scratch)));
+    VREN_LAUNCH_CHECK();
+    return VREN_OK;
 }
 
 extern "C" int vren_bucket_sort_u32x2(vren_stream_t s, const uint32_t* in, uint32_t n, void* out, uint32_t key_bits,
@@ -612,8 +1010,11 @@ extern "C" int vren_bucket_sort_u32x2(vren_stream_t s, const uint32_t* in, uint3
     cudaStream_t st = as_stream(s);
     uint32_t* out_pairs = static_cast<uint32_t*>(out);
     uint32_t* ends = reinterpret_cast<uint32_t*>(static_cast<char*>(out) + ((size_t)n * 8 + 255) / 256 * 256);
-    const uint32_t db = bucket_digit_bits(key_bits);
     uint32_t* sc = static_cast<uint32_t*>(scratch);
+    if (key_bits <= (uint32_t)kBucketBits && tuning(VREN_TUNE_BUCKET_FORM) == 0)
+        return bucket_sort_onepass(st, reinterpret_cast<const uint2*>(in), n, reinterpret_cast<uint2*>(out_pairs), ends,
+                                   key_bits, sc);
+    const uint32_t db = bucket_digit_bits(key_bits);
     uint32_t* tmp = reinterpret_cast<uint32_t*>(static_cast<char*>(scratch) + (scratch1_bytes(n, db) + 255) / 256 * 256);
     if (n > 0) {
         PassInfo passes = make_passes(key_bits, db);
