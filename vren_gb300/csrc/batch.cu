@@ -77,8 +77,8 @@ __device__ __forceinline__ uint32_t frame_of(const uint32_t* __restrict__ prefix
 // ------------------------------------------------------------------------------------------------
 // Light BVH
 // ------------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) batch_transform_kernel(const BatchDesc* __restrict__ d,
-                                                              const uint32_t* __restrict__ chunk_prefix, uint32_t n,
+__global__ void __launch_bounds__(256) batch_transform_kernel(const BatchDesc* d,
+                                                              const uint32_t* chunk_prefix, uint32_t n,
                                                               float4* __restrict__ view_pos, uint32_t* __restrict__ part,
                                                               uint32_t* __restrict__ fmm, uint32_t* __restrict__ fticket)
 {
@@ -147,10 +147,10 @@ __global__ void __launch_bounds__(256) batch_transform_kernel(const BatchDesc* _
     if (tid == 0) fticket[f] = 0u;
 }
 
-__global__ void __launch_bounds__(256) batch_morton_kernel(const BatchDesc* __restrict__ d,
-                                                           const uint32_t* __restrict__ chunk_prefix, uint32_t n,
-                                                           const float4* __restrict__ view_pos,
-                                                           const uint32_t* __restrict__ fmm, uint2* __restrict__ pairs)
+__global__ void __launch_bounds__(256) batch_morton_kernel(const BatchDesc* d,
+                                                           const uint32_t* chunk_prefix, uint32_t n,
+                                                           const float4* view_pos,
+                                                           const uint32_t* fmm, uint2* __restrict__ pairs)
 {
     pdl_enter();
     const uint32_t f = frame_of(chunk_prefix, n, blockIdx.x);
@@ -172,10 +172,10 @@ __global__ void __launch_bounds__(256) batch_morton_kernel(const BatchDesc* __re
     }
 }
 
-__global__ void __launch_bounds__(1024) batch_leaves_kernel(const BatchDesc* __restrict__ d,
-                                                            const uint32_t* __restrict__ leaf_prefix, uint32_t n,
+__global__ void __launch_bounds__(1024) batch_leaves_kernel(const BatchDesc* d,
+                                                            const uint32_t* leaf_prefix, uint32_t n,
                                                             uint2* __restrict__ light_index,
-                                                            const float4* __restrict__ view_pos,
+                                                            const float4* view_pos,
                                                             vren_bvh_node* __restrict__ bvh, float4* __restrict__ spheres)
 {
     pdl_enter();
@@ -193,7 +193,7 @@ __global__ void __launch_bounds__(1024) batch_leaves_kernel(const BatchDesc* __r
 }
 
 // Levels above the two built with the leaves (frames with at least 32768 padded leaves).
-__global__ void __launch_bounds__(1024) batch_levels_kernel(const BatchDesc* __restrict__ d,
+__global__ void __launch_bounds__(1024) batch_levels_kernel(const BatchDesc* d,
                                                             vren_bvh_node* __restrict__ bvh)
 {
     pdl_enter();
@@ -267,8 +267,8 @@ __global__ void __launch_bounds__(kFucThreads) batch_find_unique_fixup_kernel(Ba
 }
 
 // Dense cluster numbering: base[f] = sum of the unique-cluster counts of frames < f; base[n] = total.
-__global__ void __launch_bounds__(1024) batch_bases_kernel(const BatchDesc* __restrict__ d, uint32_t n,
-                                                           const uint32_t* __restrict__ key_counts,
+__global__ void __launch_bounds__(1024) batch_bases_kernel(const BatchDesc* d, uint32_t n,
+                                                           const uint32_t* key_counts,
                                                            uint32_t* __restrict__ base)
 {
     pdl_enter();
@@ -362,8 +362,8 @@ __global__ void __launch_bounds__(256) batch_assign_kernel(BatchAssign b)
 }
 
 // index_base[f] = first light index of frame f in the dense index array, totals[f] = its count.
-__global__ void batch_totals_kernel(uint32_t n, const uint32_t* __restrict__ base, const uint32_t* __restrict__ goff,
-                                    const uint32_t* __restrict__ grand_total, uint32_t* __restrict__ index_base,
+__global__ void batch_totals_kernel(uint32_t n, const uint32_t* base, const uint32_t* goff,
+                                    const uint32_t* grand_total, uint32_t* __restrict__ index_base,
                                     uint32_t* __restrict__ totals)
 {
     pdl_enter();

@@ -48,7 +48,7 @@ static LbvhLayout lbvh_layout(uint32_t L, uint32_t morton_bits, uint32_t digit_b
 }
 
 __global__ void __launch_bounds__(kLbvhThreads) lbvh_transform_kernel(
-    const float4* __restrict__ positions, uint32_t L, const vren_cs_frame* __restrict__ F,
+    const float4* positions, uint32_t L, const vren_cs_frame* F,
     float4* __restrict__ view_pos, uint32_t* __restrict__ scratch)
 {
     pdl_enter();
@@ -113,7 +113,7 @@ __global__ void __launch_bounds__(kLbvhThreads) lbvh_transform_kernel(
 }
 
 // discretize_point_light_positions.comp:30-39
-__global__ void lbvh_morton_kernel(const float4* __restrict__ view_pos, uint32_t L, const uint32_t* __restrict__ scratch,
+__global__ void lbvh_morton_kernel(const float4* view_pos, uint32_t L, const uint32_t* scratch,
                                    uint32_t bits, uint2* __restrict__ pairs)
 {
     pdl_enter();
@@ -130,7 +130,7 @@ __global__ void lbvh_morton_kernel(const float4* __restrict__ view_pos, uint32_t
 // Leaves and the two levels above them; with `done` (32768 <= P <= 2^20) the last CTA to finish also
 // builds the one or two levels up to the root.
 __global__ void __launch_bounds__(1024) lbvh_leaves_kernel(
-    const uint2* __restrict__ light_index, const float4* __restrict__ view_pos, const float4* __restrict__ lights,
+    const uint2* light_index, const float4* view_pos, const float4* lights,
     uint32_t L, uint32_t P, vren_bvh_node* __restrict__ bvh, float4* __restrict__ spheres, uint32_t* __restrict__ done)
 {
     pdl_enter();
@@ -162,8 +162,8 @@ constexpr uint32_t kSmallPathLights = 2048;   // measured: at 16384 lights the m
 constexpr int kSmallThreads = 1024;
 constexpr size_t kSmallSmem = (2 * kSmallLights + 32 * 256) * sizeof(uint32_t);
 
-__global__ void __launch_bounds__(kSmallThreads) lbvh_small_kernel(const float4* __restrict__ positions, uint32_t L,
-                                                                   const vren_cs_frame* __restrict__ F,
+__global__ void __launch_bounds__(kSmallThreads) lbvh_small_kernel(const float4* positions, uint32_t L,
+                                                                   const vren_cs_frame* F,
                                                                    float4* __restrict__ view_pos,
                                                                    uint2* __restrict__ light_index)
 {
@@ -339,8 +339,8 @@ __device__ __forceinline__ void dsmem_st(uint32_t addr, uint32_t v)
 }
 
 __global__ void __launch_bounds__(kClusterThreads) lbvh_cluster_kernel(
-    const float4* __restrict__ positions, const float4* __restrict__ lights, uint32_t L,
-    const vren_cs_frame* __restrict__ F, float4* __restrict__ view_pos, uint2* __restrict__ light_index,
+    const float4* positions, const float4* lights, uint32_t L,
+    const vren_cs_frame* F, float4* __restrict__ view_pos, uint2* __restrict__ light_index,
     vren_bvh_node* __restrict__ bvh, float4* __restrict__ spheres)
 {
     pdl_enter();
@@ -783,10 +783,10 @@ static int launch_find_unique_fused(cudaStream_t st, const float* depth, const f
 // for their lengths): out = [U, total, keys[U], counts[U], offsets[U], indices[total]], cut at cap
 // words (VREN_ERR_CAPACITY recorded when it does not fit).  `total` is the number of index entries
 // the device holds: the assignment's total, cut at its index capacity.
-__global__ void lists_to_host_kernel(const uint32_t* __restrict__ key_count, uint32_t key_cap,
-                                     const uint32_t* __restrict__ total_p, const uint32_t* __restrict__ keys,
-                                     const uint32_t* __restrict__ counts, const uint32_t* __restrict__ offsets,
-                                     const uint32_t* __restrict__ indices, uint32_t index_cap,
+__global__ void lists_to_host_kernel(const uint32_t* key_count, uint32_t key_cap,
+                                     const uint32_t* total_p, const uint32_t* keys,
+                                     const uint32_t* counts, const uint32_t* offsets,
+                                     const uint32_t* indices, uint32_t index_cap,
                                      uint32_t* __restrict__ out, uint64_t cap)
 {
     pdl_enter();
@@ -920,7 +920,7 @@ __global__ void __launch_bounds__(256) assign_fused_kernel(AssignArgs a, LevelBa
     }
 }
 
-__global__ void zero_counts_kernel(const uint32_t* __restrict__ key_count, uint32_t key_cap, uint32_t* __restrict__ counts,
+__global__ void zero_counts_kernel(const uint32_t* key_count, uint32_t key_cap, uint32_t* __restrict__ counts,
                                    uint32_t* __restrict__ offsets, uint32_t* __restrict__ total)
 {
     pdl_enter();

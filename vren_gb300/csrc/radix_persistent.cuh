@@ -145,7 +145,7 @@ __device__ __forceinline__ void persist_producer(const uint32_t* __restrict__ in
 
 template <int DB, int MODE>
 __global__ void __launch_bounds__(kPThreads, 2) onesweep_persistent_kernel(
-    const uint32_t* __restrict__ in_keys, const uint32_t* __restrict__ in_vals, uint32_t* __restrict__ out_keys,
+    const uint32_t* in_keys, const uint32_t* in_vals, uint32_t* __restrict__ out_keys,
     uint32_t* __restrict__ out_vals, uint32_t n, uint32_t pass, uint32_t shift, uint32_t width, uint32_t num_tiles,
     uint32_t* __restrict__ scratch, uint32_t wait_limit, uint32_t spin)
 {

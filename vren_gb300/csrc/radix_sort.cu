@@ -61,7 +61,7 @@ __device__ __forceinline__ uint32_t digit_of(uint32_t key, uint32_t shift, uint3
 // ------------------------------------------------------------------------------------------------
 template <int RADIX, int MODE>
 __global__ void __launch_bounds__(kSortThreads) onesweep_hist_kernel(
-    const uint32_t* __restrict__ keys, uint32_t n, PassInfo passes, uint32_t* __restrict__ scratch,
+    const uint32_t* keys, uint32_t n, PassInfo passes, uint32_t* __restrict__ scratch,
     uint32_t status_words)
 {
     pdl_enter();
@@ -342,7 +342,7 @@ __device__ __forceinline__ void onesweep_pass_body(
 
 template <int DIGIT_BITS, int ITEMS, int MODE, int RANK>
 __global__ void __launch_bounds__(kSortThreads, 4) onesweep_pass_kernel(
-    const uint32_t* __restrict__ in_keys, const uint32_t* __restrict__ in_vals,
+    const uint32_t* in_keys, const uint32_t* in_vals,
     uint32_t* __restrict__ out_keys, uint32_t* __restrict__ out_vals,
     uint32_t n, uint32_t pass, uint32_t shift, uint32_t width, uint32_t num_tiles,
     uint32_t* __restrict__ scratch, uint32_t wait_limit, uint32_t spin)
@@ -428,7 +428,7 @@ constexpr uint32_t kBucketScanRows = 8;                          // rows per sca
 // start offsets, then the count matrix [rows][1024] (16-byte aligned).
 constexpr uint32_t kBkTotals = 16, kBkStarts = kBkTotals + kBucketRadix, kBkRows = kBkStarts + kBucketRadix;
 
-__global__ void __launch_bounds__(kSortThreads) bucket_tile_hist_kernel(const uint2* __restrict__ in, uint32_t n,
+__global__ void __launch_bounds__(kSortThreads) bucket_tile_hist_kernel(const uint2* in, uint32_t n,
                                                                        uint32_t key_bits,
                                                                        uint32_t* __restrict__ scratch)
 {

@@ -64,7 +64,7 @@ __device__ __forceinline__ uint32_t take_tile(uint32_t* scratch, uint32_t total_
 template <int SLICES>
 __global__ void __launch_bounds__(kScanThreads, 4) exclusive_scan_kernel(
     const uint32_t* in, uint32_t* data, uint32_t n, uint32_t tiles_per_seg, uint32_t total_tiles,
-    uint32_t* __restrict__ scratch, uint32_t wait_limit, uint32_t spin, const uint32_t* __restrict__ n_dev,
+    uint32_t* __restrict__ scratch, uint32_t wait_limit, uint32_t spin, const uint32_t* n_dev,
     uint32_t* __restrict__ total_out)
 {
     pdl_enter();
