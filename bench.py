@@ -42,9 +42,9 @@ BYTES_PER_PX = 20  # depth 4 + normal 12 (f32x3) + cluster reference 4
 # read + 17.6 MB written, tile-count scan 0.04 MB, fix-up 34.3 MB read) scaled by the pixel count
 # (1/4).  ncu flushed the caches before each kernel, so the fix-up's read of the references
 # (L2-resident in a timed run) is counted here.
-FUC_TRAFFIC_BYTES = int((133.836032 + 17.552128 + 0.040192 + 34.295040 + 0.000512) * 1e6 / 4)
-FUC_TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the three kernels at 3840x2160 (caches "
-                      "flushed before each), scaled by pixels to 1920x1080")
+FUC_TRAFFIC_BYTES = int((133.848320 + 17.563392 + 34.263296 + 0.001024) * 1e6 / 4)
+FUC_TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the two kernels (tiles, self-offset "
+                      "fix-up) at 3840x2160 (caches flushed before each), scaled by pixels to 1920x1080")
 
 
 def peaks():
@@ -237,19 +237,33 @@ def run_ours(args, rank: int, world: int):
 
     h2d_bytes = sum(t.numel() * t.element_size() for t in (h_depth, h_norm, h_pos, h_light))
     lists_host = h_lists.numpy()  # the result is read from page-locked host memory
-    e2e_ms, d2h_total = [], 0
-    for i in range(args.warmup + args.steps):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        with torch.cuda.stream(stream):
-            ctx.cluster_host(stream, view, W, H, h_depth, h_norm, h_pos, h_light, L, h_refs, h_lists)
-            stream.synchronize()
-        u, tot = int(lists_host[0]), int(lists_host[1])
-        if i >= args.warmup:
-            e2e_ms.append((time.perf_counter() - t0) * 1e3)
-            d2h_total = 8 + W * H * 4 + u * 12 + tot * 4
-    e2e = sum(e2e_ms) / len(e2e_ms)
-    e2e_refs_ok = bool(np.array_equal(h_refs.numpy(), cs.read_device(out.cluster_refs, W * H).view(np.int32)))
+    zc_knob = vg._lib.TUNE["host_zero_copy"]
+    zc_default = vg.lib().vren_tuning_get(zc_knob)
+
+    def run_e2e(zero_copy: int):
+        vg.lib().vren_tuning_set(zc_knob, zero_copy)
+        times, d2h = [], 0
+        for i in range(args.warmup + args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            with torch.cuda.stream(stream):
+                ctx.cluster_host(stream, view, W, H, h_depth, h_norm, h_pos, h_light, L, h_refs, h_lists)
+                stream.synchronize()
+            u, tot = int(lists_host[0]), int(lists_host[1])
+            if i >= args.warmup:
+                times.append((time.perf_counter() - t0) * 1e3)
+                d2h = 8 + W * H * 4 + u * 12 + tot * 4
+        ok = bool(np.array_equal(h_refs.numpy(), cs.read_device(out.cluster_refs, W * H).view(np.int32)))
+        return sum(times) / len(times), d2h, ok
+
+    # both host-input forms (the G-buffer copied up in bands / read over the link by the kernel); the
+    # headline is the library's default form
+    e2e_forms = {}
+    for zc, name in ((0, "banded_copies"), (1, "zero_copy_kernel_reads")):
+        ms_f, _, ok_f = run_e2e(zc)
+        e2e_forms[name] = {"ms": round(ms_f, 4), "refs_match_device": ok_f}
+    e2e, d2h_total, e2e_refs_ok = run_e2e(zc_default)
+    vg.lib().vren_tuning_set(zc_knob, zc_default)
     link = link_bench(dev, stream, h2d_bytes, d2h_total, max(5, args.steps), e2e)
 
     # extra, labelled: the same frame with 16384 lights packed in front of the camera, so that the
@@ -375,9 +389,12 @@ def run_ours(args, rank: int, world: int):
             },
             "e2e": {"value": round(e2e, 4), "unit": "ms", "h2d_bytes_per_step": h2d_bytes,
                     "d2h_bytes_per_step": d2h_total,
-                    "path": "vren_cs_cluster_host from pinned buffers (banded G-buffer upload overlapping the light "
-                            "BVH and the unique-cluster tiles, reference download overlapping the assignment, light "
-                            "lists written to host memory by the device); host wall clock",
+                    "path": "vren_cs_cluster_host from pinned buffers, the library's default host-input form "
+                            "(" + ("the unique-cluster kernel reading the G-buffer and writing the references over "
+                                   "the link" if zc_default else "banded G-buffer upload overlapping the light BVH "
+                                   "and the unique-cluster tiles, reference download overlapping the assignment")
+                            + "; light lists written to host memory by the device); host wall clock",
+                    "forms_ms": e2e_forms,
                     "refs_match_device": e2e_refs_ok},
             "link": link,
             "normals_rgba16f": rgba16f,

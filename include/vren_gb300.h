@@ -102,11 +102,16 @@ int vren_test_withhold_scan_status(uint32_t tile_plus_one);
  *   VREN_TUNE_BUCKET_FORM  bucket sort of up to 10 key bits: 0 = one pass over the elements (a
  *                          histogram kernel, then one scatter kernel with a look-back over 1024
  *                          buckets; the default), 1 = stable radix passes of at most 8 bits, then
- *                          the end offsets read back from the sorted elements */
+ *                          the end offsets read back from the sorted elements
+ *   VREN_TUNE_HOST_ZERO_COPY vren_cs_cluster_host: 0 = the G-buffer copied up in bands, each band's
+ *                          tiles processed on arrival; 1 = the unique-cluster kernel (one-kernel
+ *                          form) reads depth and normals straight from the page-locked host buffers
+ *                          and writes the references to cluster_refs_out as it goes (used when the
+ *                          device can address those buffers, else the banded copies run) */
 enum { VREN_TUNE_SCAN_SLICES = 0, VREN_TUNE_SPIN_POLLS = 1, VREN_TUNE_RADIX_RANK = 2, VREN_TUNE_RADIX_ITEMS = 3,
        VREN_TUNE_SCAN_STAGED = 4, VREN_TUNE_REDUCE_FORM = 5, VREN_TUNE_LIGHT_BVH_CLUSTER = 6,
        VREN_TUNE_ASSIGN_FUSED = 7, VREN_TUNE_RADIX_PERSISTENT = 8, VREN_TUNE_FUC_FUSED = 9, VREN_TUNE_BUCKET_FORM = 10,
-       VREN_TUNE_COUNT = 11 };
+       VREN_TUNE_HOST_ZERO_COPY = 11, VREN_TUNE_COUNT = 12 };
 int vren_tuning_set(int knob, int value);
 int vren_tuning_get(int knob);
 

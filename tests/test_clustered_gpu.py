@@ -444,11 +444,24 @@ def test_cluster_and_shade_context(cuda, use_graph):
         check_context_outputs(ctx, W, H, view, depth, normals, pos, li, L)
 
 
+@pytest.fixture
+def host_zero_copy():
+    lib = vg.lib()
+    knob = vg._lib.TUNE["host_zero_copy"]
+    saved = lib.vren_tuning_get(knob)
+    yield lambda v: lib.vren_tuning_set(knob, v)
+    lib.vren_tuning_set(knob, saved)
+
+
 @pytest.mark.parametrize("use_graph", [True, False])
-def test_cluster_host_matches_device_path(cuda, use_graph):
-    """vren_cs_cluster_host (page-locked host inputs, overlapped uploads and reference download) gives
-    the same outputs as vren_cs_cluster on the same data."""
-    W, H, L = 640, 360, 3000
+@pytest.mark.parametrize("zero_copy,W,H", [(0, 640, 360), (1, 640, 360), (1, 601, 333)])
+def test_cluster_host_matches_device_path(cuda, host_zero_copy, use_graph, zero_copy, W, H):
+    """vren_cs_cluster_host (page-locked host inputs; the G-buffer copied up in bands with the
+    reference download overlapped, or read and written over the link by the unique-cluster kernel
+    itself) gives the same outputs as vren_cs_cluster on the same data; a width that is not a multiple
+    of 4 takes the kernels' scalar loads."""
+    assert host_zero_copy(zero_copy) == 0
+    L = 3000
     view = make_view(W, H)
     depth, normals = scene.depth_planes(41, W, H)
     pos, li = dense_lights(42, L)

@@ -720,7 +720,7 @@ static FucFrame fuc_frame(const float* depth, const float* normals, uint32_t W, 
                     ((uintptr_t)refs % 16u == 0u);
     return FucFrame{depth, normals, W, H, frame, keys, key_cap, key_count, refs,
                     scratch ? scratch + fuc_keys_offset_words(tiles) : nullptr, scratch,
-                    scratch ? scratch + tiles : nullptr, tiles, vec, nullptr, 0u, 0u};
+                    scratch ? scratch + tiles : nullptr, tiles, vec, nullptr, 0u, 0u, nullptr};
 }
 
 // Stage 1 over tiles [tile_begin, tile_begin + count).
@@ -768,9 +768,12 @@ static size_t fuc_lookback_bytes(uint32_t tiles) { return 16u + 8ull * tiles; }
 // before its first use.
 static int launch_find_unique_fused(cudaStream_t st, const float* depth, const float* normals, uint32_t W, uint32_t H,
                                     const vren_cs_frame* frame, uint32_t* keys, uint32_t key_cap,
-                                    uint32_t* key_count, uint32_t* refs, uint32_t* lookback)
+                                    uint32_t* key_count, uint32_t* refs, uint32_t* lookback,
+                                    uint32_t* refs2 = nullptr)
 {
     FucFrame fr = fuc_frame(depth, normals, W, H, frame, keys, key_cap, key_count, refs, nullptr);
+    fr.refs2 = refs2;
+    if ((uintptr_t)refs2 % 16u != 0u) fr.vec = 0;
     fr.status = reinterpret_cast<uint64_t*>(lookback + 4);
     fr.wait_limit = g_wait_limit;
     fr.spin = (uint32_t)tuning(VREN_TUNE_SPIN_POLLS);
@@ -1278,6 +1281,7 @@ struct vren_cluster_and_shade {
         void* refs_out;
         void* lists_out;
         uint64_t lists_cap;
+        uint64_t zero_copy;  // the form the graph was captured with
     } host_key{};
     // vren_cs_cluster_and_shade: the graph of the last clustered-and-shaded frame shape
     cudaGraphExec_t shade_graph = nullptr;
@@ -1498,9 +1502,33 @@ int refresh_frame(vren_cluster_and_shade* cs, cudaStream_t st, const vren_cs_vie
 // depth and normals go up on `st` in bands of tile rows, each band's tiles processed as it arrives;
 // then the references go down on the second stream while the light lists are assigned on `st`, and
 // the lists are written into host memory by the device.
+// The address under which the device reads or writes the host buffer `p` (page-locked and mapped,
+// or any host memory when the device has pageable-memory access), or null when it cannot.
+const void* device_view_of_host(const void* p)
+{
+    if (!p) return nullptr;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type == cudaMemoryTypeHost && a.devicePointer) return a.devicePointer;
+    if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return p;
+    int dev = 0, pageable = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return pageable ? p : nullptr;
+}
+
+// zc_depth / zc_normals: the device's views of the host G-buffer for the zero-copy form (both null
+// for the banded copies); zc_refs: the device's view of refs_out (null when no references go down).
 int cs_enqueue_host(vren_cluster_and_shade* cs, cudaStream_t st, uint32_t W, uint32_t H, const float* depth,
                     const float* normals, const float* positions, const float* lights, uint32_t L, uint32_t* refs_out,
-                    uint32_t* lists_out, uint64_t lists_cap)
+                    uint32_t* lists_out, uint64_t lists_cap, const float* zc_depth = nullptr,
+                    const float* zc_normals = nullptr, uint32_t* zc_refs = nullptr)
 {
     const PdlScope pdl(1);
     cudaStream_t aux = cs->aux, up = cs->up;
@@ -1517,42 +1545,53 @@ int cs_enqueue_host(vren_cluster_and_shade* cs, cudaStream_t st, uint32_t W, uin
         if (rc != VREN_OK) return rc;
     }
     VREN_CUDA_TRY(cudaEventRecord(cs->ev_bvh, aux));
-    // G-buffer up in bands of tile rows, each band's tiles processed as soon as it has arrived (the last
-    // tile row may wrap to the first rows, which arrive first)
-    const FucFrame fr = fuc_frame(cs->in_depth, cs->in_normals, W, H, cs->frame, cs->keys, cs->key_cap,
-                                  cs->key_count, cs->refs, static_cast<uint32_t*>(cs->fuc_scratch));
-    const uint32_t TX = (W + 31) / 32, TY = (H + 31) / 32;
-    const uint32_t bands = TY < 4u ? TY : 4u, per = (TY + bands - 1) / bands;
-    const size_t nbytes = cs->opt.normal_format == VREN_CS_NORMALS_RGBA16F ? 8 : 12;  // per pixel
-    uint32_t band = 0;
-    for (uint32_t ty0 = 0; ty0 < TY; ty0 += per, ++band) {  // uploads on `up`, one event per band
-        const uint32_t ty1 = ty0 + per < TY ? ty0 + per : TY;
-        const size_t y0 = (size_t)ty0 * 32, y1 = (size_t)ty1 * 32 < H ? (size_t)ty1 * 32 : H;
-        VREN_CUDA_TRY(cudaMemcpyAsync(cs->in_depth + y0 * W, depth + y0 * W, (y1 - y0) * W * 4,
-                                      cudaMemcpyHostToDevice, up));
-        VREN_CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<char*>(cs->in_normals) + y0 * W * nbytes,
-                                      reinterpret_cast<const char*>(normals) + y0 * W * nbytes, (y1 - y0) * W * nbytes,
-                                      cudaMemcpyHostToDevice, up));
-        VREN_CUDA_TRY(cudaEventRecord(cs->ev_band[band], up));
-    }
-    VREN_CUDA_TRY(cudaEventRecord(cs->ev_join_up, up));
-    // Each band once it has arrived: its tiles, then its tile offsets (continuing from the band above)
-    // and fix-up, after which its rows of references are final and go down on `aux` while the next
-    // bands are still coming up.
-    band = 0;
-    for (uint32_t ty0 = 0; ty0 < TY; ty0 += per, ++band) {
-        const uint32_t ty1 = ty0 + per < TY ? ty0 + per : TY;
-        VREN_CUDA_TRY(cudaStreamWaitEvent(st, cs->ev_band[band], 0));
-        rc = launch_find_unique_tiles(st, fr, ty0 * TX, (ty1 - ty0) * TX);
+    if (zc_depth && zc_normals) {
+        // Zero-copy: the one-kernel unique-cluster form reads the G-buffer over the link as its tiles
+        // run (tiles in order, offsets by look-back), so the reads and the references going down
+        // (written to both the context and refs_out as each tile finishes) share the link's two
+        // directions for the whole kernel.
+        VREN_CUDA_TRY(cudaEventRecord(cs->ev_join_up, up));
+        rc = launch_find_unique_fused(st, zc_depth, zc_normals, W, H, cs->frame, cs->keys, cs->key_cap, cs->key_count,
+                                      cs->refs, cs->fuc_lookback, zc_refs);
         if (rc != VREN_OK) return rc;
-        rc = launch_find_unique_finish(st, fr, ty0 * TX, ty1 * TX);
-        if (rc != VREN_OK) return rc;
-        if (refs_out) {
+    } else {
+        // G-buffer up in bands of tile rows, each band's tiles processed as soon as it has arrived (the last
+        // tile row may wrap to the first rows, which arrive first)
+        const FucFrame fr = fuc_frame(cs->in_depth, cs->in_normals, W, H, cs->frame, cs->keys, cs->key_cap,
+                                      cs->key_count, cs->refs, static_cast<uint32_t*>(cs->fuc_scratch));
+        const uint32_t TX = (W + 31) / 32, TY = (H + 31) / 32;
+        const uint32_t bands = TY < 4u ? TY : 4u, per = (TY + bands - 1) / bands;
+        const size_t nbytes = cs->opt.normal_format == VREN_CS_NORMALS_RGBA16F ? 8 : 12;  // per pixel
+        uint32_t band = 0;
+        for (uint32_t ty0 = 0; ty0 < TY; ty0 += per, ++band) {  // uploads on `up`, one event per band
+            const uint32_t ty1 = ty0 + per < TY ? ty0 + per : TY;
             const size_t y0 = (size_t)ty0 * 32, y1 = (size_t)ty1 * 32 < H ? (size_t)ty1 * 32 : H;
-            VREN_CUDA_TRY(cudaEventRecord(cs->ev_done[band], st));
-            VREN_CUDA_TRY(cudaStreamWaitEvent(aux, cs->ev_done[band], 0));
-            VREN_CUDA_TRY(cudaMemcpyAsync(refs_out + y0 * W, cs->refs + y0 * W, (y1 - y0) * W * 4,
-                                          cudaMemcpyDeviceToHost, aux));
+            VREN_CUDA_TRY(cudaMemcpyAsync(cs->in_depth + y0 * W, depth + y0 * W, (y1 - y0) * W * 4,
+                                          cudaMemcpyHostToDevice, up));
+            VREN_CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<char*>(cs->in_normals) + y0 * W * nbytes,
+                                          reinterpret_cast<const char*>(normals) + y0 * W * nbytes, (y1 - y0) * W * nbytes,
+                                          cudaMemcpyHostToDevice, up));
+            VREN_CUDA_TRY(cudaEventRecord(cs->ev_band[band], up));
+        }
+        VREN_CUDA_TRY(cudaEventRecord(cs->ev_join_up, up));
+        // Each band once it has arrived: its tiles, then its tile offsets (continuing from the band above)
+        // and fix-up, after which its rows of references are final and go down on `aux` while the next
+        // bands are still coming up.
+        band = 0;
+        for (uint32_t ty0 = 0; ty0 < TY; ty0 += per, ++band) {
+            const uint32_t ty1 = ty0 + per < TY ? ty0 + per : TY;
+            VREN_CUDA_TRY(cudaStreamWaitEvent(st, cs->ev_band[band], 0));
+            rc = launch_find_unique_tiles(st, fr, ty0 * TX, (ty1 - ty0) * TX);
+            if (rc != VREN_OK) return rc;
+            rc = launch_find_unique_finish(st, fr, ty0 * TX, ty1 * TX);
+            if (rc != VREN_OK) return rc;
+            if (refs_out) {
+                const size_t y0 = (size_t)ty0 * 32, y1 = (size_t)ty1 * 32 < H ? (size_t)ty1 * 32 : H;
+                VREN_CUDA_TRY(cudaEventRecord(cs->ev_done[band], st));
+                VREN_CUDA_TRY(cudaStreamWaitEvent(aux, cs->ev_done[band], 0));
+                VREN_CUDA_TRY(cudaMemcpyAsync(refs_out + y0 * W, cs->refs + y0 * W, (y1 - y0) * W * 4,
+                                              cudaMemcpyDeviceToHost, aux));
+            }
         }
     }
     VREN_CUDA_TRY(cudaStreamWaitEvent(st, cs->ev_bvh, 0));
@@ -1648,10 +1687,22 @@ extern "C" int vren_cs_cluster_host(vren_cluster_and_shade* cs, vren_stream_t s,
     key.refs_out = cluster_refs_out;
     key.lists_out = lists_out;
     key.lists_cap = lists_capacity;
+    // The zero-copy form when it is selected and the device can address the G-buffer (and refs_out)
+    const float* zc_depth = nullptr;
+    const float* zc_normals = nullptr;
+    uint32_t* zc_refs = nullptr;
+    if (tuning(VREN_TUNE_HOST_ZERO_COPY) == 1) {
+        zc_depth = static_cast<const float*>(device_view_of_host(depth));
+        zc_normals = static_cast<const float*>(device_view_of_host(normals));
+        zc_refs = cluster_refs_out ? static_cast<uint32_t*>(const_cast<void*>(device_view_of_host(cluster_refs_out)))
+                                   : nullptr;
+        if (!zc_depth || !zc_normals || (cluster_refs_out && !zc_refs)) zc_depth = zc_normals = nullptr, zc_refs = nullptr;
+    }
+    key.zero_copy = zc_depth ? 1u : 0u;
     const bool use_graph = cs->opt.use_graph && st != nullptr;
     if (!use_graph)
         return cs_enqueue_host(cs, st, width, height, depth, normals, light_positions, point_lights, light_count,
-                               cluster_refs_out, lists_out, lists_capacity);
+                               cluster_refs_out, lists_out, lists_capacity, zc_depth, zc_normals, zc_refs);
     if (cs->host_graph && std::memcmp(&key, &cs->host_key, sizeof(key)) == 0) {
         VREN_CUDA_TRY(cudaGraphLaunch(cs->host_graph, st));
         return VREN_OK;
@@ -1663,7 +1714,7 @@ extern "C" int vren_cs_cluster_host(vren_cluster_and_shade* cs, vren_stream_t s,
     cudaGraph_t g;
     VREN_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     rc = cs_enqueue_host(cs, st, width, height, depth, normals, light_positions, point_lights, light_count,
-                         cluster_refs_out, lists_out, lists_capacity);
+                         cluster_refs_out, lists_out, lists_capacity, zc_depth, zc_normals, zc_refs);
     cudaError_t e = cudaStreamEndCapture(st, &g);
     if (rc != VREN_OK) {
         if (e == cudaSuccess) cudaGraphDestroy(g);

@@ -293,6 +293,7 @@ struct FucFrame {
     // limit and the polls before back-off
     uint64_t* status;
     uint32_t wait_limit, spin;
+    uint32_t* refs2;  // one-kernel form only: a second destination of the final references, or null
 };
 
 // Stage 1 for tile `tile` of frame `fr`, all threads of the CTA; sm.bits and sm.used must be zero
@@ -525,10 +526,18 @@ __device__ __forceinline__ void find_unique_tile(const FucFrame& fr, uint32_t ti
     }
     if (full) {
         *reinterpret_cast<uint4*>(refs + (size_t)gy * W + gx0) = make_uint4(r[0], r[1], r[2], r[3]);
+        if constexpr (FUSED) {
+            if (fr.refs2) *reinterpret_cast<uint4*>(fr.refs2 + (size_t)gy * W + gx0) = make_uint4(r[0], r[1], r[2], r[3]);
+        }
     } else if (gy < H) {
 #pragma unroll
         for (int j = 0; j < 4; ++j)
-            if (gx0 + j < W) refs[(size_t)gy * W + gx0 + j] = r[j];
+            if (gx0 + j < W) {
+                refs[(size_t)gy * W + gx0 + j] = r[j];
+                if constexpr (FUSED) {
+                    if (fr.refs2) fr.refs2[(size_t)gy * W + gx0 + j] = r[j];
+                }
+            }
     }
 
 }
