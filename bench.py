@@ -436,6 +436,8 @@ def run_ours(args, rank: int, world: int):
             "adjoint_rel_err_vs_fp64": adj.get("rel_err_max_group"), "adjoint_target": 1e-4,
             "adjoint_lights_checked": adj.get("lights_checked"),
             "e2e_ms": round(e2e, 4), "e2e_link_floor_ms": link["e2e_floor_ms"],
+            "frame_ms": round(ms_frame, 5),
+            "bucket_sort_hbm_frac_2^24_10bit": ((sweep or {}).get("bucket_sort_2^24_10bit") or {}).get("hbm_frac"),
         }
         print(json.dumps(res), flush=True)
 
@@ -1160,6 +1162,16 @@ def run_profile(args):
         ctx = cs.cluster_and_shade(W, H, 65536, 1 << 24)
         bufs = [torch.from_numpy(x).to(dev) for x in (depth, normals, pos, lights)]
         fn = lambda: ctx.cluster(stream, view, W, H, *bufs, L)
+    elif args.profile == "frame_dense":
+        # the benchmark's frame with its 16384 lights packed in front of the camera (long light lists)
+        import vren_gb300.scene as scene
+
+        depth, normals, _, _, _, _ = make_inputs(0)
+        dpos, dlights = scene.lights_near_camera(SEED + 77, L)
+        view = cs.view_from_camera(cs.scene_camera(W, H), "ref")
+        ctx = cs.cluster_and_shade(W, H, 65536, 1 << 24)
+        bufs = [torch.from_numpy(x).to(dev) for x in (depth, normals, dpos, dlights)]
+        fn = lambda: ctx.cluster(stream, view, W, H, *bufs, L)
     elif args.profile in ("find_unique", "find_unique_rgba16f"):
         w, h = 3840, 2160  # 20 B/px (f32x3 normals; 16 with RGBA16F) -> 166 (133) MB > L2
         depth, normals = scene.depth_planes(SEED, w, h)
@@ -1389,7 +1401,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--quick", action="store_true", help="skip the primitive sweep and the large sorts")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--profile", choices=["frame", "batch", "find_unique", "find_unique_rgba16f", "radix", "scan",
+    ap.add_argument("--profile", choices=["frame", "frame_dense", "batch", "find_unique", "find_unique_rgba16f", "radix", "scan",
                                           "shade", "shade_backward", "pyramid", "pyramid_4k", "reduce", "bucket",
                                           "build_bvh", "assign", "karras", "bouncer", "debug_views", "kd_tree",
                                           "light_bvh_multi", "batch_small"],
