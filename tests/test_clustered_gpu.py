@@ -422,6 +422,31 @@ def test_cluster_and_shade_context_1080p(cuda, slicing, fuc_form):
         lib.vren_tuning_set(knob, 0)
 
 
+@pytest.mark.parametrize("radius_scale", [1.0, 2.0])
+def test_cluster_and_shade_context_long_lists(cuda, radius_scale):
+    """Lists around and far above the 128 lights that the count pass keeps for the write pass to copy
+    (1.0: up to 142 lights, most clusters between 65 and 128; 2.0: up to 670): the copied and the
+    re-traversed lists equal the oracle's."""
+    W, H, L = 640, 360, 20000
+    view = make_view(W, H)
+    depth, normals = scene.depth_planes(77, W, H)
+    pos, li = dense_lights(78, L)
+    li = li.reshape(-1, 4).copy()
+    li[:, 3] *= np.float32(radius_scale)
+    li = li.reshape(-1)
+    ctx = cs.cluster_and_shade(W, H, L, 1 << 22)
+    stream = torch.cuda.Stream()
+    bufs = [to_dev(x, cuda) for x in (depth, normals, pos, li)]
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        ctx.cluster(stream, view, W, H, *bufs, L)
+    stream.synchronize()
+    check_context_outputs(ctx, W, H, view, depth, normals, pos, li, L)
+    o = ctx.outputs()
+    counts = cs.read_device(o.counts, int(cs.read_device(o.key_count, 1)[0]))
+    assert counts.max() > 128 and ((counts > 64) & (counts <= 128)).any()
+
+
 @pytest.mark.parametrize("use_graph", [False, True])
 def test_cluster_and_shade_context(cuda, use_graph):
     W, H, L = 1280, 720, 5000

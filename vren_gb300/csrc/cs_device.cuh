@@ -668,7 +668,7 @@ struct AssignArgs {
 };
 
 // Lights a cluster can keep from the count pass for the write pass to copy instead of traversing again.
-constexpr uint32_t kStageLights = 64;
+constexpr uint32_t kStageLights = 128;
 
 // The reference walks the 32-ary tree with an explicit state machine over per-level overlap
 // masks (assign_lights.comp:142-240): ENTERING tests the 32 nodes of a group with one ballot,
