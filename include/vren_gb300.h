@@ -88,8 +88,11 @@ int vren_test_withhold_scan_status(uint32_t tile_plus_one);
  *   VREN_TUNE_LIGHT_BVH_CLUSTER  light BVH of 2049..32768 lights (15-bit codes): 1 = one kernel on a
  *                          16-CTA thread-block cluster when the device can hold one (default),
  *                          0 = the multi-kernel path
- *   VREN_TUNE_ASSIGN_FUSED assign_lights: 0 = count kernel, exclusive scan, write kernel (default),
- *                          1 = one kernel (count, look-back over the cluster counts, write)
+ *   VREN_TUNE_ASSIGN_FUSED assign_lights: 0 = count kernel, exclusive scan, write kernel (default);
+ *                          1 = one kernel (count, look-back over the cluster counts, write); 2 = a
+ *                          count kernel that also writes the offsets (its CTAs own ranges of
+ *                          clusters and resolve the counts before their range by look-back), then
+ *                          the write kernel
  *   VREN_TUNE_RADIX_PERSISTENT  sort passes over keys or pairs whose input starts 16-byte aligned:
  *                          1 = persistent grid whose producer warp streams tiles into shared memory
  *                          by bulk copies and publishes their digit counts on arrival, 0 = one CTA

@@ -296,11 +296,12 @@ def test_assign_lights_dense(cuda, L, spheres):
     assert et > 0 or L == 1
 
 
-@pytest.mark.parametrize("fused", [1, 0])
+@pytest.mark.parametrize("fused", [0, 1, 2])
 @pytest.mark.parametrize("L,seed", [(20, 20), (5000, 5000), (40000, 40000)])
 def test_assign_lights_fused_and_three_kernel_forms(cuda, fused, L, seed):
-    """One kernel (chunk totals resolved by look-back) and count/scan/write give the oracle's counts,
-    offsets and lists; three calls in a row reuse the scratch (epoch-tagged status words)."""
+    """Count/scan/write, one kernel (cluster counts resolved by look-back), and the count kernel that
+    writes the offsets followed by the write kernel give the oracle's counts, offsets and lists; three
+    calls in a row reuse the scratch (epoch-tagged status words)."""
     lib = vg.lib()
     knob = vg._lib.TUNE["assign_fused"]
     assert lib.vren_tuning_set(knob, fused) == 0

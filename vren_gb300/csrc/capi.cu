@@ -98,9 +98,9 @@ extern "C" int vren_tuning_set(int knob, int value)
         break;
     case VREN_TUNE_LIGHT_BVH_CLUSTER:
     case VREN_TUNE_FUC_FUSED:
+    case VREN_TUNE_ASSIGN_FUSED:
         if (value < 0 || value > 2) return VREN_ERR_ARG;
         break;
-    case VREN_TUNE_ASSIGN_FUSED:
     case VREN_TUNE_RADIX_PERSISTENT:
     case VREN_TUNE_BUCKET_FORM:
     case VREN_TUNE_HOST_ZERO_COPY:

@@ -936,6 +936,135 @@ __global__ void zero_counts_kernel(const uint32_t* key_count, uint32_t key_cap, 
     if (total && blockIdx.x == 0 && threadIdx.x == 0) *total = 0u;
 }
 
+// The count pass with the offsets step folded in (count -> exclusive scan of the counts -> offsets,
+// clustered_shading.cpp:612-640): a fixed grid of CTAs takes tickets in start order; ticket t owns the
+// clusters [t K, t K + K) with K = ceil(U / grid), its warps count (and keep) their lights, the CTA
+// sums its counts, publishes the sum and resolves the counts before its range by a decoupled
+// look-back over the preceding tickets (at most one per CTA of the grid, so the chain is short), then
+// writes its clusters' offsets; the last ticket writes the total.  State: a 64-bit [epoch | ticket]
+// word, then one 64-bit status word per CTA, at the end of the assignment scratch.  Measured at
+// 1080p / 16,384 lights it is slower than count -> scan -> write (frame 0.0547 against 0.0513 ms):
+// with all 1,216 ranges finishing their traversals together, the prefixes travel down the look-back
+// chain 32 ranges per round trip, which costs more than the scan launch it saves; selectable
+// (VREN_TUNE_ASSIGN_FUSED = 2).
+constexpr uint32_t kCountScanMaxGrid = (uint32_t)kNumSMsHint * 8u;
+constexpr uint32_t kCountScanThreads = 256;
+
+size_t count_scan_state_bytes() { return 16u + 8ull * kCountScanMaxGrid; }
+
+// The count-with-offsets state sits after the space of the other two forms, so that switching forms
+// between calls never reads one form's words as another's.
+size_t count_scan_state_offset(uint32_t key_capacity)
+{
+    const size_t a = scan_scratch_bytes(key_capacity), b = assign_fused_scratch_bytes(key_capacity);
+    return ((a > b ? a : b) + 15) / 16 * 16;
+}
+
+template <int LC, bool SPHERES>
+__global__ void __launch_bounds__(kCountScanThreads) assign_count_scan_kernel(AssignArgs a, LevelBase lb,
+                                                                            uint32_t* offsets, uint32_t* total,
+                                                                            uint32_t* state, uint32_t wait_limit,
+                                                                            uint32_t spin)
+{
+    pdl_enter();
+    constexpr uint32_t kWarps = kCountScanThreads / 32;
+    __shared__ uint32_t s_ticket, s_epoch, s_prefix;
+    __shared__ uint32_t s_warp[kWarps];
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    uint32_t U = *a.key_count;
+    if (U > a.key_cap) U = a.key_cap;
+    if (tid == 0) {
+        uint32_t e;
+        s_ticket = take_ticket(state, gridDim.x, e);
+        s_epoch = e;
+    }
+    __syncthreads();
+    const uint32_t t = s_ticket, epoch = s_epoch;
+    const uint32_t K = (U + gridDim.x - 1) / gridDim.x;
+    const uint32_t c0 = t * K < U ? t * K : U, c1 = c0 + K < U ? c0 + K : U;
+
+    // counts (a warp per cluster), the first kStageLights lights kept
+    for (uint32_t c = c0 + warp; c < c1; c += kWarps) {
+        const bool staged = a.stage != nullptr && c < a.stage_slots;
+        const uint32_t acc = staged ? assign_cluster<LC, false, SPHERES, true>(a, lb, a.keys[c], c * kStageLights, lane)
+                                    : assign_cluster<LC, false, SPHERES>(a, lb, a.keys[c], 0u, lane);
+        if (lane == 0) a.counts[c] = acc;
+    }
+    __syncthreads();
+
+    // the range's sum, published, and the counts before the range by look-back
+    uint32_t sum = 0;
+    for (uint32_t c = c0 + tid; c < c1; c += kCountScanThreads) sum += a.counts[c];
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) sum += __shfl_xor_sync(0xFFFFFFFFu, sum, d);
+    if (lane == 0) s_warp[warp] = sum;
+    __syncthreads();
+    uint64_t* status = reinterpret_cast<uint64_t*>(state + 4);
+    if (warp == 0) {
+        uint32_t range = lane < kWarps ? s_warp[lane] : 0u;
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) range += __shfl_xor_sync(0xFFFFFFFFu, range, d);
+        uint32_t prefix = 0;
+        if (t == 0) {
+            if (lane == 0) st_relaxed_u64(status, make_status(epoch, 2u, range));
+        } else {
+            if (lane == 0) st_relaxed_u64(status + t, make_status(epoch, 1u, range));
+            bool timed_out = false;
+            prefix = warp_lookback(status, t, 0u, epoch, lane, wait_limit, spin, timed_out);
+            if (__any_sync(0xFFFFFFFFu, timed_out) && lane == 0) VREN_RECORD_ERROR(VREN_ERR_TIMEOUT);
+            if (lane == 0) st_relaxed_u64(status + t, make_status(epoch, 2u, prefix + range));
+        }
+        if (lane == 0) {
+            s_prefix = prefix;
+            if (t == gridDim.x - 1 && total) *total = prefix + range;
+        }
+    }
+    __syncthreads();
+
+    // offsets of the range: block-wide exclusive scans of 256 counts at a time, from the prefix on
+    uint32_t run = s_prefix;
+    for (uint32_t seg = c0; seg < c1; seg += kCountScanThreads) {
+        const uint32_t c = seg + tid;
+        const uint32_t v = c < c1 ? a.counts[c] : 0u;
+        uint32_t incl = v;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+            if (lane >= (uint32_t)d) incl += y;
+        }
+        __syncthreads();  // s_warp of the previous segment has been read
+        if (lane == 31) s_warp[warp] = incl;
+        __syncthreads();
+        uint32_t before = 0, seg_total = 0;
+#pragma unroll
+        for (uint32_t w = 0; w < kWarps; ++w) {
+            const uint32_t x = s_warp[w];
+            if (w < warp) before += x;
+            seg_total += x;
+        }
+        if (c < c1) offsets[c] = run + before + incl - v;
+        run += seg_total;
+    }
+}
+
+template <bool SPHERES>
+static void launch_count_scan(cudaStream_t st, uint32_t lc, uint32_t grid, const AssignArgs& a, const LevelBase& lb,
+                              uint32_t* offsets, uint32_t* total, uint32_t* state)
+{
+    const uint32_t spin = (uint32_t)tuning(VREN_TUNE_SPIN_POLLS);
+#define VREN_CS(LCV) launch_kernel(assign_count_scan_kernel<LCV, SPHERES>, grid, kCountScanThreads, 0, st, a, lb, offsets, \
+                                   total, state, g_wait_limit, spin)
+    switch (lc) {
+    case 1: VREN_CS(1); break;
+    case 2: VREN_CS(2); break;
+    case 3: VREN_CS(3); break;
+    case 4: VREN_CS(4); break;
+    case 5: VREN_CS(5); break;
+    default: VREN_CS(6); break;
+    }
+#undef VREN_CS
+}
+
 template <bool WRITE, bool SPHERES>
 static void launch_assign(cudaStream_t st, uint32_t lc, dim3 grid, dim3 block, const AssignArgs& a, const LevelBase& lb)
 {
@@ -969,7 +1098,7 @@ static int assign_lights(cudaStream_t st, const uint32_t* keys, const uint32_t* 
     if (warps_per_cta < 1 || warps_per_cta > 8) warps_per_cta = 8;
     const dim3 block(32 * warps_per_cta);
     const dim3 grid(kNumSMsHint * (64 / warps_per_cta));
-    if (tuning(VREN_TUNE_ASSIGN_FUSED) != 0) {
+    if (tuning(VREN_TUNE_ASSIGN_FUSED) == 1) {
         uint32_t* sc = static_cast<uint32_t*>(scratch);
         const uint32_t spin = (uint32_t)tuning(VREN_TUNE_SPIN_POLLS);
 #define VREN_FUSED(LCV)                                                                                        \
@@ -989,11 +1118,20 @@ static int assign_lights(cudaStream_t st, const uint32_t* keys, const uint32_t* 
         VREN_LAUNCH_CHECK();
         return VREN_OK;
     }
-    if (spheres) launch_assign<false, true>(st, lc, grid, block, a, lb);
-    else launch_assign<false, false>(st, lc, grid, block, a, lb);
-    VREN_LAUNCH_CHECK();
-    int rc = scan_exclusive_u32(st, counts, offsets, key_cap, key_count, total, scratch);
-    if (rc != VREN_OK) return rc;
+    if (tuning(VREN_TUNE_ASSIGN_FUSED) == 2) {
+        // count with the offsets folded in, then write
+        uint32_t* state = reinterpret_cast<uint32_t*>(static_cast<char*>(scratch) + count_scan_state_offset(key_cap));
+        const uint32_t cs_grid = key_cap < kCountScanMaxGrid ? (key_cap ? key_cap : 1u) : kCountScanMaxGrid;
+        if (spheres) launch_count_scan<true>(st, lc, cs_grid, a, lb, offsets, total, state);
+        else launch_count_scan<false>(st, lc, cs_grid, a, lb, offsets, total, state);
+        VREN_LAUNCH_CHECK();
+    } else {
+        if (spheres) launch_assign<false, true>(st, lc, grid, block, a, lb);
+        else launch_assign<false, false>(st, lc, grid, block, a, lb);
+        VREN_LAUNCH_CHECK();
+        int rc = scan_exclusive_u32(st, counts, offsets, key_cap, key_count, total, scratch);
+        if (rc != VREN_OK) return rc;
+    }
     if (spheres) launch_assign<true, true>(st, lc, grid, block, a, lb);
     else launch_assign<true, false>(st, lc, grid, block, a, lb);
     VREN_LAUNCH_CHECK();
@@ -1211,8 +1349,7 @@ extern "C" int vren_cs_find_unique_clusters(vren_stream_t s, const float* depth,
 
 extern "C" size_t vren_cs_assign_lights_scratch_bytes(uint32_t key_capacity)
 {
-    const size_t a = scan_scratch_bytes(key_capacity), b = assign_fused_scratch_bytes(key_capacity);
-    return a > b ? a : b;
+    return count_scan_state_offset(key_capacity) + count_scan_state_bytes();
 }
 
 extern "C" int vren_cs_assign_lights(vren_stream_t s, const uint32_t* cluster_keys, const uint32_t* key_count,
