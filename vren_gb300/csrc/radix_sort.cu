@@ -469,7 +469,10 @@ __global__ void __launch_bounds__(kBucketScanThreads) bucket_column_scan_kernel(
                                                                               uint32_t rows_n, uint32_t key_bits,
                                                                               uint32_t* __restrict__ ends)
 {
-    pdl_enter();
+    // Let the scatter launch at once (it loads and ranks its tiles meanwhile and waits for this grid
+    // before it reads the matrix), then wait for the histograms.
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     constexpr uint32_t C = kBucketScanCols, R = kBucketScanRows;
     constexpr uint32_t kWarps = kBucketScanThreads / 32;
     __shared__ uint32_t s_warp[kWarps][C];
