@@ -728,6 +728,50 @@ def radix_bench(args, dev, stream, flush, keys_np, hbm_peak):
                                             "l2": "flushed before each sort" if n * 16 < (129 << 20) else
                                             "inputs larger than L2 (also flushed)"}
         del src_k, src_v, k, v, tk, tv, s1
+    if args.quick:
+        return out
+    # beyond the workload's sizes: 2^28 pairs, and keys only (the reference's radix_sort::operator(),
+    # 32 B/key over four 8-bit passes) at 2^26 and 2^28; checked for order and, for pairs, that the
+    # values are a permutation carrying their keys
+    for n, pairs in ((1 << 28, True), (1 << 26, False), (1 << 28, False)):
+        g = torch.Generator(device=dev)
+        g.manual_seed(SEED + n + pairs)
+        src_k = torch.randint(-(1 << 31), 1 << 31, (n,), dtype=torch.int32, device=dev, generator=g)
+        k, tk = torch.empty_like(src_k), torch.empty_like(src_k)
+        v = tv = src_v = None
+        if pairs:
+            src_v = torch.arange(n, dtype=torch.int32, device=dev)
+            v, tv = torch.empty_like(src_v), torch.empty_like(src_v)
+        rs = vg.radix_sort(8)
+        s1 = rs.create_scratch_buffer_1(n, dev)
+        evs = []
+        with torch.cuda.stream(stream):
+            for i in range(args.warmup + args.steps):
+                k.copy_(src_k)
+                if pairs:
+                    v.copy_(src_v)
+                flush.zero_()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                rs.sort(stream, k, v, n, s1, tk, tv)
+                b.record(stream)
+                if i >= args.warmup:
+                    evs.append((a, b))
+            stream.synchronize()
+        ms = sum(a.elapsed_time(b) for a, b in evs) / len(evs)
+        flip = torch.tensor(-(1 << 31), dtype=torch.int32, device=dev)
+        ku = k ^ flip  # unsigned order as signed order
+        ok = bool((ku[1:] >= ku[:-1]).all().item())
+        if pairs:
+            ok = ok and bool(torch.equal(src_k[v.long()], k)) and \
+                bool(torch.equal(torch.sort(v).values, src_v))
+        per = 64.0 if pairs else 32.0
+        gbs = per * n / (ms * 1e-3) / 1e9
+        out[f"n=2^{n.bit_length() - 1}" + ("" if pairs else "_keys_only")] = {
+            "ms": round(ms, 5), "gkeys_s": round(n / (ms * 1e-3) / 1e9, 3),
+            "gbs_at_%dB_per_%s" % (per, "pair" if pairs else "key"): round(gbs, 1),
+            "hbm_frac": round(gbs / hbm_peak, 4), "sorted_and_permutation": ok}
+        del src_k, src_v, k, v, tk, tv, s1, ku
     return out
 
 

@@ -7,6 +7,7 @@ import torch
 
 import oracle
 import shade_scene
+import vren_gb300 as vg
 import vren_gb300.clustered_shading as cs
 
 pytestmark = pytest.mark.gpu
@@ -28,14 +29,22 @@ def device_inputs(s, device):
     return frame, d, gb, ll
 
 
+@pytest.mark.parametrize("packed", [1, 0])  # two lights per step in f32x2 arithmetic / one light per step
 @pytest.mark.parametrize("falloff", ["ref", "windowed_inv_sq"])
 @pytest.mark.parametrize("mode", ["radiance", "color"])
-def test_shade_forward(cuda, falloff, mode):
+def test_shade_forward(cuda, falloff, mode, packed):
     s = shade_scene.make(320, 180, 512, seed=21)
     frame, d, gb, ll = device_inputs(s, cuda)
     out = torch.full((s["W"] * s["H"] * 3,), -7.0, dtype=torch.float32, device=cuda)
-    cs.shade(falloff, mode)(None, frame, s["W"], s["H"], gb, ll, d["pos"], d["lights"], s["L"], out)
-    torch.cuda.synchronize()
+    lib = vg.lib()
+    knob = vg._lib.TUNE["shade_packed"]
+    saved = lib.vren_tuning_get(knob)
+    assert lib.vren_tuning_set(knob, packed) == 0
+    try:
+        cs.shade(falloff, mode)(None, frame, s["W"], s["H"], gb, ll, d["pos"], d["lights"], s["L"], out)
+        torch.cuda.synchronize()
+    finally:
+        lib.vren_tuning_set(knob, saved)
     got = out.cpu().numpy().astype(np.float64)
     exp, shaded = oracle.cs_shade_f64(s["view"], s["W"], s["H"], shade_scene.gb(s), shade_scene.lists(s), s["pos"],
                                       s["lights"], s["L"], cs.FALLOFF[falloff], cs.SHADE_MODE[mode])

@@ -19,7 +19,7 @@ VREN_ERR_STATE = 5
 
 REDUCE_OPS = {"add": 0, "min": 1, "max": 2}
 TUNE = {"scan_slices": 0, "spin_polls": 1, "radix_rank": 2, "radix_items": 3, "scan_staged": 4, "reduce_form": 5,
-        "light_bvh_cluster": 6, "assign_fused": 7, "radix_persistent": 8, "fuc_fused": 9, "bucket_form": 10, "host_zero_copy": 11}
+        "light_bvh_cluster": 6, "assign_fused": 7, "radix_persistent": 8, "fuc_fused": 9, "bucket_form": 10, "host_zero_copy": 11, "shade_packed": 12}
 
 u32, u64, i32, sz, vp, fp = C.c_uint32, C.c_uint64, C.c_int, C.c_size_t, C.c_void_p, C.c_float
 

@@ -70,6 +70,7 @@ static int g_tuning[VREN_TUNE_COUNT] = {
     /* VREN_TUNE_FUC_FUSED */ 0,
     /* VREN_TUNE_BUCKET_FORM */ 0,
     /* VREN_TUNE_HOST_ZERO_COPY */ 0,
+    /* VREN_TUNE_SHADE_PACKED */ 1,
 };
 int tuning(int knob) { return (knob >= 0 && knob < VREN_TUNE_COUNT) ? g_tuning[knob] : 0; }
 }  // namespace vren_gb300
@@ -104,6 +105,7 @@ extern "C" int vren_tuning_set(int knob, int value)
     case VREN_TUNE_RADIX_PERSISTENT:
     case VREN_TUNE_BUCKET_FORM:
     case VREN_TUNE_HOST_ZERO_COPY:
+    case VREN_TUNE_SHADE_PACKED:
         if (value != 0 && value != 1) return VREN_ERR_ARG;
         break;
     default: break;

@@ -44,6 +44,7 @@ struct ShadeArgs {
     int falloff;
     int mode;
     float* out;
+    int packed;  // forward: two lights per step in packed f32x2 arithmetic (VREN_TUNE_SHADE_PACKED)
 };
 
 // Per-pixel shading state: position (p + plo), geometry, and the terms of pbr_apply_light that
@@ -282,6 +283,83 @@ __device__ __forceinline__ float falloff_value(int mode, float dist, float dd, f
 }
 
 // pbr_apply_point_light (pbr.glsl:75-93) for one light.
+// ------------------------------------------------------------------------------------------------
+// Two lights at once in packed single-precision pairs (Blackwell's f32x2 add / mul / fma: one
+// instruction for both lights), the same operations as point_light_fwd per light; the contributions
+// are added to `out` in list order (light 0, then light 1), as the one-light loop does.
+// ------------------------------------------------------------------------------------------------
+__device__ __forceinline__ float2 bc2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 pk2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a); }
+__device__ __forceinline__ float2 dot3x2(const float2* a, const float2* b)
+{
+    return fma2(a[2], b[2], fma2(a[1], b[1], mul2(a[0], b[0])));
+}
+
+__device__ __forceinline__ void point_light_fwd2(const Px& q, float4 lp0, float4 lc0, float4 lp1, float4 lc1,
+                                                 int falloff, float out[3])
+{
+    float2 d[3];
+    d[0] = add2(sub2(bc2(q.p[0]), pk2(lp0.x, lp1.x)), bc2(q.plo[0]));
+    d[1] = add2(sub2(bc2(q.p[1]), pk2(lp0.y, lp1.y)), bc2(q.plo[1]));
+    d[2] = add2(sub2(bc2(q.p[2]), pk2(lp0.z, lp1.z)), bc2(q.plo[2]));
+    const float2 dd = dot3x2(d, d);
+    const float2 rdist = pk2(rsqrt_a(dd.x), rsqrt_a(dd.y));
+    const float2 L[3] = {mul2(d[0], rdist), mul2(d[1], rdist), mul2(d[2], rdist)};
+    // falloff_value for both lights
+    const float2 t = mul2(mul2(dd, rdist), pk2(rcp_a(lc0.w), rcp_a(lc1.w)));
+    float2 att;
+    if (falloff == VREN_CS_FALLOFF_REF) {
+        const float2 u = pk2(fminf(t.x, 1.0f), fminf(t.y, 1.0f));
+        att = sub2(bc2(1.0f), mul2(u, pk2(sqrt_a(u.x), sqrt_a(u.y))));
+    } else {
+        const float2 t2 = mul2(t, t);
+        const float2 om = sub2(bc2(1.0f), mul2(t2, t2));
+        const float2 w = pk2(fminf(fmaxf(om.x, 0.0f), 1.0f), fminf(fmaxf(om.y, 0.0f), 1.0f));
+        const float2 den = add2(dd, bc2(1.0f));
+        att = mul2(mul2(w, w), pk2(rcp_a(den.x), rcp_a(den.y)));
+    }
+    const float2 rad[3] = {mul2(pk2(lc0.x, lc1.x), att), mul2(pk2(lc0.y, lc1.y), att), mul2(pk2(lc0.z, lc1.z), att)};
+    // brdf_accumulate for both lights
+    const float2 N2[3] = {bc2(q.N[0]), bc2(q.N[1]), bc2(q.N[2])};
+    const float2 V2[3] = {bc2(q.V[0]), bc2(q.V[1]), bc2(q.V[2])};
+    const float2 hv[3] = {sub2(V2[0], L[0]), sub2(V2[1], L[1]), sub2(V2[2], L[2])};
+    const float2 hl2 = dot3x2(hv, hv);
+    const float2 rhl = pk2(rsqrt_a(hl2.x), rsqrt_a(hl2.y));
+    const float2 H[3] = {mul2(hv[0], rhl), mul2(hv[1], rhl), mul2(hv[2], rhl)};
+    const float2 nhu = dot3x2(N2, hv);
+    // ggx_den: a2 h^2 + ((1 - |N|^2) |hv|^2 + |N x hv|^2) / |hv|^2 where N.hv > 0, else 1
+    float2 c[3];
+    c[0] = fma2(N2[1], hv[2], mul2(bc2(-q.N[2]), hv[1]));
+    c[1] = fma2(N2[2], hv[0], mul2(bc2(-q.N[0]), hv[2]));
+    c[2] = fma2(N2[0], hv[1], mul2(bc2(-q.N[1]), hv[0]));
+    const float2 gd = mul2(fma2(mul2(bc2(q.a2), nhu), nhu, fma2(hl2, bc2(q.omn2), dot3x2(c, c))), mul2(rhl, rhl));
+    const float2 D = pk2(nhu.x > 0.0f ? gd.x : 1.0f, nhu.y > 0.0f ? gd.y : 1.0f);
+    const float2 dpi = mul2(mul2(bc2(kPi), D), D);
+    const float2 NDF = mul2(bc2(q.a2), pk2(rcp_a(dpi.x), rcp_a(dpi.y)));
+    const float2 nl = dot3x2(N2, L);
+    const float2 NdotL = pk2(fmaxf(-nl.x, 0.0f), fmaxf(-nl.y, 0.0f));
+    const float2 gden = fma2(NdotL, bc2(q.k1), bc2(q.k));
+    const float2 G = mul2(mul2(bc2(q.ggxV), NdotL), pk2(rcp_a(gden.x), rcp_a(gden.y)));
+    const float2 hdv = dot3x2(H, V2);
+    const float2 x = sub2(bc2(1.0f), pk2(fmaxf(hdv.x, 0.0f), fmaxf(hdv.y, 0.0f)));
+    const float2 x2 = mul2(x, x);
+    const float2 f5 = mul2(mul2(x2, x2), x);
+    const float2 sden = fma2(bc2(q.nv4), NdotL, bc2(0.0001f));
+    const float2 spec = mul2(mul2(NDF, G), pk2(rcp_a(sden.x), rcp_a(sden.y)));
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) {
+        const float2 F = fma2(bc2(q.omF0[ch]), f5, bc2(q.F0[ch]));
+        const float2 B = fma2(sub2(bc2(1.0f), F), bc2(q.kdiff[ch]), mul2(F, spec));
+        const float2 v = mul2(mul2(B, rad[ch]), NdotL);
+        out[ch] += fmaxf(v.x, 0.0f);
+        out[ch] += fmaxf(v.y, 0.0f);
+    }
+}
+
 __device__ __forceinline__ void point_light_fwd(const Px& q, float4 lp, float4 lc, int falloff, float out[3])
 {
     float d[3];
@@ -645,7 +723,14 @@ __global__ void __launch_bounds__(kTileThreads) shade_forward_kernel(ShadeArgs a
                 if (lane == 0) VREN_RECORD_ERROR(VREN_ERR_CAPACITY);
             }
             const uint32_t* idx = a.lists.indices + off;
-            for (uint32_t i = 0; i < cnt; ++i) {
+            uint32_t i = 0;
+            if (a.packed) {
+                for (; i + 1 < cnt; i += 2) {
+                    const uint32_t l0 = idx[i], l1 = idx[i + 1];
+                    point_light_fwd2(q, a.lpos[l0], a.lights[l0], a.lpos[l1], a.lights[l1], a.falloff, Lo);
+                }
+            }
+            for (; i < cnt; ++i) {
                 const uint32_t l = idx[i];
                 point_light_fwd(q, a.lpos[l], a.lights[l], a.falloff, Lo);
             }
@@ -818,6 +903,7 @@ extern "C" int vren_cs_shade(vren_stream_t s, const vren_cs_frame* frame, uint32
     a.falloff = falloff;
     a.mode = output_mode;
     a.out = out_rgb;
+    a.packed = tuning(VREN_TUNE_SHADE_PACKED);
     const uint32_t tiles = ((width + 31) / 32) * ((height + 31) / 32);
     shade_forward_kernel<<<tiles, kTileThreads, kGroupBytes, as_stream(s)>>>(a);
     VREN_LAUNCH_CHECK();
