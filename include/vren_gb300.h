@@ -111,9 +111,10 @@ int vren_test_withhold_scan_status(uint32_t tile_plus_one);
  *                          form) reads depth and normals straight from the page-locked host buffers
  *                          and writes the references to cluster_refs_out as it goes (used when the
  *                          device can address those buffers, else the banded copies run)
- *   VREN_TUNE_SHADE_PACKED vren_cs_shade: 1 = two lights per step in packed f32x2 arithmetic (the
- *                          same operations per light, a different rounding of a few contracted
- *                          products; the default), 0 = one light per step */
+ *   VREN_TUNE_SHADE_PACKED vren_cs_shade and vren_cs_shade_backward: 1 = two lights per step in
+ *                          packed f32x2 arithmetic (the same operations per light, a different
+ *                          rounding of a few contracted products; the default), 0 = one light per
+ *                          step */
 enum { VREN_TUNE_SCAN_SLICES = 0, VREN_TUNE_SPIN_POLLS = 1, VREN_TUNE_RADIX_RANK = 2, VREN_TUNE_RADIX_ITEMS = 3,
        VREN_TUNE_SCAN_STAGED = 4, VREN_TUNE_REDUCE_FORM = 5, VREN_TUNE_LIGHT_BVH_CLUSTER = 6,
        VREN_TUNE_ASSIGN_FUSED = 7, VREN_TUNE_RADIX_PERSISTENT = 8, VREN_TUNE_FUC_FUSED = 9, VREN_TUNE_BUCKET_FORM = 10,

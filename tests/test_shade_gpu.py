@@ -65,10 +65,22 @@ def test_shade_forward(cuda, falloff, mode, packed):
 
 
 @pytest.mark.parametrize("falloff", ["windowed_inv_sq", "ref"])
-def test_shade_backward_matches_fp64_gradient(cuda, falloff):
+@pytest.mark.parametrize("packed", [1, 0])  # two slots (lights) per warp step in f32x2 arithmetic / one
+def test_shade_backward_matches_fp64_gradient(cuda, falloff, packed):
     s = shade_scene.make(640, 360, 1024, seed=31)
     frame, d, gb, ll = device_inputs(s, cuda)
     L = s["L"]
+    lib = vg.lib()
+    knob = vg._lib.TUNE["shade_packed"]
+    saved = lib.vren_tuning_get(knob)
+    assert lib.vren_tuning_set(knob, packed) == 0
+    try:
+        _backward_vs_fp64(s, frame, d, gb, ll, L, falloff, cuda)
+    finally:
+        lib.vren_tuning_set(knob, saved)
+
+
+def _backward_vs_fp64(s, frame, d, gb, ll, L, falloff, cuda):
     gpos = torch.zeros(L * 3, dtype=torch.float32, device=cuda)
     gcol = torch.zeros(L * 3, dtype=torch.float32, device=cuda)
     grad_r = torch.zeros(L, dtype=torch.float32, device=cuda)

@@ -472,6 +472,136 @@ __device__ __forceinline__ void pair_backward(const Px& q, float4 lp, float4 lc,
     }
 }
 
+// pair_backward for two lights at once (same pixel) in packed f32x2 arithmetic: the same operations
+// per light; g7a and g7b receive the two lights' partials.
+__device__ __forceinline__ float2 sel2(bool cx, float2 a, float ax, bool cy, float ay)
+{
+    return make_float2(cx ? a.x : ax, cy ? a.y : ay);
+}
+
+__device__ __forceinline__ void cross3x2(const float2* a, const float2* b, float2* c)
+{
+    c[0] = fma2(a[1], b[2], mul2(make_float2(-a[2].x, -a[2].y), b[1]));
+    c[1] = fma2(a[2], b[0], mul2(make_float2(-a[0].x, -a[0].y), b[2]));
+    c[2] = fma2(a[0], b[1], mul2(make_float2(-a[1].x, -a[1].y), b[0]));
+}
+
+__device__ __forceinline__ void pair_backward2(const Px& q, float4 lp0, float4 lc0, float4 lp1, float4 lc1,
+                                               int falloff, const float gin[3], float g7a[7], float g7b[7])
+{
+    const float2 rr = pk2(rcp_a(lc0.w), rcp_a(lc1.w));
+    float2 d[3];
+    d[0] = add2(sub2(bc2(q.p[0]), pk2(lp0.x, lp1.x)), bc2(q.plo[0]));
+    d[1] = add2(sub2(bc2(q.p[1]), pk2(lp0.y, lp1.y)), bc2(q.plo[1]));
+    d[2] = add2(sub2(bc2(q.p[2]), pk2(lp0.z, lp1.z)), bc2(q.plo[2]));
+    const float2 dd = dot3x2(d, d);
+    const float2 rdist = pk2(rsqrt_a(dd.x), rsqrt_a(dd.y));
+    const float2 dist = mul2(dd, rdist);
+    const float2 L[3] = {mul2(d[0], rdist), mul2(d[1], rdist), mul2(d[2], rdist)};
+    const float2 t = mul2(dist, rr);
+    float2 att, datt_dt, datt_ddist_direct = bc2(0.0f);
+    if (falloff == VREN_CS_FALLOFF_REF) {
+        const float2 u = pk2(fminf(t.x, 1.0f), fminf(t.y, 1.0f));
+        const float2 su = pk2(sqrt_a(u.x), sqrt_a(u.y));
+        att = sub2(bc2(1.0f), mul2(u, su));
+        const float2 m = mul2(bc2(-1.5f), su);
+        datt_dt = sel2(t.x < 1.0f, m, 0.0f, t.y < 1.0f, 0.0f);
+    } else {
+        const float2 t2 = mul2(t, t);
+        const float2 wr = sub2(bc2(1.0f), mul2(t2, t2));
+        const float2 w = pk2(fminf(fmaxf(wr.x, 0.0f), 1.0f), fminf(fmaxf(wr.y, 0.0f), 1.0f));
+        const float2 den = add2(dd, bc2(1.0f));
+        const float2 rden = pk2(rcp_a(den.x), rcp_a(den.y));
+        const float2 ww = mul2(w, w);
+        att = mul2(ww, rden);
+        const float2 dw = mul2(mul2(bc2(-4.0f), t2), t);
+        const float2 dw_dt = sel2(wr.x > 0.0f && wr.x < 1.0f, dw, 0.0f, wr.y > 0.0f && wr.y < 1.0f, 0.0f);
+        datt_dt = mul2(mul2(mul2(bc2(2.0f), w), rden), dw_dt);
+        datt_ddist_direct = mul2(mul2(mul2(mul2(make_float2(-ww.x, -ww.y), bc2(2.0f)), dist), rden), rden);
+    }
+    const float2 col[3] = {pk2(lc0.x, lc1.x), pk2(lc0.y, lc1.y), pk2(lc0.z, lc1.z)};
+
+    const float2 N2[3] = {bc2(q.N[0]), bc2(q.N[1]), bc2(q.N[2])};
+    const float2 V2[3] = {bc2(q.V[0]), bc2(q.V[1]), bc2(q.V[2])};
+    const float2 hv[3] = {sub2(V2[0], L[0]), sub2(V2[1], L[1]), sub2(V2[2], L[2])};
+    const float2 hl2 = dot3x2(hv, hv);
+    const float2 rhl = pk2(rsqrt_a(hl2.x), rsqrt_a(hl2.y));
+    const float2 H[3] = {mul2(hv[0], rhl), mul2(hv[1], rhl), mul2(hv[2], rhl)};
+    const float2 nhu = dot3x2(N2, hv);
+    const float2 nh = mul2(nhu, rhl);
+    const float2 NdotH = pk2(fmaxf(nh.x, 0.0f), fmaxf(nh.y, 0.0f));
+    float2 nxh[3];
+    cross3x2(N2, hv, nxh);
+    const float2 gd = mul2(fma2(mul2(bc2(q.a2), nhu), nhu, fma2(hl2, bc2(q.omn2), dot3x2(nxh, nxh))), mul2(rhl, rhl));
+    const float2 D = sel2(nhu.x > 0.0f, gd, 1.0f, nhu.y > 0.0f, 1.0f);
+    const float2 rD = pk2(rcp_a(D.x), rcp_a(D.y));
+    const float2 NDF = mul2(mul2(bc2(q.a2), mul2(rD, rD)), bc2(1.0f / kPi));
+    const float2 nl_raw = mul2(bc2(-1.0f), dot3x2(N2, L));
+    const float2 NdotL = pk2(fmaxf(nl_raw.x, 0.0f), fmaxf(nl_raw.y, 0.0f));
+    const float2 gden = fma2(NdotL, bc2(q.k1), bc2(q.k));
+    const float2 rdl = pk2(rcp_a(gden.x), rcp_a(gden.y));
+    const float2 G = mul2(mul2(bc2(q.ggxV), NdotL), rdl);
+    const float2 hvr = dot3x2(H, V2);
+    const float2 HdotV = pk2(fmaxf(hvr.x, 0.0f), fmaxf(hvr.y, 0.0f));
+    const float2 x = sub2(bc2(1.0f), HdotV);
+    const float2 x2 = mul2(x, x);
+    const float2 x4 = mul2(x2, x2);
+    const float2 f5 = mul2(x4, x);
+    const float2 sden = fma2(bc2(q.nv4), NdotL, bc2(0.0001f));
+    const float2 rs = pk2(rcp_a(sden.x), rcp_a(sden.y));
+    const float2 spec = mul2(mul2(NDF, G), rs);
+
+    const float2 an = mul2(att, NdotL);
+    float2 gatt = bc2(0.0f), gNdotL = bc2(0.0f), gspec = bc2(0.0f), gf5 = bc2(0.0f);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float2 F = fma2(bc2(q.omF0[c]), f5, bc2(q.F0[c]));
+        const float2 B = fma2(sub2(bc2(1.0f), F), bc2(q.kdiff[c]), mul2(F, spec));
+        const float2 bca = mul2(mul2(B, col[c]), an);
+        const float2 gv = pk2(bca.x > 0.0f ? gin[c] : 0.0f, bca.y > 0.0f ? gin[c] : 0.0f);
+        const float2 gvB = mul2(gv, B);
+        const float2 gB = mul2(mul2(gv, col[c]), an);
+        const float2 gcol = mul2(gvB, an);
+        g7a[3 + c] += gcol.x;  // colour
+        g7b[3 + c] += gcol.y;
+        gatt = fma2(mul2(gvB, col[c]), NdotL, gatt);
+        gNdotL = fma2(mul2(gvB, col[c]), att, gNdotL);
+        gspec = fma2(gB, F, gspec);
+        gf5 = fma2(mul2(gB, sub2(spec, bc2(q.kdiff[c]))), bc2(q.omF0[c]), gf5);
+    }
+    const float2 gHdotV = mul2(mul2(bc2(-5.0f), gf5), x4);
+    const float2 gNDF = mul2(mul2(gspec, G), rs);
+    const float2 gG = mul2(mul2(gspec, NDF), rs);
+    gNdotL = add2(gNdotL, mul2(mul2(mul2(mul2(make_float2(-gspec.x, -gspec.y), spec), rs), bc2(1.0f)), bc2(q.nv4)));
+    gNdotL = add2(gNdotL, mul2(mul2(mul2(gG, bc2(q.ggxV)), bc2(q.k)), mul2(rdl, rdl)));
+    const float2 gNdotH = mul2(mul2(mul2(gNDF, mul2(bc2(-4.0f * (q.a2 - 1.0f)), NdotH)), NDF), rD);
+    const float2 gnl = sel2(nl_raw.x > 0.0f, gNdotL, 0.0f, nl_raw.y > 0.0f, 0.0f);
+    const float2 gnh = sel2(nhu.x > 0.0f, gNdotH, 0.0f, nhu.y > 0.0f, 0.0f);
+    const float2 ghv = sel2(hvr.x > 0.0f, gHdotV, 0.0f, hvr.y > 0.0f, 0.0f);
+    float2 tri[3];
+    cross3x2(hv, nxh, tri);
+    const float2 rhl3 = mul2(mul2(rhl, rhl), rhl);
+    const float2 sn = mul2(gnh, rhl3), sv = mul2(ghv, rhl);
+    float2 gL[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float2 vh = sub2(V2[c], mul2(H[c], hvr));
+        gL[c] = sub2(sub2(mul2(make_float2(-gnl.x, -gnl.y), N2[c]), mul2(sn, tri[c])), mul2(sv, vh));
+    }
+    const float2 gt = mul2(gatt, datt_dt);
+    const float2 gdist = fma2(gatt, datt_ddist_direct, mul2(gt, rr));
+    const float2 grad_r = mul2(mul2(mul2(make_float2(-gt.x, -gt.y), dist), rr), rr);
+    g7a[6] += grad_r.x;  // radius
+    g7b[6] += grad_r.y;
+    const float2 gLL = dot3x2(gL, L);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float2 gd = fma2(sub2(gL[c], mul2(L[c], gLL)), rdist, mul2(gdist, L[c]));
+        g7a[c] -= gd.x;  // d = p - light position
+        g7b[c] -= gd.y;
+    }
+}
+
 // Per-pixel record staged in shared memory by the adjoint (96 bytes).
 struct PxRec {
     float4 p_ref;     // p.xyz, cluster reference (bits; 0xFFFFFFFF = not shaded)
@@ -751,7 +881,21 @@ __global__ void __launch_bounds__(kTileThreads) shade_forward_kernel(ShadeArgs a
 // ------------------------------------------------------------------------------------------------
 // Adjoint, step 1: per-slot partials
 // ------------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(kTileThreads) shade_backward_slots_kernel(ShadeArgs a, const float* __restrict__ grad,
+// The warp's sum of a slot's seven partials, stored by lane 0 as two float4 (the eighth word zero).
+__device__ __forceinline__ void write_slot_partial(float g7[7], float* __restrict__ slot_grad, uint32_t s, uint32_t lane)
+{
+#pragma unroll
+    for (int k = 0; k < 7; ++k)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) g7[k] += __shfl_xor_sync(0xFFFFFFFFu, g7[k], o);
+    if (lane == 0) {
+        float4* dst = reinterpret_cast<float4*>(slot_grad + 8 * (size_t)s);
+        dst[0] = make_float4(g7[0], g7[1], g7[2], g7[3]);
+        dst[1] = make_float4(g7[4], g7[5], g7[6], 0.0f);
+    }
+}
+
+__global__ void __launch_bounds__(kTileThreads, 2) shade_backward_slots_kernel(ShadeArgs a, const float* __restrict__ grad,
                                                                             float* __restrict__ slot_grad,
                                                                             uint32_t n_slots)
 {
@@ -773,33 +917,58 @@ __global__ void __launch_bounds__(kTileThreads) shade_backward_slots_kernel(Shad
         if (tid == 0) VREN_RECORD_ERROR(VREN_ERR_CAPACITY);
         s_end = n_slots;
     }
-    for (uint32_t s = s_begin + warp; s < s_end; s += kTileThreads / 32) {
-        uint32_t lo = 0, hi = nc - 1;  // cluster owning slot s: last c with aux[c] <= s
+    // A warp takes slots two at a time (packed: both lights of one cluster against the same pixels) or
+    // one at a time.
+    const uint32_t per = a.packed ? 2u : 1u;
+    for (uint32_t s0 = s_begin + per * warp; s0 < s_end; s0 += per * (kTileThreads / 32)) {
+        uint32_t lo = 0, hi = nc - 1;  // cluster owning slot s0: last c with aux[c] <= s0
         while (lo < hi) {
             const uint32_t mid = (lo + hi + 1) >> 1;
-            if (S.aux[mid] <= s) lo = mid;
+            if (S.aux[mid] <= s0) lo = mid;
             else hi = mid - 1;
         }
         const uint32_t c = lo;
-        const uint32_t l = a.lists.indices[s];
-        const float4 lp = a.lpos[l], lc = a.lights[l];
         const uint32_t b = S.cstart[c], n = S.cstart[c + 1] - b;
-        float g7[7] = {0, 0, 0, 0, 0, 0, 0};
-        for (uint32_t j = lane; j < n; j += 32) {
-            const PxRec& rec = S.px[S.order[b + j]];
-            Px q;
-            rec_to_px(rec, q);
-            const float gin[3] = {rec.g.x, rec.g.y, rec.g.z};
-            pair_backward(q, lp, lc, a.falloff, gin, g7);
+        if (per == 2u && s0 + 1 < s_end && s0 + 1 < S.aux[c + 1]) {
+            // slots s0 and s0 + 1 of the same cluster
+            const uint32_t l0 = a.lists.indices[s0], l1 = a.lists.indices[s0 + 1];
+            const float4 lp0 = a.lpos[l0], lc0 = a.lights[l0], lp1 = a.lpos[l1], lc1 = a.lights[l1];
+            float g7a[7] = {0, 0, 0, 0, 0, 0, 0}, g7b[7] = {0, 0, 0, 0, 0, 0, 0};
+            for (uint32_t j = lane; j < n; j += 32) {
+                const PxRec& rec = S.px[S.order[b + j]];
+                Px q;
+                rec_to_px(rec, q);
+                const float gin[3] = {rec.g.x, rec.g.y, rec.g.z};
+                pair_backward2(q, lp0, lc0, lp1, lc1, a.falloff, gin, g7a, g7b);
+            }
+            write_slot_partial(g7a, slot_grad, s0, lane);
+            write_slot_partial(g7b, slot_grad, s0 + 1, lane);
+            continue;
         }
-#pragma unroll
-        for (int k = 0; k < 7; ++k)
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) g7[k] += __shfl_xor_sync(0xFFFFFFFFu, g7[k], o);
-        if (lane == 0) {
-            float4* dst = reinterpret_cast<float4*>(slot_grad + 8 * (size_t)s);
-            dst[0] = make_float4(g7[0], g7[1], g7[2], g7[3]);
-            dst[1] = make_float4(g7[4], g7[5], g7[6], 0.0f);
+        for (uint32_t s = s0; s < s0 + per && s < s_end; ++s) {
+            // a slot alone (or each of two slots of different clusters)
+            uint32_t cs = c;
+            if (s != s0) {
+                lo = 0, hi = nc - 1;
+                while (lo < hi) {
+                    const uint32_t mid = (lo + hi + 1) >> 1;
+                    if (S.aux[mid] <= s) lo = mid;
+                    else hi = mid - 1;
+                }
+                cs = lo;
+            }
+            const uint32_t bs = S.cstart[cs], ns = S.cstart[cs + 1] - bs;
+            const uint32_t l = a.lists.indices[s];
+            const float4 lp = a.lpos[l], lc = a.lights[l];
+            float g7[7] = {0, 0, 0, 0, 0, 0, 0};
+            for (uint32_t j = lane; j < ns; j += 32) {
+                const PxRec& rec = S.px[S.order[bs + j]];
+                Px q;
+                rec_to_px(rec, q);
+                const float gin[3] = {rec.g.x, rec.g.y, rec.g.z};
+                pair_backward(q, lp, lc, a.falloff, gin, g7);
+            }
+            write_slot_partial(g7, slot_grad, s, lane);
         }
     }
 }
@@ -932,6 +1101,7 @@ extern "C" int vren_cs_shade_backward(vren_stream_t s, const vren_cs_frame* fram
     // be differentiated
     if (assignments > lists->index_capacity) return VREN_ERR_CAPACITY;
     a.falloff = falloff;
+    a.packed = tuning(VREN_TUNE_SHADE_PACKED);
     cudaStream_t st = as_stream(s);
     const BwdLayout lay = bwd_layout(light_count, assignments);
     char* sc = static_cast<char*>(scratch);
