@@ -37,11 +37,11 @@ SEED = 20240611
 RADIX_N = 1 << 20
 L2_FLUSH_BYTES = 256 << 20
 BYTES_PER_PX = 20  # depth 4 + normal 12 (f32x3) + cluster reference 4
-# DRAM bytes (read + write) of one find_unique_cluster_list call at 1920x1080 (its three kernels,
-# f32x3 normals): one ncu capture at 3840x2160 (profiles/find_unique_3840x2160.md: tile kernel 133.8 MB
-# read + 17.6 MB written, tile-count scan 0.04 MB, fix-up 34.3 MB read) scaled by the pixel count
-# (1/4).  ncu flushed the caches before each kernel, so the fix-up's read of the references
-# (L2-resident in a timed run) is counted here.
+# DRAM bytes (read + write) of one find_unique_cluster_list call at 1920x1080 (its two kernels, f32x3
+# normals): one ncu capture at 3840x2160 (`--profile find_unique`: tile kernel 133.8 MB read + 17.6 MB
+# written, self-offset fix-up 34.3 MB read) scaled by the pixel count (1/4).  ncu flushed the caches
+# before each kernel, so the fix-up's read of the references (L2-resident in a timed run) is counted
+# here.
 FUC_TRAFFIC_BYTES = int((133.848320 + 17.563392 + 34.263296 + 0.001024) * 1e6 / 4)
 FUC_TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the two kernels (tiles, self-offset "
                       "fix-up) at 3840x2160 (caches flushed before each), scaled by pixels to 1920x1080")
