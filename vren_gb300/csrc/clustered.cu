@@ -1635,10 +1635,6 @@ int refresh_frame(vren_cluster_and_shade* cs, cudaStream_t st, const vren_cs_vie
     return VREN_OK;
 }
 
-// One frame from host buffers: the lights go up and their BVH is built on the second stream while the
-// depth and normals go up on `st` in bands of tile rows, each band's tiles processed as it arrives;
-// then the references go down on the second stream while the light lists are assigned on `st`, and
-// the lists are written into host memory by the device.
 // The address under which the device reads or writes the host buffer `p` (page-locked and mapped,
 // or any host memory when the device has pageable-memory access), or null when it cannot.
 const void* device_view_of_host(const void* p)
@@ -1660,6 +1656,10 @@ const void* device_view_of_host(const void* p)
     return pageable ? p : nullptr;
 }
 
+// One frame from host buffers: the lights go up and their BVH is built on the second stream while the
+// depth and normals go up on `st` in bands of tile rows, each band's tiles processed as it arrives;
+// then the references go down on the second stream while the light lists are assigned on `st`, and
+// the lists are written into host memory by the device.
 // zc_depth / zc_normals: the device's views of the host G-buffer for the zero-copy form (both null
 // for the banded copies); zc_refs: the device's view of refs_out (null when no references go down).
 int cs_enqueue_host(vren_cluster_and_shade* cs, cudaStream_t st, uint32_t W, uint32_t H, const float* depth,
