@@ -398,9 +398,11 @@ __global__ void bucket_end_offsets_kernel(const uint2* __restrict__ sorted, uint
 // Here, over tiles of 4096 elements (one matrix row each):
 //   1. bucket_tile_hist_kernel: one CTA per row reads it once and writes its 1024 bucket counts as one
 //      row of a [rows][1024] matrix (4 KB per 32 KB of elements);
-//   2. bucket_column_scan_kernel: each CTA turns 8 columns of the matrix into exclusive prefixes over
-//      the rows (in place) and the bucket totals; the last CTA scans the totals into the bucket
-//      start offsets (scratch) and the end offsets (the output's counters region);
+//   2. bucket_column_scan_kernel: each CTA takes a block of 256 rows x 32 columns (every warp load
+//      one 128-byte line), turns it into exclusive prefixes over the rows in place, and gets the
+//      rows above from the blocks above in its columns by decoupled look-back; the last CTA scans
+//      the bucket totals into the start offsets (scratch) and the end offsets (the output's
+//      counters region);
 //   3. bucket_scatter_kernel: one CTA per row reads it again (keys first; values when staging, from
 //      L2), ranks it stably in shared memory (1024 16-bit counters per warp), stages it in bucket
 //      order and writes each element to start[bucket] + (the bucket's count in the elements before
@@ -421,12 +423,15 @@ constexpr uint32_t kBucketRadix = 1u << kBucketBits;
 constexpr int kBucketItems = 16;
 constexpr uint32_t kBucketTile = kSortThreads * kBucketItems;   // 4096 elements
 constexpr uint32_t kBucketRow = kBucketTile;                      // elements per matrix row (one tile)
-constexpr int kBucketScanThreads = 512;
-constexpr uint32_t kBucketScanCols = 8;                          // columns per scan CTA (32 B of a row)
-constexpr uint32_t kBucketScanRows = 8;                          // rows per scan thread and chunk
-// Scratch, in uint32 words: [0] scan CTA ticket, [16, 1040) bucket totals, [1040, 2064) bucket
-// start offsets, then the count matrix [rows][1024] (16-byte aligned).
+constexpr int kBucketScanThreads = 256;
+constexpr uint32_t kBucketScanCols = 32;                         // columns per scan CTA (128 B of a row)
+constexpr uint32_t kBucketScanBlock = 256;                       // rows per scan CTA (32 per warp)
+constexpr uint32_t kBucketScanGroups = kBucketRadix / kBucketScanCols;
+// Scratch, in uint32 words: [0] scan CTA ticket, [1] finished scan CTAs, [16, 1040) bucket totals,
+// [1040, 2064) bucket start offsets, then the count matrix [rows][1024] (16-byte aligned), then the
+// scan's look-back words [row blocks][1024].
 constexpr uint32_t kBkTotals = 16, kBkStarts = kBkTotals + kBucketRadix, kBkRows = kBkStarts + kBucketRadix;
+__host__ __device__ inline uint32_t bucket_scan_blocks(uint32_t rows_n) { return (rows_n + kBucketScanBlock - 1) / kBucketScanBlock; }
 
 __global__ void __launch_bounds__(kSortThreads) bucket_tile_hist_kernel(const uint2* in, uint32_t n,
                                                                        uint32_t key_bits,
@@ -436,7 +441,14 @@ __global__ void __launch_bounds__(kSortThreads) bucket_tile_hist_kernel(const ui
     __shared__ alignas(16) uint32_t s_hist[kBucketRadix];
     const uint32_t tid = threadIdx.x, row = blockIdx.x;
     reinterpret_cast<uint4*>(s_hist)[tid] = make_uint4(0u, 0u, 0u, 0u);
-    if (row == 0 && tid == 0) scratch[0] = 0u;  // the scan's CTA ticket
+    if (row == 0 && tid < 2) scratch[tid] = 0u;  // the scan's CTA ticket and finished count
+    {
+        // the scan's look-back words start unpublished
+        const uint32_t rows_n = gridDim.x;
+        const uint32_t words = bucket_scan_blocks(rows_n) * kBucketRadix;
+        uint32_t* status = scratch + kBkRows + (size_t)rows_n * kBucketRadix;
+        for (uint32_t i = row * kSortThreads + tid; i < words; i += rows_n * kSortThreads) status[i] = 0u;
+    }
     __syncthreads();
     const uint32_t mask = (1u << key_bits) - 1u;
     const uint32_t base = row * kBucketRow;
@@ -465,112 +477,117 @@ __global__ void __launch_bounds__(kSortThreads) bucket_tile_hist_kernel(const ui
         reinterpret_cast<const uint4*>(s_hist)[tid];
 }
 
-__global__ void __launch_bounds__(kBucketScanThreads) bucket_column_scan_kernel(uint32_t* __restrict__ scratch,
-                                                                              uint32_t rows_n, uint32_t key_bits,
-                                                                              uint32_t* __restrict__ ends)
+__global__ void __launch_bounds__(kBucketScanThreads) bucket_column_scan_kernel(uint32_t* scratch, uint32_t rows_n,
+                                                                              uint32_t key_bits, uint32_t* ends,
+                                                                              uint32_t wait_limit, uint32_t spin)
 {
     // Let the scatter launch at once (it loads and ranks its tiles meanwhile and waits for this grid
     // before it reads the matrix), then wait for the histograms.
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     asm volatile("griddepcontrol.wait;" ::: "memory");
-    constexpr uint32_t C = kBucketScanCols, R = kBucketScanRows;
-    constexpr uint32_t kWarps = kBucketScanThreads / 32;
-    __shared__ uint32_t s_warp[kWarps][C];
-    __shared__ uint32_t s_carry[C];
-    __shared__ uint32_t s_wsum[kWarps];
+    constexpr uint32_t kWarps = kBucketScanThreads / 32u;
+    constexpr uint32_t kRowsPerWarp = kBucketScanBlock / kWarps;
+    __shared__ uint32_t s_wsum[kWarps][32];
+    __shared__ uint32_t s_look[kWarps][32];
+    __shared__ uint32_t s_unit;
     __shared__ bool s_last;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-    const uint32_t c0 = blockIdx.x * C;
-    uint32_t* rows = scratch + kBkRows + c0;
-    if (tid < C) s_carry[tid] = 0u;
+    // Units in the order the CTAs start, so a unit's predecessors in its column group have started.
+    if (tid == 0) s_unit = atomicAdd(scratch, 1u);
     __syncthreads();
-    for (uint32_t r0 = 0; r0 < rows_n; r0 += kBucketScanThreads * R) {
-        const uint32_t rb = r0 + tid * R;
-        uint32_t v[R][C], sum[C];
+    const uint32_t unit = s_unit;
+    const uint32_t blocks = bucket_scan_blocks(rows_n);
+    const uint32_t rb = unit / kBucketScanGroups;
+    const uint32_t col = (unit % kBucketScanGroups) * kBucketScanCols + lane;
+    uint32_t* mat = scratch + kBkRows;
+    uint32_t* status = mat + (size_t)rows_n * kBucketRadix;
+
+    // Warp w: rows r0 .. r0+31 of the block, lane = column (each load one 128-byte line).
+    const uint32_t r0 = rb * kBucketScanBlock + warp * kRowsPerWarp;
+    uint32_t v[kRowsPerWarp];
 #pragma unroll
-        for (uint32_t c = 0; c < C; ++c) sum[c] = 0u;
+    for (uint32_t i = 0; i < kRowsPerWarp; ++i)
+        v[i] = r0 + i < rows_n ? mat[(size_t)(r0 + i) * kBucketRadix + col] : 0u;
+    uint32_t run = 0;
 #pragma unroll
-        for (uint32_t r = 0; r < R; ++r) {
-            uint4 lo = make_uint4(0u, 0u, 0u, 0u), hi = lo;
-            if (rb + r < rows_n) {
-                const uint4* p = reinterpret_cast<const uint4*>(rows + (size_t)(rb + r) * kBucketRadix);
-                lo = p[0];
-                hi = p[1];
-            }
-            v[r][0] = lo.x; v[r][1] = lo.y; v[r][2] = lo.z; v[r][3] = lo.w;
-            v[r][4] = hi.x; v[r][5] = hi.y; v[r][6] = hi.z; v[r][7] = hi.w;
-#pragma unroll
-            for (uint32_t c = 0; c < C; ++c) sum[c] += v[r][c];
-        }
-        // exclusive prefix of each column over the threads (rows before mine), plus the carry
-        uint32_t incl[C];
-#pragma unroll
-        for (uint32_t c = 0; c < C; ++c) {
-            incl[c] = sum[c];
-#pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl[c], d);
-                if (lane >= (uint32_t)d) incl[c] += y;
-            }
-        }
-        if (lane == 31) {
-#pragma unroll
-            for (uint32_t c = 0; c < C; ++c) s_warp[warp][c] = incl[c];
-        }
-        __syncthreads();
-        uint32_t run[C];
-#pragma unroll
-        for (uint32_t c = 0; c < C; ++c) {
-            run[c] = s_carry[c] + incl[c] - sum[c];
-            for (uint32_t w = 0; w < warp; ++w) run[c] += s_warp[w][c];
-        }
-#pragma unroll
-        for (uint32_t r = 0; r < R; ++r) {
-            if (rb + r < rows_n) {
-                uint4* p = reinterpret_cast<uint4*>(rows + (size_t)(rb + r) * kBucketRadix);
-                p[0] = make_uint4(run[0], run[1], run[2], run[3]);
-                p[1] = make_uint4(run[4], run[5], run[6], run[7]);
-            }
-#pragma unroll
-            for (uint32_t c = 0; c < C; ++c) run[c] += v[r][c];
-        }
-        __syncthreads();  // every thread has read s_carry and s_warp
-        if (tid == kBucketScanThreads - 1) {
-#pragma unroll
-            for (uint32_t c = 0; c < C; ++c) s_carry[c] = run[c];
-        }
-        __syncthreads();
+    for (uint32_t i = 0; i < kRowsPerWarp; ++i) {
+        const uint32_t x = v[i];
+        v[i] = run;
+        run += x;
     }
-    if (tid < C) {
-        scratch[kBkTotals + c0 + tid] = s_carry[tid];
-        __threadfence();
-    }
+    s_wsum[warp][lane] = run;
     __syncthreads();
-    if (tid == 0) {
-        __threadfence();
-        s_last = (atomicAdd(scratch, 1u) == gridDim.x - 1);
+    uint32_t agg = 0, before = 0;
+#pragma unroll
+    for (uint32_t w = 0; w < kWarps; ++w) {
+        const uint32_t x = s_wsum[w][lane];
+        before += w < warp ? x : 0u;
+        agg += x;
     }
+    uint32_t* my_status = status + (size_t)rb * kBucketRadix + col;
+    if (warp == 0) st_relaxed_u32(my_status, (rb == 0 ? kFlagPrefix : kFlagAggregate) | agg);
+
+    // Look-back over the blocks above in the same columns, eight blocks a round (warp w reads block
+    // base - w); every warp folds the round's words the same way, so all hold the prefix.
+    uint32_t excl = 0;
+    if (rb != 0) {
+        bool done = false;
+        for (int64_t base = (int64_t)rb - 1;; base -= kWarps) {
+            const int64_t p = base - (int64_t)warp;
+            uint32_t word = kFlagPrefix;  // above the first block: a zero prefix
+            if (p >= 0 && !done)
+                word = wait_for_flag(status + (size_t)p * kBucketRadix + col, wait_limit, spin,
+                                     [] { VREN_RECORD_ERROR(VREN_ERR_TIMEOUT); });
+            s_look[warp][lane] = word;
+            __syncthreads();
+#pragma unroll
+            for (uint32_t w = 0; w < kWarps; ++w) {
+                const uint32_t x = s_look[w][lane];
+                if (!done) {
+                    excl += x & kValueMask;
+                    done = (x & kFlagPrefix) != 0;
+                }
+            }
+            if (__syncthreads_and(done)) break;  // also keeps s_look until every warp has read it
+        }
+        if (warp == 0) st_relaxed_u32(my_status, kFlagPrefix | (excl + agg));
+    }
+    if (warp == 0 && rb == blocks - 1) scratch[kBkTotals + col] = excl + agg;
+    const uint32_t add = excl + before;
+#pragma unroll
+    for (uint32_t i = 0; i < kRowsPerWarp; ++i)
+        if (r0 + i < rows_n) mat[(size_t)(r0 + i) * kBucketRadix + col] = v[i] + add;
+
+    // The last CTA to finish turns the totals into the bucket start offsets (scratch) and end
+    // offsets (the output's counters region), four buckets per thread.
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) s_last = atomicAdd(scratch + 1, 1u) == gridDim.x - 1;
     __syncthreads();
     if (!s_last) return;
     __threadfence();
-    // Bucket starts (exclusive) and ends (inclusive) from the totals, two buckets per thread.
-    const uint32_t b = 2u * tid;
-    const uint32_t t0 = ld_relaxed_u32(scratch + kBkTotals + b), t1 = ld_relaxed_u32(scratch + kBkTotals + b + 1u);
-    uint32_t incl2 = t0 + t1;
+    const uint32_t b = 4u * tid;
+    uint32_t t[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) t[k] = ld_relaxed_u32(scratch + kBkTotals + b + k);
+    const uint32_t sum4 = t[0] + t[1] + t[2] + t[3];
+    uint32_t incl = sum4;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl2, d);
-        if (lane >= (uint32_t)d) incl2 += y;
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+        if (lane >= (uint32_t)d) incl += y;
     }
-    if (lane == 31) s_wsum[warp] = incl2;
+    if (lane == 31) s_wsum[0][warp] = incl;
     __syncthreads();
-    for (uint32_t w = 0; w < warp; ++w) incl2 += s_wsum[w];
-    const uint32_t start0 = incl2 - t0 - t1;
-    scratch[kBkStarts + b] = start0;
-    scratch[kBkStarts + b + 1u] = start0 + t0;
+    for (uint32_t w = 0; w < warp; ++w) incl += s_wsum[0][w];
+    uint32_t start = incl - sum4;
     const uint32_t mask = (1u << key_bits) - 1u;
-    if (b <= mask) ends[b] = start0 + t0;
-    if (b + 1u <= mask) ends[b + 1u] = incl2;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        scratch[kBkStarts + b + k] = start;
+        if (b + k <= mask) ends[b + k] = start + t[k];
+        start += t[k];
+    }
 }
 
 __device__ __forceinline__ uint4 ld_v4_after_wait(const uint32_t* p)
@@ -954,8 +971,9 @@ extern "C" size_t vren_bucket_sort_output_bytes(uint32_t n, uint32_t key_bits)
 // of the count matrix per 4096-element tile.
 static size_t bucket_onepass_scratch_bytes(uint32_t n)
 {
-    const uint64_t rows = ((uint64_t)n + kBucketRow - 1) / kBucketRow;
-    return (size_t)(kBkRows + (rows ? rows : 1) * kBucketRadix) * sizeof(uint32_t);
+    uint64_t rows = ((uint64_t)n + kBucketRow - 1) / kBucketRow;
+    if (rows == 0) rows = 1;
+    return (size_t)(kBkRows + (rows + bucket_scan_blocks((uint32_t)rows)) * kBucketRadix) * sizeof(uint32_t);
 }
 
 // The radix-pass form: digit-pass scratch, then a ping-pong element buffer.
@@ -987,8 +1005,9 @@ static int bucket_sort_onepass(cudaStream_t st, const uint2* in, uint32_t n, uin
     VREN_CUDA_TRY(launch_kernel(bucket_tile_hist_kernel, rows, kSortThreads, 0, st, in, n, key_bits, scratch));
     VREN_LAUNCH_CHECK();
     PdlScope pdl(1);  // the scan and the scatter start early and wait for their predecessor in-kernel
-    VREN_CUDA_TRY(launch_kernel(bucket_column_scan_kernel, kBucketRadix / kBucketScanCols, kBucketScanThreads, 0, st,
-                                scratch, rows, key_bits, ends));
+    const uint32_t scan_ctas = bucket_scan_blocks(rows) * kBucketScanGroups;
+    VREN_CUDA_TRY(launch_kernel(bucket_column_scan_kernel, scan_ctas, kBucketScanThreads, 0, st, scratch, rows, key_bits,
+                                ends, g_wait_limit, (uint32_t)tuning(VREN_TUNE_SPIN_POLLS)));
     VREN_LAUNCH_CHECK();
     constexpr size_t smem = (size_t)kBucketTile * sizeof(uint2);
     const int rank = tuning(VREN_TUNE_RADIX_RANK);
