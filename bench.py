@@ -373,6 +373,8 @@ def run_ours(args, rank: int, world: int):
             "steps": args.steps,
             "warmup": args.warmup,
             "ms_per_step": round(ms_frame, 5),
+            "step_ms": {"median": round(float(np.median(step_ms)), 5), "min": round(min(step_ms), 5),
+                        "max": round(max(step_ms), 5), "first": round(step_ms[0], 5)},
             "higher_is_better": False,
             "scaling": "weak",
             "vs_baseline": None,
