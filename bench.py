@@ -84,6 +84,13 @@ class ClockSampler:
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
+    def wait_first(self, timeout: float = 5.0):
+        """Returns once nvidia-smi has printed its first sample, i.e. is past its start-up."""
+        t0 = time.perf_counter()
+        while self.proc is not None and not self.lines and time.perf_counter() - t0 < timeout:
+            time.sleep(0.01)
+        return self
+
     def __exit__(self, *exc):
         if self.proc is not None:
             self.proc.terminate()
@@ -156,6 +163,9 @@ def run_ours(args, rank: int, world: int):
     depth, normals, normals_h, pos, lights, radix_keys = make_inputs(rank)
     stream = torch.cuda.Stream(device=dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
+    # Written once here: the first write to the fresh 256 MiB buffer is slow and, measured, adds
+    # ~40 us to the device time of the frame that follows it.
+    flush.zero_()
 
     cam = cs.scene_camera(W, H)
     view = cs.view_from_camera(cam, "ref")
@@ -169,6 +179,10 @@ def run_ours(args, rank: int, world: int):
     def frame():
         ctx.cluster(stream, view, W, H, d_depth, d_norm, d_pos, d_light, L)
 
+    # The clock sampler spans the warm-up and all GPU work below (the frame loop alone is ~10 ms).  It
+    # is started, and past its start-up, before the warm-up: a stall of this thread inside the timed
+    # loop lets the device drain its queue and idle between a step's start event and its frame.
+    clocks = ClockSampler(dev.index).__enter__().wait_first()
     # warm-up (captures the graph on the first call)
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
@@ -184,8 +198,10 @@ def run_ours(args, rank: int, world: int):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     t_wall0 = time.perf_counter()
-    clocks = ClockSampler(dev.index).__enter__()  # spans all GPU work below (the frame loop alone is ~10 ms)
     with torch.cuda.stream(stream):
+        # A 1 ms spin ahead of the first step (outside every step's events), so the host queues the
+        # steps ahead of the device and no step's device time can take in the host's launch latency.
+        torch.cuda._sleep(2_000_000)
         for i in range(args.steps):
             flush.zero_()
             ev[i][0].record(stream)
