@@ -1369,6 +1369,9 @@ extern "C" int vren_cs_assign_lights(vren_stream_t s, const uint32_t* cluster_ke
 // ================================================================================================
 // cluster_and_shade context (clustered_shading.cpp:817-1172): owns its buffers.
 // ================================================================================================
+// Bands of tile rows the host-input frame uploads (and processes, and downloads) one after another.
+constexpr uint32_t kHostBands = 4;
+
 struct vren_cluster_and_shade {
     uint32_t max_w = 0, max_h = 0, max_lights = 0, max_assign = 0;
     uint32_t key_cap = 0;
@@ -1397,6 +1400,10 @@ struct vren_cluster_and_shade {
     // host frame block (pinned) and the CUDA graph of the last frame shape
     vren_cs_frame* host_frame = nullptr;
     bool frame_valid = false;
+    // what the frame block was last built from: the block is built again only when these change
+    vren_cs_view last_view{};
+    uint32_t last_w = 0, last_h = 0, last_fmt = 0;
+    int last_off = 0;
     cudaGraphExec_t graph = nullptr;
     struct Key {
         uint32_t w, h, L, off;
@@ -1410,8 +1417,8 @@ struct vren_cluster_and_shade {
     float *in_depth = nullptr, *in_normals = nullptr, *in_pos = nullptr, *in_lights = nullptr;
     cudaStream_t aux = nullptr, up = nullptr;  // light BVH and downloads; G-buffer uploads
     cudaEvent_t ev_fork = nullptr, ev_bvh = nullptr, ev_join = nullptr, ev_join_up = nullptr;
-    cudaEvent_t ev_band[4] = {nullptr, nullptr, nullptr, nullptr};
-    cudaEvent_t ev_done[4] = {nullptr, nullptr, nullptr, nullptr};  // a band's references final
+    cudaEvent_t ev_band[kHostBands] = {};  // a band of the G-buffer has arrived
+    cudaEvent_t ev_done[kHostBands] = {};  // a band's references are final
     cudaGraphExec_t host_graph = nullptr;
     struct HostKey {
         Key k;
@@ -1563,10 +1570,11 @@ extern "C" int vren_cs_create(vren_cluster_and_shade** out, uint32_t max_width, 
     // the second and third streams (light BVH beside the tiles; banded uploads) and their events
     bool ok = cudaStreamCreateWithFlags(&cs->aux, cudaStreamNonBlocking) == cudaSuccess &&
               cudaStreamCreateWithFlags(&cs->up, cudaStreamNonBlocking) == cudaSuccess;
-    for (cudaEvent_t* e : {&cs->ev_fork, &cs->ev_bvh, &cs->ev_join, &cs->ev_join_up, &cs->ev_band[0],
-                           &cs->ev_band[1], &cs->ev_band[2], &cs->ev_band[3], &cs->ev_done[0], &cs->ev_done[1],
-                           &cs->ev_done[2], &cs->ev_done[3]})
+    for (cudaEvent_t* e : {&cs->ev_fork, &cs->ev_bvh, &cs->ev_join, &cs->ev_join_up})
         ok = ok && cudaEventCreateWithFlags(e, cudaEventDisableTiming) == cudaSuccess;
+    for (uint32_t b = 0; b < kHostBands; ++b)
+        ok = ok && cudaEventCreateWithFlags(&cs->ev_band[b], cudaEventDisableTiming) == cudaSuccess &&
+             cudaEventCreateWithFlags(&cs->ev_done[b], cudaEventDisableTiming) == cudaSuccess;
     if (!ok) {
         vren_cs_destroy(cs);
         return VREN_ERR_CUDA;
@@ -1583,10 +1591,12 @@ extern "C" void vren_cs_destroy(vren_cluster_and_shade* cs)
     if (cs->shade_graph) cudaGraphExecDestroy(cs->shade_graph);
     if (cs->aux) cudaStreamDestroy(cs->aux);
     if (cs->up) cudaStreamDestroy(cs->up);
-    for (cudaEvent_t e : {cs->ev_fork, cs->ev_bvh, cs->ev_join, cs->ev_join_up, cs->ev_band[0],
-                          cs->ev_band[1], cs->ev_band[2], cs->ev_band[3], cs->ev_done[0], cs->ev_done[1],
-                          cs->ev_done[2], cs->ev_done[3]})
+    for (cudaEvent_t e : {cs->ev_fork, cs->ev_bvh, cs->ev_join, cs->ev_join_up})
         if (e) cudaEventDestroy(e);
+    for (uint32_t b = 0; b < kHostBands; ++b) {
+        if (cs->ev_band[b]) cudaEventDestroy(cs->ev_band[b]);
+        if (cs->ev_done[b]) cudaEventDestroy(cs->ev_done[b]);
+    }
     cudaFree(cs->inputs);
     cudaFree(cs->arena);
     cudaFreeHost(cs->host_frame);
@@ -1622,6 +1632,9 @@ namespace {
 int refresh_frame(vren_cluster_and_shade* cs, cudaStream_t st, const vren_cs_view* view, uint32_t width,
                   uint32_t height, int offscreen)
 {
+    if (cs->frame_valid && width == cs->last_w && height == cs->last_h && offscreen == cs->last_off &&
+        cs->opt.normal_format == cs->last_fmt && std::memcmp(view, &cs->last_view, sizeof(vren_cs_view)) == 0)
+        return VREN_OK;  // same camera and frame shape: the block on the device is current
     static thread_local vren_cs_frame fresh;
     int rc = vren_cs_frame_build(view, width, height, offscreen, &fresh);
     if (rc != VREN_OK) return rc;
@@ -1632,6 +1645,11 @@ int refresh_frame(vren_cluster_and_shade* cs, cudaStream_t st, const vren_cs_vie
         VREN_CUDA_TRY(cudaMemcpyAsync(cs->frame, cs->host_frame, sizeof(vren_cs_frame), cudaMemcpyHostToDevice, st));
         cs->frame_valid = true;
     }
+    cs->last_view = *view;
+    cs->last_w = width;
+    cs->last_h = height;
+    cs->last_off = offscreen;
+    cs->last_fmt = cs->opt.normal_format;
     return VREN_OK;
 }
 
@@ -1697,7 +1715,7 @@ int cs_enqueue_host(vren_cluster_and_shade* cs, cudaStream_t st, uint32_t W, uin
         const FucFrame fr = fuc_frame(cs->in_depth, cs->in_normals, W, H, cs->frame, cs->keys, cs->key_cap,
                                       cs->key_count, cs->refs, static_cast<uint32_t*>(cs->fuc_scratch));
         const uint32_t TX = (W + 31) / 32, TY = (H + 31) / 32;
-        const uint32_t bands = TY < 4u ? TY : 4u, per = (TY + bands - 1) / bands;
+        const uint32_t bands = TY < kHostBands ? TY : kHostBands, per = (TY + bands - 1) / bands;
         const size_t nbytes = cs->opt.normal_format == VREN_CS_NORMALS_RGBA16F ? 8 : 12;  // per pixel
         uint32_t band = 0;
         for (uint32_t ty0 = 0; ty0 < TY; ty0 += per, ++band) {  // uploads on `up`, one event per band
