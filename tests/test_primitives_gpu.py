@@ -364,6 +364,32 @@ def test_bucket_sort_forms(cuda, bucket_form, form, rank, keys, key_bits, n):
     assert vg.lib().vren_device_error(1) == 0
 
 
+@pytest.mark.parametrize("n", [(1 << 26) + 12345])
+def test_bucket_sort_many_row_blocks(cuda, n):
+    """The one-scatter form past one wave of column-scan CTAs: 16,388 tile rows in 65 blocks of 256
+    rows (the last one 4 rows, its last tile ragged), so blocks look back over blocks whose CTAs
+    started in earlier waves.  Checked by properties: buckets ascending, values (the input indices)
+    ascending within a bucket, a permutation, and the end offsets equal to the bucket counts' prefix."""
+    key_bits = 10
+    rng = np.random.default_rng(2026)
+    keys = rng.integers(0, 2**32, n, dtype=np.uint64).astype(np.uint32)
+    pairs = np.stack([keys, np.arange(n, dtype=np.uint32)], 1).reshape(-1)
+    bs = vg.bucket_sort(key_bits)
+    out = torch.empty(bs.get_required_output_buffer_size(n) // 4, dtype=torch.int32, device=cuda)
+    bs(None, dev_u32(pairs, cuda), n, 0, out, 0)
+    got = host_u32(out)
+    k, v = got[0: 2 * n: 2], got[1: 2 * n: 2]
+    b = k & ((1 << key_bits) - 1)
+    assert np.all(np.diff(b.astype(np.int64)) >= 0)
+    assert np.all((np.diff(b.astype(np.int64)) > 0) | (np.diff(v.astype(np.int64)) > 0))
+    assert np.array_equal(k, keys[v])
+    assert np.array_equal(np.bincount(v, minlength=n), np.ones(n, np.int64))
+    off = ((8 * n + 255) // 256 * 256) // 4
+    ends = np.cumsum(np.bincount(keys & ((1 << key_bits) - 1), minlength=1 << key_bits))
+    assert np.array_equal(got[off: off + (1 << key_bits)], ends.astype(np.uint32))
+    assert vg.lib().vren_device_error(1) == 0
+
+
 # ------------------------------------------------------------------------------------------------
 # BVH
 # ------------------------------------------------------------------------------------------------
