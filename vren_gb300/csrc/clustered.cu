@@ -1674,6 +1674,24 @@ const void* device_view_of_host(const void* p)
     return pageable ? p : nullptr;
 }
 
+// Band edges in tile rows for the host-input frame: band i gets a share bands - i of the rows (4/10,
+// 3/10, 2/10, 1/10 for four bands), at least one row each, so that the last band, whose tiles,
+// fix-up and download come after the last upload, is the smallest.
+constexpr bool kHostBandTaper = true;
+void host_band_edges(uint32_t rows, uint32_t bands, uint32_t* edge)
+{
+    const uint32_t total = kHostBandTaper ? bands * (bands + 1) / 2 : bands;
+    uint32_t cum = 0;
+    edge[0] = 0;
+    for (uint32_t i = 0; i < bands; ++i) {
+        cum += kHostBandTaper ? bands - i : 1u;
+        uint32_t e = (uint32_t)(((uint64_t)rows * cum + total / 2) / total);
+        if (e < edge[i] + 1u) e = edge[i] + 1u;               // at least one row
+        if (e > rows - (bands - 1u - i)) e = rows - (bands - 1u - i);  // one row left for each later band
+        edge[i + 1] = e;
+    }
+}
+
 // One frame from host buffers: the lights go up and their BVH is built on the second stream while the
 // depth and normals go up on `st` in bands of tile rows, each band's tiles processed as it arrives;
 // then the references go down on the second stream while the light lists are assigned on `st`, and
@@ -1715,11 +1733,12 @@ int cs_enqueue_host(vren_cluster_and_shade* cs, cudaStream_t st, uint32_t W, uin
         const FucFrame fr = fuc_frame(cs->in_depth, cs->in_normals, W, H, cs->frame, cs->keys, cs->key_cap,
                                       cs->key_count, cs->refs, static_cast<uint32_t*>(cs->fuc_scratch));
         const uint32_t TX = (W + 31) / 32, TY = (H + 31) / 32;
-        const uint32_t bands = TY < kHostBands ? TY : kHostBands, per = (TY + bands - 1) / bands;
+        const uint32_t bands = TY < kHostBands ? TY : kHostBands;
+        uint32_t edge[kHostBands + 1];
+        host_band_edges(TY, bands, edge);
         const size_t nbytes = cs->opt.normal_format == VREN_CS_NORMALS_RGBA16F ? 8 : 12;  // per pixel
-        uint32_t band = 0;
-        for (uint32_t ty0 = 0; ty0 < TY; ty0 += per, ++band) {  // uploads on `up`, one event per band
-            const uint32_t ty1 = ty0 + per < TY ? ty0 + per : TY;
+        for (uint32_t band = 0; band < bands; ++band) {  // uploads on `up`, one event per band
+            const uint32_t ty0 = edge[band], ty1 = edge[band + 1];
             const size_t y0 = (size_t)ty0 * 32, y1 = (size_t)ty1 * 32 < H ? (size_t)ty1 * 32 : H;
             VREN_CUDA_TRY(cudaMemcpyAsync(cs->in_depth + y0 * W, depth + y0 * W, (y1 - y0) * W * 4,
                                           cudaMemcpyHostToDevice, up));
@@ -1732,9 +1751,8 @@ int cs_enqueue_host(vren_cluster_and_shade* cs, cudaStream_t st, uint32_t W, uin
         // Each band once it has arrived: its tiles, then its tile offsets (continuing from the band above)
         // and fix-up, after which its rows of references are final and go down on `aux` while the next
         // bands are still coming up.
-        band = 0;
-        for (uint32_t ty0 = 0; ty0 < TY; ty0 += per, ++band) {
-            const uint32_t ty1 = ty0 + per < TY ? ty0 + per : TY;
+        for (uint32_t band = 0; band < bands; ++band) {
+            const uint32_t ty0 = edge[band], ty1 = edge[band + 1];
             VREN_CUDA_TRY(cudaStreamWaitEvent(st, cs->ev_band[band], 0));
             rc = launch_find_unique_tiles(st, fr, ty0 * TX, (ty1 - ty0) * TX);
             if (rc != VREN_OK) return rc;
