@@ -921,6 +921,15 @@ extern "C" size_t vren_radix_sort_scratch1_bytes(uint32_t n, uint32_t digit_bits
     return scratch1_bytes(n, digit_bits);
 }
 
+// Once a pass has more tiles than one wave of resident CTAs, each pass launches while the one
+// before ends and waits for it in-kernel (measured: 2^22 pairs 0.181 -> 0.167 ms, 2^26 1.83 ->
+// 1.81 ms).  With fewer tiles the next pass's CTAs would all wait resident and start at once,
+// which measured slower (2^20 pairs: 0.085 -> 0.094 ms), so those sorts keep the caller's setting.
+static int passes_pdl(uint32_t n, uint32_t digit_bits)
+{
+    return n / tile_of(digit_bits, tuning(VREN_TUNE_RADIX_ITEMS) == 1 ? 1 : 0) > 4u * kNumSMsHint ? 1 : g_pdl;
+}
+
 extern "C" int vren_radix_sort_u32_ex(vren_stream_t s, uint32_t* keys, uint32_t* values, uint32_t n, uint32_t digit_bits,
                                       void* scratch1, uint32_t* scratch_keys, uint32_t* scratch_values)
 {
@@ -930,11 +939,7 @@ extern "C" int vren_radix_sort_u32_ex(vren_stream_t s, uint32_t* keys, uint32_t*
     if (((uintptr_t)keys & 15u) || ((uintptr_t)scratch1 & 15u)) return VREN_ERR_ARG;
     if (n <= 1) return VREN_OK;
     cudaStream_t st = as_stream(s);
-    // Once a pass has more tiles than one wave of resident CTAs, each pass launches while the one
-    // before ends and waits for it in-kernel (measured: 2^22 pairs 0.181 -> 0.167 ms, 2^26 1.83 ->
-    // 1.81 ms).  With fewer tiles the next pass's CTAs would all wait resident and start at once,
-    // which measured slower (2^20 pairs: 0.085 -> 0.094 ms), so those sorts keep the caller's setting.
-    const PdlScope pdl(n / tile_of(digit_bits, tuning(VREN_TUNE_RADIX_ITEMS) == 1 ? 1 : 0) > 4u * kNumSMsHint ? 1 : g_pdl);
+    const PdlScope pdl(passes_pdl(n, digit_bits));
     PassInfo passes = make_passes(32, digit_bits);
     uint32_t* sc = static_cast<uint32_t*>(scratch1);
     const uint32_t* src_k = keys;
@@ -1044,6 +1049,7 @@ extern "C" int vren_bucket_sort_u32x2(vren_stream_t s, const uint32_t* in, uint3
     const uint32_t db = bucket_digit_bits(key_bits);
     uint32_t* tmp = reinterpret_cast<uint32_t*>(static_cast<char*>(scratch) + (scratch1_bytes(n, db) + 255) / 256 * 256);
     if (n > 0) {
+        const PdlScope pdl(passes_pdl(n, db));
         PassInfo passes = make_passes(key_bits, db);
         int rc = radix_dispatch<kUvec2>(st, db, in, nullptr, out_pairs, nullptr, tmp, nullptr, n, passes, sc);
         if (rc != VREN_OK) return rc;
