@@ -67,6 +67,22 @@ def test_size_helpers_match_oracle_formulas(native):
                 assert native.vren_round_to_next_power_of(n, b) == ol.oracle_round_to_next_power_of(n, b), (n, b)
 
 
+def test_bucket_sort_scratch_covers_the_one_scatter_layout(native):
+    """For up to 10 key bits the scratch holds the one-scatter form's layout: 2,064 header words
+    (scan ticket and counters, bucket totals, bucket starts), a 1,024-word count row per
+    4,096-element tile and a 1,024-word look-back row per block of 256 tile rows; and it covers the
+    radix-pass form too, which either key width may select."""
+    for n in [0, 1, 4096, 4097, 1 << 20, (1 << 24) + 5, (1 << 26) + 12345, (1 << 30) - 1]:
+        rows = max(1, -(-n // 4096))
+        blocks = -(-rows // 256)
+        one_scatter = (2064 + (rows + blocks) * 1024) * 4
+        for kb in (1, 7, 10):
+            assert native.vren_bucket_sort_scratch_bytes(n, kb) >= one_scatter, (n, kb)
+        assert native.vren_bucket_sort_scratch_bytes(n, 16) > 0
+    assert native.vren_bucket_sort_scratch_bytes(100, 0) == 0
+    assert native.vren_bucket_sort_scratch_bytes(100, 17) == 0
+
+
 def test_status_strings(native):
     assert native.vren_status_string(0) == b"ok"
     assert native.vren_status_string(2) == b"capacity exceeded"
