@@ -69,6 +69,14 @@ uint32_t vren_set_wait_limit(uint32_t rounds);
  * scratch must be zero-filled again before its next use. */
 int vren_test_withhold_scan_status(uint32_t tile_plus_one);
 
+/* Test hook (no counterpart in the reference): on the current device, the bucket sort's column scan
+ * (the one-scatter form, up to 10 key bits) stops publishing the look-back words of its row block
+ * `block_plus_one - 1`, so the blocks after it wait until the wait limit and record
+ * VREN_ERR_TIMEOUT; the call still returns and its kernels end (that call's output is not sorted).
+ * 0 restores normal operation.  Call it with no bucket sort in flight.  The next call needs no
+ * action: the sort resets its look-back words itself. */
+int vren_test_withhold_bucket_scan_status(uint32_t block_plus_one);
+
 /* Kernel variant knobs, read when work is enqueued (no counterpart in the reference; the autotuner
  * and benchmarks set them).  Every variant gives identical results.
  *   VREN_TUNE_SCAN_SLICES  128-element slices per warp in a scan tile: 4 (4096/tile) or 8 (8192/tile)
@@ -102,9 +110,9 @@ int vren_test_withhold_scan_status(uint32_t tile_plus_one);
  *                          tile-count scan and fix-up (three kernels), 2 = in the context's device
  *                          frames one kernel (tiles taken by ticket, offsets by look-back over the
  *                          tile counts)
- *   VREN_TUNE_BUCKET_FORM  bucket sort of up to 10 key bits: 0 = one pass over the elements (a
- *                          histogram kernel, then one scatter kernel with a look-back over 1024
- *                          buckets; the default), 1 = stable radix passes of at most 8 bits, then
+ *   VREN_TUNE_BUCKET_FORM  bucket sort of up to 10 key bits: 0 = one scatter pass (per-tile bucket
+ *                          histograms, a column scan of the tiles' count matrix, then one stable
+ *                          scatter; the default), 1 = stable radix passes of at most 8 bits, then
  *                          the end offsets read back from the sorted elements
  *   VREN_TUNE_HOST_ZERO_COPY vren_cs_cluster_host: 0 = the G-buffer copied up in bands, each band's
  *                          tiles processed on arrival; 1 = the unique-cluster kernel (one-kernel

@@ -29,6 +29,7 @@ PROTOTYPES: dict[str, tuple] = {
     "vren_device_error": (i32, [i32]),
     "vren_set_wait_limit": (u32, [u32]),
     "vren_test_withhold_scan_status": (i32, [u32]),
+    "vren_test_withhold_bucket_scan_status": (i32, [u32]),
     "vren_tuning_set": (i32, [i32, i32]),
     "vren_tuning_get": (i32, [i32]),
     "vren_round_to_next_power_of_2": (u32, [u32]),

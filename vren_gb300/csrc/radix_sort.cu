@@ -477,6 +477,11 @@ __global__ void __launch_bounds__(kSortThreads) bucket_tile_hist_kernel(const ui
         reinterpret_cast<const uint4*>(s_hist)[tid];
 }
 
+// Test hook (vren_test_withhold_bucket_scan_status): row block + 1 whose look-back words the column
+// scan never publishes, so the blocks after it run out their bounded waits; 0 (the default)
+// publishes every block.
+__device__ uint32_t g_bucket_withheld_block = 0;
+
 __global__ void __launch_bounds__(kBucketScanThreads) bucket_column_scan_kernel(uint32_t* scratch, uint32_t rows_n,
                                                                               uint32_t key_bits, uint32_t* ends,
                                                                               uint32_t wait_limit, uint32_t spin)
@@ -525,7 +530,8 @@ __global__ void __launch_bounds__(kBucketScanThreads) bucket_column_scan_kernel(
         agg += x;
     }
     uint32_t* my_status = status + (size_t)rb * kBucketRadix + col;
-    if (warp == 0) st_relaxed_u32(my_status, (rb == 0 ? kFlagPrefix : kFlagAggregate) | agg);
+    const bool publish = rb + 1u != *reinterpret_cast<volatile uint32_t*>(&g_bucket_withheld_block);
+    if (warp == 0 && publish) st_relaxed_u32(my_status, (rb == 0 ? kFlagPrefix : kFlagAggregate) | agg);
 
     // Look-back over the blocks above in the same columns, eight blocks a round (warp w reads block
     // base - w); every warp folds the round's words the same way, so all hold the prefix.
@@ -550,7 +556,7 @@ __global__ void __launch_bounds__(kBucketScanThreads) bucket_column_scan_kernel(
             }
             if (__syncthreads_and(done)) break;  // also keeps s_look until every warp has read it
         }
-        if (warp == 0) st_relaxed_u32(my_status, kFlagPrefix | (excl + agg));
+        if (warp == 0 && publish) st_relaxed_u32(my_status, kFlagPrefix | (excl + agg));
     }
     if (warp == 0 && rb == blocks - 1) scratch[kBkTotals + col] = excl + agg;
     const uint32_t add = excl + before;
@@ -1031,6 +1037,13 @@ static int bucket_sort_onepass(cudaStream_t st, const uint2* in, uint32_t n, uin
                                 static_cast<const uint32_t*>(scratch)));
     VREN_LAUNCH_CHECK();
     return VREN_OK;
+}
+
+extern "C" int vren_test_withhold_bucket_scan_status(uint32_t block_plus_one)
+{
+    return cudaMemcpyToSymbol(g_bucket_withheld_block, &block_plus_one, sizeof(block_plus_one)) == cudaSuccess
+               ? VREN_OK
+               : VREN_ERR_CUDA;
 }
 
 extern "C" int vren_bucket_sort_u32x2(vren_stream_t s, const uint32_t* in, uint32_t n, void* out, uint32_t key_bits,
